@@ -1,0 +1,306 @@
+/*
+ * volpt.h — C ABI of the GB300 progressive volume path tracer.
+ *
+ * A drop-in for the path-tracing compute path of volview's `render` crate
+ * (crates/render/src/lib.rs:14-23): volume, label, transfer-function and light
+ * map upload, camera, clip planes, label visibility, accumulate-frame and
+ * tone-mapped readback. Every type here is plain C (fixed-size integers, floats,
+ * pointers and sizes); the Rust binding a maintainer would add is in
+ * INTEGRATION.md.
+ *
+ * Conventions
+ *  - Every call returns vv_status; on failure vv_last_error() describes why.
+ *  - The renderer owns its device memory; inputs are borrowed and copied.
+ *  - One renderer per host thread; calls on one renderer are serialised. All
+ *    device work runs on the context's CUDA stream.
+ *  - There is no CPU fallback: without a CUDA device every call that needs one
+ *    returns VV_ERR_CUDA.
+ */
+#ifndef VOLPT_H
+#define VOLPT_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define VV_LABEL_COUNT 256
+
+typedef enum vv_status {
+    VV_OK = 0,
+    VV_ERR_ARG = 1,     /* invalid argument (null pointer, size mismatch, bad enum) */
+    VV_ERR_OOM = 2,     /* device allocation failed */
+    VV_ERR_CUDA = 3,    /* CUDA runtime error or no device */
+    VV_ERR_TIMEOUT = 4, /* a bounded device-side wait ran out */
+    VV_ERR_STATE = 5,   /* call out of order (e.g. record before resize) */
+    VV_ERR_LIMIT = 6    /* size above a documented maximum */
+} vv_status;
+
+typedef struct vv_context vv_context;
+typedef struct vv_renderer vv_renderer;
+
+/* ------------------------------------------------------------------ inputs */
+
+/* A scalar CT volume in Hounsfield units (volio::Volume,
+ * crates/volio/src/volume.rs:9-19): voxel (i, j, k) at hu[i + dims[0] * (j +
+ * dims[1] * k)]; `direction` is column-major, its columns the unit patient-space
+ * (LPS, mm) directions of the i, j, k axes. */
+typedef struct vv_volume {
+    uint32_t dims[3];
+    double spacing[3];
+    double origin[3];
+    double direction[9];
+    const int16_t* hu;
+} vv_volume;
+
+/* A transfer-function control point (crates/render/src/transfer.rs:8-14). */
+typedef struct vv_control_point {
+    float hu;
+    float color[3];   /* linear RGB albedo */
+    float extinction; /* 1/mm */
+} vv_control_point;
+
+/* A piecewise-linear transfer function over HU (transfer.rs:26-29). */
+typedef struct vv_transfer_function {
+    uint32_t count;
+    const vv_control_point* points;
+} vv_transfer_function;
+
+/* The segmentation model's decision margins on its own grid
+ * (renderer.rs:104-114): per node, grid axis 0 fastest, 4 bytes: best label,
+ * runner-up label, margin x 16, and 1 where finer labels replaced them. */
+typedef struct vv_soft_label_grid {
+    uint32_t dims[3];
+    uint32_t src_axis[3]; /* volume axis each grid axis runs along */
+    uint32_t flip[3];     /* 1 = that grid axis runs reversed */
+    const uint8_t* data;
+} vv_soft_label_grid;
+
+/* Equirectangular linear-RGB light map, rows from the zenith down
+ * (crates/render/src/environment.rs:13-17). */
+typedef struct vv_environment_map {
+    uint32_t width, height;
+    const float* rgb;
+} vv_environment_map;
+
+/* ------------------------------------------------------- per-frame settings */
+
+/* Orbit camera in patient space (crates/render/src/camera.rs:9-23). */
+typedef struct vv_orbit_camera {
+    float target[3];
+    float distance;
+    float yaw;
+    float pitch;
+    float fov_y;
+} vv_orbit_camera;
+
+enum { VV_LABEL_OFF = 0, VV_LABEL_TINT = 1, VV_LABEL_ISOLATE = 2, VV_LABEL_HYBRID = 3 };
+
+/* LabelParams (renderer.rs:129-183). */
+typedef struct vv_label_params {
+    int32_t mode;
+    float tint;
+    float extinction;
+    float ghost_opacity;
+    float cut_margin_mm;
+    uint32_t smoothing;
+    float colors[VV_LABEL_COUNT][4];    /* rgb albedo, a visibility (0 hidden) */
+    float materials[VV_LABEL_COUNT][4]; /* roughness, metalness, subsurface, coat */
+    uint8_t ghost[VV_LABEL_COUNT];      /* 1 = drawn translucently */
+    float density[VV_LABEL_COUNT][4];   /* hybrid ramp start/end, median, IQR */
+    float surface[VV_LABEL_COUNT][4];   /* pattern, colour variation, relief, size */
+    float optics[VV_LABEL_COUNT][4];    /* measured mu_s' rgb, w = 1 if measured */
+} vv_label_params;
+
+enum { VV_ENV_DOME = 0, VV_ENV_STUDIO = 1, VV_ENV_MAP = 2 };
+enum { VV_TONE_NONE = 0, VV_TONE_ACES = 1, VV_TONE_AGX = 2 };
+
+/* Lighting (renderer.rs:206-307). */
+typedef struct vv_lighting {
+    float azimuth;
+    float elevation;
+    float intensity;
+    float ambient;
+    int32_t environment;
+    float light_size;
+    float env_rotation;
+    float anisotropy;
+    float chromatic;
+    int32_t shadows;
+    int32_t ambient_occlusion;
+    float exposure;
+    int32_t auto_exposure;
+    float bloom;
+    float vignette;
+    float grain;
+    int32_t tone_mapper;
+    float roughness;
+    float metalness;
+    float subsurface;
+    float scattering_distance;
+    float subsurface_strength;
+    float surface_detail;
+} vv_lighting;
+
+enum { VV_PLANE_SAGITTAL = 0, VV_PLANE_CORONAL = 1, VV_PLANE_AXIAL = 2 };
+
+/* ClipPlane / Clipping (renderer.rs:400-429). */
+typedef struct vv_clip_plane {
+    int32_t enabled;
+    int32_t plane;
+    int32_t cut_positive;
+    float position;
+} vv_clip_plane;
+
+typedef struct vv_clipping {
+    vv_clip_plane planes[3];
+    int32_t all;
+} vv_clipping;
+
+enum { VV_DENOISE_OFF = 0, VV_DENOISE_ATROUS = 1, VV_DENOISE_OIDN = 2 };
+
+/* Option<PathTracing> (renderer.rs:333-373); enabled = 0 is None. */
+typedef struct vv_path_tracing {
+    int32_t enabled;
+    uint32_t bounces;
+    uint32_t samples_per_frame;
+    int32_t denoiser;
+    float aperture;
+    int32_t has_focus;
+    float focus[3];
+} vv_path_tracing;
+
+/* FrameParams (renderer.rs:309-331). */
+typedef struct vv_frame_params {
+    vv_orbit_camera camera;
+    float step_mm;
+    int32_t srgb_encode;
+    vv_label_params labels;
+    vv_lighting lighting;
+    int32_t preintegrate;
+    int32_t skip_empty_space;
+    vv_clipping clipping;
+    vv_path_tracing path_tracing;
+    int32_t smooth_sampling;
+} vv_frame_params;
+
+/* Geometry of an uploaded volume (renderer.rs:546-551, 944-946). */
+typedef struct vv_renderer_info {
+    float bounds_lo[3];
+    float bounds_hi[3];
+    float min_spacing;
+    float center[3];
+    float diagonal;
+    uint32_t dims[3];
+} vv_renderer_info;
+
+/* Size in bytes of the uniform block (the reference's std140 `Uniforms`,
+ * renderer.rs:43-74 = shaders/common.glsl:4-33). */
+#define VV_UNIFORMS_BYTES 21200
+
+/* ---------------------------------------------------------------- defaults */
+
+/* Lighting::default (renderer.rs:264-292). */
+void vv_lighting_default(vv_lighting* out);
+/* LabelParams::default (renderer.rs:166-182). */
+void vv_label_params_default(vv_label_params* out);
+/* PathTracing::default (renderer.rs:359-373), enabled; denoiser a-trous. */
+void vv_path_tracing_default(vv_path_tracing* out);
+/* Clipping::default (renderer.rs:418-429). */
+void vv_clipping_default(vv_clipping* out);
+/* OrbitCamera::framing (camera.rs:25-34). */
+void vv_orbit_camera_framing(const float center[3], float diagonal, vv_orbit_camera* out);
+
+/* ----------------------------------------------------------------- context */
+
+/* Replaces ash/Vulkan `Context::new` (crates/render/src/context.rs:37): a CUDA
+ * device and a stream owned by the context. */
+vv_status vv_context_create(int device, vv_context** out);
+/* As vv_context_create, but on the caller's stream (a cudaStream_t, or NULL for
+ * the legacy default stream); the caller keeps ownership of the stream. */
+vv_status vv_context_create_on_stream(int device, void* stream, vv_context** out);
+vv_status vv_context_destroy(vv_context* ctx);
+
+/* ---------------------------------------------------------------- renderer */
+
+/* Renderer::new (renderer.rs:555): converts HU to normalised density on the
+ * device, uploads the transfer function and computes the normal volume. */
+vv_status vv_renderer_create(vv_context* ctx, const vv_volume* volume,
+                             const vv_transfer_function* tf, vv_renderer** out);
+/* Renderer::destroy (renderer.rs:2072). */
+vv_status vv_renderer_destroy(vv_renderer* r);
+vv_status vv_renderer_get_info(const vv_renderer* r, vv_renderer_info* out);
+/* Renderer::default_camera (renderer.rs:944-946). */
+vv_status vv_default_camera(const vv_renderer* r, vv_orbit_camera* out);
+
+/* Renderer::set_transfer_function (renderer.rs:1226). */
+vv_status vv_set_transfer_function(vv_renderer* r, const vv_transfer_function* tf);
+/* Renderer::set_labels (renderer.rs:1241): n must equal the voxel count;
+ * `soft` may be NULL. */
+vv_status vv_set_labels(vv_renderer* r, const uint8_t* labels, size_t n,
+                        const vv_soft_label_grid* soft);
+/* Renderer::set_environment_map (renderer.rs:1283); NULL removes the map. */
+vv_status vv_set_environment_map(vv_renderer* r, const vv_environment_map* map);
+/* Renderer::resize (renderer.rs:1313): (re)allocates the output images. */
+vv_status vv_resize(vv_renderer* r, uint32_t width, uint32_t height);
+
+/* Renderer::record (renderer.rs:1499): one accumulate-frame (samples_per_frame
+ * paths per pixel), then the denoiser and the display passes. Returns
+ * VV_ERR_STATE where the reference panics (record before resize). Asynchronous
+ * on the context's stream. */
+vv_status vv_record(vv_renderer* r, uint64_t frame, const vv_frame_params* params);
+/* `frames` consecutive accumulate-frames with the same params in one persistent
+ * launch; the denoiser and display passes run once, after the last. Equivalent
+ * to `frames` calls of vv_record except that intermediate displays are skipped. */
+vv_status vv_record_frames(vv_renderer* r, uint64_t first_frame, uint32_t frames,
+                           const vv_frame_params* params);
+/* Renderer::accumulated_samples (renderer.rs:1217). */
+uint32_t vv_accumulated_samples(const vv_renderer* r);
+/* Waits for the renderer's work on its stream. */
+vv_status vv_synchronize(vv_renderer* r);
+
+/* Tone-mapped RGBA8 output (the image render_to_rgba reads back), width*height*4 bytes. */
+vv_status vv_read_output(vv_renderer* r, uint8_t* rgba, size_t capacity);
+/* The RGBA16F HDR image as raw half bits, width*height*4 values. */
+vv_status vv_read_hdr(vv_renderer* r, uint16_t* rgba_half, size_t capacity);
+/* The RGBA32F accumulation images (radiance+background, albedo+lum^2,
+ * normal+depth), width*height*4 floats each; any pointer may be NULL. */
+vv_status vv_read_accumulation(vv_renderer* r, float* accum, float* albedo, float* normal,
+                               size_t capacity_floats);
+
+/* render_to_rgba (crates/render/src/offscreen.rs:11): resize, `frames`
+ * accumulate-frames, display passes, read back width*height*4 bytes. */
+vv_status vv_render_to_rgba(vv_renderer* r, const vv_frame_params* params, uint32_t width,
+                            uint32_t height, uint32_t frames, uint8_t* out, size_t capacity);
+
+/* ------------------------------------------------------------ introspection */
+
+/* The uniform block `record` would upload for `params` at the current
+ * accumulation count (the reference's std140 layout, VV_UNIFORMS_BYTES). */
+vv_status vv_pack_uniforms(vv_renderer* r, const vv_frame_params* params, uint64_t frame,
+                           void* out, size_t capacity);
+
+enum {
+    VV_VOLUME_DENSITY = 0,  /* uint16 per voxel (R16_UNORM) */
+    VV_VOLUME_NORMALS = 1,  /* 4 x int8 per voxel (RGBA8_SNORM) */
+    VV_VOLUME_MASK = 2,     /* 2 x uint16 per voxel (RG16_UNORM) */
+    VV_VOLUME_LABELS = 3,   /* uint8 per voxel */
+    VV_VOLUME_MAJORANT = 4  /* float per brick, brick grid x-fastest */
+};
+/* Copies a device volume out in x-fastest voxel order (whatever its layout on
+ * the device). */
+vv_status vv_read_volume(vv_renderer* r, int which, void* out, size_t capacity);
+
+/* Kernel launches this renderer has issued since creation (for accounting). */
+uint64_t vv_kernel_launches(const vv_renderer* r);
+
+/* Description of the last error on this thread ("" if none). */
+const char* vv_last_error(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* VOLPT_H */

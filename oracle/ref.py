@@ -1,0 +1,151 @@
+"""Drives the reference's own shaders compiled as CPU code (test infrastructure).
+
+oracle/build_ref.py compiles shaders/{pt,majorant,normals,mask,denoise,tonemap,
+bloom}.comp into oracle/_ref/libref_<shader>.so. This module binds the same
+buffers the reference's Renderer binds (crates/render/src/renderer.rs:1938-1971:
+linear CLAMP_TO_EDGE for density, transfer function, normals and mask; nearest
+for labels, majorants, pre-integration, soft labels and the mask's blur partner)
+and runs the shaders' invocations over the same grids the reference dispatches.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REF_DIR = os.path.join(HERE, "_ref")
+P = C.c_void_p
+
+# glsl::Format
+R16_UNORM, RG16_UNORM, RGBA8_SNORM, RGBA8_UNORM, R32F, RG32F, RGBA32F, RGBA16F, R16F, R8_UINT, RGBA8_UINT = range(11)
+NEAREST, LINEAR = 0, 1
+
+_libs = {}
+
+
+def available():
+    return all(os.path.exists(os.path.join(REF_DIR, f"libref_{n}.so")) for n in ("pt", "majorant", "normals", "mask",
+                                                                                  "denoise"))
+
+
+def shader(name):
+    if name not in _libs:
+        l = C.CDLL(os.path.join(REF_DIR, f"libref_{name}.so"))
+        l.ref_bind_texture.argtypes = [C.c_char_p, P, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int]
+        l.ref_bind_image.argtypes = [C.c_char_p, P, C.c_int, C.c_int, C.c_int, C.c_int]
+        l.ref_set_uniforms.argtypes = [P, C.c_long]
+        l.ref_run.argtypes = [C.c_int] * 7
+        if hasattr(l, "ref_set_push"):
+            l.ref_set_push.argtypes = [P, C.c_long]
+        _libs[name] = l
+    return _libs[name]
+
+
+def _p(a):
+    return C.c_void_p(a.ctypes.data)
+
+
+def bind_common(l, r, dummy):
+    """Binds the renderer's textures the way write_descriptors does."""
+    w, h, d = r.dims
+    l.ref_bind_texture(b"density_tex", _p(r.density), R16_UNORM, w, h, d, LINEAR, 0)
+    l.ref_bind_texture(b"tf_tex", _p(r.lut), RGBA16F, 4096, 1, 1, LINEAR, 0)
+    lw, lh, ld = r.labels.shape[::-1]
+    l.ref_bind_texture(b"label_tex", _p(r.labels), R8_UINT, lw, lh, ld, NEAREST, 0)
+    l.ref_bind_texture(b"normal_tex", _p(r.normals), RGBA8_SNORM, w, h, d, LINEAR, 0)
+    l.ref_bind_texture(b"preint_tex", _p(r.preint), RGBA32F, 4096, 1, 1, NEAREST, 0)
+    if r.mask is not None:
+        l.ref_bind_texture(b"mask_tex", _p(r.mask), RG16_UNORM, w, h, d, LINEAR, 0)
+    else:
+        l.ref_bind_texture(b"mask_tex", _p(dummy), RG16_UNORM, 1, 1, 1, LINEAR, 0)
+    if getattr(r, "majorant", None) is not None:
+        bw, bh, bd = r.majorant.shape[::-1]
+        l.ref_bind_texture(b"majorant_tex", _p(r.majorant), R32F, bw, bh, bd, NEAREST, 0)
+
+
+def normals(r, uniforms):
+    l = shader("normals")
+    dummy = np.zeros(16, np.uint8)
+    out = np.zeros(r.density.shape + (4,), np.int8)
+    l.ref_set_uniforms(_p(uniforms), 21200)
+    bind_common(l, r, dummy)
+    w, h, d = r.dims
+    l.ref_bind_image(b"normal_image", _p(out), RGBA8_SNORM, w, h, d)
+    l.ref_run(0, w, 0, h, 0, d, _threads())
+    return out
+
+
+def mask(r, uniforms, margin, radius):
+    """mask.comp passes 0-3 (renderer.rs:1671-1694)."""
+    l = shader("mask")
+    dummy = np.zeros(16, np.uint8)
+    w, h, d = r.dims
+    a = np.zeros(r.density.shape + (2,), np.uint16)
+    b = np.zeros_like(a)
+    l.ref_set_uniforms(_p(uniforms), 21200)
+    saved = r.mask
+    r.mask = a
+    bind_common(l, r, dummy)
+    r.mask = saved
+    soft = r.soft if r.soft is not None else np.zeros((1, 1, 1, 4), np.uint8)
+    sw, sh, sd = soft.shape[2::-1]
+    l.ref_bind_texture(b"soft_tex", _p(soft), RGBA8_UINT, sw, sh, sd, NEAREST, 0)
+    l.ref_bind_texture(b"mask_b_tex", _p(b), RG16_UNORM, w, h, d, NEAREST, 0)
+    l.ref_bind_image(b"mask_image", _p(a), RG16_UNORM, w, h, d)
+    l.ref_bind_image(b"mask_b_image", _p(b), RG16_UNORM, w, h, d)
+    for pas in range(4):
+        push = np.array([w, h, d, 0, margin, pas, radius, 0] + list(r.soft_push), np.int32)
+        l.ref_set_push(_p(push), push.nbytes)
+        l.ref_run(0, w, 0, h, 0, d, _threads())
+    return a
+
+
+def majorant(r, uniforms):
+    l = shader("majorant")
+    dummy = np.zeros(16, np.uint8)
+    l.ref_set_uniforms(_p(uniforms), 21200)
+    bind_common(l, r, dummy)
+    bw, bh, bd = r.brick_dims()
+    out = np.zeros((bd, bh, bw), np.float32)
+    l.ref_bind_image(b"majorant_image", _p(out), R32F, bw, bh, bd)
+    l.ref_run(0, bw, 0, bh, 0, bd, _threads())
+    return out
+
+
+def pt_frame(r, uniforms, accum, albedo, normal, hdr, rows=None):
+    """pt.comp over the image (or rows [y0, y1)), updating the images in place."""
+    l = shader("pt")
+    dummy = np.zeros(16, np.uint8)
+    l.ref_set_uniforms(_p(uniforms), 21200)
+    bind_common(l, r, dummy)
+    H, W = accum.shape[:2]
+    l.ref_bind_image(b"accum_image", _p(accum), RGBA32F, W, H, 1)
+    l.ref_bind_image(b"guide_albedo_image", _p(albedo), RGBA32F, W, H, 1)
+    l.ref_bind_image(b"guide_normal_image", _p(normal), RGBA32F, W, H, 1)
+    l.ref_bind_image(b"hdr_image", _p(hdr), RGBA16F, W, H, 1)
+    y0, y1 = rows if rows is not None else (0, H)
+    l.ref_run(0, W, y0, y1, 0, 1, _threads())
+
+
+def denoise(uniforms, accum, albedo, normal):
+    """record_denoise's 7 passes (renderer.rs:1868-1904); returns the HDR image."""
+    l = shader("denoise")
+    H, W = accum.shape[:2]
+    ping = np.zeros((H, W, 4), np.float32)
+    pong = np.zeros_like(ping)
+    hdr = np.zeros((H, W, 4), np.uint16)
+    l.ref_set_uniforms(_p(uniforms), 21200)
+    for name, img in ((b"accum_image", accum), (b"guide_albedo_image", albedo), (b"guide_normal_image", normal),
+                      (b"ping_image", ping), (b"pong_image", pong)):
+        l.ref_bind_image(name, _p(img), RGBA32F, W, H, 1)
+    l.ref_bind_image(b"hdr_image", _p(hdr), RGBA16F, W, H, 1)
+    passes = [[0, 0, 0, 0]] + [[1 + k, 1 << k, k % 2, 0] for k in range(5)] + [[-1, 0, 1, 0]]
+    for sweep in passes:
+        push = np.array([W, H, 1, 0] + sweep, np.int32)
+        l.ref_set_push(_p(push), push.nbytes)
+        l.ref_run(0, W, 0, H, 0, 1, _threads())
+    return hdr
+
+
+def _threads():
+    return max(1, min(os.cpu_count() or 1, 64))

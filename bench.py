@@ -1,0 +1,386 @@
+"""Throughput of the progressive path tracer: path samples/s at 1024^2 on the
+512x512x400 head/neck phantom, one GB300.
+
+A step is one accumulate-frame (vv_record: the path-tracing launch, the a-trous
+denoiser and the display passes, as the reference's `record` runs them) of one
+path per pixel over the 1024x1024 image. Inputs stay resident in HBM (the density,
+mask, normal and label volumes, 1.2 GB, are larger than the 129 MB L2, so no
+flush is needed between steps).
+
+  value     device-timed throughput (CUDA events on the renderer's stream)
+  e2e       the same through the C ABI with a host readback of the tone-mapped
+            RGBA8 image every step (host wall clock)
+  roofline  the path-tracing kernel: algorithmic bytes per launch (event counts
+            x unique element bytes) / its CUDA-event time, against measured HBM
+  cpu_baseline  the CPU oracle timed on the host cores on a sample of rows
+
+`--impl reference` times the reference's own shaders compiled as CPU code
+(oracle/_ref; the CPU restatement where those were not built) on the same
+workload. With torchrun and --gpus N > 1, each rank renders its own replica.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "path samples/s at 1024² on 512²×400 CT (1 GB300); time & p50/p99 latency to fixed RMSE"
+UNIT = "path samples/s"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=40)
+    ap.add_argument("--warmup", type=int, default=4)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--size", type=int, default=1024)
+    ap.add_argument("--dims", default="512,512,400")
+    ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    return ap.parse_args()
+
+
+def dist_init(n):
+    rank, world, local = 0, 1, 0
+    if n > 1 or "WORLD_SIZE" in os.environ:
+        import torch.distributed as dist
+        rank = int(os.environ.get("RANK", 0))
+        world = int(os.environ.get("WORLD_SIZE", 1))
+        local = int(os.environ.get("LOCAL_RANK", 0))
+        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+        os.environ.setdefault("MASTER_PORT", "29533")
+        import torch
+        backend = "nccl" if torch.cuda.is_available() else "gloo"
+        if backend == "nccl":
+            torch.cuda.set_device(local)
+        dist.init_process_group(backend)
+    return rank, world, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(x, world):
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device="cuda" if torch.cuda.is_available() else "cpu")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+class Clocks:
+    """Samples SM clocks and throttle reasons with nvidia-smi while running."""
+
+    def __init__(self, device):
+        self.device = device
+        self.rows = []
+        self.proc = None
+
+    def __enter__(self):
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={q}", "--format=csv,noheader,nounits",
+                                          "-i", str(self.device), "-lms", "200"], stdout=subprocess.PIPE,
+                                         stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([c.strip() for c in line.split(",")])
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            self.proc.wait(timeout=5)
+
+    def summary(self):
+        if not self.rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        sm = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in self.rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in self.rows for i in range(4) if len(r) > 5 + i and r[5 + i] == "Active"})
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.rows)}
+
+
+def workload(args):
+    from volview_gb300 import scene
+    dims = tuple(int(v) for v in args.dims.split(","))
+    cfg = scene.head_neck_config(seed=2, dims=dims, spacing=(0.5, 0.5, 1.0), size=args.size, spp=1024)
+    return cfg
+
+
+def frame_params(cfg, center, diagonal):
+    from volview_gb300 import scene
+    # CLI defaults (main.rs): hybrid labels, g = 0.6, studio light, a-trous; sagittal cut.
+    return scene.frame_params_for(cfg, center, diagonal, clip_sagittal=True, anisotropy=0.6, spf=1)
+
+
+def peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def ncu_traffic():
+    """DRAM bytes per path-tracing launch from the committed ncu summary, if any."""
+    path = os.path.join(ROOT, "profiles", "pt_persistent_head_neck.md")
+    if not os.path.exists(path):
+        return None
+    for line in open(path):
+        if line.strip().startswith("dram_bytes_per_launch:"):
+            try:
+                return float(line.split(":", 1)[1].split()[0])
+            except ValueError:
+                return None
+    return None
+
+
+def cpu_sample(cpu, params, width, height, seconds, ref_lib=None):
+    """Times the CPU path tracer on spread-out rows; returns (samples/s, rows, threads, seconds)."""
+    import ctypes as C
+    from oracle import oracle as O
+    threads = O.threads()
+    u = cpu.uniforms(params, 1, width, height)
+    scene_c = cpu.scene()
+
+    def run(rows):
+        rows = np.ascontiguousarray(rows, np.int32)
+        t = time.perf_counter()
+        if ref_lib is None:
+            O.lib().vvo_pt_rows(O.ptr(u), C.byref(scene_c), O.ptr(cpu.accum), O.ptr(cpu.albedo), O.ptr(cpu.normal),
+                                O.ptr(cpu.hdr), O.ptr(rows), len(rows), threads)
+        else:
+            ref_lib.ref_run_rows(0, width, C.c_void_p(rows.ctypes.data), len(rows), threads)
+        return time.perf_counter() - t
+
+    # Calibrate on a few rows spread over the frame, then size the sample.
+    probe = np.linspace(0, height - 1, 8).astype(np.int32)
+    t = run(probe)
+    per_row = max(t / len(probe), 1e-4)
+    n = int(min(height, max(8, seconds / per_row)))
+    rows = np.linspace(0, height - 1, n).astype(np.int32)
+    rows = np.unique(rows)
+    t = run(rows)
+    return len(rows) * width / t, len(rows), threads, t
+
+
+def run_ours(args, rank, world, local):
+    import torch
+    from volview_gb300 import renderer as R
+    torch.cuda.set_device(local)
+    cfg = workload(args)
+    W = H = args.size
+    stream = torch.cuda.Stream()
+    ctx = R.Context(local, stream=stream.cuda_stream)
+    r = R.Renderer(ctx, cfg["volume"], cfg["tf"])
+    from volview_gb300 import abi
+    r.set_labels(cfg["labels_vol"], abi.soft_struct(cfg["soft"]))
+    params = frame_params(cfg, list(r.center), r.diagonal)
+    r.resize(W, H)
+    frame = 1
+    r.record(frame, params)  # masks, majorants and the first frame
+    frame += 1
+    # Event counts of one frame (untimed) for the roofline's byte model.
+    r.count_events(True)
+    r.record(frame, params)
+    frame += 1
+    counts = r.count_events(False)
+    for _ in range(args.warmup):
+        r.record(frame, params)
+        frame += 1
+    r.synchronize()
+    spf = int(params.path_tracing.samples_per_frame)
+    launches0 = r.kernel_launches()
+    barrier(world)
+    start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with Clocks(local) as clocks:
+        torch.cuda.synchronize()
+        r.time_pt(True)
+        start.record(stream)
+        for _ in range(args.steps):
+            r.record(frame, params)
+            frame += 1
+        end.record(stream)
+        torch.cuda.synchronize()
+        pt_ms, pt_launches = r.time_pt(False)
+    barrier(world)
+    launches = r.kernel_launches() - launches0
+    ms = max_over_ranks(start.elapsed_time(end), world)
+    samples = args.steps * W * H * spf * world
+    value = samples / (ms / 1e3)
+    # e2e through the C ABI: record + tone-mapped readback into pinned memory.
+    e2e = None
+    if not args.no_e2e:
+        host = torch.empty((H, W, 4), dtype=torch.uint8).pin_memory()
+        out = host.numpy()
+        barrier(world)
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            r.record(frame, params)
+            frame += 1
+            r.read_output(out)
+        t1 = max_over_ranks(time.perf_counter() - t0, world)
+        e2e = {"value": samples / t1, "unit": UNIT, "h2d_bytes_per_step": 720,
+               "d2h_bytes_per_step": W * H * 4}
+    acc_samples = r.accumulated_samples()
+    # Roofline of the path-tracing kernel.
+    from volview_gb300.renderer import COUNT_BYTES, COUNT_NAMES
+    alg_bytes = float(sum(counts[n] * b for n, b in zip(COUNT_NAMES, COUNT_BYTES)))
+    pt_avg_ms = pt_ms / max(pt_launches, 1)
+    achieved = alg_bytes / (pt_avg_ms / 1e3) / 1e9
+    peak, peak_kind = peaks()
+    traffic = ncu_traffic()
+    result = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded head/neck phantom; no CT data ships)",
+        "config": {"workload": f"head_neck {args.dims.replace(',', 'x')} int16 HU at 0.5x0.5x1 mm, 120 labels, "
+                               f"soft labels, hybrid mode, sagittal clip, g=0.6, studio light, {W}x{H}, "
+                               f"1 path/pixel/frame, a-trous + tone-mapped readback per frame",
+                   "frames_per_step": 1, "l2": "inputs larger than L2 (1.2 GB of volumes)",
+                   "parallelism": "replicas" if world > 1 else "single GPU"},
+        "gpu_launches": int(launches),
+        "path_vertices_per_s": counts["vertex"] / max(counts["pixel"], 1) * value,
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "traffic": traffic, "kernel": "k_pt_persistent",
+                     "peak_source": peak_kind, "alg_bytes_per_launch": alg_bytes,
+                     "avg_launch_ms": pt_avg_ms, "events_per_frame": counts},
+        "accumulated_samples": acc_samples,
+    }
+    result["clocks"] = clocks.summary()
+    if rank == 0 and not args.no_cpu_baseline:
+        result["cpu_baseline"] = cpu_baseline(cfg, r, params, args)
+    r.destroy()
+    ctx.destroy()
+    if rank == 0:
+        print(json.dumps(result))
+
+
+def cpu_renderer_from_device(cfg, r, params):
+    """The oracle's CPU renderer with the device's pre-pass volumes (bit-exact or
+    within one quantum of the oracle's own, see tests) so only the path tracer
+    is timed."""
+    from oracle import oracle as O
+    from volview_gb300 import abi
+    cpu = O.CpuRenderer.__new__(O.CpuRenderer)
+    cpu.volume = cfg["volume"]
+    cpu.hu = cfg["hu"]
+    cpu.dims = tuple(cfg["volume"].dims)
+    cpu.geo = O.geometry(cfg["volume"])
+    cpu.density = r.read_volume(abi.VOLUME_DENSITY)
+    cpu.set_transfer_function(cfg["tf"])
+    cpu.normals = r.read_volume(abi.VOLUME_NORMALS)
+    cpu.set_labels(cfg["labels_vol"], cfg["soft"])
+    cpu.mask = r.read_volume(abi.VOLUME_MASK)
+    cpu.majorant = r.read_volume(abi.VOLUME_MAJORANT)
+    cpu.accumulated = 0
+    cpu.accum_key = None
+    cpu.resize(r.width, r.height)
+    cpu.mask_key = "device"
+    return cpu
+
+
+def cpu_baseline(cfg, r, params, args):
+    cpu = cpu_renderer_from_device(cfg, r, params)
+    rate, rows, threads, secs = cpu_sample(cpu, params, r.width, r.height, args.cpu_seconds)
+    return {"value": rate, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"{rows} rows spread over the {r.width}x{r.height} frame, 1 path/pixel "
+                      f"({rows * r.width} paths, {secs:.1f} s); CPU restatement of pt.comp, "
+                      f"pre-pass volumes from the device"}
+
+
+def run_reference(args, rank, world):
+    """The reference's shaders compiled as CPU code on the same workload."""
+    if rank != 0:
+        return
+    from oracle import oracle as O
+    from oracle import ref as REF
+    cfg = workload(args)
+    W = H = args.size
+    cpu = O.CpuRenderer(cfg["volume"], cfg["tf"], cfg["hu"])
+    cpu.set_labels(cfg["labels_vol"], cfg["soft"])
+    g = cpu.geo
+    params = frame_params(cfg, list(g.center), g.diagonal)
+    cpu.resize(W, H)
+    kind = "port"
+    ref_lib = None
+    if REF.available():
+        kind = "reference"
+        cpu.normals = REF.normals(cpu, cpu._uniforms_geometry_only())
+        u = cpu.uniforms(params, 1, W, H)
+        cpu.mask = REF.mask(cpu, u, O.mask_margin(cfg["volume"], params.labels), int(params.labels.smoothing))
+        cpu.majorant = REF.majorant(cpu, u)
+        cpu.mask_key = "reference"
+        ref_lib = REF.shader("pt")
+        ref_lib.ref_set_uniforms(REF._p(u), 21200)
+        REF.bind_common(ref_lib, cpu, np.zeros(16, np.uint8))
+        for name, img, fmt in ((b"accum_image", cpu.accum, REF.RGBA32F), (b"guide_albedo_image", cpu.albedo, REF.RGBA32F),
+                               (b"guide_normal_image", cpu.normal, REF.RGBA32F), (b"hdr_image", cpu.hdr, REF.RGBA16F)):
+            ref_lib.ref_bind_image(name, REF._p(img), fmt, W, H, 1)
+        ref_lib.ref_run_rows.argtypes = [__import__("ctypes").c_int, __import__("ctypes").c_int,
+                                         __import__("ctypes").c_void_p, __import__("ctypes").c_int,
+                                         __import__("ctypes").c_int]
+    else:
+        cpu.prepare(params, W, H)
+    rates = []
+    per_step = args.cpu_seconds / max(args.steps, 1) * 4
+    for i in range(args.warmup + args.steps):
+        rate, rows, threads, secs = cpu_sample(cpu, params, W, H, max(per_step, 1.0), ref_lib)
+        if i >= args.warmup:
+            rates.append((rate, rows, secs))
+    total_paths = sum(rt * s for rt, _, s in rates)
+    total_s = sum(s for _, _, s in rates)
+    value = total_paths / total_s
+    print(json.dumps({
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": total_s / len(rates) * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded head/neck phantom)",
+        "config": {"workload": f"head_neck {args.dims.replace(',', 'x')}, {W}x{H}, 1 path/pixel/frame"},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": O.threads(), "kind": kind,
+                         "sample": f"per step {rates[0][1]} rows spread over the frame; "
+                                   + ("shaders/pt.comp compiled as CPU code" if kind == "reference"
+                                      else "CPU restatement of pt.comp")},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }))
+
+
+def main():
+    args = parse()
+    rank, world, local = dist_init(args.gpus)
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+    else:
+        run_ours(args, rank, world, local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

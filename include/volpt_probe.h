@@ -1,0 +1,46 @@
+/*
+ * volpt_probe.h — test hooks of libvolpt.so.
+ *
+ * These entry points have no counterpart in the reference: they run single
+ * device functions of the path tracer on a renderer's current state so that the
+ * parity tests can compare them with the CPU oracle one sample at a time.
+ */
+#ifndef VOLPT_PROBE_H
+#define VOLPT_PROBE_H
+
+#include "volpt.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Cubic B-spline density and its gradient (per index unit) at n continuous
+ * voxel indices idx[3n] (common.glsl:124-136): out[4n] = value, gx, gy, gz.
+ * Runs record's preparation (masks, majorants) for `params` first. */
+vv_status vv_probe_bspline(vv_renderer* r, const vv_frame_params* params, const float* idx, size_t n,
+                           float* out);
+
+/* pt.comp's per-pixel result for n pixels (x, y pairs) at accumulation count
+ * `accumulated`: out[12n] = radiance sum (rgb), background, albedo sum (rgb,
+ * luminance^2), normal sum (rgb, depth). */
+vv_status vv_probe_paths(vv_renderer* r, const vv_frame_params* params, uint32_t accumulated,
+                         const int* pixels, size_t n, float* out);
+
+/* Event counting for the roofline's algorithmic-byte model: enable = 1 starts
+ * counting the path tracer's memory events over the following records (at
+ * some cost in speed); enable = 0 stops and copies up to n totals to out, in
+ * the order: majorant lookups, cubic densities, trilinear densities, mask
+ * lookups, label fetches, normal lookups, cubic gradients, pixel
+ * accumulations, paths, path vertices. */
+vv_status vv_count_events(vv_renderer* r, int enable, uint64_t* out, size_t n);
+
+/* Device time of the path-tracing launches: enable = 1 starts recording CUDA
+ * events around each launch on the renderer's stream; enable = 0 stops, waits,
+ * and returns the summed milliseconds and the number of launches. */
+vv_status vv_time_pt(vv_renderer* r, int enable, double* ms, uint64_t* launches);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* VOLPT_PROBE_H */

@@ -22,6 +22,8 @@ void majorant_pass(const Uniforms& u, const Scene& sc, float* out);
 void pt_frame(const Uniforms& u, const Scene& sc, float* accum, float* albedo, float* normal, uint16_t* hdr,
               int y0, int y1, int threads);
 void pt_pixel(const Uniforms& u, const Scene& sc, int x, int y, float out[12]);
+void pt_rows(const Uniforms& u, const Scene& sc, float* accum, float* albedo, float* normal, uint16_t* hdr,
+             const int* rows, int nrows, int threads);
 void bspline(const Uniforms& u, const Scene& sc, const float* idx, long n, float* out);
 void denoise(const Uniforms& u, const float* accum, const float* albedo, const float* normal, uint16_t* hdr,
              float* ping, float* pong, int threads);
@@ -121,6 +123,10 @@ void vvo_majorant(const void* u, const vvo_scene* s, float* out) { majorant_pass
 void vvo_pt_frame(const void* u, const vvo_scene* s, float* accum, float* albedo, float* normal, uint16_t* hdr,
                   int y0, int y1, int threads) {
     pt_frame(U(u), to_scene(s), accum, albedo, normal, hdr, y0, y1, threads);
+}
+void vvo_pt_rows(const void* u, const vvo_scene* s, float* accum, float* albedo, float* normal, uint16_t* hdr,
+                 const int* rows, int nrows, int threads) {
+    pt_rows(U(u), to_scene(s), accum, albedo, normal, hdr, rows, nrows, threads);
 }
 void vvo_pt_pixel(const void* u, const vvo_scene* s, int x, int y, float out[12]) {
     pt_pixel(U(u), to_scene(s), x, y, out);

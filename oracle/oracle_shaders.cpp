@@ -1002,6 +1002,28 @@ void pt_frame(const Uniforms& u, const Scene& sc, float* accum, float* albedo, f
     });
 }
 
+// pt.comp over a list of pixel rows (a bounded, spread-out sample of a frame).
+void pt_rows(const Uniforms& u, const Scene& sc, float* accum, float* albedo, float* normal, uint16_t* hdr,
+             const int* rows, int nrows, int threads) {
+    Units t = bind_scene(sc);
+    int W = int(u.flags.z);
+    bool first = u.path.x == 0u;
+    parallel_rows((long)nrows * W, threads, [&](long k) {
+        int y = rows[k / W], x = int(k % W);
+        Tracer tr{Shading{u, t}};
+        Tracer::PixelResult R = tr.trace_pixel(uint(x), uint(y));
+        long i = (long)y * W + x;
+        vec4 acc = (first ? vec4(0.0f) : vec4(accum[4 * i], accum[4 * i + 1], accum[4 * i + 2], accum[4 * i + 3])) +
+                   vec4(R.sum, R.background);
+        for (int c = 0; c < 4; c++) {
+            accum[4 * i + c] = acc[c];
+            albedo[4 * i + c] = (first ? 0.0f : albedo[4 * i + c]) + R.albedo_sum[c];
+            normal[4 * i + c] = (first ? 0.0f : normal[4 * i + c]) + R.normal_sum[c];
+        }
+        if (hdr) glsl::encode(hdr, glsl::RGBA16F, i, acc / float(u.path.x + u.path.z));
+    });
+}
+
 // One path of pixel (x, y): the same stream as pt_frame's first sample.
 void pt_pixel(const Uniforms& u, const Scene& sc, int x, int y, float out[12]) {
     Units t = bind_scene(sc);

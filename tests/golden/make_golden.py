@@ -1,0 +1,63 @@
+"""Generates tests/golden/small_scene.npz from the reference's own shaders.
+
+Runs shaders/{normals,mask,majorant,pt,denoise}.comp — compiled as CPU code by
+oracle/build_ref.py from the reference sources — on a 24^3 seeded phantom with
+soft labels, hybrid label mode and a sagittal clip plane, 24x24 pixels, two
+accumulate-frames of two paths each. Inputs that the reference computes on the
+host (density normalisation, LUT, uniforms) come from the oracle's restatement
+of the render crate; the density normalisation and LUT are themselves pinned by
+the reference's unit tests (crates/render/src/transfer.rs:130-149).
+
+Usage (needs the reference sources): python tests/golden/make_golden.py
+"""
+import os
+import sys
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+sys.path.insert(0, ROOT)
+
+from oracle import build_ref  # noqa: E402
+from oracle import oracle as O  # noqa: E402
+from oracle import ref as R  # noqa: E402
+from volview_gb300 import abi, scene  # noqa: E402
+
+
+def main():
+    if not R.available():
+        build_ref.main([])
+    n, size, frames, spf = 24, 24, 2, 2
+    cfg = scene.small_config(n=n, size=size, spp=frames * spf)
+    r = O.CpuRenderer(cfg["volume"], cfg["tf"], cfg["hu"])
+    r.set_labels(cfg["labels_vol"], cfg["soft"])
+    g = r.geo
+    params = scene.frame_params_for(cfg, list(g.center), g.diagonal, clip_sagittal=True, spf=spf)
+    r.resize(size, size)
+    normals = R.normals(r, r._uniforms_geometry_only())
+    r.normals = normals
+    u1 = r.uniforms(params, 1, size, size)
+    mask = R.mask(r, u1, O.mask_margin(cfg["volume"], params.labels), int(params.labels.smoothing))
+    r.mask = mask
+    majorant = R.majorant(r, u1)
+    r.majorant = majorant
+    acc = np.zeros((size, size, 4), np.float32)
+    alb, nor = np.zeros_like(acc), np.zeros_like(acc)
+    hdr = np.zeros((size, size, 4), np.uint16)
+    for f in range(frames):
+        r.accumulated = f * spf
+        u = r.uniforms(params, f + 1, size, size)
+        R.pt_frame(r, u, acc, alb, nor, hdr)
+    r.accumulated = (frames - 1) * spf
+    denoised = R.denoise(r.uniforms(params, frames, size, size), acc, alb, nor)
+    out = os.path.join(os.path.dirname(os.path.abspath(__file__)), "small_scene.npz")
+    np.savez_compressed(out, hu=cfg["hu"], labels=cfg["labels_vol"], soft=cfg["soft"],
+                        spacing=np.array(cfg["spacing"]), params=np.frombuffer(bytes(params), np.uint8),
+                        width=size, height=size, frames=frames, density=r.density, normals=normals, mask=mask,
+                        majorant=majorant, uniforms_frame1=u1, accum=acc, albedo=alb, normal=nor, hdr=hdr,
+                        denoised=denoised)
+    print(out, os.path.getsize(out), "bytes; background share", float(acc[..., 3].mean()) / (frames * spf))
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,108 @@
+"""Behaviour of the C ABI as the render crate defines it (GPU)."""
+import numpy as np
+import pytest
+
+from volview_gb300 import abi, scene
+from volview_gb300 import renderer as R
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture()
+def rend(small_cfg, gpu_ctx):
+    cfg = small_cfg
+    r = R.Renderer(gpu_ctx, cfg["volume"], cfg["tf"])
+    r.set_labels(cfg["labels_vol"], abi.soft_struct(cfg["soft"]))
+    p = scene.frame_params_for(cfg, list(r.center), r.diagonal)
+    yield cfg, r, p
+    r.destroy()
+
+
+def test_record_before_resize_is_a_state_error(rend):
+    cfg, r, p = rend
+    with pytest.raises(R.VolptError) as e:
+        r.record(1, p)
+    assert e.value.status == abi.VV_ERR_STATE
+
+
+def test_label_size_mismatch(rend):
+    cfg, r, p = rend
+    with pytest.raises(R.VolptError) as e:
+        r.set_labels(np.zeros(10, np.uint8))
+    assert e.value.status == abi.VV_ERR_ARG
+
+
+def test_ray_marcher_not_provided(rend):
+    cfg, r, p = rend
+    r.resize(16, 16)
+    p.path_tracing.enabled = 0
+    with pytest.raises(R.VolptError):
+        r.record(1, p)
+
+
+def test_accumulation_keys(rend):
+    cfg, r, p = rend
+    r.resize(32, 32)
+    r.record(1, p)
+    r.record(2, p)
+    assert r.accumulated_samples() == 2
+    p.path_tracing.denoiser = abi.DENOISE_OFF  # display only: keeps accumulating
+    r.record(3, p)
+    assert r.accumulated_samples() == 3
+    p.camera.yaw = 0.3
+    r.record(4, p)
+    assert r.accumulated_samples() == 1
+    p.path_tracing.samples_per_frame = 3
+    r.record(5, p)
+    assert r.accumulated_samples() == 3
+
+
+def test_record_frames_equals_records(small_cfg, gpu_ctx):
+    cfg = small_cfg
+    out = []
+    for batched in (False, True):
+        r = R.Renderer(gpu_ctx, cfg["volume"], cfg["tf"])
+        r.set_labels(cfg["labels_vol"], abi.soft_struct(cfg["soft"]))
+        p = scene.frame_params_for(cfg, list(r.center), r.diagonal)
+        p.path_tracing.denoiser = abi.DENOISE_OFF
+        r.resize(40, 24)
+        if batched:
+            r.record_frames(1, 6, p)
+        else:
+            for f in range(1, 7):
+                r.record(f, p)
+        assert r.accumulated_samples() == 6
+        out.append(r.read_accumulation()[0])
+        r.destroy()
+    a, b = out
+    assert np.allclose(a, b, rtol=1e-5, atol=1e-6)
+
+
+def test_frame_and_persistent_kernels_agree(small_cfg, gpu_ctx, monkeypatch):
+    cfg = small_cfg
+    out = []
+    for kernel in ("frame", "persistent"):
+        monkeypatch.setenv("VV_PT_KERNEL", kernel)
+        r = R.Renderer(gpu_ctx, cfg["volume"], cfg["tf"])
+        r.set_labels(cfg["labels_vol"], abi.soft_struct(cfg["soft"]))
+        p = scene.frame_params_for(cfg, list(r.center), r.diagonal, spf=2)
+        r.resize(48, 40)
+        r.record(1, p)
+        r.record(2, p)
+        out.append(r.read_accumulation()[0])
+        r.destroy()
+    ok = np.all(np.abs(out[0] - out[1]) <= 1e-4 * np.abs(out[1]) + 1e-6, axis=-1)
+    assert ok.mean() >= 0.98
+
+
+def test_render_to_rgba(small_cfg, gpu_ctx):
+    cfg = small_cfg
+    r = R.Renderer(gpu_ctx, cfg["volume"], cfg["tf"])
+    r.set_labels(cfg["labels_vol"], abi.soft_struct(cfg["soft"]))
+    p = scene.frame_params_for(cfg, list(r.center), r.diagonal)
+    img = R.render_to_rgba(r, p, 64, 48, 4)
+    assert img.shape == (48, 64, 4)
+    assert (img[..., 3] == 255).all()
+    assert r.accumulated_samples() == 4
+    assert img[..., :3].std() > 0  # something was drawn
+    r.destroy()

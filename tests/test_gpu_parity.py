@@ -1,0 +1,163 @@
+"""Parity of the CUDA path against the CPU oracle, through the C ABI (GPU).
+
+Tolerances (written here, checked below):
+* density, normals, majorant: bit-exact (integer/quantised outputs);
+* masks: every voxel within one RG16 quantum, >= 99.9% exact (the soft masks
+  call expf, whose last bit may differ between CUDA and the C library);
+* cubic B-spline value and gradient: 1e-4 relative (scale: the value range);
+* single-path replays: 1e-4 relative per pixel; the share of pixels whose
+  paths branch differently (a float comparison flipped by a last-bit
+  difference) is reported and must stay below 2%;
+* converged image: within 3 sigma of the per-pixel Monte Carlo error for
+  >= 99% of pixels;
+* a-trous denoiser on identical accumulation inputs: within one FP16 ulp.
+"""
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+from volview_gb300 import abi, scene
+from volview_gb300 import renderer as R
+
+pytestmark = pytest.mark.gpu
+
+
+def make_params(cfg, center, diagonal, zoom=0.45, **kw):
+    p = scene.frame_params_for(cfg, center, diagonal, **kw)
+    p.camera.distance = abi.f32(p.camera.distance * zoom)
+    return p
+
+
+@pytest.fixture(scope="module")
+def pair(small_cfg, gpu_ctx):
+    cfg = small_cfg
+    gpu = R.Renderer(gpu_ctx, cfg["volume"], cfg["tf"])
+    gpu.set_labels(cfg["labels_vol"], abi.soft_struct(cfg["soft"]))
+    cpu = O.CpuRenderer(cfg["volume"], cfg["tf"], cfg["hu"])
+    cpu.set_labels(cfg["labels_vol"], cfg["soft"])
+    params = make_params(cfg, list(gpu.center), gpu.diagonal, clip_sagittal=True)
+    gpu.resize(48, 48)
+    cpu.resize(48, 48)
+    yield cfg, gpu, cpu, params
+    gpu.destroy()
+
+
+def test_geometry_matches(pair):
+    cfg, gpu, cpu, params = pair
+    g = cpu.geo
+    assert list(gpu.center) == list(g.center)
+    assert gpu.diagonal == g.diagonal
+    assert gpu.min_spacing == g.min_spacing
+
+
+def test_density_bit_exact(pair):
+    cfg, gpu, cpu, params = pair
+    assert np.array_equal(gpu.read_volume(abi.VOLUME_DENSITY), cpu.density)
+
+
+def test_normals_bit_exact(pair):
+    cfg, gpu, cpu, params = pair
+    assert np.array_equal(gpu.read_volume(abi.VOLUME_NORMALS), cpu.normals)
+
+
+def test_uniforms_bit_exact(pair):
+    cfg, gpu, cpu, params = pair
+    a = gpu.pack_uniforms(params, 1)
+    b = cpu.uniforms(params, 1, 48, 48)
+    assert np.array_equal(a, b), np.nonzero(a != b)[0][:16]
+
+
+def test_masks_and_majorant(pair):
+    cfg, gpu, cpu, params = pair
+    gpu.probe_bspline(params, np.zeros((1, 3), np.float32))  # runs record's mask and majorant passes
+    cpu.prepare(params, 48, 48)
+    m_gpu = gpu.read_volume(abi.VOLUME_MASK)
+    d = np.abs(m_gpu.astype(np.int32) - cpu.mask.astype(np.int32))
+    assert d.max() <= 1
+    assert (d == 0).mean() >= 0.999
+    # Majorant: bit-exact against the oracle run on the same mask.
+    cpu_mask = cpu.mask
+    cpu.mask = m_gpu
+    u = cpu.uniforms(params, 1, 48, 48)
+    maj = np.zeros_like(cpu.majorant)
+    O.lib().vvo_majorant(O.ptr(u), O.C.byref(cpu.scene()), O.ptr(maj))
+    cpu.mask = cpu_mask
+    assert np.array_equal(gpu.read_volume(abi.VOLUME_MAJORANT), maj)
+
+
+def test_bspline_value_and_gradient(pair):
+    cfg, gpu, cpu, params = pair
+    rng = np.random.default_rng(7)
+    idx = rng.uniform(-0.5, 47.5, size=(4096, 3)).astype(np.float32)
+    a = gpu.probe_bspline(params, idx)
+    b = cpu.bspline(params, idx)
+    scale = max(float(np.abs(b[:, 0]).max()), 1e-6)
+    assert np.abs(a[:, 0] - b[:, 0]).max() <= 1e-4 * scale
+    gscale = max(float(np.abs(b[:, 1:]).max()), 1e-6)
+    assert np.abs(a[:, 1:] - b[:, 1:]).max() <= 1e-4 * gscale
+
+
+def _rel_close(a, b, rtol=1e-4, atol=1e-6):
+    return np.all(np.abs(a - b) <= rtol * np.abs(b) + atol, axis=-1)
+
+
+def test_single_path_replays(pair):
+    cfg, gpu, cpu, params = pair
+    ys, xs = np.mgrid[0:48, 0:48]
+    pix = np.stack([xs.ravel(), ys.ravel()], 1).astype(np.int32)
+    flips = 0
+    total = 0
+    for acc in (0, 5):
+        a = gpu.probe_paths(params, acc, pix)
+        b = np.stack([cpu.trace_pixel(params, int(x), int(y), acc) for x, y in pix])
+        ok = _rel_close(a, b)
+        flips += int((~ok).sum())
+        total += ok.size
+    rate = flips / total
+    print(f"single-path replay branch-flip rate: {rate:.4%} of {total} pixel-paths")
+    assert rate < 0.02
+
+
+def test_converged_image_within_3_sigma(pair, gpu_ctx):
+    cfg, gpu, cpu, params = pair
+    p = make_params(cfg, list(gpu.center), gpu.diagonal, clip_sagittal=True)
+    p.path_tracing.denoiser = abi.DENOISE_OFF
+    n_gpu = 1024
+    gpu.resize(48, 48)
+    gpu.record_frames(1, n_gpu, p)
+    acc, alb, _ = gpu.read_accumulation()
+    # The oracle traces 64 independent paths per pixel (other RNG streams).
+    cpu.resize(48, 48)
+    for f in range(64):
+        cpu.record(p, f + 1)
+    w = np.array([0.2126, 0.7152, 0.0722], np.float32)
+
+    def stats(acc, alb, n):
+        mean = (acc[..., :3] @ w) / n
+        m2 = alb[..., 3] / n
+        var = np.maximum(m2 - mean * mean, 0.0) / n
+        return mean, var
+
+    mg, vg = stats(acc, alb, n_gpu)
+    mc, vc = stats(cpu.accum, cpu.albedo, 64)
+    sigma = np.sqrt(vg + vc) + 1e-6
+    inside = np.abs(mg - mc) <= 3.0 * sigma
+    print(f"converged image: {inside.mean():.4%} of pixels within 3 sigma")
+    assert inside.mean() >= 0.99
+
+
+def test_denoiser_on_identical_inputs(pair):
+    cfg, gpu, cpu, params = pair
+    p = make_params(cfg, list(gpu.center), gpu.diagonal, clip_sagittal=True)
+    gpu.resize(48, 48)
+    for f in range(1, 5):
+        gpu.record(f, p)
+    acc, alb, nor = gpu.read_accumulation()
+    hdr_gpu = gpu.read_hdr()
+    cpu.resize(48, 48)
+    cpu.accum[:], cpu.albedo[:], cpu.normal[:] = acc, alb, nor
+    cpu.accumulated = gpu.accumulated_samples()
+    hdr_cpu = cpu.denoise(p)
+    a = hdr_gpu.view(np.float16).astype(np.float32)
+    b = hdr_cpu.view(np.float16).astype(np.float32)
+    assert np.all(np.abs(a - b) <= np.abs(b) * 2.0 ** -10 + 1e-7)

@@ -1,0 +1,104 @@
+"""The oracle against the reference's own known answers (CPU only).
+
+transfer.rs:130-149 holds the reference's only tests on this path; they pin the
+density normalisation and the transfer-function LUT. The shader restatement is
+pinned by golden vectors produced by the reference's shaders compiled as CPU
+code (tests/golden/make_golden.py), and live against those shaders when
+oracle/_ref was built here.
+"""
+import os
+
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+from volview_gb300 import abi
+
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden", "small_scene.npz")
+
+
+def test_interpolates_between_points():
+    # transfer.rs:130-139
+    tf = abi.tf_struct([(0.0, (0.0, 0.0, 0.0), 0.0), (100.0, (1.0, 1.0, 1.0), 2.0)])
+    assert list(O.tf_evaluate(tf, -50.0)) == [0.0, 0.0, 0.0, 0.0]
+    assert list(O.tf_evaluate(tf, 50.0)) == [0.5, 0.5, 0.5, 1.0]
+    assert list(O.tf_evaluate(tf, 500.0)) == [1.0, 1.0, 1.0, 2.0]
+
+
+def test_lut_matches_density_normalisation():
+    # transfer.rs:141-149
+    assert O.hu_to_unorm16(np.array([-1024, 3071, -2000], np.int16)).tolist() == [0, 65535, 0]
+    tf = abi.tf_struct(abi.PRESETS["bone"])
+    lut = O.tf_lut(tf)
+    assert np.array_equal(lut[1024 + 300], O.tf_evaluate(tf, 300.0))
+
+
+def test_bucket_max_covers_the_next_entry():
+    tf = abi.tf_struct(abi.PRESETS["bone"])
+    lut = O.tf_lut(tf)
+    b = O.bucket_max(tf)
+    for k in range(64):
+        assert b[k] == lut[64 * k:min(64 * k + 65, 4096), 3].max()
+
+
+def _golden():
+    if not os.path.exists(GOLDEN):
+        pytest.skip("golden fixtures not generated")
+    return np.load(GOLDEN)
+
+
+def _scene_from_golden(g):
+    from volview_gb300 import scene
+    vol = abi.volume_struct(g["hu"], tuple(g["spacing"]))
+    tf = abi.tf_struct(abi.PRESETS["bone"])
+    r = O.CpuRenderer(vol, tf, g["hu"])
+    r.set_labels(g["labels"], g["soft"])
+    params = abi.FrameParams.from_buffer_copy(g["params"].tobytes())
+    r.resize(int(g["width"]), int(g["height"]))
+    return r, params
+
+
+def test_oracle_matches_reference_golden_volumes():
+    g = _golden()
+    r, params = _scene_from_golden(g)
+    u = r.record(params, 1)
+    assert np.array_equal(r.density, g["density"])
+    assert np.array_equal(r.normals, g["normals"])
+    assert np.array_equal(r.mask, g["mask"])
+    assert np.array_equal(r.majorant, g["majorant"])
+    assert np.array_equal(u, g["uniforms_frame1"])
+
+
+def test_oracle_matches_reference_golden_frames():
+    g = _golden()
+    r, params = _scene_from_golden(g)
+    for f in range(1, int(g["frames"]) + 1):
+        r.record(params, f)
+    # Same arithmetic, same order: bit-exact.
+    assert np.array_equal(r.accum, g["accum"])
+    assert np.array_equal(r.albedo, g["albedo"])
+    assert np.array_equal(r.normal, g["normal"])
+    assert np.array_equal(r.hdr, g["hdr"])
+    assert np.array_equal(r.denoise(params), g["denoised"])
+
+
+def test_oracle_matches_reference_shaders_live(small_cfg):
+    from oracle import ref as R
+    if not R.available():
+        pytest.skip("oracle/_ref not built (needs the reference sources)")
+    cfg = small_cfg
+    r = O.CpuRenderer(cfg["volume"], cfg["tf"], cfg["hu"])
+    r.set_labels(cfg["labels_vol"], cfg["soft"])
+    g = r.geo
+    from volview_gb300 import scene
+    params = scene.frame_params_for(cfg, list(g.center), g.diagonal, clip_sagittal=True)
+    r.resize(48, 48)
+    assert np.array_equal(R.normals(r, r._uniforms_geometry_only()), r.normals)
+    u = r.record(params, 1)
+    assert np.array_equal(R.mask(r, u, O.mask_margin(cfg["volume"], params.labels), 1), r.mask)
+    assert np.array_equal(R.majorant(r, u), r.majorant)
+    acc = np.zeros((48, 48, 4), np.float32)
+    alb, nor = np.zeros_like(acc), np.zeros_like(acc)
+    hdr = np.zeros((48, 48, 4), np.uint16)
+    R.pt_frame(r, u, acc, alb, nor, hdr)
+    assert np.array_equal(acc, r.accum) and np.array_equal(alb, r.albedo) and np.array_equal(nor, r.normal)

@@ -173,13 +173,28 @@ def clipping_default():
     return c
 
 
+_libm = None
+
+
+def tanf(x):
+    """The C library's single-precision tangent (what Rust's f32::tan calls)."""
+    global _libm
+    if _libm is None:
+        import ctypes.util
+        _libm = C.CDLL(ctypes.util.find_library("m") or "libm.so.6")
+        _libm.tanf.restype = C.c_float
+        _libm.tanf.argtypes = [C.c_float]
+    return _libm.tanf(x)
+
+
 def camera_framing(center, diagonal):
     """OrbitCamera::framing (camera.rs:25-34)."""
     cam = OrbitCamera()
     fov = to_radians(30.0)
     for i in range(3):
         cam.target[i] = center[i]
-    cam.distance = f32(np.float32(0.55) * np.float32(diagonal) / np.tan(np.float32(fov) / np.float32(2.0)))
+    cam.distance = f32(np.float32(np.float32(0.55) * np.float32(diagonal)) /
+                       np.float32(tanf(f32(np.float32(fov) / np.float32(2.0)))))
     cam.yaw = 0.0
     cam.pitch = 0.0
     cam.fov_y = fov

@@ -1,0 +1,1098 @@
+// vv_host.cpp — the renderer behind include/volpt.h.
+//
+// Restates the host side of volview's `render` crate for the path-tracing
+// path: Renderer::new / set_transfer_function / set_labels / resize / record
+// (crates/render/src/renderer.rs), render_to_rgba (offscreen.rs), the transfer
+// function (transfer.rs) and the orbit camera (camera.rs). Vulkan images become
+// device buffers on one CUDA stream; descriptor sets become kernel arguments.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/volpt.h"
+#include "vv_device.cuh"
+#include "vv_kernels.h"
+
+using namespace vv;
+
+// ------------------------------------------------------------------ errors
+static thread_local std::string g_error;
+
+static vv_status fail(vv_status s, const std::string& msg) {
+    g_error = msg;
+    return s;
+}
+static vv_status cuda_fail(cudaError_t e, const char* what) {
+    return fail(e == cudaErrorMemoryAllocation ? VV_ERR_OOM : VV_ERR_CUDA,
+                std::string(what) + ": " + cudaGetErrorString(e));
+}
+#define CK(call)                                               \
+    do {                                                       \
+        cudaError_t e_ = (call);                               \
+        if (e_ != cudaSuccess) return cuda_fail(e_, #call);    \
+    } while (0)
+
+extern "C" const char* vv_last_error(void) { return g_error.c_str(); }
+
+// ---------------------------------------------------------------- defaults
+static float to_radians(float deg) { return deg * (3.14159265358979323846f / 180.0f); }
+
+extern "C" void vv_lighting_default(vv_lighting* L) {
+    std::memset(L, 0, sizeof(*L));
+    L->azimuth = to_radians(-60.0f);
+    L->elevation = to_radians(40.0f);
+    L->intensity = 3.0f;
+    L->ambient = 0.3f;
+    L->environment = VV_ENV_STUDIO;
+    L->light_size = to_radians(12.0f);
+    L->env_rotation = 0.0f;
+    L->anisotropy = 0.0f;
+    L->chromatic = 1.0f;
+    L->shadows = 1;
+    L->ambient_occlusion = 1;
+    L->exposure = 0.0f;
+    L->auto_exposure = 1;
+    L->bloom = 0.04f;
+    L->vignette = 0.25f;
+    L->grain = 0.012f;
+    L->tone_mapper = VV_TONE_ACES;
+    L->roughness = 0.5f;
+    L->metalness = 0.0f;
+    L->subsurface = 0.3f;
+    L->scattering_distance = 4.0f;
+    L->subsurface_strength = 1.0f;
+    L->surface_detail = 1.0f;
+}
+
+extern "C" void vv_label_params_default(vv_label_params* p) {
+    std::memset(p, 0, sizeof(*p));
+    p->mode = VV_LABEL_OFF;
+    p->tint = 0.7f;
+    p->extinction = 0.5f;
+    p->ghost_opacity = 0.08f;
+    p->cut_margin_mm = 2.0f;
+    p->smoothing = 1;
+    for (int i = 0; i < VV_LABEL_COUNT; i++) {
+        for (int c = 0; c < 4; c++) p->colors[i][c] = 1.0f;
+        p->materials[i][0] = 0.5f; p->materials[i][1] = 0.0f; p->materials[i][2] = 0.3f; p->materials[i][3] = 0.0f;
+        p->density[i][0] = 0.0f; p->density[i][1] = 1e-3f; p->density[i][2] = 0.5f; p->density[i][3] = 1.0f;
+    }
+}
+
+extern "C" void vv_path_tracing_default(vv_path_tracing* pt) {
+    std::memset(pt, 0, sizeof(*pt));
+    pt->enabled = 1;
+    pt->bounces = 4;
+    pt->samples_per_frame = 1;
+    pt->denoiser = VV_DENOISE_ATROUS;
+}
+
+extern "C" void vv_clipping_default(vv_clipping* c) {
+    std::memset(c, 0, sizeof(*c));
+    for (int i = 0; i < 3; i++) c->planes[i].plane = i;
+}
+
+extern "C" void vv_orbit_camera_framing(const float center[3], float diagonal, vv_orbit_camera* out) {
+    float fov = to_radians(30.0f);
+    for (int i = 0; i < 3; i++) out->target[i] = center[i];
+    out->distance = 0.55f * diagonal / std::tan(fov / 2.0f);
+    out->yaw = 0.0f;
+    out->pitch = 0.0f;
+    out->fov_y = fov;
+}
+
+// ----------------------------------------------------------------- context
+struct vv_context {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    bool owns_stream = false;
+    int sms = 0;
+};
+
+extern "C" vv_status vv_context_create_on_stream(int device, void* stream, vv_context** out) {
+    if (!out) return fail(VV_ERR_ARG, "null output pointer");
+    int n = 0;
+    cudaError_t e = cudaGetDeviceCount(&n);
+    if (e != cudaSuccess || n == 0) return fail(VV_ERR_CUDA, "no CUDA device");
+    if (device < 0 || device >= n) return fail(VV_ERR_ARG, "device index out of range");
+    CK(cudaSetDevice(device));
+    vv_context* c = new vv_context();
+    c->device = device;
+    CK(cudaDeviceGetAttribute(&c->sms, cudaDevAttrMultiProcessorCount, device));
+    if (stream) {
+        c->stream = (cudaStream_t)stream;
+    } else {
+        e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+        if (e != cudaSuccess) {
+            delete c;
+            return cuda_fail(e, "cudaStreamCreate");
+        }
+        c->owns_stream = true;
+    }
+    *out = c;
+    return VV_OK;
+}
+
+extern "C" vv_status vv_context_create(int device, vv_context** out) {
+    return vv_context_create_on_stream(device, nullptr, out);
+}
+
+extern "C" vv_status vv_context_destroy(vv_context* c) {
+    if (!c) return VV_OK;
+    cudaSetDevice(c->device);
+    if (c->owns_stream) cudaStreamDestroy(c->stream);
+    delete c;
+    return VV_OK;
+}
+
+// ---------------------------------------------------------- device buffers
+struct DBuf {
+    void* p = nullptr;
+    size_t n = 0;
+    cudaError_t alloc(size_t bytes) {
+        if (p && n == bytes) return cudaSuccess;
+        release();
+        cudaError_t e = cudaMalloc(&p, bytes);
+        if (e == cudaSuccess) n = bytes;
+        else p = nullptr;
+        return e;
+    }
+    void release() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        n = 0;
+    }
+    template <class T> T* as() const { return (T*)p; }
+};
+
+// Everything that decides which voxels are opaque (renderer.rs:436-449).
+struct OpacityKey {
+    uint64_t generation;
+    int mode;
+    uint32_t extinction_bits;
+    uint64_t visible[4], ghost[4];
+    uint32_t ghost_opacity_bits;
+    int margin;
+    uint32_t smoothing;
+    bool operator==(const OpacityKey& o) const { return std::memcmp(this, &o, sizeof(*this)) == 0; }
+};
+
+struct vv_renderer {
+    vv_context* ctx;
+    Vol vol;
+    double spacing[3];
+    // geometry
+    float w2i[16], i2w[16];
+    float dims[3];
+    float bounds_lo[3], bounds_hi[3];
+    float min_spacing, max_spacing;
+    float center[3];
+    float diagonal;
+    // transfer function
+    float bucket[64];
+    // device volumes
+    DBuf density, normals, mask_a, mask_b, labels, majorant, lut, bucket_dev, tables, soft, work, exposure;
+    int soft_dims[3] = {1, 1, 1};
+    int soft_push[4] = {0, 0, 0, 0};
+    bool has_labels = false;
+    uint64_t generation = 0;
+    bool have_mask_key = false, have_majorant_key = false;
+    OpacityKey mask_key, majorant_key;
+    // outputs
+    uint32_t width = 0, height = 0;
+    DBuf accum, albedo, normal, ping, pong, hdr, out, bloom[4];
+    int bw[4], bh[4];
+    // accumulation
+    uint32_t accumulated = 0;
+    bool have_params = false;
+    vv_frame_params accumulated_params;
+    // host staging for the label tables
+    LabelTables* tables_host = nullptr;
+    bool tables_valid = false;
+    uint64_t launches = 0;
+    unsigned long long* counters = nullptr;  // set while counting events
+    // CUDA events around each path-tracing launch while timing is on.
+    bool timing = false;
+    std::vector<std::pair<cudaEvent_t, cudaEvent_t>> pt_events;
+};
+
+// Records the start event of a timed path-tracing launch (if timing is on).
+static void pt_timer_start(vv_renderer* r) {
+    if (!r->timing) return;
+    cudaEvent_t a, b;
+    cudaEventCreate(&a);
+    cudaEventCreate(&b);
+    cudaEventRecord(a, r->ctx->stream);
+    r->pt_events.push_back({a, b});
+}
+static void pt_timer_stop(vv_renderer* r) {
+    if (r->timing && !r->pt_events.empty()) cudaEventRecord(r->pt_events.back().second, r->ctx->stream);
+}
+
+// ------------------------------------------------------------ host math
+// Vector arithmetic follows glam (normalize multiplies by the reciprocal length).
+struct h3 {
+    float x, y, z;
+};
+static h3 add(h3 a, h3 b) { return {a.x + b.x, a.y + b.y, a.z + b.z}; }
+static h3 sub(h3 a, h3 b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
+static h3 scl(h3 a, float s) { return {a.x * s, a.y * s, a.z * s}; }
+static float hdot(h3 a, h3 b) { return (a.x * b.x) + (a.y * b.y) + (a.z * b.z); }
+static h3 hcross(h3 a, h3 b) { return {a.y * b.z - b.y * a.z, a.z * b.x - b.z * a.x, a.x * b.y - b.x * a.y}; }
+static h3 hnorm(h3 a) { return scl(a, 1.0f / std::sqrt(hdot(a, a))); }
+
+// camera.rs:34-48
+static h3 cam_forward(const vv_orbit_camera& c) {
+    float sy = std::sin(c.yaw), cy = std::cos(c.yaw), sp = std::sin(c.pitch), cp = std::cos(c.pitch);
+    return {cp * sy, cp * cy, -sp};
+}
+
+// transfer.rs:72-86
+static void tf_eval(const vv_transfer_function* tf, float hu, float out[4]) {
+    const vv_control_point* p = tf->points;
+    auto put = [&](const vv_control_point& c) {
+        out[0] = c.color[0]; out[1] = c.color[1]; out[2] = c.color[2]; out[3] = c.extinction;
+    };
+    if (hu <= p[0].hu) { put(p[0]); return; }
+    for (uint32_t k = 0; k + 1 < tf->count; k++) {
+        if (hu <= p[k + 1].hu) {
+            float t = (hu - p[k].hu) / std::fmax(p[k + 1].hu - p[k].hu, 1e-6f);
+            float a[4] = {p[k].color[0], p[k].color[1], p[k].color[2], p[k].extinction};
+            float b[4] = {p[k + 1].color[0], p[k + 1].color[1], p[k + 1].color[2], p[k + 1].extinction};
+            for (int i = 0; i < 4; i++) out[i] = a[i] + (b[i] - a[i]) * t;
+            return;
+        }
+    }
+    put(p[tf->count - 1]);
+}
+
+// Uploads the LUT (transfer.rs:90-97, f16-rounded as upload_tf does,
+// renderer.rs:2177-2182) and computes the bucket maxima (renderer.rs:2164-2174).
+static vv_status upload_tf(vv_renderer* r, const vv_transfer_function* tf) {
+    if (!tf || tf->count == 0 || !tf->points) return fail(VV_ERR_ARG, "empty transfer function");
+    std::vector<float> lut(4 * 4096);
+    for (int i = 0; i < 4096; i++) {
+        float t = (float)i / 4095.0f;
+        tf_eval(tf, -1024.0f + t * (3071.0f - -1024.0f), &lut[4 * i]);
+    }
+    for (int b = 0; b < 64; b++) {
+        int end = std::min((b + 1) * 64 + 1, 4096);
+        float m = 0.0f;
+        for (int i = b * 64; i < end; i++) m = std::fmax(m, lut[4 * i + 3]);
+        r->bucket[b] = m;
+    }
+    std::vector<float> lut_half(4 * 4096);
+    for (int i = 0; i < 4 * 4096; i++) lut_half[i] = (float)(_Float16)lut[i];
+    CK(r->lut.alloc(lut_half.size() * sizeof(float)));
+    CK(cudaMemcpyAsync(r->lut.p, lut_half.data(), lut_half.size() * sizeof(float), cudaMemcpyHostToDevice,
+                       r->ctx->stream));
+    CK(r->bucket_dev.alloc(64 * sizeof(float)));
+    CK(cudaMemcpyAsync(r->bucket_dev.p, r->bucket, sizeof(r->bucket), cudaMemcpyHostToDevice, r->ctx->stream));
+    CK(cudaStreamSynchronize(r->ctx->stream));
+    return VV_OK;
+}
+
+// volio Volume::index_to_world / world_to_index (volume.rs:22-35) in f64, cast to
+// f32; bounds, centre and diagonal as in Renderer::new (renderer.rs:819-834).
+static void set_geometry(vv_renderer* r, const vv_volume* v) {
+    double m[9];
+    for (int c = 0; c < 3; c++)
+        for (int k = 0; k < 3; k++) m[3 * c + k] = v->direction[3 * c + k] * v->spacing[c];
+    double a = m[0], b = m[3], c = m[6], d = m[1], e = m[4], f = m[7], g = m[2], h = m[5], k = m[8];
+    double A = e * k - f * h, B = -(d * k - f * g), C = d * h - e * g;
+    double det = a * A + b * B + c * C;
+    double inv[9] = {A / det, -(b * k - c * h) / det, (b * f - c * e) / det,
+                     B / det, (a * k - c * g) / det, -(a * f - c * d) / det,
+                     C / det, -(a * h - b * g) / det, (a * e - b * d) / det};  // column-major
+    for (int col = 0; col < 3; col++) {
+        for (int row = 0; row < 3; row++) {
+            r->w2i[4 * col + row] = (float)inv[3 * col + row];
+            r->i2w[4 * col + row] = (float)m[3 * col + row];
+        }
+        r->w2i[4 * col + 3] = 0.0f;
+        r->i2w[4 * col + 3] = 0.0f;
+    }
+    for (int row = 0; row < 3; row++) {
+        double t = -(inv[row] * v->origin[0] + inv[3 + row] * v->origin[1] + inv[6 + row] * v->origin[2]);
+        r->w2i[12 + row] = (float)t;
+        r->i2w[12 + row] = (float)v->origin[row];
+    }
+    r->w2i[15] = 1.0f;
+    r->i2w[15] = 1.0f;
+    auto world = [&](double x, double y, double z, double* o) {
+        for (int q = 0; q < 3; q++) o[q] = m[q] * x + m[3 + q] * y + m[6 + q] * z + v->origin[q];
+    };
+    double cw[3];
+    world((v->dims[0] - 1.0) * 0.5, (v->dims[1] - 1.0) * 0.5, (v->dims[2] - 1.0) * 0.5, cw);
+    for (int q = 0; q < 3; q++) {
+        r->center[q] = (float)cw[q];
+        r->dims[q] = (float)v->dims[q];
+        r->bounds_lo[q] = 3.4028235e38f;
+        r->bounds_hi[q] = -3.4028235e38f;
+        r->spacing[q] = v->spacing[q];
+    }
+    for (int i = 0; i < 8; i++) {
+        double w[3];
+        world((i & 1) ? v->dims[0] - 0.5 : -0.5, (i & 2) ? v->dims[1] - 0.5 : -0.5, (i & 4) ? v->dims[2] - 0.5 : -0.5, w);
+        for (int q = 0; q < 3; q++) {
+            r->bounds_lo[q] = std::fmin(r->bounds_lo[q], (float)w[q]);
+            r->bounds_hi[q] = std::fmax(r->bounds_hi[q], (float)w[q]);
+        }
+    }
+    r->min_spacing = (float)std::fmin(v->spacing[0], std::fmin(v->spacing[1], v->spacing[2]));
+    r->max_spacing = (float)std::fmax(v->spacing[0], std::fmax(v->spacing[1], v->spacing[2]));
+    double ext = 0.0;
+    for (int q = 0; q < 3; q++) {
+        double x = std::fmax((double)v->dims[q] - 1.0, 0.0) * v->spacing[q];
+        ext += x * x;
+    }
+    r->diagonal = (float)std::sqrt(ext);
+}
+
+// renderer.rs:80-87
+static float tissue_majorant(const vv_label_params& l, float anisotropy, float limit) {
+    float g = std::fmin(std::fmax(anisotropy, 0.0f), 0.95f);
+    float largest = 0.0f;
+    for (int i = 0; i < 256; i++)
+        if (l.colors[i][3] > 0.5f && !l.ghost[i] && l.optics[i][3] > 0.0f) {
+            float m = 0.0f;
+            for (int c = 0; c < 3; c++) m = std::fmax(m, l.optics[i][c]);
+            largest = std::fmax(largest, m);
+        }
+    return std::fmin(largest / (1.0f - g), limit);
+}
+
+// The uniform block `record` writes (renderer.rs:1516-1660) and the clip planes
+// of clip_uniforms (renderer.rs:1449-1466), std140.
+static void pack(const vv_renderer* r, const vv_frame_params& p, uint32_t accumulated, uint64_t frame,
+                 UHead& u, LabelTables& t) {
+    std::memset(&u, 0, sizeof(u));
+    const vv_orbit_camera& cam = p.camera;
+    h3 f = cam_forward(cam);
+    h3 right = hnorm(hcross(f, {0.0f, 0.0f, 1.0f}));
+    h3 up = hcross(right, f);
+    h3 eye = sub({cam.target[0], cam.target[1], cam.target[2]}, scl(f, cam.distance));
+    float tan_half = std::tan(cam.fov_y / 2.0f);
+    float aspect = (float)r->width / (float)r->height;
+    const vv_lighting& L = p.lighting;
+    float se = std::sin(L.elevation), ce = std::cos(L.elevation), sa = std::sin(L.azimuth), ca = std::cos(L.azimuth);
+    h3 ld = hnorm(add(add(scl(scl(scl(f, -1.0f), ce), ca), scl(scl(right, ce), sa)), scl(up, se)));
+    int environment = L.environment == VV_ENV_MAP ? VV_ENV_STUDIO : L.environment;  // no light map bound
+    const vv_label_params& lab = p.labels;
+    std::memcpy(u.w2i, r->w2i, sizeof(u.w2i));
+    auto put3 = [](float* d, h3 v, float w) { d[0] = v.x; d[1] = v.y; d[2] = v.z; d[3] = w; };
+    put3(u.eye, eye, 1.0f);
+    put3(u.forward, f, 0.0f);
+    put3(u.right, scl(scl(right, tan_half), aspect), 0.0f);
+    put3(u.up, scl(up, tan_half), 0.0f);
+    u.dims[0] = r->dims[0]; u.dims[1] = r->dims[1]; u.dims[2] = r->dims[2]; u.dims[3] = p.step_mm;
+    u.flags[0] = (uint32_t)frame; u.flags[1] = p.srgb_encode ? 1u : 0u; u.flags[2] = r->width; u.flags[3] = r->height;
+    u.labels[0] = r->has_labels ? (float)lab.mode : 0.0f;
+    u.labels[1] = lab.tint; u.labels[2] = lab.extinction; u.labels[3] = lab.ghost_opacity;
+    put3(u.light_dir, ld, L.intensity);
+    float amb = environment == VV_ENV_STUDIO ? 0.5f * L.ambient : L.ambient;
+    u.ambient[0] = amb; u.ambient[1] = amb; u.ambient[2] = amb; u.ambient[3] = std::exp2(L.exposure);
+    u.material[0] = L.roughness; u.material[1] = L.metalness; u.material[2] = (float)L.tone_mapper;
+    u.material[3] = L.light_size;
+    u.lighting[0] = L.shadows ? 1u : 0u; u.lighting[1] = L.ambient_occlusion ? 1u : 0u;
+    u.lighting[2] = p.preintegrate ? 1u : 0u; u.lighting[3] = (uint32_t)environment;
+    u.light_cells[0] = 2.0f * r->max_spacing; u.light_cells[1] = 4.0f * r->max_spacing;
+    {
+        h3 col[3] = {{r->i2w[0], r->i2w[1], r->i2w[2]}, {r->i2w[4], r->i2w[5], r->i2w[6]}, {r->i2w[8], r->i2w[9], r->i2w[10]}};
+        h3 b = {r->i2w[12], r->i2w[13], r->i2w[14]};
+        uint32_t n = 0;
+        for (int i = 0; i < 3; i++) {
+            const vv_clip_plane& cp = p.clipping.planes[i];
+            if (!cp.enabled) continue;
+            float sign = cp.cut_positive ? 1.0f : -1.0f;
+            h3 normal = {0.0f, 0.0f, 0.0f};
+            int axis = cp.plane < 0 ? 0 : (cp.plane > 2 ? 2 : cp.plane);
+            (&normal.x)[axis] = 1.0f;
+            normal = scl(normal, sign);
+            h3 an = {hdot(col[0], normal), hdot(col[1], normal), hdot(col[2], normal)};
+            put3(u.clip_planes + 4 * n, an, sign * cp.position - hdot(normal, b));
+            put3(u.clip_normals + 4 * n, normal, 0.0f);
+            n++;
+        }
+        u.clip[0] = n; u.clip[1] = p.clipping.all ? 1u : 0u;
+    }
+    uint32_t skip = p.skip_empty_space ? 1u : 0u;
+    const vv_path_tracing& pt = p.path_tracing;
+    if (pt.enabled) {
+        u.path[0] = accumulated; u.path[1] = pt.bounces; u.path[2] = std::max(pt.samples_per_frame, 1u); u.path[3] = skip;
+        float focus = cam.distance;
+        if (pt.has_focus) focus = hdot(sub({pt.focus[0], pt.focus[1], pt.focus[2]}, eye), f);
+        u.lens[0] = pt.aperture; u.lens[1] = std::fmax(focus, 1.0f);
+    } else {
+        u.path[3] = skip;
+    }
+    u.env[0] = 0.0f; u.env[1] = p.smooth_sampling ? 1.0f : 0.0f; u.env[2] = L.anisotropy; u.env[3] = L.chromatic;
+    u.finish[0] = L.bloom; u.finish[1] = L.vignette; u.finish[2] = L.grain; u.finish[3] = L.auto_exposure ? 1.0f : 0.0f;
+    std::memcpy(u.tf_bucket_max, r->bucket, sizeof(r->bucket));
+    u.subsurface[0] = L.subsurface * L.subsurface_strength;
+    u.subsurface[1] = 10.0f / std::fmax(L.scattering_distance, 0.1f);
+    u.subsurface[2] = 0.7f;
+    u.subsurface[3] = 2.0f * r->max_spacing;
+    for (int i = 0; i < 256; i++) {
+        const float* c = lab.colors[i];
+        t.colors[i] = make_float4(c[0], c[1], c[2], (c[3] > 0.5f && lab.ghost[i]) ? 2.0f : c[3]);
+        const float* m = lab.materials[i];
+        t.materials[i] = make_float4(m[0], m[1], m[3], m[2] * L.subsurface_strength);
+        const float* d = lab.density[i];
+        t.density[i] = make_float4(d[0], d[1], d[2], d[3]);
+        const float* s = lab.surface[i];
+        t.surface[i] = make_float4(s[0], s[1] * L.surface_detail, s[2] * L.surface_detail, s[3]);
+        const float* o = lab.optics[i];
+        t.optics[i] = make_float4(o[0], o[1], o[2], o[3]);
+    }
+    float limit = 1.0f / (2.0f * r->max_spacing);
+    u.tissue[0] = tissue_majorant(lab, L.anisotropy, limit);
+    u.tissue[1] = limit;
+}
+
+static OpacityKey opacity_key(const vv_renderer* r, const vv_label_params& l) {
+    OpacityKey k;
+    std::memset(&k, 0, sizeof(k));
+    k.generation = r->generation;
+    k.mode = r->has_labels ? l.mode : VV_LABEL_OFF;
+    std::memcpy(&k.extinction_bits, &l.extinction, 4);
+    for (int i = 0; i < 256; i++) {
+        if (l.colors[i][3] > 0.5f) k.visible[i / 64] |= 1ull << (i % 64);
+        if (l.ghost[i]) k.ghost[i / 64] |= 1ull << (i % 64);
+    }
+    std::memcpy(&k.ghost_opacity_bits, &l.ghost_opacity, 4);
+    float m = std::round(l.cut_margin_mm / r->min_spacing);
+    k.margin = (int)std::fmin(std::fmax(m, 0.0f), 3.0f);
+    k.smoothing = std::min(l.smoothing, 8u);
+    return k;
+}
+
+// FrameParams equality except the denoiser (renderer.rs:1537-1544), with f32
+// comparisons as Rust's PartialEq makes them (-0 == 0, NaN != NaN).
+static bool feq(const float* a, const float* b, size_t n) {
+    for (size_t i = 0; i < n; i++)
+        if (!(a[i] == b[i])) return false;
+    return true;
+}
+static bool same_accumulation(const vv_frame_params& a, const vv_frame_params& b) {
+#define F(x) feq(&a.x, &b.x, 1)
+#define I(x) (a.x == b.x)
+    const vv_label_params &la = a.labels, &lb = b.labels;
+    const vv_lighting &A = a.lighting, &B = b.lighting;
+    bool cam = feq(a.camera.target, b.camera.target, 3) && F(camera.distance) && F(camera.yaw) && F(camera.pitch) &&
+               F(camera.fov_y);
+    bool labels = la.mode == lb.mode && la.tint == lb.tint && la.extinction == lb.extinction &&
+                  la.ghost_opacity == lb.ghost_opacity && la.cut_margin_mm == lb.cut_margin_mm &&
+                  la.smoothing == lb.smoothing && feq(&la.colors[0][0], &lb.colors[0][0], 1024) &&
+                  feq(&la.materials[0][0], &lb.materials[0][0], 1024) && !std::memcmp(la.ghost, lb.ghost, 256) &&
+                  feq(&la.density[0][0], &lb.density[0][0], 1024) && feq(&la.surface[0][0], &lb.surface[0][0], 1024) &&
+                  feq(&la.optics[0][0], &lb.optics[0][0], 1024);
+    bool light = A.azimuth == B.azimuth && A.elevation == B.elevation && A.intensity == B.intensity &&
+                 A.ambient == B.ambient && A.environment == B.environment && A.light_size == B.light_size &&
+                 A.env_rotation == B.env_rotation && A.anisotropy == B.anisotropy && A.chromatic == B.chromatic &&
+                 A.shadows == B.shadows && A.ambient_occlusion == B.ambient_occlusion && A.exposure == B.exposure &&
+                 A.auto_exposure == B.auto_exposure && A.bloom == B.bloom && A.vignette == B.vignette &&
+                 A.grain == B.grain && A.tone_mapper == B.tone_mapper && A.roughness == B.roughness &&
+                 A.metalness == B.metalness && A.subsurface == B.subsurface &&
+                 A.scattering_distance == B.scattering_distance && A.subsurface_strength == B.subsurface_strength &&
+                 A.surface_detail == B.surface_detail;
+    bool clip = I(clipping.all);
+    for (int i = 0; i < 3; i++)
+        clip = clip && I(clipping.planes[i].enabled) && I(clipping.planes[i].plane) &&
+               I(clipping.planes[i].cut_positive) && F(clipping.planes[i].position);
+    bool pt = I(path_tracing.enabled);
+    if (pt && a.path_tracing.enabled)
+        pt = I(path_tracing.bounces) && I(path_tracing.samples_per_frame) && F(path_tracing.aperture) &&
+             I(path_tracing.has_focus) && (!a.path_tracing.has_focus || feq(a.path_tracing.focus, b.path_tracing.focus, 3));
+    return cam && F(step_mm) && I(srgb_encode) && labels && light && I(preintegrate) && I(skip_empty_space) && clip &&
+           pt && I(smooth_sampling);
+#undef F
+#undef I
+}
+
+// ---------------------------------------------------------------- renderer
+static vv_status use_device(const vv_renderer* r) {
+    CK(cudaSetDevice(r->ctx->device));
+    return VV_OK;
+}
+
+static m3 w2i_m3(const vv_renderer* r) {
+    const float* m = r->w2i;
+    return {mk(m[0], m[1], m[2]), mk(m[4], m[5], m[6]), mk(m[8], m[9], m[10])};
+}
+
+extern "C" vv_status vv_renderer_create(vv_context* ctx, const vv_volume* volume, const vv_transfer_function* tf,
+                                        vv_renderer** out) {
+    if (!ctx || !volume || !tf || !out) return fail(VV_ERR_ARG, "null argument");
+    if (!volume->hu) return fail(VV_ERR_ARG, "volume has no voxels");
+    for (int i = 0; i < 3; i++)
+        if (volume->dims[i] == 0) return fail(VV_ERR_ARG, "volume has a zero dimension");
+    Vol v = make_vol((int)volume->dims[0], (int)volume->dims[1], (int)volume->dims[2]);
+    if ((double)v.bx * v.by * v.bz * 512.0 > 2147483647.0 || volume->dims[0] > 16384 || volume->dims[1] > 16384 ||
+        volume->dims[2] > 16384)
+        return fail(VV_ERR_LIMIT, "volume exceeds 2^31 bricked voxels or 16384 per axis");
+    CK(cudaSetDevice(ctx->device));
+    vv_renderer* r = new vv_renderer();
+    r->ctx = ctx;
+    r->vol = v;
+    set_geometry(r, volume);
+    r->tables_host = nullptr;
+    cudaError_t e = cudaMallocHost((void**)&r->tables_host, sizeof(LabelTables));
+    if (e != cudaSuccess) {
+        delete r;
+        return cuda_fail(e, "cudaMallocHost");
+    }
+    auto bail = [&](vv_status s) {
+        vv_renderer_destroy(r);
+        return s;
+    };
+    vv_status s = upload_tf(r, tf);
+    if (s != VV_OK) return bail(s);
+    long n = (long)volume->dims[0] * volume->dims[1] * volume->dims[2];
+    long elems = vol_elems(v);
+    DBuf hu;
+    if ((e = hu.alloc(n * sizeof(int16_t))) != cudaSuccess) return bail(cuda_fail(e, "cudaMalloc"));
+    if ((e = r->density.alloc(elems * sizeof(uint16_t))) != cudaSuccess ||
+        (e = r->normals.alloc(elems * sizeof(uint32_t))) != cudaSuccess ||
+        (e = r->majorant.alloc((size_t)v.bx * v.by * v.bz * sizeof(float))) != cudaSuccess ||
+        (e = r->tables.alloc(sizeof(LabelTables))) != cudaSuccess ||
+        (e = r->work.alloc(256)) != cudaSuccess || (e = r->exposure.alloc(sizeof(float))) != cudaSuccess) {
+        hu.release();
+        return bail(cuda_fail(e, "cudaMalloc"));
+    }
+    cudaStream_t st = ctx->stream;
+    e = cudaMemcpyAsync(hu.p, volume->hu, n * sizeof(int16_t), cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) e = launch_density(hu.as<int16_t>(), r->density.as<uint16_t>(), v, st);
+    if (e == cudaSuccess) e = launch_normals(r->density.as<uint16_t>(), r->normals.as<uint32_t>(), v, w2i_m3(r), st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(r->exposure.p, 0, sizeof(float), st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(r->work.p, 0, 256, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    hu.release();
+    if (e != cudaSuccess) return bail(cuda_fail(e, "volume upload"));
+    r->launches += 2;
+    *out = r;
+    return VV_OK;
+}
+
+extern "C" vv_status vv_renderer_destroy(vv_renderer* r) {
+    if (!r) return VV_OK;
+    cudaSetDevice(r->ctx->device);
+    cudaStreamSynchronize(r->ctx->stream);
+    DBuf* all[] = {&r->density, &r->normals, &r->mask_a, &r->mask_b, &r->labels, &r->majorant, &r->lut,
+                   &r->bucket_dev, &r->tables, &r->soft, &r->work, &r->exposure, &r->accum, &r->albedo,
+                   &r->normal, &r->ping, &r->pong, &r->hdr, &r->out, &r->bloom[0], &r->bloom[1], &r->bloom[2],
+                   &r->bloom[3]};
+    for (DBuf* b : all) b->release();
+    if (r->tables_host) cudaFreeHost(r->tables_host);
+    if (r->counters) cudaFree(r->counters);
+    delete r;
+    return VV_OK;
+}
+
+extern "C" vv_status vv_renderer_get_info(const vv_renderer* r, vv_renderer_info* out) {
+    if (!r || !out) return fail(VV_ERR_ARG, "null argument");
+    for (int i = 0; i < 3; i++) {
+        out->bounds_lo[i] = r->bounds_lo[i];
+        out->bounds_hi[i] = r->bounds_hi[i];
+        out->center[i] = r->center[i];
+    }
+    out->min_spacing = r->min_spacing;
+    out->diagonal = r->diagonal;
+    out->dims[0] = r->vol.nx; out->dims[1] = r->vol.ny; out->dims[2] = r->vol.nz;
+    return VV_OK;
+}
+
+extern "C" vv_status vv_default_camera(const vv_renderer* r, vv_orbit_camera* out) {
+    if (!r || !out) return fail(VV_ERR_ARG, "null argument");
+    vv_orbit_camera_framing(r->center, r->diagonal, out);
+    return VV_OK;
+}
+
+extern "C" vv_status vv_set_transfer_function(vv_renderer* r, const vv_transfer_function* tf) {
+    if (!r) return fail(VV_ERR_ARG, "null renderer");
+    vv_status s = use_device(r);
+    if (s != VV_OK) return s;
+    CK(cudaStreamSynchronize(r->ctx->stream));
+    s = upload_tf(r, tf);
+    if (s != VV_OK) return s;
+    r->generation++;
+    return VV_OK;
+}
+
+extern "C" vv_status vv_set_labels(vv_renderer* r, const uint8_t* labels, size_t n, const vv_soft_label_grid* soft) {
+    if (!r || !labels) return fail(VV_ERR_ARG, "null argument");
+    size_t voxels = (size_t)r->vol.nx * r->vol.ny * r->vol.nz;
+    if (n != voxels)
+        return fail(VV_ERR_ARG, "label volume has " + std::to_string(n) + " voxels, expected " + std::to_string(voxels));
+    if (soft) {
+        if (!soft->data) return fail(VV_ERR_ARG, "soft label grid has no data");
+        for (int a = 0; a < 3; a++) {
+            if (soft->dims[a] == 0) return fail(VV_ERR_ARG, "soft label grid has a zero dimension");
+            if (soft->src_axis[a] > 2) return fail(VV_ERR_ARG, "soft label grid axis out of range");
+        }
+    }
+    vv_status s = use_device(r);
+    if (s != VV_OK) return s;
+    cudaStream_t st = r->ctx->stream;
+    CK(cudaStreamSynchronize(st));
+    long elems = vol_elems(r->vol);
+    CK(r->labels.alloc(elems));
+    CK(r->mask_a.alloc(elems * sizeof(uint32_t)));
+    CK(r->mask_b.alloc(elems * sizeof(uint32_t)));
+    DBuf lin;
+    CK(lin.alloc(voxels));
+    cudaError_t e = cudaMemcpyAsync(lin.p, labels, voxels, cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) e = launch_brick_u8(lin.as<uint8_t>(), r->labels.as<uint8_t>(), r->vol, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    lin.release();
+    if (e != cudaSuccess) return cuda_fail(e, "label upload");
+    r->launches += 1;
+    if (soft) {
+        size_t nodes = (size_t)soft->dims[0] * soft->dims[1] * soft->dims[2];
+        CK(r->soft.alloc(nodes * 4));
+        CK(cudaMemcpyAsync(r->soft.p, soft->data, nodes * 4, cudaMemcpyHostToDevice, st));
+        CK(cudaStreamSynchronize(st));
+        for (int a = 0; a < 3; a++) r->soft_dims[a] = (int)soft->dims[a];
+        int flips = 0;
+        for (int a = 0; a < 3; a++) flips |= (soft->flip[a] ? 1 : 0) << a;
+        r->soft_push[0] = (int)soft->src_axis[0];
+        r->soft_push[1] = (int)soft->src_axis[1];
+        r->soft_push[2] = (int)soft->src_axis[2];
+        r->soft_push[3] = flips | 8;
+    } else {
+        r->soft.release();
+        r->soft_dims[0] = r->soft_dims[1] = r->soft_dims[2] = 1;
+        r->soft_push[0] = r->soft_push[1] = r->soft_push[2] = r->soft_push[3] = 0;
+    }
+    r->has_labels = true;
+    r->generation++;
+    return VV_OK;
+}
+
+extern "C" vv_status vv_set_environment_map(vv_renderer* r, const vv_environment_map* map) {
+    if (!r) return fail(VV_ERR_ARG, "null renderer");
+    if (map) return fail(VV_ERR_LIMIT, "light maps are not supported by this build; the studio environment is used");
+    r->have_params = false;
+    return VV_OK;
+}
+
+extern "C" vv_status vv_resize(vv_renderer* r, uint32_t width, uint32_t height) {
+    if (!r) return fail(VV_ERR_ARG, "null renderer");
+    if (width == 0 || height == 0 || width > 16384 || height > 16384)
+        return fail(VV_ERR_ARG, "image size must be 1..16384 per axis");
+    vv_status s = use_device(r);
+    if (s != VV_OK) return s;
+    CK(cudaStreamSynchronize(r->ctx->stream));
+    size_t px = (size_t)width * height;
+    CK(r->accum.alloc(px * 16));
+    CK(r->albedo.alloc(px * 16));
+    CK(r->normal.alloc(px * 16));
+    CK(r->ping.alloc(px * 16));
+    CK(r->pong.alloc(px * 16));
+    CK(r->hdr.alloc(px * 8));
+    CK(r->out.alloc(px * 4));
+    uint32_t qw = (width + 3) / 4, qh = (height + 3) / 4;
+    uint32_t ew = (qw + 1) / 2, eh = (qh + 1) / 2;
+    uint32_t ws[4] = {qw, qw, ew, ew}, hs[4] = {qh, qh, eh, eh};
+    for (int i = 0; i < 4; i++) {
+        CK(r->bloom[i].alloc((size_t)ws[i] * hs[i] * 8));
+        r->bw[i] = (int)ws[i];
+        r->bh[i] = (int)hs[i];
+    }
+    r->width = width;
+    r->height = height;
+    r->have_params = false;
+    return VV_OK;
+}
+
+extern "C" uint32_t vv_accumulated_samples(const vv_renderer* r) { return r ? r->accumulated : 0; }
+extern "C" uint64_t vv_kernel_launches(const vv_renderer* r) { return r ? r->launches : 0; }
+
+extern "C" vv_status vv_synchronize(vv_renderer* r) {
+    if (!r) return fail(VV_ERR_ARG, "null renderer");
+    vv_status s = use_device(r);
+    if (s != VV_OK) return s;
+    CK(cudaStreamSynchronize(r->ctx->stream));
+    int32_t status = 0;
+    CK(cudaMemcpy(&status, r->work.as<uint8_t>() + 4, 4, cudaMemcpyDeviceToHost));
+    if (status != 0) return fail(VV_ERR_TIMEOUT, "a device-side bounded wait ran out");
+    return VV_OK;
+}
+
+// The accumulated count `record` would use for `p` (0 after a reset).
+static uint32_t accumulated_for(const vv_renderer* r, const vv_frame_params& p) {
+    if (!r->have_params || !same_accumulation(r->accumulated_params, p)) return 0;
+    return r->accumulated;
+}
+
+static PtArgs pt_args(vv_renderer* r, const UHead& u) {
+    PtArgs a;
+    std::memset(&a, 0, sizeof(a));
+    a.u = u;
+    a.density = r->density.as<uint16_t>();
+    a.mask = r->mask_a.as<uint32_t>();
+    a.normals = r->normals.as<uint32_t>();
+    a.labels = r->labels.as<uint8_t>();
+    a.majorant = r->majorant.as<float>();
+    a.lut = r->lut.as<float4>();
+    a.tab = r->tables.as<LabelTables>();
+    a.vol = r->vol;
+    a.accum = r->accum.as<float4>();
+    a.albedo = r->albedo.as<float4>();
+    a.normal = r->normal.as<float4>();
+    a.hdr = r->hdr.as<ushort4>();
+    a.width = r->width;
+    a.height = r->height;
+    a.frames = 1;
+    a.tiles_x = (r->width + 7) / 8;
+    a.tiles_y = (r->height + 3) / 4;
+    a.counter = r->work.as<uint32_t>();
+    a.status = r->work.as<int32_t>() + 1;
+    a.counters = r->counters;
+    const char* k = std::getenv("VV_PT_KERNEL");
+    a.persistent = !(k && std::strcmp(k, "frame") == 0);
+    return a;
+}
+
+static PostArgs post_args(vv_renderer* r, const UHead& u) {
+    PostArgs a;
+    std::memset(&a, 0, sizeof(a));
+    a.u = u;
+    a.width = r->width;
+    a.height = r->height;
+    a.accum = r->accum.as<float4>();
+    a.albedo = r->albedo.as<float4>();
+    a.normal = r->normal.as<float4>();
+    a.ping = r->ping.as<float4>();
+    a.pong = r->pong.as<float4>();
+    a.hdr = r->hdr.as<ushort4>();
+    for (int i = 0; i < 4; i++) {
+        a.bloom[i] = r->bloom[i].as<ushort4>();
+        a.bw[i] = r->bw[i];
+        a.bh[i] = r->bh[i];
+    }
+    a.exposure = r->exposure.as<float>();
+    a.out = r->out.as<uchar4>();
+    return a;
+}
+
+// Uniform upload, masks and majorants when their inputs changed
+// (renderer.rs:1554-1706); returns the packed head.
+static vv_status prepare_frame(vv_renderer* r, const vv_frame_params& p, uint64_t frame, UHead& u) {
+    if (!r->accum.p) return fail(VV_ERR_STATE, "resize() must be called before record()");
+    if (!p.path_tracing.enabled)
+        return fail(VV_ERR_ARG, "only path tracing is supported (path_tracing.enabled = 0 selects the ray marcher)");
+    if (p.labels.mode < 0 || p.labels.mode > 3) return fail(VV_ERR_ARG, "label mode out of range");
+    vv_status s = use_device(r);
+    if (s != VV_OK) return s;
+    cudaStream_t st = r->ctx->stream;
+    if (!r->have_params || !same_accumulation(r->accumulated_params, p)) {
+        r->accumulated = 0;
+        r->accumulated_params = p;
+        r->have_params = true;
+    }
+    LabelTables* t = new LabelTables();
+    pack(r, p, r->accumulated, frame, u, *t);
+    // The tables go to the device through pinned staging, only when they
+    // changed; the previous copy must have finished before the staging buffer
+    // is overwritten.
+    if (!r->tables_valid || std::memcmp(t, r->tables_host, sizeof(LabelTables)) != 0) {
+        cudaError_t e = cudaStreamSynchronize(st);
+        if (e == cudaSuccess) {
+            std::memcpy(r->tables_host, t, sizeof(LabelTables));
+            e = cudaMemcpyAsync(r->tables.p, r->tables_host, sizeof(LabelTables), cudaMemcpyHostToDevice, st);
+        }
+        if (e != cudaSuccess) {
+            delete t;
+            return cuda_fail(e, "label table upload");
+        }
+        r->tables_valid = true;
+    }
+    delete t;
+    OpacityKey key = opacity_key(r, p.labels);
+    if (key.mode != VV_LABEL_OFF && !(r->have_mask_key && r->mask_key == key)) {
+        MaskLaunch L;
+        L.v = r->vol;
+        L.density = r->density.as<uint16_t>();
+        L.labels = r->labels.as<uint8_t>();
+        static const uint8_t* none = nullptr;
+        L.soft = r->soft.p ? r->soft.as<uint8_t>() : none;
+        for (int a = 0; a < 3; a++) L.soft_dims[a] = r->soft_dims[a];
+        for (int a = 0; a < 4; a++) L.soft_push[a] = r->soft.p ? r->soft_push[a] : 0;
+        L.margin = key.margin;
+        L.radius = (int)key.smoothing;
+        L.mode = key.mode;
+        L.colors = r->tables.as<LabelTables>()->colors;
+        L.scratch = r->mask_b.as<uint32_t>();
+        L.out = r->mask_a.as<uint32_t>();
+        CK(launch_masks(L, st));
+        r->launches += 4;
+        r->mask_key = key;
+        r->have_mask_key = true;
+    }
+    if (!(r->have_majorant_key && r->majorant_key == key)) {
+        CK(launch_majorant(r->density.as<uint16_t>(), r->mask_a.as<uint32_t>(), r->vol, key.mode, p.labels.extinction,
+                           r->bucket_dev.as<float>(), r->majorant.as<float>(), st));
+        r->launches += 1;
+        r->majorant_key = key;
+        r->have_majorant_key = true;
+    }
+    if (r->accumulated == 0) {
+        size_t bytes = (size_t)r->width * r->height * 16;
+        CK(cudaMemsetAsync(r->accum.p, 0, bytes, st));
+        CK(cudaMemsetAsync(r->albedo.p, 0, bytes, st));
+        CK(cudaMemsetAsync(r->normal.p, 0, bytes, st));
+    }
+    return VV_OK;
+}
+
+// Denoiser and display passes after the frame(s) (renderer.rs:1793-1803).
+static vv_status finish_frame(vv_renderer* r, const vv_frame_params& p, const UHead& u) {
+    cudaStream_t st = r->ctx->stream;
+    int launches = 0;
+    PostArgs pa = post_args(r, u);
+    if (p.path_tracing.denoiser == VV_DENOISE_ATROUS) CK(launch_denoise(pa, st, &launches));
+    r->accumulated += std::max(p.path_tracing.samples_per_frame, 1u);
+    if (p.path_tracing.denoiser != VV_DENOISE_OIDN) CK(launch_post(pa, st, &launches));
+    r->launches += launches;
+    return VV_OK;
+}
+
+extern "C" vv_status vv_record(vv_renderer* r, uint64_t frame, const vv_frame_params* params) {
+    if (!r || !params) return fail(VV_ERR_ARG, "null argument");
+    UHead u;
+    vv_status s = prepare_frame(r, *params, frame, u);
+    if (s != VV_OK) return s;
+    PtArgs a = pt_args(r, u);
+    int launches = 0;
+    pt_timer_start(r);
+    CK(launch_pt(a, r->ctx->sms, r->ctx->stream, &launches));
+    pt_timer_stop(r);
+    r->launches += launches;
+    return finish_frame(r, *params, u);
+}
+
+extern "C" vv_status vv_record_frames(vv_renderer* r, uint64_t first_frame, uint32_t frames,
+                                      const vv_frame_params* params) {
+    if (!r || !params) return fail(VV_ERR_ARG, "null argument");
+    if (frames == 0) return VV_OK;
+    UHead u;
+    vv_status s = prepare_frame(r, *params, first_frame + frames - 1, u);
+    if (s != VV_OK) return s;
+    uint32_t spf = std::max(params->path_tracing.samples_per_frame, 1u);
+    PtArgs a = pt_args(r, u);
+    a.frames = frames;
+    a.persistent = 1;
+    int launches = 0;
+    pt_timer_start(r);
+    CK(launch_pt(a, r->ctx->sms, r->ctx->stream, &launches));
+    pt_timer_stop(r);
+    // The last frame's view of the counts: accumulated before it, spf after.
+    r->accumulated += (frames - 1) * spf;
+    u.path[0] = r->accumulated;
+    PostArgs pa = post_args(r, u);
+    if (frames > 1) {
+        CK(launch_hdr_resolve(pa, (float)(r->accumulated + spf), r->ctx->stream));
+        launches += 1;
+    }
+    r->launches += launches;
+    return finish_frame(r, *params, u);
+}
+
+static vv_status read_dev(vv_renderer* r, void* dst, const DBuf& src, size_t bytes, size_t capacity) {
+    if (!r || !dst) return fail(VV_ERR_ARG, "null argument");
+    if (!src.p) return fail(VV_ERR_STATE, "resize() must be called first");
+    if (capacity < bytes) return fail(VV_ERR_ARG, "output buffer too small");
+    vv_status s = use_device(r);
+    if (s != VV_OK) return s;
+    CK(cudaMemcpyAsync(dst, src.p, bytes, cudaMemcpyDeviceToHost, r->ctx->stream));
+    CK(cudaStreamSynchronize(r->ctx->stream));
+    return VV_OK;
+}
+
+extern "C" vv_status vv_read_output(vv_renderer* r, uint8_t* rgba, size_t capacity) {
+    if (!r) return fail(VV_ERR_ARG, "null renderer");
+    return read_dev(r, rgba, r->out, (size_t)r->width * r->height * 4, capacity);
+}
+
+extern "C" vv_status vv_read_hdr(vv_renderer* r, uint16_t* rgba, size_t capacity) {
+    if (!r) return fail(VV_ERR_ARG, "null renderer");
+    return read_dev(r, rgba, r->hdr, (size_t)r->width * r->height * 8, capacity * 2);
+}
+
+extern "C" vv_status vv_read_accumulation(vv_renderer* r, float* accum, float* albedo, float* normal,
+                                          size_t capacity_floats) {
+    if (!r) return fail(VV_ERR_ARG, "null renderer");
+    size_t bytes = (size_t)r->width * r->height * 16;
+    vv_status s;
+    if (accum && (s = read_dev(r, accum, r->accum, bytes, capacity_floats * 4)) != VV_OK) return s;
+    if (albedo && (s = read_dev(r, albedo, r->albedo, bytes, capacity_floats * 4)) != VV_OK) return s;
+    if (normal && (s = read_dev(r, normal, r->normal, bytes, capacity_floats * 4)) != VV_OK) return s;
+    return VV_OK;
+}
+
+extern "C" vv_status vv_render_to_rgba(vv_renderer* r, const vv_frame_params* params, uint32_t width,
+                                       uint32_t height, uint32_t frames, uint8_t* out, size_t capacity) {
+    if (!r || !params || !out) return fail(VV_ERR_ARG, "null argument");
+    if (capacity < (size_t)width * height * 4) return fail(VV_ERR_ARG, "output buffer too small");
+    vv_status s = vv_resize(r, width, height);
+    if (s != VV_OK) return s;
+    // offscreen.rs:30-51: with OIDN requested but unavailable, `frames` frames are
+    // traced without display and one more with the a-trous filter.
+    bool oidn = params->path_tracing.denoiser == VV_DENOISE_OIDN;
+    uint32_t last = oidn ? frames + 1 : frames;
+    for (uint32_t f = 1; f < last; f++)
+        if ((s = vv_record(r, f, params)) != VV_OK) return s;
+    vv_frame_params p = *params;
+    if (oidn) p.path_tracing.denoiser = VV_DENOISE_ATROUS;
+    if ((s = vv_record(r, frames, &p)) != VV_OK) return s;
+    return vv_read_output(r, out, capacity);
+}
+
+extern "C" vv_status vv_pack_uniforms(vv_renderer* r, const vv_frame_params* params, uint64_t frame, void* out,
+                                      size_t capacity) {
+    if (!r || !params || !out) return fail(VV_ERR_ARG, "null argument");
+    if (capacity < VV_UNIFORMS_BYTES) return fail(VV_ERR_ARG, "output buffer too small");
+    if (!r->width) return fail(VV_ERR_STATE, "resize() must be called first");
+    UHead u;
+    LabelTables* t = new LabelTables();
+    pack(r, *params, accumulated_for(r, *params), frame, u, *t);
+    std::memcpy(out, &u, sizeof(u));
+    std::memcpy((uint8_t*)out + sizeof(u), t, sizeof(*t));
+    delete t;
+    return VV_OK;
+}
+
+extern "C" vv_status vv_read_volume(vv_renderer* r, int which, void* out, size_t capacity) {
+    if (!r || !out) return fail(VV_ERR_ARG, "null argument");
+    vv_status s = use_device(r);
+    if (s != VV_OK) return s;
+    cudaStream_t st = r->ctx->stream;
+    size_t voxels = (size_t)r->vol.nx * r->vol.ny * r->vol.nz;
+    if (which == VV_VOLUME_MAJORANT) {
+        size_t bytes = (size_t)r->vol.bx * r->vol.by * r->vol.bz * 4;
+        if (capacity < bytes) return fail(VV_ERR_ARG, "output buffer too small");
+        CK(cudaMemcpyAsync(out, r->majorant.p, bytes, cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+        return VV_OK;
+    }
+    const DBuf* src = nullptr;
+    int elem = 0;
+    switch (which) {
+        case VV_VOLUME_DENSITY: src = &r->density; elem = 2; break;
+        case VV_VOLUME_NORMALS: src = &r->normals; elem = 4; break;
+        case VV_VOLUME_MASK: src = &r->mask_a; elem = 4; break;
+        case VV_VOLUME_LABELS: src = &r->labels; elem = 1; break;
+        default: return fail(VV_ERR_ARG, "unknown volume");
+    }
+    if (!src->p) return fail(VV_ERR_STATE, "that volume has not been computed");
+    if (capacity < voxels * elem) return fail(VV_ERR_ARG, "output buffer too small");
+    DBuf tmp;
+    CK(tmp.alloc(voxels * elem));
+    cudaError_t e = launch_unbrick(src->p, tmp.p, r->vol, elem, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(out, tmp.p, voxels * elem, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    tmp.release();
+    if (e != cudaSuccess) return cuda_fail(e, "volume readback");
+    return VV_OK;
+}
+
+// ------------------------------------------------------------ event counts
+// Counts the path tracer's memory events (COUNT_* in vv_kernels.h) over the
+// next records until vv_count_events(r, 0, out) returns the totals.
+extern "C" vv_status vv_count_events(vv_renderer* r, int enable, uint64_t* out, size_t n) {
+    if (!r) return fail(VV_ERR_ARG, "null renderer");
+    vv_status s = use_device(r);
+    if (s != VV_OK) return s;
+    if (enable) {
+        if (!r->counters) CK(cudaMalloc((void**)&r->counters, COUNT_N * sizeof(unsigned long long)));
+        CK(cudaMemsetAsync(r->counters, 0, COUNT_N * sizeof(unsigned long long), r->ctx->stream));
+        return VV_OK;
+    }
+    if (!r->counters) return fail(VV_ERR_STATE, "counting was not enabled");
+    unsigned long long c[COUNT_N];
+    CK(cudaStreamSynchronize(r->ctx->stream));
+    CK(cudaMemcpy(c, r->counters, sizeof(c), cudaMemcpyDeviceToHost));
+    cudaFree(r->counters);
+    r->counters = nullptr;
+    for (size_t i = 0; i < n && i < (size_t)COUNT_N; i++) out[i] = c[i];
+    return VV_OK;
+}
+
+// Device time of the path-tracing launches: enable = 1 starts recording CUDA
+// events around each launch on the renderer's stream; enable = 0 stops, waits,
+// and returns the summed milliseconds and the number of launches.
+extern "C" vv_status vv_time_pt(vv_renderer* r, int enable, double* ms, uint64_t* launches) {
+    if (!r) return fail(VV_ERR_ARG, "null renderer");
+    vv_status s = use_device(r);
+    if (s != VV_OK) return s;
+    if (enable) {
+        r->timing = true;
+        return VV_OK;
+    }
+    r->timing = false;
+    CK(cudaStreamSynchronize(r->ctx->stream));
+    double total = 0.0;
+    for (auto& ev : r->pt_events) {
+        float t = 0.0f;
+        cudaError_t e = cudaEventElapsedTime(&t, ev.first, ev.second);
+        if (e == cudaSuccess) total += t;
+        cudaEventDestroy(ev.first);
+        cudaEventDestroy(ev.second);
+    }
+    if (ms) *ms = total;
+    if (launches) *launches = r->pt_events.size();
+    r->pt_events.clear();
+    return VV_OK;
+}
+
+// ---------------------------------------------------------- parity probes
+// Not part of the reference's interface: entry points the parity tests use to
+// run single device functions on the renderer's current state.
+extern "C" vv_status vv_probe_bspline(vv_renderer* r, const vv_frame_params* params, const float* idx, size_t n,
+                                      float* out) {
+    if (!r || !params || !idx || !out) return fail(VV_ERR_ARG, "null argument");
+    UHead u;
+    vv_status s = prepare_frame(r, *params, 1, u);
+    if (s != VV_OK) return s;
+    DBuf di, dout;
+    CK(di.alloc(n * 12));
+    CK(dout.alloc(n * 16));
+    cudaStream_t st = r->ctx->stream;
+    PtArgs a = pt_args(r, u);
+    cudaError_t e = cudaMemcpyAsync(di.p, idx, n * 12, cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) e = launch_bspline_probe(a, di.as<float>(), dout.as<float>(), (int)n, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(out, dout.p, n * 16, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    di.release();
+    dout.release();
+    if (e != cudaSuccess) return cuda_fail(e, "bspline probe");
+    return VV_OK;
+}
+
+extern "C" vv_status vv_probe_paths(vv_renderer* r, const vv_frame_params* params, uint32_t accumulated,
+                                    const int* pixels, size_t n, float* out) {
+    if (!r || !params || !pixels || !out) return fail(VV_ERR_ARG, "null argument");
+    UHead u;
+    vv_status s = prepare_frame(r, *params, 1, u);
+    if (s != VV_OK) return s;
+    u.path[0] = accumulated;
+    DBuf dp, dout;
+    CK(dp.alloc(n * 8));
+    CK(dout.alloc(n * 48));
+    cudaStream_t st = r->ctx->stream;
+    PtArgs a = pt_args(r, u);
+    cudaError_t e = cudaMemcpyAsync(dp.p, pixels, n * 8, cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) e = launch_pt_pixels(a, dp.as<int>(), dout.as<float>(), (int)n, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(out, dout.p, n * 48, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    dp.release();
+    dout.release();
+    if (e != cudaSuccess) return cuda_fail(e, "path probe");
+    return VV_OK;
+}

@@ -1,0 +1,100 @@
+// vv_kernels.h — launch interface between the host renderer and the kernels.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "vv_device.cuh"
+
+namespace vv {
+
+struct MaskLaunch {
+    Vol v;
+    const uint16_t* density;
+    const uint8_t* labels;
+    const uint8_t* soft;
+    int soft_dims[3];
+    int soft_push[4];
+    int margin;
+    int radius;
+    int mode;
+    const float4* colors;
+    uint32_t* scratch;  // mask B
+    uint32_t* out;      // mask A (what rendering samples)
+};
+
+// Everything one path-tracing launch reads and writes.
+struct PtArgs {
+    UHead u;
+    const uint16_t* density;
+    const uint32_t* mask;
+    const uint32_t* normals;
+    const uint8_t* labels;
+    const float* majorant;
+    const float4* lut;          // transfer function, RGBA16F values as float
+    const LabelTables* tab;
+    Vol vol;
+    float4* accum;
+    float4* albedo;
+    float4* normal;
+    ushort4* hdr;
+    uint32_t width, height;
+    uint32_t frames;            // accumulate-frames in this launch
+    uint32_t tiles_x, tiles_y;  // 8x4-pixel tiles
+    uint32_t* counter;          // work-item counter, zero at launch
+    int32_t* status;            // device status word (0 ok)
+    int persistent;             // 1: persistent warps with path regeneration
+    unsigned long long* counters;  // event counters (COUNT_*), or null
+};
+
+// Event counters of a counting launch (for the algorithmic-byte model).
+enum {
+    COUNT_MAJORANT = 0,   // brick-majorant lookups (free flight and shadow rays), 4 B
+    COUNT_CUBIC = 1,      // cubic B-spline densities, 4^3 x 2 B
+    COUNT_TRILINEAR = 2,  // trilinear densities, 2^3 x 2 B
+    COUNT_MASK = 3,       // trilinear mask lookups, 2^3 x 4 B
+    COUNT_LABEL = 4,      // label fetches, 1 B
+    COUNT_NORMAL = 5,     // trilinear normal lookups, 2^3 x 4 B
+    COUNT_GRADIENT = 6,   // cubic B-spline gradients, 4^3 x 2 B
+    COUNT_PIXEL = 7,      // pixel accumulations, 3 x (16 B read + 16 B write) + 8 B
+    COUNT_PATH = 8,       // paths started
+    COUNT_VERTEX = 9,     // path vertices (bounce-loop iterations)
+    COUNT_N = 10
+};
+
+cudaError_t launch_density(const int16_t* hu, uint16_t* out, const Vol& v, cudaStream_t s);
+cudaError_t launch_normals(const uint16_t* d, uint32_t* out, const Vol& v, const m3& w2i, cudaStream_t s);
+cudaError_t launch_masks(const MaskLaunch& L, cudaStream_t s);
+cudaError_t launch_majorant(const uint16_t* d, const uint32_t* mask, const Vol& v, int mode, float label_ext,
+                            const float* bucket, float* out, cudaStream_t s);
+cudaError_t launch_unbrick(const void* src, void* dst, const Vol& v, int elem, cudaStream_t s);
+cudaError_t launch_brick_u8(const uint8_t* src, uint8_t* dst, const Vol& v, cudaStream_t s);
+
+// One or more accumulate-frames (pt.comp). Returns the number of kernel launches.
+cudaError_t launch_pt(const PtArgs& a, int sms, cudaStream_t s, int* launches);
+// B-spline density and gradient at n continuous indices (parity probe).
+cudaError_t launch_bspline_probe(const PtArgs& a, const float* idx, float* out, int n, cudaStream_t s);
+// One path per listed pixel at accumulation count a.u.path[0] (parity probe): 12 floats each.
+cudaError_t launch_pt_pixels(const PtArgs& a, const int* px, float* out, int n, cudaStream_t s);
+
+struct PostArgs {
+    UHead u;
+    uint32_t width, height;
+    const float4* accum;
+    const float4* albedo;
+    const float4* normal;
+    float4* ping;
+    float4* pong;
+    ushort4* hdr;
+    ushort4* bloom[4];   // A, B (quarter), C, D (eighth)
+    int bw[4], bh[4];
+    float* exposure;     // 1 texel, adapted across frames
+    uchar4* out;
+};
+// record_denoise (renderer.rs:1868-1904): 7 passes.
+cudaError_t launch_denoise(const PostArgs& a, cudaStream_t s, int* launches);
+// record_post (renderer.rs:1817-1866): bloom, exposure, tone mapping.
+cudaError_t launch_post(const PostArgs& a, cudaStream_t s, int* launches);
+// hdr = accum / n (the HDR store at the end of pt.comp) for batched frames.
+cudaError_t launch_hdr_resolve(const PostArgs& a, float n, cudaStream_t s);
+
+}  // namespace vv

@@ -1,0 +1,238 @@
+"""Python mirror of volview's `render` crate API over libvolpt.so (include/volpt.h).
+
+`Context`, `Renderer` and `render_to_rgba` follow crates/render/src/lib.rs:14-23:
+Renderer(ctx, volume, tf) ~ Renderer::new (renderer.rs:555), set_transfer_function
+(:1226), set_labels (:1241), set_environment_map (:1283), resize (:1313), record
+(:1499), accumulated_samples (:1217), destroy (:2072), render_to_rgba
+(offscreen.rs:11). Errors raise VolptError where the Rust returns Err; `record`
+raises where the Rust panics (record before resize).
+
+There is no CPU fallback: importing works anywhere, but every call needs the CUDA
+library and a device, and fails loudly without them.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import abi
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libvolpt.so")
+P = C.c_void_p
+
+# Every entry point include/volpt.h declares: (name, restype, argtypes).
+EXPORTS = [
+    ("vv_last_error", C.c_char_p, []),
+    ("vv_lighting_default", None, [P]),
+    ("vv_label_params_default", None, [P]),
+    ("vv_path_tracing_default", None, [P]),
+    ("vv_clipping_default", None, [P]),
+    ("vv_orbit_camera_framing", None, [P, C.c_float, P]),
+    ("vv_context_create", C.c_int, [C.c_int, P]),
+    ("vv_context_create_on_stream", C.c_int, [C.c_int, P, P]),
+    ("vv_context_destroy", C.c_int, [P]),
+    ("vv_renderer_create", C.c_int, [P, P, P, P]),
+    ("vv_renderer_destroy", C.c_int, [P]),
+    ("vv_renderer_get_info", C.c_int, [P, P]),
+    ("vv_default_camera", C.c_int, [P, P]),
+    ("vv_set_transfer_function", C.c_int, [P, P]),
+    ("vv_set_labels", C.c_int, [P, P, C.c_size_t, P]),
+    ("vv_set_environment_map", C.c_int, [P, P]),
+    ("vv_resize", C.c_int, [P, C.c_uint32, C.c_uint32]),
+    ("vv_record", C.c_int, [P, C.c_uint64, P]),
+    ("vv_record_frames", C.c_int, [P, C.c_uint64, C.c_uint32, P]),
+    ("vv_accumulated_samples", C.c_uint32, [P]),
+    ("vv_synchronize", C.c_int, [P]),
+    ("vv_read_output", C.c_int, [P, P, C.c_size_t]),
+    ("vv_read_hdr", C.c_int, [P, P, C.c_size_t]),
+    ("vv_read_accumulation", C.c_int, [P, P, P, P, C.c_size_t]),
+    ("vv_render_to_rgba", C.c_int, [P, P, C.c_uint32, C.c_uint32, C.c_uint32, P, C.c_size_t]),
+    ("vv_pack_uniforms", C.c_int, [P, P, C.c_uint64, P, C.c_size_t]),
+    ("vv_read_volume", C.c_int, [P, C.c_int, P, C.c_size_t]),
+    ("vv_kernel_launches", C.c_uint64, [P]),
+]
+# Test hooks (include/volpt_probe.h).
+PROBES = [
+    ("vv_probe_bspline", C.c_int, [P, P, P, C.c_size_t, P]),
+    ("vv_probe_paths", C.c_int, [P, P, C.c_uint32, P, C.c_size_t, P]),
+    ("vv_count_events", C.c_int, [P, C.c_int, P, C.c_size_t]),
+    ("vv_time_pt", C.c_int, [P, C.c_int, P, P]),
+]
+
+COUNT_NAMES = ["majorant", "cubic", "trilinear", "mask", "label", "normal", "gradient", "pixel", "path", "vertex"]
+# Unique element bytes each event must read (and write, for pixels).
+COUNT_BYTES = [4, 128, 16, 32, 1, 32, 128, 104, 0, 0]
+
+_lib = None
+
+
+class VolptError(RuntimeError):
+    def __init__(self, status, message):
+        super().__init__(f"volpt status {status}: {message}")
+        self.status = status
+
+
+def load():
+    """Loads libvolpt.so (building it first if the sources are newer)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            from . import build
+            build.build()
+        lib = C.CDLL(LIB_PATH)
+        for name, res, args in EXPORTS + PROBES:
+            fn = getattr(lib, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = lib
+    return _lib
+
+
+def check(status):
+    if status != abi.VV_OK:
+        raise VolptError(status, load().vv_last_error().decode())
+
+
+def _ref(x):
+    return C.byref(x) if x is not None else None
+
+
+def _ptr(a):
+    return C.c_void_p(a.ctypes.data)
+
+
+class Context:
+    """CUDA device + stream (replaces the Vulkan Context, context.rs:37)."""
+
+    def __init__(self, device=0, stream=None):
+        self.handle = C.c_void_p()
+        if stream is None:
+            check(load().vv_context_create(device, C.byref(self.handle)))
+        else:
+            check(load().vv_context_create_on_stream(device, C.c_void_p(stream), C.byref(self.handle)))
+
+    def destroy(self):
+        if self.handle:
+            load().vv_context_destroy(self.handle)
+            self.handle = C.c_void_p()
+
+
+class Renderer:
+    def __init__(self, ctx, volume, tf):
+        self.ctx = ctx
+        self.handle = C.c_void_p()
+        check(load().vv_renderer_create(ctx.handle, C.byref(volume), C.byref(tf), C.byref(self.handle)))
+        info = abi.RendererInfo()
+        check(load().vv_renderer_get_info(self.handle, C.byref(info)))
+        self.info = info
+        self.bounds = (tuple(info.bounds_lo), tuple(info.bounds_hi))
+        self.min_spacing = info.min_spacing
+        self.center = tuple(info.center)
+        self.diagonal = info.diagonal
+        self.dims = tuple(info.dims)
+        self.width = self.height = 0
+
+    def default_camera(self):
+        cam = abi.OrbitCamera()
+        check(load().vv_default_camera(self.handle, C.byref(cam)))
+        return cam
+
+    def set_transfer_function(self, tf):
+        check(load().vv_set_transfer_function(self.handle, C.byref(tf)))
+
+    def set_labels(self, labels, soft=None):
+        labels = np.ascontiguousarray(labels, np.uint8)
+        check(load().vv_set_labels(self.handle, _ptr(labels), labels.size, _ref(soft)))
+
+    def set_environment_map(self, env):
+        check(load().vv_set_environment_map(self.handle, _ref(env)))
+
+    def resize(self, width, height):
+        check(load().vv_resize(self.handle, width, height))
+        self.width, self.height = width, height
+
+    def record(self, frame, params):
+        check(load().vv_record(self.handle, frame, C.byref(params)))
+
+    def record_frames(self, first_frame, frames, params):
+        check(load().vv_record_frames(self.handle, first_frame, frames, C.byref(params)))
+
+    def accumulated_samples(self):
+        return load().vv_accumulated_samples(self.handle)
+
+    def synchronize(self):
+        check(load().vv_synchronize(self.handle))
+
+    def read_output(self, out=None):
+        out = np.empty((self.height, self.width, 4), np.uint8) if out is None else out
+        check(load().vv_read_output(self.handle, _ptr(out), out.nbytes))
+        return out
+
+    def read_hdr(self):
+        out = np.empty((self.height, self.width, 4), np.uint16)
+        check(load().vv_read_hdr(self.handle, _ptr(out), out.size))
+        return out
+
+    def read_accumulation(self):
+        shape = (self.height, self.width, 4)
+        a, b, c = (np.empty(shape, np.float32) for _ in range(3))
+        check(load().vv_read_accumulation(self.handle, _ptr(a), _ptr(b), _ptr(c), a.size))
+        return a, b, c
+
+    def pack_uniforms(self, params, frame=1):
+        out = np.zeros(abi.VV_UNIFORMS_BYTES, np.uint8)
+        check(load().vv_pack_uniforms(self.handle, C.byref(params), frame, _ptr(out), out.nbytes))
+        return out
+
+    def read_volume(self, which):
+        nx, ny, nz = self.dims
+        if which == abi.VOLUME_MAJORANT:
+            shape, dt = ((nz + 7) // 8, (ny + 7) // 8, (nx + 7) // 8), np.float32
+        else:
+            shape, dt = {abi.VOLUME_DENSITY: ((nz, ny, nx), np.uint16),
+                         abi.VOLUME_NORMALS: ((nz, ny, nx, 4), np.int8),
+                         abi.VOLUME_MASK: ((nz, ny, nx, 2), np.uint16),
+                         abi.VOLUME_LABELS: ((nz, ny, nx), np.uint8)}[which]
+        out = np.empty(shape, dt)
+        check(load().vv_read_volume(self.handle, which, _ptr(out), out.nbytes))
+        return out
+
+    def kernel_launches(self):
+        return load().vv_kernel_launches(self.handle)
+
+    def probe_bspline(self, params, idx):
+        idx = np.ascontiguousarray(idx, np.float32).reshape(-1, 3)
+        out = np.zeros((idx.shape[0], 4), np.float32)
+        check(load().vv_probe_bspline(self.handle, C.byref(params), _ptr(idx), idx.shape[0], _ptr(out)))
+        return out
+
+    def probe_paths(self, params, accumulated, pixels):
+        pix = np.ascontiguousarray(pixels, np.int32).reshape(-1, 2)
+        out = np.zeros((pix.shape[0], 12), np.float32)
+        check(load().vv_probe_paths(self.handle, C.byref(params), accumulated, _ptr(pix), pix.shape[0], _ptr(out)))
+        return out
+
+    def time_pt(self, enable):
+        """Starts (True) or stops (False -> (ms, launches)) timing the path-tracing launches."""
+        ms, n = C.c_double(0.0), C.c_uint64(0)
+        check(load().vv_time_pt(self.handle, int(enable), C.byref(ms), C.byref(n)))
+        return None if enable else (ms.value, n.value)
+
+    def count_events(self, enable):
+        out = np.zeros(len(COUNT_NAMES), np.uint64)
+        check(load().vv_count_events(self.handle, int(enable), _ptr(out), out.size))
+        return None if enable else dict(zip(COUNT_NAMES, (int(v) for v in out)))
+
+    def destroy(self):
+        if self.handle:
+            load().vv_renderer_destroy(self.handle)
+            self.handle = C.c_void_p()
+
+
+def render_to_rgba(renderer, params, width, height, frames):
+    """offscreen.rs:11: resize, `frames` accumulate-frames, tone-mapped RGBA8."""
+    out = np.empty((height, width, 4), np.uint8)
+    check(load().vv_render_to_rgba(renderer.handle, C.byref(params), width, height, frames, _ptr(out), out.nbytes))
+    renderer.width, renderer.height = width, height
+    return out

@@ -212,8 +212,8 @@ def head_neck_phantom(seed=2, dims=(512, 512, 400), spacing=(0.5, 0.5, 1.0)):
         # 57 body regions (62..118): angular sectors x height bands.
         ang = np.arctan2(y_mm, x_mm)
         sector = ((ang + np.pi) / (2 * np.pi) * 8).astype(np.int32) % 8
-        band = min(int(zz / ext_z * 8), 7)
-        reg = 62 + (band * 8 + sector) % 57
+        band = min(int(zz / (head_cz - 0.6 * head_r[2]) * 8), 7)
+        reg = 62 + np.minimum(band * 8 + sector, 56)
         lab[k][inside] = np.broadcast_to(reg, (Y, X))[inside].astype(np.uint8)
         # Skull: 6 mm shell of the head ellipsoid above the neck junction.
         inner = (x_mm / (head_r[0] - 6)) ** 2 + (y_mm / (head_r[1] - 6)) ** 2 + ((zz - head_cz) / (head_r[2] - 6)) ** 2
@@ -228,8 +228,8 @@ def head_neck_phantom(seed=2, dims=(512, 512, 400), spacing=(0.5, 0.5, 1.0)):
         hu[k][air] = -900.0 + 30.0 * noise[k][air]
         lab[k][air] = 57
         # Spine: vertebral bodies (labels 2..25) separated by discs, posterior.
-        vert = int(zz // 16.0)
-        if zz < head_cz - 0.4 * head_r[2] and (zz % 16.0) < 12.0 and vert < 24:
+        vert = int(zz // 10.0)
+        if zz < head_cz - 0.4 * head_r[2] and (zz % 10.0) < 7.5 and vert < 24:
             body = ((x_mm / 13.0) ** 2 + ((y_mm - 22.0) / 11.0) ** 2 <= 1.0) | (
                 (x_mm / 4.0) ** 2 + ((y_mm - 40.0) / 9.0) ** 2 <= 1.0)
             hu[k][body] = 700.0 + 80.0 * noise[k][body]

@@ -251,6 +251,17 @@ class CpuRenderer:
                           ptr(pong), threads())
         return hdr
 
+    def post(self, params, hdr, exposure, frame=1):
+        """record_post: bloom, auto exposure (updates `exposure`, a 1-float array) and tone mapping."""
+        saved = self.accumulated
+        spf = max(int(params.path_tracing.samples_per_frame), 1)
+        self.accumulated -= spf
+        u = self.uniforms(params, frame, self.width, self.height)
+        self.accumulated = saved
+        out = np.zeros((self.height, self.width, 4), np.uint8)
+        lib().vvo_post(ptr(u), ptr(np.ascontiguousarray(hdr, np.uint16)), ptr(exposure), ptr(out))
+        return out
+
     def bspline(self, params, idx):
         idx = np.ascontiguousarray(idx, np.float32).reshape(-1, 3)
         out = np.zeros((idx.shape[0], 4), np.float32)

@@ -27,6 +27,7 @@ void pt_rows(const Uniforms& u, const Scene& sc, float* accum, float* albedo, fl
 void bspline(const Uniforms& u, const Scene& sc, const float* idx, long n, float* out);
 void denoise(const Uniforms& u, const float* accum, const float* albedo, const float* normal, uint16_t* hdr,
              float* ping, float* pong, int threads);
+void post(const Uniforms& u, const uint16_t* hdr, float* exposure, uint8_t* out);
 }  // namespace vvo
 
 using namespace vvo;
@@ -138,5 +139,7 @@ void vvo_denoise(const void* u, const float* accum, const float* albedo, const f
                  float* ping, float* pong, int threads) {
     denoise(U(u), accum, albedo, normal, hdr, ping, pong, threads);
 }
+
+void vvo_post(const void* u, const uint16_t* hdr, float* exposure, uint8_t* out) { post(U(u), hdr, exposure, out); }
 
 }  // extern "C"

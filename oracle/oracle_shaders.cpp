@@ -1153,4 +1153,132 @@ void denoise(const Uniforms& u, const float* accum, const float* albedo, const f
     });
 }
 
+// ===================================================== bloom.comp, tonemap.comp
+// record_post (renderer.rs:1817-1866): bloom passes 0-6 (pass 1 is the
+// auto-exposure metering, one workgroup of 64 invocations), then tone mapping.
+// `exposure` is the adapted exposure texel, read and updated.
+void post(const Uniforms& u, const uint16_t* hdr, float* exposure, uint8_t* out) {
+    int W = int(u.flags.z), H = int(u.flags.w);
+    int qw = (W + 3) / 4, qh = (H + 3) / 4, ew = (qw + 1) / 2, eh = (qh + 1) / 2;
+    std::vector<uint16_t> A(4 * qw * qh), B(4 * qw * qh), Cc(4 * ew * eh), D(4 * ew * eh);
+    auto ld = [](const uint16_t* img, int w, int x, int y) { return glsl::decode(img, glsl::RGBA16F, (long)y * w + x); };
+    auto st = [](uint16_t* img, int w, int x, int y, vec4 v) { glsl::encode(img, glsl::RGBA16F, (long)y * w + x, v); };
+    // Pass 0 (bloom.comp:333-351)
+    for (int y = 0; y < qh; y++)
+        for (int x = 0; x < qw; x++) {
+            vec3 sum(0.0f);
+            float weights = 0.0f, coverage = 0.0f;
+            for (int dy = 0; dy < 4; dy++)
+                for (int dx = 0; dx < 4; dx++) {
+                    vec4 h = ld(hdr, W, min(x * 4 + dx, W - 1), min(y * 4 + dy, H - 1));
+                    float w = 1.0f / (1.0f + lum(vec3(h.x, h.y, h.z)));
+                    sum += vec3(h.x, h.y, h.z) * w;
+                    weights += w;
+                    coverage += 1.0f - h.w;
+                }
+            st(A.data(), qw, x, y, vec4(sum / weights, coverage / 16.0f));
+        }
+    // Pass 1 (bloom.comp:294-327): 64 partial sums, then the tree reduction.
+    {
+        float ls[64], ws[64];
+        int n = qw * qh;
+        for (int t = 0; t < 64; t++) {
+            float s = 0.0f, w = 0.0f;
+            for (int i = t; i < n; i += 64) {
+                vec4 c = ld(A.data(), qw, i % qw, i / qw);
+                s += c.w * log(max(lum(vec3(c.x, c.y, c.z)), 1e-4f));
+                w += c.w;
+            }
+            ls[t] = s;
+            ws[t] = w;
+        }
+        for (int stride = 32; stride > 0; stride >>= 1)
+            for (int t = 0; t < stride; t++) {
+                ls[t] += ls[t + stride];
+                ws[t] += ws[t + stride];
+            }
+        float target = ws[0] > 1.0f ? clamp(0.24f / exp(ls[0] / ws[0]), 0.25f, 4.0f) : 1.0f;
+        float previous = *exposure;
+        *exposure = previous <= 0.0f ? target : exp(mix(log(previous), log(target), 0.15f));
+    }
+    // Passes 2-6 (bloom.comp:276-285, 352-367)
+    const float k[5] = {0.2270f, 0.1945f, 0.1216f, 0.0540f, 0.0162f};
+    auto blur = [&](const uint16_t* src, uint16_t* dst, int w, int h, int ax, int ay) {
+        for (int y = 0; y < h; y++)
+            for (int x = 0; x < w; x++) {
+                vec4 s = ld(src, w, x, y) * k[0];
+                for (int i = 1; i < 5; i++)
+                    s += k[i] * (ld(src, w, clamp(x + ax * i, 0, w - 1), clamp(y + ay * i, 0, h - 1)) +
+                                 ld(src, w, clamp(x - ax * i, 0, w - 1), clamp(y - ay * i, 0, h - 1)));
+                st(dst, w, x, y, s);
+            }
+    };
+    blur(A.data(), B.data(), qw, qh, 1, 0);
+    blur(B.data(), A.data(), qw, qh, 0, 1);
+    for (int y = 0; y < eh; y++)
+        for (int x = 0; x < ew; x++) {
+            vec4 s(0.0f);
+            for (int i = 0; i < 4; i++) s += ld(A.data(), qw, min(x * 2 + (i & 1), qw - 1), min(y * 2 + (i >> 1), qh - 1));
+            st(Cc.data(), ew, x, y, s * 0.25f);
+        }
+    blur(Cc.data(), D.data(), ew, eh, 1, 0);
+    blur(D.data(), Cc.data(), ew, eh, 0, 1);
+    // tonemap.comp:47-85
+    sampler2D narrow, wide;
+    narrow.data = A.data(); narrow.format = glsl::RGBA16F; narrow.w = qw; narrow.h = qh; narrow.filter = glsl::LINEAR;
+    wide.data = Cc.data(); wide.format = glsl::RGBA16F; wide.w = ew; wide.h = eh; wide.filter = glsl::LINEAR;
+    const mat3 inset(0.842479062253094f, 0.0423282422610123f, 0.0423756549057051f, 0.0784335999999992f,
+                     0.878468636469772f, 0.0784336f, 0.0792237451477643f, 0.0791661274605434f, 0.879142973793104f);
+    const mat3 outset(1.19687900512017f, -0.0528968517574562f, -0.0529716355144438f, -0.0980208811401368f,
+                      1.15190312990417f, -0.0980434501171241f, -0.0990297440797205f, -0.0989611768448433f,
+                      1.15107367264116f);
+    auto agx = [&](vec3 c) {
+        const float min_ev = -12.47393f, max_ev = 4.026069f;
+        c = inset * c;
+        c = clamp(log2(max(c, 1e-10f)), min_ev, max_ev);
+        c = (c - min_ev) / (max_ev - min_ev);
+        vec3 c2 = c * c, c4 = c2 * c2;
+        c = 15.5f * c4 * c2 - 40.14f * c4 * c + 31.96f * c4 - 6.868f * c2 * c + 0.4298f * c2 + 0.1191f * c - 0.00232f;
+        c = outset * c;
+        return pow(clamp(c, 0.0f, 1.0f), vec3(2.2f));
+    };
+    auto aces = [](vec3 x) { return clamp((x * (2.51f * x + 0.03f)) / (x * (2.43f * x + 0.59f) + 0.14f), 0.0f, 1.0f); };
+    auto hash01 = [](uint v) {
+        uint state = v * 747796405u + 2891336453u;
+        uint word = ((state >> ((state >> 28u) + 4u)) ^ state) * 277803737u;
+        return float((word >> 22u) ^ word) * (1.0f / 4294967296.0f);
+    };
+    Units none;
+    Shading sh{u, none};
+    for (int y = 0; y < H; y++)
+        for (int x = 0; x < W; x++) {
+            vec4 h = ld(hdr, W, x, y);
+            float e = u.ambient.w;
+            if (u.finish.w > 0.5f) e *= *exposure;
+            vec3 c(h.x, h.y, h.z);
+            vec2 uv = (vec2(float(x), float(y)) + 0.5f) / vec2(float(W), float(H));
+            if (u.finish.x > 0.0f) {
+                vec4 a = textureLod(narrow, uv, 0.0f), b = textureLod(wide, uv, 0.0f);
+                vec3 glow = 0.6f * vec3(a.x, a.y, a.z) + 0.4f * vec3(b.x, b.y, b.z);
+                c = mix(c, glow, u.finish.x);
+            }
+            float r = length(uv * 2.0f - 1.0f) * 0.7071f;
+            float vignette = 1.0f - u.finish.y * pow(r, 2.5f);
+            c *= e * vignette;
+            uint op = uint(u.material.z);
+            c = op == 1u ? aces(c) : op == 2u ? agx(c) : clamp(c, 0.0f, 1.0f);
+            c += h.w * sh.background(sh.camera_ray(vec2(float(x), float(y)) + 0.5f));
+            if (u.flags.y != 0u) {
+                vec3 cc = clamp(c, 0.0f, 1.0f);
+                c = mix(12.92f * cc, 1.055f * pow(cc, vec3(1.0f / 2.4f)) - 0.055f, step(0.0031308f, cc));
+            }
+            if (u.finish.z > 0.0f) {
+                float nn = hash01(uint(x) + 4099u * uint(y)) + hash01(uint(x) * 7919u + uint(y) + 1u) - 1.0f;
+                float yl = clamp(dot(c, vec3(0.2126f, 0.7152f, 0.0722f)), 0.0f, 1.0f);
+                c = clamp(c + nn * u.finish.z * (0.3f + 2.8f * yl * (1.0f - yl)), 0.0f, 1.0f);
+            }
+            glsl::encode(out, glsl::RGBA8_UNORM, (long)y * W + x, vec4(c, 1.0f));
+        }
+}
+
 }  // namespace vvo

@@ -147,5 +147,41 @@ def denoise(uniforms, accum, albedo, normal):
     return hdr
 
 
+def post(uniforms, hdr, exposure):
+    """record_post (renderer.rs:1817-1866): bloom passes 0-6, then tonemap.comp."""
+    H, W = hdr.shape[:2]
+    qw, qh = (W + 3) // 4, (H + 3) // 4
+    ew, eh = (qw + 1) // 2, (qh + 1) // 2
+    imgs = [np.zeros((qh, qw, 4), np.uint16), np.zeros((qh, qw, 4), np.uint16),
+            np.zeros((eh, ew, 4), np.uint16), np.zeros((eh, ew, 4), np.uint16)]
+    exp_img = np.ascontiguousarray(exposure, np.float32)
+    l = shader("bloom")
+    l.ref_set_uniforms(_p(uniforms), 21200)
+    l.ref_bind_image(b"hdr_image", _p(hdr), RGBA16F, W, H, 1)
+    for name, img in zip((b"bloom_a", b"bloom_b", b"bloom_c", b"bloom_d"), imgs):
+        l.ref_bind_image(name, _p(img), RGBA16F, img.shape[1], img.shape[0], 1)
+    l.ref_bind_image(b"exposure_image", _p(exp_img), R32F, 1, 1, 1)
+    for pas in range(7):
+        e = 1 if pas >= 4 else 0
+        w, h = imgs[2 * e].shape[1], imgs[2 * e].shape[0]
+        push = np.array([w, h, 1, 0, pas, 0, 0, 0, 0, 0, 0, 0], np.int32)
+        l.ref_set_push(_p(push), push.nbytes)
+        if pas == 1:
+            l.ref_run_workgroup64()
+        else:
+            l.ref_run(0, w, 0, h, 0, 1, _threads())
+    t = shader("tonemap")
+    out = np.zeros((H, W, 4), np.uint8)
+    t.ref_set_uniforms(_p(uniforms), 21200)
+    t.ref_bind_image(b"hdr_image", _p(hdr), RGBA16F, W, H, 1)
+    t.ref_bind_texture(b"bloom_narrow", _p(imgs[0]), RGBA16F, qw, qh, 1, LINEAR, 0)
+    t.ref_bind_texture(b"bloom_wide", _p(imgs[2]), RGBA16F, ew, eh, 1, LINEAR, 0)
+    t.ref_bind_image(b"exposure_image", _p(exp_img), R32F, 1, 1, 1)
+    t.ref_bind_image(b"out_image", _p(out), RGBA8_UNORM, W, H, 1)
+    t.ref_run(0, W, 0, H, 0, 1, _threads())
+    exposure[...] = exp_img
+    return out
+
+
 def _threads():
     return max(1, min(os.cpu_count() or 1, 64))

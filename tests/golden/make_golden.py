@@ -49,13 +49,17 @@ def main():
         u = r.uniforms(params, f + 1, size, size)
         R.pt_frame(r, u, acc, alb, nor, hdr)
     r.accumulated = (frames - 1) * spf
-    denoised = R.denoise(r.uniforms(params, frames, size, size), acc, alb, nor)
+    ud = r.uniforms(params, frames, size, size)
+    denoised = R.denoise(ud, acc, alb, nor)
+    exposure = np.zeros(1, np.float32)
+    post1 = R.post(ud, denoised, exposure)
+    post2 = R.post(ud, denoised, exposure)  # a second frame adapts the exposure
     out = os.path.join(os.path.dirname(os.path.abspath(__file__)), "small_scene.npz")
     np.savez_compressed(out, hu=cfg["hu"], labels=cfg["labels_vol"], soft=cfg["soft"],
                         spacing=np.array(cfg["spacing"]), params=np.frombuffer(bytes(params), np.uint8),
                         width=size, height=size, frames=frames, density=r.density, normals=normals, mask=mask,
                         majorant=majorant, uniforms_frame1=u1, accum=acc, albedo=alb, normal=nor, hdr=hdr,
-                        denoised=denoised)
+                        denoised=denoised, post1=post1, post2=post2, exposure=exposure)
     print(out, os.path.getsize(out), "bytes; background share", float(acc[..., 3].mean()) / (frames * spf))
 
 

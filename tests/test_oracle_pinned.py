@@ -80,6 +80,10 @@ def test_oracle_matches_reference_golden_frames():
     assert np.array_equal(r.normal, g["normal"])
     assert np.array_equal(r.hdr, g["hdr"])
     assert np.array_equal(r.denoise(params), g["denoised"])
+    exposure = np.zeros(1, np.float32)
+    assert np.array_equal(r.post(params, g["denoised"], exposure, int(g["frames"])), g["post1"])
+    assert np.array_equal(r.post(params, g["denoised"], exposure, int(g["frames"])), g["post2"])
+    assert np.array_equal(exposure, g["exposure"])
 
 
 def test_oracle_matches_reference_shaders_live(small_cfg):

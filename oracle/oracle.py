@@ -184,8 +184,21 @@ class CpuRenderer:
         return pack_uniforms(self.volume, self.bucket, params, self.accumulated, frame, width, height,
                              has_labels=self.has_labels)
 
+    def adopt(self, mask=None, majorant=None, normals=None):
+        """Takes the pre-pass volumes from elsewhere (e.g. the device), so that a
+        later stage is compared on identical inputs; `prepare` then keeps them."""
+        if normals is not None:
+            self.normals = np.ascontiguousarray(normals, np.int8)
+        if mask is not None:
+            self.mask = np.ascontiguousarray(mask, np.uint16)
+        if majorant is not None:
+            self.majorant = np.ascontiguousarray(majorant, np.float32)
+        self.mask_key = "adopted"
+
     def prepare(self, params, width, height):
         """The mask and majorant passes `record` runs when the opacity key changed."""
+        if self.mask_key == "adopted":
+            return
         u = self.uniforms(params, 0, width, height)
         mode = int(params.labels.mode) if self.has_labels else 0
         lp = params.labels

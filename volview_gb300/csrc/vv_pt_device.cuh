@@ -8,6 +8,10 @@
 #include "vv_kernels.h"
 
 namespace vv {
+// Internal linkage: every translation unit that includes this header gets its
+// own copy of the device functions (some are out of line).
+namespace {
+
 
 constexpr float PI = 3.14159265358979f;
 constexpr float MAX_EXTINCTION = 8.0f;       // pt.comp:34
@@ -1064,4 +1068,5 @@ __device__ void accumulate(const PtArgs& A, uint32_t px, uint32_t py, const Pixe
     }
 }
 
+}  // namespace
 }  // namespace vv

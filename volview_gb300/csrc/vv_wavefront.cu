@@ -14,11 +14,14 @@
 // numbers are consumed in the reference's order (pt.comp), so a slot replays
 // the same path as the reference-shaped kernel.
 //
-// One slot per pixel; a slot traces its pixel's samples and frames in turn
-// (the reference's per-pixel stream), so accumulation needs no atomics. When
-// few paths are left, the rest run to completion in one launch of the
-// single-kernel tracer (k_wf_finish), which avoids hundreds of nearly empty
-// waves for the longest random walks.
+// Work items are (frame, pixel) pairs; a slot traces one item's samples in
+// turn (the reference's per-pixel stream for one frame), then takes the next
+// item from a global counter, so the frames of one pixel run in parallel and
+// slow pixels do not queue their frames behind each other. With one frame per
+// launch each slot owns its pixel and accumulates without atomics. When few
+// paths are left, the rest run to completion in one launch of the
+// single-kernel tracer (k_wf_finish), instead of many nearly empty waves for
+// the longest random walks.
 #include <cuda_runtime.h>
 
 #include <cstdlib>
@@ -132,8 +135,9 @@ __device__ __forceinline__ void push(uint32_t* q, uint32_t* count, uint32_t slot
     if (pred) q[base + __popc(m & ((1u << lane) - 1u))] = slot;
 }
 
-// Ends a sample path: firefly clamp and sums, then the pixel's next sample or
-// frame (pt.comp:403, 546-560). Returns true when the slot has a new path.
+// Ends a sample path: firefly clamp and sums, then the pixel's next sample
+// (pt.comp:403, 546-560). Returns true when the slot has a new path; false when
+// the work item (one pixel of one frame) is done and accumulated.
 __device__ bool end_path(const PtArgs& A, const Consts& C, Path& P, PixelSums& S, Ctl& c) {
     finish_path(P, S);
     uint32_t spf = A.u.path[2];
@@ -142,15 +146,51 @@ __device__ bool end_path(const PtArgs& A, const Consts& C, Path& P, PixelSums& S
         start_path(A, C, P, px, py);
         return true;
     }
-    bool last = c.frame + 1 >= A.frames;
-    accumulate(A, px, py, S, false, last, (float)(A.u.path[0] + A.frames * spf));
-    if (last) return false;
-    c.frame++;
-    c.sample = 0;
-    S = {mk(0.0f), 0.0f, make_float4(0, 0, 0, 0), make_float4(0, 0, 0, 0)};
-    P.rng.s = seed_of(px, py, A.u.path[0] + c.frame * spf);
+    // One frame per launch: this slot owns the pixel; several: frames of one
+    // pixel may finish concurrently in different slots.
+    bool multi = A.frames > 1;
+    accumulate(A, px, py, S, multi, !multi, (float)(A.u.path[0] + spf));
+    return false;
+}
+
+// Starts work item `item` (frame item / pixels, pixel item % pixels) in a slot.
+__device__ void start_item(const PtArgs& A, const Consts& C, uint32_t item, Path& P, PixelSums& S, Ctl& c) {
+    uint32_t pixels = A.width * A.height;
+    c.pixel = item % pixels;
+    c.frame = item / pixels;
+    c.sample = 0u;
+    uint32_t px = c.pixel % A.width, py = c.pixel / A.width;
+    P.rng.s = seed_of(px, py, A.u.path[0] + c.frame * A.u.path[2]);
     P.rng.pcg();
+    S = {mk(0.0f), 0.0f, make_float4(0, 0, 0, 0), make_float4(0, 0, 0, 0)};
     start_path(A, C, P, px, py);
+}
+
+// Hands the next work items to the lanes with `need` set (all 32 lanes call
+// it together; one atomicAdd per warp). Returns the lane's item, or ~0u.
+__device__ __forceinline__ uint32_t take_item(uint32_t* counter, uint32_t total, bool need) {
+    unsigned m = __ballot_sync(0xffffffffu, need);
+    if (!m) return ~0u;
+    int lane = (int)(threadIdx.x & 31u);
+    int leader = __ffs(m) - 1;
+    uint32_t base = 0;
+    if (lane == leader) base = atomicAdd(counter, (uint32_t)__popc(m));
+    base = __shfl_sync(0xffffffffu, base, leader);
+    uint32_t item = base + __popc(m & ((1u << lane) - 1u));
+    return (need && item < total) ? item : ~0u;
+}
+
+// A lane whose item ended takes the next one and starts it in its slot.
+__device__ __forceinline__ bool refill(const PtArgs& A, const WfArgs& W, const Consts& C, uint32_t slot, bool need) {
+    uint32_t item = take_item(&W.counts[WF_ITEMS], A.frames * A.width * A.height, need);
+    if (item == ~0u) return false;
+    Path P;
+    PixelSums S;
+    Ctl c;
+    start_item(A, C, item, P, S, c);
+    float4* q = slot_of(W, slot);
+    store_path(q, P, c);
+    store_sums(q, S);
     return true;
 }
 
@@ -160,24 +200,22 @@ __device__ bool end_path(const PtArgs& A, const Consts& C, Path& P, PixelSums& S
     for (uint32_t base_ = (blockIdx.x * blockDim.x + threadIdx.x) & ~31u; base_ < (n);          \
          base_ += gridDim.x * blockDim.x)
 
-__global__ void __launch_bounds__(256) k_wf_init(const __grid_constant__ PtArgs A, const WfArgs W) {
-    uint32_t n = A.width * A.height;
+__global__ void __launch_bounds__(256) k_wf_init(const __grid_constant__ PtArgs A, const WfArgs W, uint32_t slots) {
     Consts C = make_consts(A);
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < slots; i += gridDim.x * blockDim.x) {
         Path P;
-        Ctl c = {i, 0u, 0u};
-        uint32_t px = i % A.width, py = i / A.width;
-        P.rng.s = seed_of(px, py, A.u.path[0]);
-        P.rng.pcg();
-        start_path(A, C, P, px, py);
+        PixelSums S;
+        Ctl c;
+        start_item(A, C, i, P, S, c);
         float4* q = slot_of(W, i);
         store_path(q, P, c);
-        store_sums(q, PixelSums{mk(0.0f), 0.0f, make_float4(0, 0, 0, 0), make_float4(0, 0, 0, 0)});
+        store_sums(q, S);
         W.ext[0][i] = i;
     }
     if (blockIdx.x == 0 && threadIdx.x == 0) {
-        W.counts[0] = n;
-        for (int k = 1; k < WF_COUNTERS; k++) W.counts[k] = 0;
+        for (int k = 0; k < WF_COUNTERS; k++) W.counts[k] = 0;
+        W.counts[WF_EXT0] = slots;
+        W.counts[WF_ITEMS] = slots;
     }
 }
 
@@ -189,7 +227,7 @@ __global__ void __launch_bounds__(128, 4) k_wf_extend(const __grid_constant__ Pt
         uint32_t i = base_ + (threadIdx.x & 31u);
         bool valid = i < n;
         uint32_t slot = valid ? W.ext[cur][i] : 0u;
-        bool to_shade = false, to_ext = false;
+        bool to_shade = false, to_ext = false, need = false;
         if (valid) {
             float4* q = slot_of(W, slot);
             Path P;
@@ -205,10 +243,12 @@ __global__ void __launch_bounds__(128, 4) k_wf_extend(const __grid_constant__ Pt
                 load_sums(q, S);
                 if (escaped) stage_escape(A, C, P, S);
                 to_ext = end_path(A, C, P, S, c);
+                need = !to_ext;
                 store_sums(q, S);
             }
             store_path(q, P, c);
         }
+        if (refill(A, W, C, slot, need)) to_ext = true;
         push(W.shade, &W.counts[WF_SHADE], slot, to_shade);
         push(W.ext[nxt], &W.counts[nxt], slot, to_ext);
     }
@@ -276,7 +316,7 @@ __global__ void __launch_bounds__(128, 6) k_wf_scatter(const __grid_constant__ P
         uint32_t i = base_ + (threadIdx.x & 31u);
         bool valid = i < n;
         uint32_t slot = valid ? W.scatter[i] : 0u;
-        bool to_ext = false;
+        bool to_ext = false, need = false;
         if (valid) {
             float4* q = slot_of(W, slot);
             Path P;
@@ -293,10 +333,12 @@ __global__ void __launch_bounds__(128, 6) k_wf_scatter(const __grid_constant__ P
                 PixelSums S;
                 load_sums(q, S);
                 to_ext = end_path(A, C, P, S, c);
+                need = !to_ext;
                 store_sums(q, S);
             }
             store_path(q, P, c);
         }
+        if (refill(A, W, C, slot, need)) to_ext = true;
         push(W.ext[nxt], &W.counts[nxt], slot, to_ext);
     }
     if (blockIdx.x == 0 && threadIdx.x == 0) W.counts[WF_SHADOW] = 0;
@@ -315,10 +357,16 @@ __global__ void __launch_bounds__(128, 4) k_wf_finish(const __grid_constant__ Pt
         PixelSums S;
         load_path(q, P, c);
         load_sums(q, S);
-        do {
-            while (bounce_step(A, C, P, S)) {
-            }
-        } while (end_path(A, C, P, S, c));
+        uint32_t total = A.frames * A.width * A.height;
+        for (;;) {
+            do {
+                while (bounce_step(A, C, P, S)) {
+                }
+            } while (end_path(A, C, P, S, c));
+            uint32_t item = atomicAdd(&W.counts[WF_ITEMS], 1u);
+            if (item >= total) break;
+            start_item(A, C, item, P, S, c);
+        }
     }
 }
 
@@ -340,9 +388,10 @@ cudaError_t launch_pt_wavefront(const PtArgs& a, const WfArgs& w, int sms, cudaS
         g_finish = sms * blocks_per_sm(k_wf_finish, 128);
     }
     const char* env = std::getenv("VV_WF_TAIL");
-    uint32_t tail = env ? (uint32_t)std::atoi(env) : 32768u;
+    uint32_t tail = env ? (uint32_t)std::atoi(env) : 1024u;
     uint32_t pixels = a.width * a.height;
-    k_wf_init<<<(pixels + 255) / 256 < (uint32_t)(sms * 8) ? (pixels + 255) / 256 : sms * 8, 256, 0, s>>>(a, w);
+    uint32_t slots = pixels;  // one frame's worth of paths in flight
+    k_wf_init<<<(slots + 255) / 256 < (uint32_t)(sms * 8) ? (slots + 255) / 256 : sms * 8, 256, 0, s>>>(a, w, slots);
     *launches += 1;
     int cur = 0;
     const int check = 2;

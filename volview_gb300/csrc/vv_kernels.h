@@ -74,7 +74,12 @@ cudaError_t launch_pt(const PtArgs& a, int sms, cudaStream_t s, int* launches);
 
 // Wavefront tracer state: one 256-byte slot per pixel, the stage queues (slot
 // indices) and their counters.
-enum { WF_EXT0 = 0, WF_EXT1 = 1, WF_SHADE = 2, WF_SHADOW = 3, WF_SCATTER = 4, WF_ITEMS = 5, WF_COUNTERS = 8 };
+enum {
+    WF_EXT0 = 0, WF_EXT1 = 1, WF_SHADE = 2, WF_SHADOW = 3, WF_SCATTER = 4,
+    WF_ITEMS = 5,     // next (frame, pixel) work item
+    WF_TAKE_EXT = 6,  // entries of the extend queue taken so far
+    WF_COUNTERS = 8
+};
 struct WfArgs {
     float4* slots;
     uint32_t* ext[2];

@@ -787,33 +787,63 @@ __device__ float extinction_at(const PtArgs& A, f3 idx, f3 dir, bool smooth, Sam
     return s.extinction;
 }
 
-// pt.comp:300-334: delta tracking against the brick majorants, hero channel.
+// pt.comp:300-334: delta tracking against the brick majorants, hero channel,
+// as a resumable loop: ff_begin sets up the ray, each ff_step is one iteration.
+struct Flight {
+    f3 d_idx, inv_d;
+    float tt, t_end;
+    int iter;
+};
+enum { FF_CONTINUE = 0, FF_HIT = 1, FF_ESCAPE = 2 };
+
+__device__ __forceinline__ void ff_begin(const PtArgs& A, f3 origin, f3 dir, Flight& F) {
+    F.d_idx = mul(w2i3(A), dir);
+    float2 tr = intersect_volume(A, origin, F.d_idx);
+    F.inv_d = brick_inv_dir(F.d_idx);
+    F.tt = tr.x;
+    F.t_end = tr.y;
+    F.iter = 0;
+}
+
+__device__ __forceinline__ int ff_step(const PtArgs& A, f3 origin, f3 dir, bool smooth, int hero, f3& spectral,
+                                       Flight& F, f3& idx, Sample& s, int& cap_plane, float& cut, Rng& rng) {
+    if (!(F.iter < 4096 && F.tt < F.t_end)) return FF_ESCAPE;
+    F.iter++;
+    f3 p = origin + F.d_idx * F.tt;
+    float majorant = flight_majorant(A, p);
+    float exit = F.tt + brick_exit(p, F.inv_d) + 1e-3f;
+    if (majorant <= 0.0f) {
+        F.tt = exit;
+        return FF_CONTINUE;
+    }
+    float next = F.tt - logf(1.0f - rng.rand()) / majorant;
+    if (next >= exit) {
+        F.tt = exit;
+        return FF_CONTINUE;
+    }
+    F.tt = next;
+    idx = origin + F.d_idx * F.tt;
+    float ext = extinction_at(A, idx, dir, smooth, s, cap_plane, cut);
+    if (ext <= 0.0f) return FF_CONTINUE;
+    f3 sigma = path_sigma(A, s, ext);
+    float sh = comp(sigma, hero);
+    if (rng.rand() * majorant < sh) {
+        spectral *= sigma / sh;
+        return FF_HIT;
+    }
+    spectral *= gmax(majorant - sigma, 0.0f) / (majorant - sh);
+    return FF_CONTINUE;
+}
+
 __device__ bool free_flight(const PtArgs& A, f3 origin, f3 dir, bool smooth, int hero, f3& spectral, f3& idx,
                             Sample& s, int& cap_plane, float& cut, Rng& rng) {
-    f3 d_idx = mul(w2i3(A), dir);
-    float2 tr = intersect_volume(A, origin, d_idx);
-    f3 inv_d = brick_inv_dir(d_idx);
-    float tt = tr.x;
-    for (int i = 0; i < 4096 && tt < tr.y; i++) {
-        f3 p = origin + d_idx * tt;
-        float majorant = flight_majorant(A, p);
-        float exit = tt + brick_exit(p, inv_d) + 1e-3f;
-        if (majorant <= 0.0f) { tt = exit; continue; }
-        float next = tt - logf(1.0f - rng.rand()) / majorant;
-        if (next >= exit) { tt = exit; continue; }
-        tt = next;
-        idx = origin + d_idx * tt;
-        float ext = extinction_at(A, idx, dir, smooth, s, cap_plane, cut);
-        if (ext <= 0.0f) continue;
-        f3 sigma = path_sigma(A, s, ext);
-        float sh = comp(sigma, hero);
-        if (rng.rand() * majorant < sh) {
-            spectral *= sigma / sh;
-            return true;
-        }
-        spectral *= gmax(majorant - sigma, 0.0f) / (majorant - sh);
+    Flight F;
+    ff_begin(A, origin, dir, F);
+    for (;;) {
+        int r = ff_step(A, origin, dir, smooth, hero, spectral, F, idx, s, cap_plane, cut, rng);
+        if (r == FF_HIT) return true;
+        if (r == FF_ESCAPE) return false;
     }
-    return false;
 }
 
 // pt.comp:339-371: ratio tracking with Russian roulette.

@@ -219,38 +219,70 @@ __global__ void __launch_bounds__(256) k_wf_init(const __grid_constant__ PtArgs 
     }
 }
 
+// Extend, persistent over its queue: every lane advances its path by one
+// free-flight step per iteration; a lane whose flight ended (a vertex, an
+// escape, or the bounce limits) hands the path on and takes the next queued
+// path, so lanes with long empty-space flights do not hold up the others.
+// ff_step is the loop body of free_flight (pt.comp:307-332).
+enum { EXT_END = 3 };
 __global__ void __launch_bounds__(128, 4) k_wf_extend(const __grid_constant__ PtArgs A, const WfArgs W, int cur) {
-    uint32_t n = W.counts[cur];
-    int nxt = cur ^ 1;
-    Consts C = make_consts(A);
-    WF_FOR_EACH(n) {
-        uint32_t i = base_ + (threadIdx.x & 31u);
-        bool valid = i < n;
-        uint32_t slot = valid ? W.ext[cur][i] : 0u;
-        bool to_shade = false, to_ext = false, need = false;
-        if (valid) {
-            float4* q = slot_of(W, slot);
-            Path P;
-            Ctl c;
-            Vertex V;
-            bool escaped;
-            load_path(q, P, c);
-            if (stage_extend(A, C, P, V, escaped)) {
-                store_vertex(q, V);
-                to_shade = true;
-            } else {
-                PixelSums S;
-                load_sums(q, S);
-                if (escaped) stage_escape(A, C, P, S);
-                to_ext = end_path(A, C, P, S, c);
-                need = !to_ext;
-                store_sums(q, S);
+    const uint32_t n = W.counts[cur];
+    const int nxt = cur ^ 1;
+    const Consts C = make_consts(A);
+    uint32_t slot = 0;
+    Path P;
+    Ctl c;
+    Flight F;
+    Vertex V;
+    bool active = false, drained = false;
+    for (;;) {
+        int done = 0;
+        bool need = !active && !drained;
+        if (__any_sync(0xffffffffu, need)) {
+            uint32_t k = take_item(&W.counts[WF_TAKE_EXT], n, need);
+            if (need && k != ~0u) {
+                slot = W.ext[cur][k];
+                load_path(slot_of(W, slot), P, c);
+                if (!(P.surfaces <= C.max_bounces && P.volumes <= C.volume_limit)) {
+                    done = EXT_END;
+                } else {
+                    count(A, COUNT_VERTEX);
+                    ff_begin(A, P.origin, P.dir, F);
+                    active = true;
+                }
             }
-            store_path(q, P, c);
+            drained = __any_sync(0xffffffffu, need && k == ~0u);
         }
-        if (refill(A, W, C, slot, need)) to_ext = true;
-        push(W.shade, &W.counts[WF_SHADE], slot, to_shade);
-        push(W.ext[nxt], &W.counts[nxt], slot, to_ext);
+        if (active) {
+            int r = ff_step(A, P.origin, P.dir, P.bounce == 0u, P.hero, P.spectral, F, V.idx, V.s, V.cap_plane, V.cut,
+                            P.rng);
+            if (r != FF_CONTINUE) {
+                active = false;
+                done = r;
+            }
+        }
+        if (__any_sync(0xffffffffu, done != 0)) {
+            bool to_shade = false, to_ext = false, need_item = false;
+            if (done != 0) {
+                float4* q = slot_of(W, slot);
+                if (done == FF_HIT) {
+                    store_vertex(q, V);
+                    to_shade = true;
+                } else {
+                    PixelSums S;
+                    load_sums(q, S);
+                    if (done == FF_ESCAPE) stage_escape(A, C, P, S);
+                    to_ext = end_path(A, C, P, S, c);
+                    need_item = !to_ext;
+                    store_sums(q, S);
+                }
+                store_path(q, P, c);
+            }
+            if (refill(A, W, C, slot, need_item)) to_ext = true;
+            push(W.shade, &W.counts[WF_SHADE], slot, to_shade);
+            push(W.ext[nxt], &W.counts[nxt], slot, to_ext);
+        }
+        if (drained && !__any_sync(0xffffffffu, active)) break;
     }
     if (blockIdx.x == 0 && threadIdx.x == 0) W.counts[WF_SCATTER] = 0;
 }
@@ -282,7 +314,10 @@ __global__ void __launch_bounds__(128, 4) k_wf_shade(const __grid_constant__ PtA
         }
         push(W.shadow, &W.counts[WF_SHADOW], slot, valid);
     }
-    if (blockIdx.x == 0 && threadIdx.x == 0) W.counts[cur] = 0;
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        W.counts[cur] = 0;
+        W.counts[WF_TAKE_EXT] = 0;
+    }
 }
 
 __global__ void __launch_bounds__(128, 6) k_wf_shadow(const __grid_constant__ PtArgs A, const WfArgs W) {

@@ -78,6 +78,7 @@ enum {
     WF_EXT0 = 0, WF_EXT1 = 1, WF_SHADE = 2, WF_SHADOW = 3, WF_SCATTER = 4,
     WF_ITEMS = 5,     // next (frame, pixel) work item
     WF_TAKE_EXT = 6,  // entries of the extend queue taken so far
+    WF_TAKE_SHADOW = 7,  // entries of the shadow queue taken so far
     WF_COUNTERS = 8
 };
 struct WfArgs {

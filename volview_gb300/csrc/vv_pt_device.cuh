@@ -846,30 +846,59 @@ __device__ bool free_flight(const PtArgs& A, f3 origin, f3 dir, bool smooth, int
     }
 }
 
+// pt.comp:339-371 as a resumable loop: tr_begin sets up the shadow ray, each
+// tr_step is one iteration; the estimate is in Shadow::result.
+struct Shadow {
+    f3 d_idx, inv_d, result;
+    float tt, t_end;
+    int iter;
+};
+__device__ __forceinline__ void tr_begin(const PtArgs& A, f3 origin, f3 dir, Shadow& T) {
+    T.d_idx = mul(w2i3(A), dir);
+    float2 tr = intersect_volume(A, origin, T.d_idx);
+    T.inv_d = brick_inv_dir(T.d_idx);
+    T.tt = tr.x;
+    T.t_end = tr.y;
+    T.iter = 0;
+    T.result = mk(1.0f);
+}
+// Returns false when the estimate is final.
+__device__ __forceinline__ bool tr_step(const PtArgs& A, f3 origin, Shadow& T, Rng& rng) {
+    if (!(T.iter < 4096 && T.tt < T.t_end)) return false;
+    T.iter++;
+    float peak = maxc(T.result);
+    if (peak < 0.1f) {
+        if (rng.rand() * 0.1f >= peak) {
+            T.result = mk(0.0f);
+            return false;
+        }
+        T.result *= 0.1f / peak;
+    }
+    f3 p = origin + T.d_idx * T.tt;
+    float majorant = flight_majorant(A, p);
+    float exit = T.tt + brick_exit(p, T.inv_d) + 1e-3f;
+    if (majorant <= 0.0f) {
+        T.tt = exit;
+        return true;
+    }
+    float next = T.tt - logf(1.0f - rng.rand()) / majorant;
+    if (next >= exit) {
+        T.tt = exit;
+        return true;
+    }
+    T.tt = next;
+    Sample m = sample_point(A, origin + T.d_idx * T.tt);
+    T.result *= gmax(1.0f - path_sigma(A, m, m.extinction) / majorant, 0.0f);
+    return true;
+}
+
 // pt.comp:339-371: ratio tracking with Russian roulette.
 __device__ __noinline__ f3 transmittance(const PtArgs& A, f3 origin, f3 dir, Rng& rng) {
-    f3 d_idx = mul(w2i3(A), dir);
-    float2 tr = intersect_volume(A, origin, d_idx);
-    float tt = tr.x;
-    f3 result = mk(1.0f);
-    f3 inv_d = brick_inv_dir(d_idx);
-    for (int i = 0; i < 4096 && tt < tr.y; i++) {
-        float peak = maxc(result);
-        if (peak < 0.1f) {
-            if (rng.rand() * 0.1f >= peak) return mk(0.0f);
-            result *= 0.1f / peak;
-        }
-        f3 p = origin + d_idx * tt;
-        float majorant = flight_majorant(A, p);
-        float exit = tt + brick_exit(p, inv_d) + 1e-3f;
-        if (majorant <= 0.0f) { tt = exit; continue; }
-        float next = tt - logf(1.0f - rng.rand()) / majorant;
-        if (next >= exit) { tt = exit; continue; }
-        tt = next;
-        Sample m = sample_point(A, origin + d_idx * tt);
-        result *= gmax(1.0f - path_sigma(A, m, m.extinction) / majorant, 0.0f);
+    Shadow T;
+    tr_begin(A, origin, dir, T);
+    while (tr_step(A, origin, T, rng)) {
     }
-    return result;
+    return T.result;
 }
 
 // ------------------------------------------------------------- path state

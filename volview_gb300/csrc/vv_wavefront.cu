@@ -223,15 +223,21 @@ __global__ void __launch_bounds__(256) k_wf_init(const __grid_constant__ PtArgs 
 // free-flight step per iteration; a lane whose flight ended (a vertex, an
 // escape, or the bounce limits) hands the path on and takes the next queued
 // path, so lanes with long empty-space flights do not hold up the others.
-// ff_step is the loop body of free_flight (pt.comp:307-332).
+// ff_step is the loop body of free_flight (pt.comp:307-332). Only what the
+// flight needs stays in registers; the rest of the path is read when it ends.
+#ifndef VV_EXTEND_MIN_BLOCKS
+#define VV_EXTEND_MIN_BLOCKS 4
+#endif
 enum { EXT_END = 3 };
-__global__ void __launch_bounds__(128, 4) k_wf_extend(const __grid_constant__ PtArgs A, const WfArgs W, int cur) {
+__global__ void __launch_bounds__(128, VV_EXTEND_MIN_BLOCKS)
+    k_wf_extend(const __grid_constant__ PtArgs A, const WfArgs W, int cur) {
     const uint32_t n = W.counts[cur];
     const int nxt = cur ^ 1;
     const Consts C = make_consts(A);
     uint32_t slot = 0;
-    Path P;
-    Ctl c;
+    f3 origin, dir, spectral;
+    Rng rng;
+    uint32_t hero = 0, bounce = 0;
     Flight F;
     Vertex V;
     bool active = false, drained = false;
@@ -242,20 +248,27 @@ __global__ void __launch_bounds__(128, 4) k_wf_extend(const __grid_constant__ Pt
             uint32_t k = take_item(&W.counts[WF_TAKE_EXT], n, need);
             if (need && k != ~0u) {
                 slot = W.ext[cur][k];
-                load_path(slot_of(W, slot), P, c);
-                if (!(P.surfaces <= C.max_bounces && P.volumes <= C.volume_limit)) {
+                const float4* q = slot_of(W, slot);
+                float4 a = q[Q_ORIGIN], b = q[Q_DIR], s = q[Q_SPEC];
+                origin = xyz(a);
+                dir = xyz(b);
+                rng.s = ubits(b.w);
+                spectral = xyz(s);
+                bounce = ubits(s.w) & 0xffffu;
+                uint32_t surfaces = ubits(s.w) >> 16, volumes = ubits(q[Q_RAD].w);
+                hero = ubits(q[Q_CTL].z);
+                if (!(surfaces <= C.max_bounces && volumes <= C.volume_limit)) {
                     done = EXT_END;
                 } else {
                     count(A, COUNT_VERTEX);
-                    ff_begin(A, P.origin, P.dir, F);
+                    ff_begin(A, origin, dir, F);
                     active = true;
                 }
             }
             drained = __any_sync(0xffffffffu, need && k == ~0u);
         }
         if (active) {
-            int r = ff_step(A, P.origin, P.dir, P.bounce == 0u, P.hero, P.spectral, F, V.idx, V.s, V.cap_plane, V.cut,
-                            P.rng);
+            int r = ff_step(A, origin, dir, bounce == 0u, (int)hero, spectral, F, V.idx, V.s, V.cap_plane, V.cut, rng);
             if (r != FF_CONTINUE) {
                 active = false;
                 done = r;
@@ -267,16 +280,24 @@ __global__ void __launch_bounds__(128, 4) k_wf_extend(const __grid_constant__ Pt
                 float4* q = slot_of(W, slot);
                 if (done == FF_HIT) {
                     store_vertex(q, V);
+                    q[Q_DIR] = f4(dir, fbits(rng.s));
+                    float4 s = q[Q_SPEC];
+                    q[Q_SPEC] = f4(spectral, s.w);
                     to_shade = true;
                 } else {
+                    Path P;
+                    Ctl c;
                     PixelSums S;
+                    load_path(q, P, c);
+                    P.rng = rng;
+                    P.spectral = spectral;
                     load_sums(q, S);
                     if (done == FF_ESCAPE) stage_escape(A, C, P, S);
                     to_ext = end_path(A, C, P, S, c);
                     need_item = !to_ext;
                     store_sums(q, S);
+                    store_path(q, P, c);
                 }
-                store_path(q, P, c);
             }
             if (refill(A, W, C, slot, need_item)) to_ext = true;
             push(W.shade, &W.counts[WF_SHADE], slot, to_shade);
@@ -320,25 +341,48 @@ __global__ void __launch_bounds__(128, 4) k_wf_shade(const __grid_constant__ PtA
     }
 }
 
-__global__ void __launch_bounds__(128, 6) k_wf_shadow(const __grid_constant__ PtArgs A, const WfArgs W) {
-    uint32_t n = W.counts[WF_SHADOW];
-    WF_FOR_EACH(n) {
-        uint32_t i = base_ + (threadIdx.x & 31u);
-        bool valid = i < n;
-        uint32_t slot = valid ? W.shadow[i] : 0u;
-        if (valid) {
-            float4* q = slot_of(W, slot);
-            Path P;
-            float4 d = q[Q_DIR];
-            P.rng.s = ubits(d.w);
-            Vertex V;
-            V.idx = xyz(q[Q_IDX]);
-            V.light_dir = xyz(q[Q_LD]);
-            stage_shadow(A, P, V);
-            q[Q_DIR] = make_float4(d.x, d.y, d.z, fbits(P.rng.s));
-            q[Q_LT] = f4(V.light_t, 0.0f);
+// Shadow rays, persistent over their queue like extend: one ratio-tracking
+// step (tr_step, the loop body of transmittance, pt.comp:344-369) per
+// iteration, lanes refilled as their rays finish.
+#ifndef VV_SHADOW_MIN_BLOCKS
+#define VV_SHADOW_MIN_BLOCKS 6
+#endif
+__global__ void __launch_bounds__(128, VV_SHADOW_MIN_BLOCKS) k_wf_shadow(const __grid_constant__ PtArgs A, const WfArgs W) {
+    const uint32_t n = W.counts[WF_SHADOW];
+    uint32_t slot = 0;
+    f3 origin;
+    Rng rng;
+    Shadow T;
+    bool active = false, drained = false;
+    for (;;) {
+        bool need = !active && !drained;
+        if (__any_sync(0xffffffffu, need)) {
+            uint32_t k = take_item(&W.counts[WF_TAKE_SHADOW], n, need);
+            if (need && k != ~0u) {
+                slot = W.shadow[k];
+                const float4* q = slot_of(W, slot);
+                rng.s = ubits(q[Q_DIR].w);
+                origin = xyz(q[Q_IDX]);
+                tr_begin(A, origin, xyz(q[Q_LD]), T);
+                active = true;
+            }
+            drained = __any_sync(0xffffffffu, need && k == ~0u);
         }
-        push(W.scatter, &W.counts[WF_SCATTER], slot, valid);
+        bool done = false;
+        if (active && !tr_step(A, origin, T, rng)) {
+            active = false;
+            done = true;
+        }
+        if (__any_sync(0xffffffffu, done)) {
+            if (done) {
+                float4* q = slot_of(W, slot);
+                float4 d = q[Q_DIR];
+                q[Q_DIR] = make_float4(d.x, d.y, d.z, fbits(rng.s));
+                q[Q_LT] = f4(T.result, 0.0f);
+            }
+            push(W.scatter, &W.counts[WF_SCATTER], slot, done);
+        }
+        if (drained && !__any_sync(0xffffffffu, active)) break;
     }
     if (blockIdx.x == 0 && threadIdx.x == 0) W.counts[WF_SHADE] = 0;
 }
@@ -376,7 +420,10 @@ __global__ void __launch_bounds__(128, 6) k_wf_scatter(const __grid_constant__ P
         if (refill(A, W, C, slot, need)) to_ext = true;
         push(W.ext[nxt], &W.counts[nxt], slot, to_ext);
     }
-    if (blockIdx.x == 0 && threadIdx.x == 0) W.counts[WF_SHADOW] = 0;
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        W.counts[WF_SHADOW] = 0;
+        W.counts[WF_TAKE_SHADOW] = 0;
+    }
 }
 
 // The paths still alive, run to completion one thread each (the reference's

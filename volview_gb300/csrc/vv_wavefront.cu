@@ -226,7 +226,7 @@ __global__ void __launch_bounds__(256) k_wf_init(const __grid_constant__ PtArgs 
 // ff_step is the loop body of free_flight (pt.comp:307-332). Only what the
 // flight needs stays in registers; the rest of the path is read when it ends.
 #ifndef VV_EXTEND_MIN_BLOCKS
-#define VV_EXTEND_MIN_BLOCKS 4
+#define VV_EXTEND_MIN_BLOCKS 8
 #endif
 enum { EXT_END = 3 };
 __global__ void __launch_bounds__(128, VV_EXTEND_MIN_BLOCKS)
@@ -345,7 +345,7 @@ __global__ void __launch_bounds__(128, 4) k_wf_shade(const __grid_constant__ PtA
 // step (tr_step, the loop body of transmittance, pt.comp:344-369) per
 // iteration, lanes refilled as their rays finish.
 #ifndef VV_SHADOW_MIN_BLOCKS
-#define VV_SHADOW_MIN_BLOCKS 6
+#define VV_SHADOW_MIN_BLOCKS 8
 #endif
 __global__ void __launch_bounds__(128, VV_SHADOW_MIN_BLOCKS) k_wf_shadow(const __grid_constant__ PtArgs A, const WfArgs W) {
     const uint32_t n = W.counts[WF_SHADOW];

@@ -296,6 +296,29 @@ vv_status vv_read_volume(vv_renderer* r, int which, void* out, size_t capacity);
 /* Kernel launches this renderer has issued since creation (for accounting). */
 uint64_t vv_kernel_launches(const vv_renderer* r);
 
+/* --------------------------------------------------- allocation-free denoise */
+
+/* The a-trous denoiser (the passes `record` runs after a frame) on device
+ * buffers the caller owns, for callers that cannot allocate device memory when
+ * they need the image: e.g. a per-frame callback running under a device-memory
+ * budget fixed at start-up, or a process where another runtime owns every
+ * device allocation. No counterpart in the reference.
+ *
+ * accum, albedo, normal: the RGBA32F accumulation images (width*height*4
+ * floats each, as vv_read_accumulation lays them out) on the current device;
+ * hdr: the RGBA16F output (width*height*4 half values); samples: the paths per
+ * pixel accumulated in them. Work is queued on `stream` (a cudaStream_t, NULL
+ * for the legacy default stream) and the call returns without waiting.
+ *
+ * Allocates nothing: its two scratch images live in a fixed device array of
+ * 512 x 512 pixels each (8 MiB, held by every device that loads the library
+ * until the process exits); larger images return VV_ERR_LIMIT. The first call
+ * on a device looks the array's device address up (make it before any stream
+ * capture). All calls share the array: calls that overlap on the GPU race on
+ * it. Each call overwrites the scratch before reading it. */
+vv_status vv_denoise_atrous_noalloc(const float* accum, const float* albedo, const float* normal, uint16_t* hdr,
+                                    uint32_t width, uint32_t height, uint32_t samples, void* stream);
+
 /* Description of the last error on this thread ("" if none). */
 const char* vv_last_error(void);
 

@@ -39,6 +39,11 @@ static vv_status cuda_fail(cudaError_t e, const char* what) {
 
 extern "C" const char* vv_last_error(void) { return g_error.c_str(); }
 
+namespace vv {
+// Error reporting for entry points defined in other translation units.
+vv_status internal_fail(vv_status s, const std::string& msg) { return fail(s, msg); }
+}  // namespace vv
+
 // ---------------------------------------------------------------- defaults
 static float to_radians(float deg) { return deg * (3.14159265358979323846f / 180.0f); }
 

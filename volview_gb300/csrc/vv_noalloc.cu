@@ -1,0 +1,89 @@
+// vv_noalloc.cu — the a-trous denoiser on caller-provided device buffers,
+// without allocating any device memory.
+//
+// Some callers cannot allocate device memory when they want a denoised image:
+// a host application whose per-frame callback runs under a device-memory
+// budget fixed at start-up (an allocation there can fail or stall the frame),
+// or a process where another runtime owns every device allocation and hands
+// out only buffers it manages. This entry point takes the accumulation images
+// and the output from the caller and keeps its two scratch images (the
+// a-trous ping and pong) in a file-scope __device__ array instead.
+//
+// The array holds NOALLOC_MAX_PIXELS pixels per image (512 x 512 RGBA32F,
+// 2 x 4 MiB), and every device that loads the library keeps it until the
+// process exits. Every call shares it: calls whose work overlaps on the GPU
+// (different streams, or different host threads on one device) race on it.
+// Each call overwrites every pixel of the scratch it uses before reading it,
+// so nothing needs clearing between calls.
+#include <cuda_runtime.h>
+
+#include <cstring>
+#include <mutex>
+#include <string>
+
+#include "../../include/volpt.h"
+#include "vv_kernels.h"
+
+namespace vv {
+
+// Largest image, in pixels, the allocation-free denoiser accepts.
+constexpr size_t NOALLOC_MAX_PIXELS = 512 * 512;
+
+// Ping and pong of the a-trous passes (denoise.comp bindings 20-21).
+static __device__ __align__(256) float4 g_atrous_scratch[2 * NOALLOC_MAX_PIXELS];
+
+// Device addresses of g_atrous_scratch, looked up once per device. In host
+// code the array's name is only a host-side stand-in, never a device address.
+static std::mutex g_scratch_mutex;
+static float4* g_scratch_addr[64] = {};
+
+static cudaError_t scratch_on_current_device(float4** out) {
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
+    std::lock_guard<std::mutex> lock(g_scratch_mutex);
+    if (!g_scratch_addr[dev]) {
+        void* p = nullptr;
+        e = cudaGetSymbolAddress(&p, g_atrous_scratch);
+        if (e != cudaSuccess) return e;
+        g_scratch_addr[dev] = (float4*)p;
+    }
+    *out = g_scratch_addr[dev];
+    return cudaSuccess;
+}
+
+vv_status internal_fail(vv_status s, const std::string& msg);
+
+}  // namespace vv
+
+using namespace vv;
+
+extern "C" vv_status vv_denoise_atrous_noalloc(const float* accum, const float* albedo, const float* normal,
+                                               uint16_t* hdr, uint32_t width, uint32_t height, uint32_t samples,
+                                               void* stream) {
+    if (!accum || !albedo || !normal || !hdr) return internal_fail(VV_ERR_ARG, "null buffer");
+    if (width == 0 || height == 0 || samples == 0) return internal_fail(VV_ERR_ARG, "empty image or no samples");
+    if ((size_t)width * height > NOALLOC_MAX_PIXELS)
+        return internal_fail(VV_ERR_LIMIT, "the allocation-free denoiser takes at most " +
+                                               std::to_string(NOALLOC_MAX_PIXELS) + " pixels (512 x 512); got " +
+                                               std::to_string((size_t)width * height));
+    float4* scratch = nullptr;
+    cudaError_t e = scratch_on_current_device(&scratch);
+    if (e != cudaSuccess) return internal_fail(VV_ERR_CUDA, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
+    PostArgs a;
+    memset(&a, 0, sizeof(a));
+    a.u.path[0] = samples;  // samples() of denoise.comp is path.x + path.z
+    a.width = width;
+    a.height = height;
+    a.accum = (const float4*)accum;
+    a.albedo = (const float4*)albedo;
+    a.normal = (const float4*)normal;
+    a.ping = scratch;
+    a.pong = scratch + NOALLOC_MAX_PIXELS;
+    a.hdr = (ushort4*)hdr;
+    int launches = 0;
+    e = launch_denoise(a, (cudaStream_t)stream, &launches);
+    if (e != cudaSuccess) return internal_fail(VV_ERR_CUDA, std::string("denoise launch: ") + cudaGetErrorString(e));
+    return VV_OK;
+}

@@ -51,6 +51,7 @@ EXPORTS = [
     ("vv_pack_uniforms", C.c_int, [P, P, C.c_uint64, P, C.c_size_t]),
     ("vv_read_volume", C.c_int, [P, C.c_int, P, C.c_size_t]),
     ("vv_kernel_launches", C.c_uint64, [P]),
+    ("vv_denoise_atrous_noalloc", C.c_int, [P, P, P, P, C.c_uint32, C.c_uint32, C.c_uint32, P]),
 ]
 # Test hooks (include/volpt_probe.h).
 PROBES = [

@@ -1,17 +1,19 @@
 """Throughput of the progressive path tracer: path samples/s at 1024^2 on the
 512x512x400 head/neck phantom, one GB300.
 
-A step is one accumulate-frame (vv_record: the path-tracing launch, the a-trous
-denoiser and the display passes, as the reference's `record` runs them) of one
-path per pixel over the 1024x1024 image. Inputs stay resident in HBM (the density,
+A step is 16 accumulate-frames of one path per pixel over the 1024x1024 image in
+one wavefront pass (vv_record_frames), then the a-trous denoiser and the display
+passes once; `per_frame_record` times the reference's shape, one vv_record
+(accumulate-frame, a-trous, display) per call. Inputs stay resident in HBM (the density,
 mask, normal and label volumes, 1.2 GB, are larger than the 129 MB L2, so no
 flush is needed between steps).
 
   value     device-timed throughput (CUDA events on the renderer's stream)
   e2e       the same through the C ABI with a host readback of the tone-mapped
             RGBA8 image every step (host wall clock)
-  roofline  the path-tracing kernel: algorithmic bytes per launch (event counts
-            x unique element bytes) / its CUDA-event time, against measured HBM
+  roofline  the path-tracing pass (the wavefront stage kernels of a frame):
+            algorithmic bytes per frame (event counts x unique element bytes)
+            / its CUDA-event time per frame, against measured HBM
   cpu_baseline  the CPU oracle timed on the host cores on a sample of rows
 
 `--impl reference` times the reference's own shaders compiled as CPU code
@@ -46,8 +48,10 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
-    ap.add_argument("--frames-per-step", type=int, default=1,
-                    help="accumulate-frames per step; >1 batches them in one persistent launch (vv_record_frames)")
+    ap.add_argument("--frames-per-step", type=int, default=16,
+                    help="accumulate-frames per step; >1 batches them in one wavefront pass (vv_record_frames)")
+    ap.add_argument("--record-steps", type=int, default=10,
+                    help="also time this many single-frame vv_record calls (0: skip)")
     return ap.parse_args()
 
 
@@ -139,6 +143,18 @@ def frame_params(cfg, center, diagonal):
     return scene.frame_params_for(cfg, center, diagonal, clip_sagittal=True, anisotropy=0.6, spf=1)
 
 
+def bench_config(args, F):
+    W = H = args.size
+    return {"workload": f"head_neck {args.dims.replace(',', 'x')} int16 HU at 0.5x0.5x1 mm, 120 labels, "
+                        f"soft labels, hybrid mode, sagittal clip, g=0.6, studio light, {W}x{H}, "
+                        f"1 path/pixel/frame",
+            "frames_per_step": F,
+            "step": ("vv_record_frames: %d accumulate-frames in one wavefront pass, then a-trous and the "
+                     "tone-mapped display once" % F) if F > 1 else "vv_record",
+            "l2": "inputs larger than L2 (1.2 GB of volumes)",
+            "parallelism": "replicas" if args.gpus > 1 else "single GPU"}
+
+
 def peaks():
     path = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(path):
@@ -149,12 +165,12 @@ def peaks():
 
 
 def ncu_traffic():
-    """DRAM bytes per path-tracing launch from the committed ncu summary, if any."""
-    path = os.path.join(ROOT, "profiles", "pt_persistent_head_neck.md")
+    """DRAM bytes per frame of the path-tracing pass from the committed ncu summary, if any."""
+    path = os.path.join(ROOT, "profiles", "pt_wavefront_head_neck.md")
     if not os.path.exists(path):
         return None
     for line in open(path):
-        if line.strip().startswith("dram_bytes_per_launch:"):
+        if line.strip().startswith("dram_bytes_per_frame:"):
             try:
                 return float(line.split(":", 1)[1].split()[0])
             except ValueError:
@@ -193,38 +209,42 @@ def cpu_sample(cpu, params, width, height, seconds, ref_lib=None):
 
 def run_ours(args, rank, world, local):
     import torch
+    from volview_gb300 import abi
     from volview_gb300 import renderer as R
+    from volview_gb300.renderer import COUNT_BYTES, COUNT_NAMES
     torch.cuda.set_device(local)
     cfg = workload(args)
     W = H = args.size
     stream = torch.cuda.Stream()
     ctx = R.Context(local, stream=stream.cuda_stream)
     r = R.Renderer(ctx, cfg["volume"], cfg["tf"])
-    from volview_gb300 import abi
     r.set_labels(cfg["labels_vol"], abi.soft_struct(cfg["soft"]))
     params = frame_params(cfg, list(r.center), r.diagonal)
     r.resize(W, H)
     F = max(args.frames_per_step, 1)
+    spf = int(params.path_tracing.samples_per_frame)
+    frame = [1]
 
-    def step(f):
+    def step():
+        """One step: F accumulate-frames, then the denoiser and display passes."""
         if F == 1:
-            r.record(f, params)
+            r.record(frame[0], params)
         else:
-            r.record_frames(f, F, params)
-        return f + F
+            r.record_frames(frame[0], F, params)
+        frame[0] += F
 
-    frame = 1
-    r.record(frame, params)  # masks, majorants and the first frame
-    frame += 1
+    def record():
+        r.record(frame[0], params)
+        frame[0] += 1
+
+    record()  # masks, majorants and the first frame
     # Event counts of one frame (untimed) for the roofline's byte model.
     r.count_events(True)
-    r.record(frame, params)
-    frame += 1
+    record()
     counts = r.count_events(False)
     for _ in range(args.warmup):
-        frame = step(frame)
+        step()
     r.synchronize()
-    spf = int(params.path_tracing.samples_per_frame)
     launches0 = r.kernel_launches()
     barrier(world)
     start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -233,7 +253,7 @@ def run_ours(args, rank, world, local):
         r.time_pt(True)
         start.record(stream)
         for _ in range(args.steps):
-            frame = step(frame)
+            step()
         end.record(stream)
         torch.cuda.synchronize()
         pt_ms, pt_launches = r.time_pt(False)
@@ -242,7 +262,27 @@ def run_ours(args, rank, world, local):
     ms = max_over_ranks(start.elapsed_time(end), world)
     samples = args.steps * F * W * H * spf * world
     value = samples / (ms / 1e3)
-    # e2e through the C ABI: record + tone-mapped readback into pinned memory.
+    # The reference's shape for comparison: one vv_record (one accumulate-frame
+    # with the denoiser and display passes) per step.
+    per_frame = None
+    if args.record_steps > 0:
+        for _ in range(2):
+            record()
+        r.synchronize()
+        barrier(world)
+        s0, s1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        s0.record(stream)
+        for _ in range(args.record_steps):
+            record()
+        s1.record(stream)
+        torch.cuda.synchronize()
+        rms = max_over_ranks(s0.elapsed_time(s1), world)
+        per_frame = {"value": args.record_steps * W * H * spf * world / (rms / 1e3), "unit": UNIT,
+                     "ms_per_frame": rms / args.record_steps, "steps": args.record_steps,
+                     "call": "vv_record (one accumulate-frame + a-trous + display per call)"}
+    # e2e through the C ABI: a step plus the tone-mapped RGBA8 readback into
+    # pinned host memory, every step (host wall clock).
     e2e = None
     if not args.no_e2e:
         host = torch.empty((H, W, 4), dtype=torch.uint8).pin_memory()
@@ -250,35 +290,33 @@ def run_ours(args, rank, world, local):
         barrier(world)
         t0 = time.perf_counter()
         for _ in range(args.steps):
-            frame = step(frame)
+            step()
             r.read_output(out)
         t1 = max_over_ranks(time.perf_counter() - t0, world)
         e2e = {"value": samples / t1, "unit": UNIT, "h2d_bytes_per_step": 720,
-               "d2h_bytes_per_step": W * H * 4}
-    acc_samples = r.accumulated_samples()
-    # Roofline of the path-tracing kernel.
-    from volview_gb300.renderer import COUNT_BYTES, COUNT_NAMES
+               "d2h_bytes_per_step": W * H * 4,
+               "call": "vv_record_frames + vv_read_output" if F > 1 else "vv_record + vv_read_output"}
+    # Roofline of the path-tracing pass (the wavefront stage kernels of a frame).
     alg_bytes = float(sum(counts[n] * b for n, b in zip(COUNT_NAMES, COUNT_BYTES)))
-    pt_avg_ms = pt_ms / max(pt_launches, 1) / F
-    achieved = alg_bytes / (pt_avg_ms / 1e3) / 1e9
+    pt_frame_ms = pt_ms / (args.steps * F)
+    achieved = alg_bytes / (pt_frame_ms / 1e3) / 1e9
     peak, peak_kind = peaks()
     traffic = ncu_traffic()
     result = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded head/neck phantom; no CT data ships)",
-        "config": {"workload": f"head_neck {args.dims.replace(',', 'x')} int16 HU at 0.5x0.5x1 mm, 120 labels, "
-                               f"soft labels, hybrid mode, sagittal clip, g=0.6, studio light, {W}x{H}, "
-                               f"1 path/pixel/frame, a-trous + tone-mapped readback per " + ("frame" if F == 1 else f"{F} frames"),
-                   "frames_per_step": F, "l2": "inputs larger than L2 (1.2 GB of volumes)",
-                   "parallelism": "replicas" if world > 1 else "single GPU"},
+        "config": bench_config(args, F),
         "gpu_launches": int(launches),
         "path_vertices_per_s": counts["vertex"] / max(counts["pixel"], 1) * value,
+        "per_frame_record": per_frame,
+        "e2e": e2e,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak, "traffic": traffic, "kernel": "k_pt_persistent",
-                     "peak_source": peak_kind, "alg_bytes_per_launch": alg_bytes,
-                     "avg_launch_ms": pt_avg_ms, "events_per_frame": counts},
-        "accumulated_samples": acc_samples,
+                     "frac": achieved / peak, "traffic": traffic,
+                     "kernel": "path-tracing pass (k_wf_* stage kernels of one frame)",
+                     "peak_source": peak_kind, "alg_bytes_per_frame": alg_bytes,
+                     "ms_per_frame": pt_frame_ms, "pt_launches": int(pt_launches), "events_per_frame": counts},
+        "accumulated_samples": r.accumulated_samples(),
     }
     result["clocks"] = clocks.summary()
     if rank == 0 and not args.no_cpu_baseline:
@@ -369,7 +407,7 @@ def run_reference(args, rank, world):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": total_s / len(rates) * 1e3,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded head/neck phantom)",
-        "config": {"workload": f"head_neck {args.dims.replace(',', 'x')}, {W}x{H}, 1 path/pixel/frame"},
+        "config": bench_config(args, max(args.frames_per_step, 1)),
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": O.threads(), "kind": kind,
                          "sample": f"per step {rates[0][1]} rows spread over the frame; "
                                    + ("shaders/pt.comp compiled as CPU code" if kind == "reference"

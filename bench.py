@@ -35,6 +35,10 @@ sys.path.insert(0, ROOT)
 
 METRIC = "path samples/s at 1024² on 512²×400 CT (1 GB300); time & p50/p99 latency to fixed RMSE"
 UNIT = "path samples/s"
+# Luminance RMSE (against the tracer's converged image) the default view of the
+# 512x512x400 head/neck workload reaches after 1024 paths per pixel at 1024^2.
+RMSE_TARGET = 0.0
+RMSE_TARGET_SPP = 1024
 
 
 def parse():
@@ -52,6 +56,10 @@ def parse():
                     help="accumulate-frames per step; >1 batches them in one wavefront pass (vv_record_frames)")
     ap.add_argument("--record-steps", type=int, default=10,
                     help="also time this many single-frame vv_record calls (0: skip)")
+    ap.add_argument("--rmse-requests", type=int, default=8,
+                    help="views rendered to the fixed RMSE for the time-to-RMSE latencies (0: skip)")
+    ap.add_argument("--rmse-target", type=float, default=RMSE_TARGET,
+                    help="luminance RMSE to reach; 0 measures it on the default view at 1024 paths/pixel")
     return ap.parse_args()
 
 
@@ -179,32 +187,94 @@ def ncu_traffic():
 
 
 def cpu_sample(cpu, params, width, height, seconds, ref_lib=None):
-    """Times the CPU path tracer on spread-out rows; returns (samples/s, rows, threads, seconds)."""
+    """Times the CPU path tracer on about `seconds` of work: rows spread over the
+    frame, or whole frames at successive accumulation indices when one frame
+    takes less. Returns (samples/s, paths, threads, seconds, description)."""
     import ctypes as C
     from oracle import oracle as O
     threads = O.threads()
-    u = cpu.uniforms(params, 1, width, height)
-    scene_c = cpu.scene()
+    scene_c = cpu.scene() if ref_lib is None else None
+    saved = cpu.accumulated
 
-    def run(rows):
+    def run(rows, accumulated):
         rows = np.ascontiguousarray(rows, np.int32)
+        cpu.accumulated = accumulated
+        u = cpu.uniforms(params, accumulated + 1, width, height)
         t = time.perf_counter()
         if ref_lib is None:
             O.lib().vvo_pt_rows(O.ptr(u), C.byref(scene_c), O.ptr(cpu.accum), O.ptr(cpu.albedo), O.ptr(cpu.normal),
                                 O.ptr(cpu.hdr), O.ptr(rows), len(rows), threads)
         else:
+            ref_lib.ref_set_uniforms(O.ptr(u), u.nbytes)
             ref_lib.ref_run_rows(0, width, C.c_void_p(rows.ctypes.data), len(rows), threads)
         return time.perf_counter() - t
 
     # Calibrate on a few rows spread over the frame, then size the sample.
     probe = np.linspace(0, height - 1, 8).astype(np.int32)
-    t = run(probe)
-    per_row = max(t / len(probe), 1e-4)
+    per_row = max(run(probe, 0) / len(probe), 1e-5)
     n = int(min(height, max(8, seconds / per_row)))
-    rows = np.linspace(0, height - 1, n).astype(np.int32)
-    rows = np.unique(rows)
-    t = run(rows)
-    return len(rows) * width / t, len(rows), threads, t
+    rows = np.unique(np.linspace(0, height - 1, n).astype(np.int32))
+    frames, total, k = 0, 0.0, 0
+    while True:
+        total += run(rows, k)
+        frames += 1
+        k += max(int(params.path_tracing.samples_per_frame), 1)
+        if len(rows) < height or total >= seconds:
+            break
+    cpu.accumulated = saved
+    paths = frames * len(rows) * width
+    what = (f"{frames} frames of {width}x{height}" if len(rows) == height else
+            f"{len(rows)} rows spread over the {width}x{height} frame") + f", 1 path/pixel ({paths} paths, {total:.1f} s)"
+    return paths / total, paths, threads, total, what
+
+
+def time_to_rmse(r, params, args, frame, stream):
+    """Latency to a fixed RMSE: views picked at random around the volume, each
+    accumulated (batched frames, display once per chunk) until the RMSE
+    estimated from its accumulation reaches the target; host wall clock from
+    the view's first frame to the check that passes, readbacks included."""
+    import copy
+    from volview_gb300 import convergence as CV
+    target = args.rmse_target
+    source = "fixed (default view, %d paths/pixel)" % RMSE_TARGET_SPP
+    if target <= 0:
+        # Measure the target: the default view at RMSE_TARGET_SPP paths per pixel.
+        done = 0
+        while done < RMSE_TARGET_SPP:
+            n = min(256, RMSE_TARGET_SPP - done)
+            r.record_frames(frame[0], n, params)
+            frame[0] += n
+            done += n
+        acc, alb, _ = r.read_accumulation()
+        target = CV.rmse_estimate(acc, alb, r.accumulated_samples())
+        source = "measured in this run (default view, %d paths/pixel)" % RMSE_TARGET_SPP
+    rng = np.random.default_rng(7)
+    latencies, spps = [], []
+    for _ in range(args.rmse_requests):
+        p = copy.deepcopy(params)
+        p.camera.yaw = float(rng.uniform(0.0, 2.0 * np.pi))
+        p.camera.pitch = float(rng.uniform(-0.5, 0.5))
+        r.synchronize()
+        t0 = time.perf_counter()
+        chunk = 64
+        while True:
+            r.record_frames(frame[0], chunk, p)
+            frame[0] += chunk
+            acc, alb, _ = r.read_accumulation()
+            n = r.accumulated_samples()
+            e = CV.rmse_estimate(acc, alb, n)
+            if e <= target:
+                break
+            chunk = int(min(max(CV.samples_for(e, n, target) - n, 8), 1024))
+        latencies.append(time.perf_counter() - t0)
+        spps.append(n)
+    lat = np.array(latencies)
+    return {"target_rmse": target, "target": source, "requests": len(lat),
+            "p50_s": float(np.percentile(lat, 50)), "p99_s": float(np.percentile(lat, 99)),
+            "mean_s": float(lat.mean()), "paths_per_pixel": spps,
+            "views": "seeded random yaw in [0, 2pi), pitch in [-0.5, 0.5] around the default orbit",
+            "error": "luminance RMSE of the accumulation against the tracer's converged image, "
+                     "estimated from per-pixel sums of luminance and squared luminance"}
 
 
 def run_ours(args, rank, world, local):
@@ -296,6 +366,7 @@ def run_ours(args, rank, world, local):
         e2e = {"value": samples / t1, "unit": UNIT, "h2d_bytes_per_step": 720,
                "d2h_bytes_per_step": W * H * 4,
                "call": "vv_record_frames + vv_read_output" if F > 1 else "vv_record + vv_read_output"}
+    to_rmse = time_to_rmse(r, params, args, frame, stream) if args.rmse_requests > 0 else None
     # Roofline of the path-tracing pass (the wavefront stage kernels of a frame).
     alg_bytes = float(sum(counts[n] * b for n, b in zip(COUNT_NAMES, COUNT_BYTES)))
     pt_frame_ms = pt_ms / (args.steps * F)
@@ -310,6 +381,7 @@ def run_ours(args, rank, world, local):
         "gpu_launches": int(launches),
         "path_vertices_per_s": counts["vertex"] / max(counts["pixel"], 1) * value,
         "per_frame_record": per_frame,
+        "time_to_rmse": to_rmse,
         "e2e": e2e,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": traffic,
@@ -353,11 +425,9 @@ def cpu_renderer_from_device(cfg, r, params):
 
 def cpu_baseline(cfg, r, params, args):
     cpu = cpu_renderer_from_device(cfg, r, params)
-    rate, rows, threads, secs = cpu_sample(cpu, params, r.width, r.height, args.cpu_seconds)
+    rate, paths, threads, secs, what = cpu_sample(cpu, params, r.width, r.height, args.cpu_seconds)
     return {"value": rate, "unit": UNIT, "cores": threads, "kind": "port",
-            "sample": f"{rows} rows spread over the {r.width}x{r.height} frame, 1 path/pixel "
-                      f"({rows * r.width} paths, {secs:.1f} s); CPU restatement of pt.comp, "
-                      f"pre-pass volumes from the device"}
+            "sample": f"{what}; CPU restatement of pt.comp, pre-pass volumes from the device"}
 
 
 def run_reference(args, rank, world):
@@ -396,11 +466,11 @@ def run_reference(args, rank, world):
     rates = []
     per_step = args.cpu_seconds / max(args.steps, 1) * 4
     for i in range(args.warmup + args.steps):
-        rate, rows, threads, secs = cpu_sample(cpu, params, W, H, max(per_step, 1.0), ref_lib)
+        rate, paths, threads, secs, what = cpu_sample(cpu, params, W, H, max(per_step, 1.0), ref_lib)
         if i >= args.warmup:
-            rates.append((rate, rows, secs))
-    total_paths = sum(rt * s for rt, _, s in rates)
-    total_s = sum(s for _, _, s in rates)
+            rates.append((paths, secs, what))
+    total_paths = sum(p for p, _, _ in rates)
+    total_s = sum(s for _, s, _ in rates)
     value = total_paths / total_s
     print(json.dumps({
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
@@ -409,7 +479,7 @@ def run_reference(args, rank, world):
         "data": "synthetic (seeded head/neck phantom)",
         "config": bench_config(args, max(args.frames_per_step, 1)),
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": O.threads(), "kind": kind,
-                         "sample": f"per step {rates[0][1]} rows spread over the frame; "
+                         "sample": f"per step {rates[0][2]}; "
                                    + ("shaders/pt.comp compiled as CPU code" if kind == "reference"
                                       else "CPU restatement of pt.comp")},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},

@@ -251,9 +251,11 @@ vv_status vv_resize(vv_renderer* r, uint32_t width, uint32_t height);
  * VV_ERR_STATE where the reference panics (record before resize). Asynchronous
  * on the context's stream. */
 vv_status vv_record(vv_renderer* r, uint64_t frame, const vv_frame_params* params);
-/* `frames` consecutive accumulate-frames with the same params in one persistent
- * launch; the denoiser and display passes run once, after the last. Equivalent
- * to `frames` calls of vv_record except that intermediate displays are skipped. */
+/* `frames` consecutive accumulate-frames with the same params in one
+ * path-tracing pass; the denoiser and display passes run once, after the last.
+ * Equivalent to `frames` calls of vv_record except that intermediate displays
+ * are skipped. frames x width x height may not exceed 2^31 (VV_ERR_LIMIT).
+ * No counterpart in the reference. */
 vv_status vv_record_frames(vv_renderer* r, uint64_t first_frame, uint32_t frames,
                            const vv_frame_params* params);
 /* Renderer::accumulated_samples (renderer.rs:1217). */

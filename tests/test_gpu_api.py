@@ -109,3 +109,34 @@ def test_render_to_rgba(small_cfg, gpu_ctx):
     assert r.accumulated_samples() == 4
     assert img[..., :3].std() > 0  # something was drawn
     r.destroy()
+
+
+def test_record_frames_rejects_too_many_items(rend):
+    cfg, r, p = rend
+    r.resize(2048, 1024)
+    with pytest.raises(R.VolptError) as e:
+        r.record_frames(1, 1025, p)
+    assert e.value.status == abi.VV_ERR_LIMIT
+    assert r.accumulated_samples() == 0
+
+
+def test_rmse_estimate_matches_a_converged_render(rend):
+    """The RMSE the time-to-RMSE latencies use, estimated from the accumulation,
+    against the error of the same image measured on a 64x longer render."""
+    from volview_gb300 import convergence as CV
+    cfg, r, p = rend
+    p.path_tracing.denoiser = abi.DENOISE_OFF
+    r.resize(64, 48)
+    r.record_frames(1, 64, p)
+    acc, alb, _ = r.read_accumulation()
+    est = CV.rmse_estimate(acc, alb, 64)
+    lum64 = acc[..., :3].astype(np.float64) @ CV.LUMA / 64
+    r.record_frames(65, 4096 - 64, p)
+    assert r.accumulated_samples() == 4096
+    acc2, _, _ = r.read_accumulation()
+    lum4096 = acc2[..., :3].astype(np.float64) @ CV.LUMA / 4096
+    # The long render contains the short one: the difference's expected
+    # square is (63/64)^2 (s^2/64 + s^2/4032) = 0.984 s^2/64.
+    actual = np.sqrt(np.mean((lum64 - lum4096) ** 2)) / np.sqrt(0.984)
+    assert est > 0
+    assert abs(est / actual - 1.0) < 0.1

@@ -920,6 +920,10 @@ extern "C" vv_status vv_record_frames(vv_renderer* r, uint64_t first_frame, uint
                                       const vv_frame_params* params) {
     if (!r || !params) return fail(VV_ERR_ARG, "null argument");
     if (frames == 0) return VV_OK;
+    // Work items are (frame, pixel) pairs counted in 32 bits on the device,
+    // with room left for the counter's overshoot at the end of the pass.
+    if ((uint64_t)frames * r->width * r->height > (1ull << 31))
+        return fail(VV_ERR_LIMIT, "at most 2^31 (frame, pixel) pairs per vv_record_frames call; split the frames");
     UHead u;
     vv_status s = prepare_frame(r, *params, first_frame + frames - 1, u);
     if (s != VV_OK) return s;

@@ -337,11 +337,11 @@ __device__ __forceinline__ float clip_depth(const PtArgs& A, f3 idx, int& plane)
     return depth;
 }
 
-// common.glsl:385-391
-__device__ __forceinline__ Sample sample_point(const PtArgs& A, f3 idx) {
+// sample_point (common.glsl:385-391) at an `idx` the caller has found inside
+// the kept part (clip_depth(idx) <= 0); clipped points have extinction 0.
+__device__ __forceinline__ Sample sample_point_unclipped(const PtArgs& A, f3 idx) {
     Sample s = apply_labels(A, tf_point(A, density_tri(A, idx)), idx);
-    int plane;
-    if (s.ghost || clip_depth(A, idx, plane) > 0.0f) s.extinction = 0.0f;
+    if (s.ghost) s.extinction = 0.0f;
     return s;
 }
 
@@ -363,14 +363,13 @@ __device__ __forceinline__ float2 intersect_volume(const PtArgs& A, f3 o, f3 d) 
     return make_float2(gmax(gmax(tmin.x, tmin.y), gmax(tmin.z, 0.0f)), gmin(gmin(tmax.x, tmax.y), tmax.z));
 }
 
-// common.glsl:421-436
-__device__ __forceinline__ float brick_majorant(const PtArgs& A, f3 idx) {
-    if (A.u.path[3] == 0u) return 1e30f;
-    count(A, COUNT_MAJORANT);
+// The brick of continuous index `idx` whose majorant brick_majorant
+// (common.glsl:421-428) fetches, as an index into the majorant grid.
+__device__ __forceinline__ int brick_index(const PtArgs& A, f3 idx) {
     int bx = clampi((int)floorf((idx.x + 0.5f) * 0.125f), 0, A.vol.bx - 1);
     int by = clampi((int)floorf((idx.y + 0.5f) * 0.125f), 0, A.vol.by - 1);
     int bz = clampi((int)floorf((idx.z + 0.5f) * 0.125f), 0, A.vol.bz - 1);
-    return __ldg(A.majorant + ((long)bz * A.vol.by + by) * A.vol.bx + bx);
+    return (bz * A.vol.by + by) * A.vol.bx + bx;
 }
 // The reciprocal of a ray's index-space direction, zero components replaced
 // by 1e-9 as brick_exit does (common.glsl:433).
@@ -716,8 +715,13 @@ __device__ __forceinline__ f3 event_albedo(const PtArgs& A, const Sample& s) {
     f3 reduced = single_scattering_albedo(s.albedo);
     return measured(A, s) ? 1.0f - (1.0f - reduced) * (1.0f - gclamp(A.u.env[2], 0.0f, 0.95f)) : reduced;
 }
-__device__ __forceinline__ float flight_majorant(const PtArgs& A, f3 p) {
-    float m = brick_majorant(A, p);
+// flight_majorant (pt.comp:157-163) of brick `b` (brick_index).
+__device__ __forceinline__ float flight_majorant_of(const PtArgs& A, int b) {
+    float m = 1e30f;
+    if (A.u.path[3] != 0u) {
+        count(A, COUNT_MAJORANT);
+        m = __ldg(A.majorant + b);
+    }
     if (m > 0.0f && A.u.labels[0] >= 2.0f) m = gmax(m, A.u.tissue[0]);
     return gmin(m, gmax(MAX_EXTINCTION, gmax(A.u.labels[2], A.u.tissue[0])));
 }
@@ -773,9 +777,10 @@ __device__ __noinline__ float bsdf_pdf(f3 n, f3 v, f3 l, const Sample& s) {
 }
 
 // pt.comp:277-292
-__device__ float extinction_at(const PtArgs& A, f3 idx, f3 dir, bool smooth, Sample& s, int& cap_plane, float& cut) {
-    cut = clip_depth(A, idx, cap_plane);
-    if (cut > 0.0f) return 0.0f;
+// extinction_at (pt.comp:277-292) after its clip test: the caller has found
+// `idx` inside the kept part (cut = clip_depth(idx) <= 0).
+__device__ float extinction_unclipped(const PtArgs& A, f3 idx, f3 dir, bool smooth, Sample& s, int& cap_plane,
+                                      float& cut) {
     float d = (smooth && A.u.env[1] > 0.5f) ? density_cubic(A, idx) : density_tri(A, idx);
     s = apply_labels(A, tf_point(A, d), idx);
     if (s.extinction <= 0.0f) return 0.0f;
@@ -793,6 +798,8 @@ struct Flight {
     f3 d_idx, inv_d;
     float tt, t_end;
     int iter;
+    int brick;    // brick whose flight majorant `maj` holds (-1: none yet)
+    float maj;
 };
 enum { FF_CONTINUE = 0, FF_HIT = 1, FF_ESCAPE = 2 };
 
@@ -803,27 +810,43 @@ __device__ __forceinline__ void ff_begin(const PtArgs& A, f3 origin, f3 dir, Fli
     F.tt = tr.x;
     F.t_end = tr.y;
     F.iter = 0;
+    F.brick = -1;
 }
 
 __device__ __forceinline__ int ff_step(const PtArgs& A, f3 origin, f3 dir, bool smooth, int hero, f3& spectral,
                                        Flight& F, f3& idx, Sample& s, int& cap_plane, float& cut, Rng& rng) {
-    if (!(F.iter < 4096 && F.tt < F.t_end)) return FF_ESCAPE;
-    F.iter++;
-    f3 p = origin + F.d_idx * F.tt;
-    float majorant = flight_majorant(A, p);
-    float exit = F.tt + brick_exit(p, F.inv_d) + 1e-3f;
-    if (majorant <= 0.0f) {
-        F.tt = exit;
-        return FF_CONTINUE;
+    // The iterations of pt.comp:307-333 that fetch no voxel run back to back:
+    // empty bricks, samples beyond the brick exit, and tentative collisions in
+    // the clipped part (extinction_at returns 0 there before any fetch). The
+    // step ends at the first tentative collision that needs the volume. The
+    // majorant of the brick the ray is in is fetched once per brick.
+    float majorant;
+    for (;;) {
+        if (!(F.iter < 4096 && F.tt < F.t_end)) return FF_ESCAPE;
+        f3 p = origin + F.d_idx * F.tt;
+        int b = brick_index(A, p);
+        if (b != F.brick) {
+            F.brick = b;
+            F.maj = flight_majorant_of(A, b);
+        }
+        F.iter++;
+        majorant = F.maj;
+        float exit = F.tt + brick_exit(p, F.inv_d) + 1e-3f;
+        if (majorant <= 0.0f) {
+            F.tt = exit;
+            continue;
+        }
+        float next = F.tt - logf(1.0f - rng.rand()) / majorant;
+        if (next >= exit) {
+            F.tt = exit;
+            continue;
+        }
+        F.tt = next;
+        idx = origin + F.d_idx * F.tt;
+        cut = clip_depth(A, idx, cap_plane);
+        if (cut <= 0.0f) break;
     }
-    float next = F.tt - logf(1.0f - rng.rand()) / majorant;
-    if (next >= exit) {
-        F.tt = exit;
-        return FF_CONTINUE;
-    }
-    F.tt = next;
-    idx = origin + F.d_idx * F.tt;
-    float ext = extinction_at(A, idx, dir, smooth, s, cap_plane, cut);
+    float ext = extinction_unclipped(A, idx, dir, smooth, s, cap_plane, cut);
     if (ext <= 0.0f) return FF_CONTINUE;
     f3 sigma = path_sigma(A, s, ext);
     float sh = comp(sigma, hero);
@@ -864,6 +887,9 @@ __device__ __forceinline__ void tr_begin(const PtArgs& A, f3 origin, f3 dir, Sha
 }
 // Returns false when the estimate is final.
 __device__ __forceinline__ bool tr_step(const PtArgs& A, f3 origin, Shadow& T, Rng& rng) {
+    // One iteration of pt.comp:345-370 per call. Samples in the clipped part
+    // need no fetch: sample_point's extinction is 0 there, path_sigma is 0 and
+    // the estimate is multiplied by exactly 1.
     if (!(T.iter < 4096 && T.tt < T.t_end)) return false;
     T.iter++;
     float peak = maxc(T.result);
@@ -875,7 +901,7 @@ __device__ __forceinline__ bool tr_step(const PtArgs& A, f3 origin, Shadow& T, R
         T.result *= 0.1f / peak;
     }
     f3 p = origin + T.d_idx * T.tt;
-    float majorant = flight_majorant(A, p);
+    float majorant = flight_majorant_of(A, brick_index(A, p));
     float exit = T.tt + brick_exit(p, T.inv_d) + 1e-3f;
     if (majorant <= 0.0f) {
         T.tt = exit;
@@ -887,7 +913,10 @@ __device__ __forceinline__ bool tr_step(const PtArgs& A, f3 origin, Shadow& T, R
         return true;
     }
     T.tt = next;
-    Sample m = sample_point(A, origin + T.d_idx * T.tt);
+    f3 q = origin + T.d_idx * T.tt;
+    int plane;
+    if (clip_depth(A, q, plane) > 0.0f) return true;
+    Sample m = sample_point_unclipped(A, q);
     T.result *= gmax(1.0f - path_sigma(A, m, m.extinction) / majorant, 0.0f);
     return true;
 }

@@ -709,7 +709,7 @@ extern "C" vv_status vv_resize(vv_renderer* r, uint32_t width, uint32_t height) 
     CK(r->hdr.alloc(px * 8));
     CK(r->out.alloc(px * 4));
     CK(r->wf_slots.alloc(px * 256));
-    CK(r->wf_queues.alloc(px * 5 * sizeof(uint32_t)));
+    CK(r->wf_queues.alloc(px * 7 * sizeof(uint32_t)));
     CK(r->wf_counts.alloc(WF_COUNTERS * sizeof(uint32_t)));
     if (!r->wf_host_count) CK(cudaMallocHost((void**)&r->wf_host_count, sizeof(uint32_t)));
     uint32_t qw = (width + 3) / 4, qh = (height + 3) / 4;
@@ -793,6 +793,8 @@ static cudaError_t run_pt(vv_renderer* r, PtArgs& a, int* launches) {
     w.shade = q + 2 * px;
     w.shadow = q + 3 * px;
     w.scatter = q + 4 * px;
+    w.esc[0] = q + 5 * px;
+    w.esc[1] = q + 6 * px;
     w.counts = r->wf_counts.as<uint32_t>();
     w.host_count = r->wf_host_count;
     return launch_pt_wavefront(a, w, r->ctx->sms, r->ctx->stream, launches);

@@ -79,11 +79,13 @@ enum {
     WF_ITEMS = 5,     // next (frame, pixel) work item
     WF_TAKE_EXT = 6,  // entries of the extend queue taken so far
     WF_TAKE_SHADOW = 7,  // entries of the shadow queue taken so far
-    WF_COUNTERS = 8
+    WF_ESC0 = 8, WF_ESC1 = 9,  // flights that left the volume or hit the bounce limits
+    WF_COUNTERS = 10
 };
 struct WfArgs {
     float4* slots;
     uint32_t* ext[2];
+    uint32_t* esc[2];
     uint32_t* shade;
     uint32_t* shadow;
     uint32_t* scatter;

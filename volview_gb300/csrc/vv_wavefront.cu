@@ -224,7 +224,9 @@ __global__ void __launch_bounds__(256) k_wf_init(const __grid_constant__ PtArgs 
 // escape, or the bounce limits) hands the path on and takes the next queued
 // path, so lanes with long empty-space flights do not hold up the others.
 // ff_step is the loop body of free_flight (pt.comp:307-332). Only what the
-// flight needs stays in registers; the rest of the path is read when it ends.
+// flight needs stays in registers. Vertices go to shade; escapes and paths at
+// the bounce limits go to this wave's scatter kernel, which finishes them, so
+// this kernel carries none of the escape, accumulation or path-start code.
 #ifndef VV_EXTEND_MIN_BLOCKS
 #define VV_EXTEND_MIN_BLOCKS 8
 #endif
@@ -232,7 +234,6 @@ enum { EXT_END = 3 };
 __global__ void __launch_bounds__(128, VV_EXTEND_MIN_BLOCKS)
     k_wf_extend(const __grid_constant__ PtArgs A, const WfArgs W, int cur) {
     const uint32_t n = W.counts[cur];
-    const int nxt = cur ^ 1;
     const Consts C = make_consts(A);
     uint32_t slot = 0;
     f3 origin, dir, spectral;
@@ -275,33 +276,17 @@ __global__ void __launch_bounds__(128, VV_EXTEND_MIN_BLOCKS)
             }
         }
         if (__any_sync(0xffffffffu, done != 0)) {
-            bool to_shade = false, to_ext = false, need_item = false;
             if (done != 0) {
                 float4* q = slot_of(W, slot);
-                if (done == FF_HIT) {
-                    store_vertex(q, V);
-                    q[Q_DIR] = f4(dir, fbits(rng.s));
-                    float4 s = q[Q_SPEC];
-                    q[Q_SPEC] = f4(spectral, s.w);
-                    to_shade = true;
-                } else {
-                    Path P;
-                    Ctl c;
-                    PixelSums S;
-                    load_path(q, P, c);
-                    P.rng = rng;
-                    P.spectral = spectral;
-                    load_sums(q, S);
-                    if (done == FF_ESCAPE) stage_escape(A, C, P, S);
-                    to_ext = end_path(A, C, P, S, c);
-                    need_item = !to_ext;
-                    store_sums(q, S);
-                    store_path(q, P, c);
-                }
+                if (done == FF_HIT) store_vertex(q, V);
+                q[Q_DIR] = f4(dir, fbits(rng.s));
+                float4 s = q[Q_SPEC];
+                q[Q_SPEC] = f4(spectral, s.w);
+                // Q_CTL.w: whether the scatter kernel runs the escape (pt.comp:431-447).
+                if (done != FF_HIT) ((float*)(q + Q_CTL))[3] = fbits(done == FF_ESCAPE ? 1u : 0u);
             }
-            if (refill(A, W, C, slot, need_item)) to_ext = true;
-            push(W.shade, &W.counts[WF_SHADE], slot, to_shade);
-            push(W.ext[nxt], &W.counts[nxt], slot, to_ext);
+            push(W.shade, &W.counts[WF_SHADE], slot, done == FF_HIT);
+            push(W.esc[cur], &W.counts[WF_ESC0 + cur], slot, done != 0 && done != FF_HIT);
         }
         if (drained && !__any_sync(0xffffffffu, active)) break;
     }
@@ -338,6 +323,7 @@ __global__ void __launch_bounds__(128, 4) k_wf_shade(const __grid_constant__ PtA
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         W.counts[cur] = 0;
         W.counts[WF_TAKE_EXT] = 0;
+        W.counts[WF_ESC0 + (cur ^ 1)] = 0;  // finished by the previous wave's scatter
     }
 }
 
@@ -387,30 +373,36 @@ __global__ void __launch_bounds__(128, VV_SHADOW_MIN_BLOCKS) k_wf_shadow(const _
     if (blockIdx.x == 0 && threadIdx.x == 0) W.counts[WF_SHADE] = 0;
 }
 
+// Scatter, and the end of the flights that left the volume or hit the bounce
+// limits in this wave's extend (queued after the scatter entries).
 __global__ void __launch_bounds__(128, 6) k_wf_scatter(const __grid_constant__ PtArgs A, const WfArgs W, int cur) {
-    uint32_t n = W.counts[WF_SCATTER];
+    uint32_t n_scatter = W.counts[WF_SCATTER], n = n_scatter + W.counts[WF_ESC0 + cur];
     int nxt = cur ^ 1;
     Consts C = make_consts(A);
     WF_FOR_EACH(n) {
         uint32_t i = base_ + (threadIdx.x & 31u);
         bool valid = i < n;
-        uint32_t slot = valid ? W.scatter[i] : 0u;
+        bool ended = i >= n_scatter;
+        uint32_t slot = valid ? (ended ? W.esc[cur][i - n_scatter] : W.scatter[i]) : 0u;
         bool to_ext = false, need = false;
         if (valid) {
             float4* q = slot_of(W, slot);
             Path P;
             Ctl c;
             load_path(q, P, c);
-            Vertex V;
-            load_vertex(q, V);
-            V.n = xyz(q[Q_N]);
-            V.light_dir = xyz(q[Q_LD]);
-            V.light_t = xyz(q[Q_LT]);
-            if (stage_scatter(A, C, P, V)) {
-                to_ext = true;
-            } else {
+            bool escaped = ended && ubits(q[Q_CTL].w) != 0u;
+            if (!ended) {
+                Vertex V;
+                load_vertex(q, V);
+                V.n = xyz(q[Q_N]);
+                V.light_dir = xyz(q[Q_LD]);
+                V.light_t = xyz(q[Q_LT]);
+                to_ext = stage_scatter(A, C, P, V);
+            }
+            if (!to_ext) {
                 PixelSums S;
                 load_sums(q, S);
+                if (escaped) stage_escape(A, C, P, S);
                 to_ext = end_path(A, C, P, S, c);
                 need = !to_ext;
                 store_sums(q, S);

@@ -312,8 +312,8 @@ uint64_t vv_kernel_launches(const vv_renderer* r);
  * pixel accumulated in them. Work is queued on `stream` (a cudaStream_t, NULL
  * for the legacy default stream) and the call returns without waiting.
  *
- * Allocates nothing: its two scratch images live in a fixed device array of
- * 512 x 512 pixels each (8 MiB, held by every device that loads the library
+ * Allocates nothing: its four scratch images live in a fixed device array of
+ * 512 x 512 pixels each (16 MiB, held by every device that loads the library
  * until the process exits); larger images return VV_ERR_LIMIT. The first call
  * on a device looks the array's device address up (make it before any stream
  * capture). All calls share the array: calls that overlap on the GPU race on

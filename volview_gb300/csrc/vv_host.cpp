@@ -210,7 +210,7 @@ struct vv_renderer {
     OpacityKey mask_key, majorant_key;
     // outputs
     uint32_t width = 0, height = 0;
-    DBuf accum, albedo, normal, ping, pong, hdr, out, bloom[4];
+    DBuf accum, albedo, normal, ping, pong, guide_nd, guide_alb, hdr, out, bloom[4];
     int bw[4], bh[4];
     // wavefront tracer: path slots, stage queues, counters
     DBuf wf_slots, wf_queues, wf_counts;
@@ -593,7 +593,7 @@ extern "C" vv_status vv_renderer_destroy(vv_renderer* r) {
     cudaStreamSynchronize(r->ctx->stream);
     DBuf* all[] = {&r->density, &r->normals, &r->mask_a, &r->mask_b, &r->labels, &r->majorant, &r->lut,
                    &r->bucket_dev, &r->tables, &r->soft, &r->work, &r->exposure, &r->accum, &r->albedo,
-                   &r->normal, &r->ping, &r->pong, &r->hdr, &r->out, &r->bloom[0], &r->bloom[1], &r->bloom[2],
+                   &r->normal, &r->ping, &r->pong, &r->guide_nd, &r->guide_alb, &r->hdr, &r->out, &r->bloom[0], &r->bloom[1], &r->bloom[2],
                    &r->bloom[3]};
     for (DBuf* b : all) b->release();
     r->wf_slots.release();
@@ -706,6 +706,8 @@ extern "C" vv_status vv_resize(vv_renderer* r, uint32_t width, uint32_t height) 
     CK(r->normal.alloc(px * 16));
     CK(r->ping.alloc(px * 16));
     CK(r->pong.alloc(px * 16));
+    CK(r->guide_nd.alloc(px * 16));
+    CK(r->guide_alb.alloc(px * 16));
     CK(r->hdr.alloc(px * 8));
     CK(r->out.alloc(px * 4));
     CK(r->wf_slots.alloc(px * 256));
@@ -811,6 +813,8 @@ static PostArgs post_args(vv_renderer* r, const UHead& u) {
     a.normal = r->normal.as<float4>();
     a.ping = r->ping.as<float4>();
     a.pong = r->pong.as<float4>();
+    a.guide_nd = r->guide_nd.as<float4>();
+    a.guide_alb = r->guide_alb.as<float4>();
     a.hdr = r->hdr.as<ushort4>();
     for (int i = 0; i < 4; i++) {
         a.bloom[i] = r->bloom[i].as<ushort4>();

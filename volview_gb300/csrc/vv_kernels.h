@@ -107,6 +107,8 @@ struct PostArgs {
     const float4* normal;
     float4* ping;
     float4* pong;
+    float4* guide_nd;    // denoiser guides per pixel: mean normal (normalised) and depth
+    float4* guide_alb;   // mean albedo (floored at 0.02), w unused
     ushort4* hdr;
     ushort4* bloom[4];   // A, B (quarter), C, D (eighth)
     int bw[4], bh[4];

@@ -6,12 +6,12 @@
 // budget fixed at start-up (an allocation there can fail or stall the frame),
 // or a process where another runtime owns every device allocation and hands
 // out only buffers it manages. This entry point takes the accumulation images
-// and the output from the caller and keeps its two scratch images (the
-// a-trous ping and pong) in a file-scope __device__ array instead.
+// and the output from the caller and keeps its scratch images (the a-trous
+// ping and pong and the guides) in a file-scope __device__ array instead.
 //
-// The array holds NOALLOC_MAX_PIXELS pixels per image (512 x 512 RGBA32F,
-// 2 x 4 MiB), and every device that loads the library keeps it until the
-// process exits. Every call shares it: calls whose work overlaps on the GPU
+// The array holds four images of NOALLOC_MAX_PIXELS pixels (512 x 512
+// RGBA32F: ping, pong and the two edge-stopping guides, 4 x 4 MiB), and every
+// device that loads the library keeps it until the process exits. Every call shares it: calls whose work overlaps on the GPU
 // (different streams, or different host threads on one device) race on it.
 // Each call overwrites every pixel of the scratch it uses before reading it,
 // so nothing needs clearing between calls.
@@ -29,8 +29,9 @@ namespace vv {
 // Largest image, in pixels, the allocation-free denoiser accepts.
 constexpr size_t NOALLOC_MAX_PIXELS = 512 * 512;
 
-// Ping and pong of the a-trous passes (denoise.comp bindings 20-21).
-static __device__ __align__(256) float4 g_atrous_scratch[2 * NOALLOC_MAX_PIXELS];
+// Ping and pong of the a-trous passes (denoise.comp bindings 20-21), then the
+// per-pixel guides the passes read.
+static __device__ __align__(256) float4 g_atrous_scratch[4 * NOALLOC_MAX_PIXELS];
 
 // Device addresses of g_atrous_scratch, looked up once per device. In host
 // code the array's name is only a host-side stand-in, never a device address.
@@ -81,6 +82,8 @@ extern "C" vv_status vv_denoise_atrous_noalloc(const float* accum, const float* 
     a.normal = (const float4*)normal;
     a.ping = scratch;
     a.pong = scratch + NOALLOC_MAX_PIXELS;
+    a.guide_nd = scratch + 2 * NOALLOC_MAX_PIXELS;
+    a.guide_alb = scratch + 3 * NOALLOC_MAX_PIXELS;
     a.hdr = (ushort4*)hdr;
     int launches = 0;
     e = launch_denoise(a, (cudaStream_t)stream, &launches);

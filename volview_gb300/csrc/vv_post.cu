@@ -60,6 +60,9 @@ __global__ void k_denoise_prepare(const PostArgs a) {
         }
     float spatial = gmax(s2 / 25.0f - (s1 / 25.0f) * (s1 / 25.0f), 0.0f);
     float variance = gmax(temporal, spatial * gmin(1.0f, 4.0f / n));
+    // The edge-stopping guides every level reads at every tap, computed once.
+    a.guide_nd[i] = mean_normal_depth(a, i, n);
+    a.guide_alb[i] = make_float4(alb.x, alb.y, alb.z, 0.0f);
     float al = lum(alb.x, alb.y, alb.z);
     a.ping[i] = make_float4(irr.x, irr.y, irr.z, variance / (al * al));
 }
@@ -71,12 +74,12 @@ __global__ void k_denoise_level(const PostArgs a, int step, int from_pong) {
     if (x >= W || y >= H) return;
     const float4* src = from_pong ? a.pong : a.ping;
     float4* dst = from_pong ? a.ping : a.pong;
-    float n = samples_of(a);
     int i = y * W + x;
     float4 center = src[i];
-    float4 geo = mean_normal_depth(a, i, n);
+    float4 geo = a.guide_nd[i];
     f3 gxyz = mk(geo.x, geo.y, geo.z);
-    f3 alb = mean_albedo(a, i, n);
+    float4 ga = a.guide_alb[i];
+    f3 alb = mk(ga.x, ga.y, ga.z);
     float l_center = lum(center.x, center.y, center.z);
     float bv = 0.0f;
     for (int dy = -1; dy <= 1; dy++)
@@ -95,13 +98,14 @@ __global__ void k_denoise_level(const PostArgs a, int step, int from_pong) {
             if (qx < 0 || qy < 0 || qx >= W || qy >= H) continue;
             int j = qy * W + qx;
             float4 c = src[j];
-            float4 g = mean_normal_depth(a, j, n);
+            float4 g = a.guide_nd[j];
             f3 gq = mk(g.x, g.y, g.z);
             float w_normal = powf(gmax(dot(gxyz, gq), 0.0f), 64.0f);
             bool q_flat = dot(gq, gq) < 0.5f;
             if (center_flat || q_flat) w_normal = (center_flat && q_flat) ? 1.0f : 0.0f;
             float w_depth = expf(-fabsf(geo.w - g.w) / (0.02f * geo.w + 1e-3f));
-            f3 da = alb - mean_albedo(a, j, n);
+            float4 gb = a.guide_alb[j];
+            f3 da = alb - mk(gb.x, gb.y, gb.z);
             float w_albedo = expf(-dot(da, da) / 0.01f);
             float w_lum = expf(-fabsf(l_center - lum(c.x, c.y, c.z)) / sigma_l);
             float w = kernel[abs(dx)] * kernel[abs(dy)] * w_normal * w_depth * w_albedo * w_lum;
@@ -122,7 +126,8 @@ __global__ void k_denoise_finish(const PostArgs a, int from_pong) {
     float n = samples_of(a);
     int i = y * W + x;
     float4 c = (from_pong ? a.pong : a.ping)[i];
-    f3 alb = mean_albedo(a, i, n);
+    float4 ga = a.guide_alb[i];
+    f3 alb = mk(ga.x, ga.y, ga.z);
     a.hdr[i] = to_h4(make_float4(c.x * alb.x, c.y * alb.y, c.z * alb.z, a.accum[i].w / n));
 }
 
@@ -153,16 +158,29 @@ __global__ void k_bloom_down4(const PostArgs a) {
     a.bloom[0][y * a.bw[0] + x] = to_h4(make_float4(sum.x / weights, sum.y / weights, sum.z / weights, coverage / 16.0f));
 }
 
-// bloom.comp pass 1: one 64-thread block meters the covered pixels and adapts.
-__global__ void k_exposure(const PostArgs a) {
+// bloom.comp pass 1 (auto exposure), in two kernels. The terms of the
+// exposure sums, one thread per pixel of A (coverage-weighted log luminance,
+// coverage), into `terms` (a float2 per pixel).
+__global__ void k_exposure_terms(const PostArgs a, float2* terms) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= a.bw[0] * a.bh[0]) return;
+    float4 c = h4(a.bloom[0][i]);
+    float l = logf(gmax(lum(c.x, c.y, c.z), 1e-4f));
+    terms[i] = make_float2(__fmul_rn(c.w, l), c.w);
+}
+
+// The sums themselves, in the workgroup's order (thread t adds pixels t,
+// t + 64, ... in turn, then a tree over the 64 partial sums), so the result
+// is the one-workgroup shader's to the bit.
+__global__ void k_exposure(const PostArgs a, const float2* terms) {
     __shared__ float log_sum[64], weight_sum[64];
     int t = threadIdx.x;
     int n = a.bw[0] * a.bh[0];
     float s = 0.0f, w = 0.0f;
     for (int i = t; i < n; i += 64) {
-        float4 c = h4(a.bloom[0][i]);
-        s += c.w * logf(gmax(lum(c.x, c.y, c.z), 1e-4f));
-        w += c.w;
+        float2 term = terms[i];
+        s += term.x;
+        w += term.y;
     }
     log_sum[t] = s;
     weight_sum[t] = w;
@@ -317,14 +335,17 @@ cudaError_t launch_denoise(const PostArgs& a, cudaStream_t s, int* launches) {
 
 cudaError_t launch_post(const PostArgs& a, cudaStream_t s, int* launches) {
     k_bloom_down4<<<grid16(a.bw[0], a.bh[0]), 256, 0, s>>>(a);
-    k_exposure<<<1, 64, 0, s>>>(a);
+    // The exposure terms go to the denoiser's ping image, free after the denoiser.
+    int npx = a.bw[0] * a.bh[0];
+    k_exposure_terms<<<(npx + 255) / 256, 256, 0, s>>>(a, (float2*)a.ping);
+    k_exposure<<<1, 64, 0, s>>>(a, (const float2*)a.ping);
     k_bloom_blur<<<grid16(a.bw[0], a.bh[0]), 256, 0, s>>>(a.bloom[0], a.bloom[1], a.bw[0], a.bh[0], 1, 0);
     k_bloom_blur<<<grid16(a.bw[0], a.bh[0]), 256, 0, s>>>(a.bloom[1], a.bloom[0], a.bw[0], a.bh[0], 0, 1);
     k_bloom_down2<<<grid16(a.bw[2], a.bh[2]), 256, 0, s>>>(a);
     k_bloom_blur<<<grid16(a.bw[2], a.bh[2]), 256, 0, s>>>(a.bloom[2], a.bloom[3], a.bw[2], a.bh[2], 1, 0);
     k_bloom_blur<<<grid16(a.bw[2], a.bh[2]), 256, 0, s>>>(a.bloom[3], a.bloom[2], a.bw[2], a.bh[2], 0, 1);
     k_tonemap<<<grid16(a.width, a.height), 256, 0, s>>>(a);
-    *launches += 8;
+    *launches += 9;
     return cudaGetLastError();
 }
 

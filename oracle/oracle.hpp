@@ -62,6 +62,9 @@ struct Scene {
     ivec3 brick_dims;
     const uint16_t* tf_lut = nullptr;    // RGBA16F, 4096 entries
     const float* preint = nullptr;       // RGBA32F, 4096 entries
+    const uint16_t* env_rad = nullptr;   // light map radiance, RGBA16F, env_dims
+    const float* env_table = nullptr;    // light map sampling table, RG32F, (env_dims.x + 1) x env_dims.y
+    ivec2 env_dims = ivec2(1, 1);
 };
 
 }  // namespace vvo

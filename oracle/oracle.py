@@ -18,7 +18,7 @@ P = C.c_void_p
 class Scene(C.Structure):
     _fields_ = [("dims", C.c_int * 3), ("density", P), ("normals", P), ("mask", P), ("labels", P),
                 ("label_dims", C.c_int * 3), ("majorant", P), ("brick_dims", C.c_int * 3), ("tf_lut", P),
-                ("preint", P)]
+                ("preint", P), ("env_rad", P), ("env_table", P), ("env_dims", C.c_int * 2)]
 
 
 class Geometry(C.Structure):
@@ -41,6 +41,8 @@ def lib():
         _lib.vvo_tf_evaluate.argtypes = [P, C.c_float, P]
         _lib.vvo_pack_uniforms.argtypes = [P, P, C.c_int, C.c_int, C.c_float, P, C.c_uint32, C.c_uint64,
                                            C.c_uint32, C.c_uint32, P]
+        _lib.vvo_env_prepare.restype = C.c_float
+        _lib.vvo_env_prepare.argtypes = [C.c_int, C.c_int, P, P, P]
     return _lib
 
 
@@ -83,6 +85,18 @@ def hu_to_unorm16(hu):
     out = np.zeros(hu.shape, np.uint16)
     lib().vvo_hu_to_unorm16(ptr(hu), C.c_long(hu.size), ptr(out))
     return out
+
+
+def env_prepare(rgb):
+    """EnvironmentMap::prepare + upload (environment.rs:57-130, renderer.rs:2224-2290) of an
+    (h, w, 3) linear-RGB light map: (RGBA16F radiance (h, w, 4) uint16, RG32F table
+    (h, w + 1, 2), peak_u)."""
+    rgb = np.ascontiguousarray(rgb, np.float32)
+    h, w = rgb.shape[:2]
+    rad = np.zeros((h, w, 4), np.uint16)
+    table = np.zeros((h, w + 1, 2), np.float32)
+    peak = lib().vvo_env_prepare(w, h, ptr(rgb), ptr(rad), ptr(table))
+    return rad, table, float(peak)
 
 
 def geometry(volume):
@@ -130,6 +144,8 @@ class CpuRenderer:
         self.mask_key = None
         self.accumulated = 0
         self.accum_key = None
+        self.env_rad = self.env_table = None
+        self.env_peak_u = 0.0
         zero = self._uniforms_geometry_only()
         self.normals = np.zeros(self.density.shape + (4,), np.int8)
         lib().vvo_normals(ptr(zero), C.byref(self.scene()), ptr(self.normals), threads())
@@ -162,6 +178,15 @@ class CpuRenderer:
         self.has_labels = True
         self.mask_key = None
 
+    def set_environment_map(self, rgb=None):
+        """Renderer::set_environment_map (renderer.rs:1283): (h, w, 3) linear RGB, or None."""
+        if rgb is None:
+            self.env_rad = self.env_table = None
+            self.env_peak_u = 0.0
+        else:
+            self.env_rad, self.env_table, self.env_peak_u = env_prepare(rgb)
+        self.accum_key = None
+
     def brick_dims(self):
         return tuple((d + 7) // 8 for d in self.dims)
 
@@ -177,12 +202,19 @@ class CpuRenderer:
         s.brick_dims[:] = self.brick_dims()
         s.tf_lut = ptr(self.lut)
         s.preint = ptr(self.preint)
+        if self.env_rad is not None:
+            s.env_rad = ptr(self.env_rad)
+            s.env_table = ptr(self.env_table)
+            s.env_dims[:] = (self.env_rad.shape[1], self.env_rad.shape[0])
+        else:
+            s.env_dims[:] = (1, 1)
         s._keep = self
         return s
 
     def uniforms(self, params, frame, width, height):
         return pack_uniforms(self.volume, self.bucket, params, self.accumulated, frame, width, height,
-                             has_labels=self.has_labels)
+                             has_labels=self.has_labels, has_env_map=self.env_rad is not None,
+                             env_peak_u=self.env_peak_u)
 
     def adopt(self, mask=None, majorant=None, normals=None):
         """Takes the pre-pass volumes from elsewhere (e.g. the device), so that a

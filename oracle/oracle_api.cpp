@@ -28,6 +28,7 @@ void bspline(const Uniforms& u, const Scene& sc, const float* idx, long n, float
 void denoise(const Uniforms& u, const float* accum, const float* albedo, const float* normal, uint16_t* hdr,
              float* ping, float* pong, int threads);
 void post(const Uniforms& u, const uint16_t* hdr, float* exposure, uint8_t* out);
+float env_prepare(int w, int h, const float* pixels, uint16_t* radiance, float* table);
 }  // namespace vvo
 
 using namespace vvo;
@@ -46,6 +47,9 @@ typedef struct vvo_scene {
     int brick_dims[3];
     const uint16_t* tf_lut;
     const float* preint;
+    const uint16_t* env_rad;
+    const float* env_table;
+    int env_dims[2];
 } vvo_scene;
 
 typedef struct vvo_geometry {
@@ -70,11 +74,21 @@ static Scene to_scene(const vvo_scene* s) {
     sc.brick_dims = ivec3(s->brick_dims[0], s->brick_dims[1], s->brick_dims[2]);
     sc.tf_lut = s->tf_lut;
     sc.preint = s->preint;
+    sc.env_rad = s->env_rad;
+    sc.env_table = s->env_table;
+    sc.env_dims = ivec2(s->env_dims[0], s->env_dims[1]);
     return sc;
 }
 static const Uniforms& U(const void* p) { return *(const Uniforms*)p; }
 
 long vvo_uniform_size(void) { return (long)sizeof(Uniforms); }
+
+// EnvironmentMap::prepare (environment.rs:57-130) and the RGBA16F upload
+// (renderer.rs:2224-2290): radiance as half RGBA (w x h), the sampling table
+// (RG32F, (w + 1) x h); returns peak_u.
+float vvo_env_prepare(int w, int h, const float* pixels, uint16_t* radiance, float* table) {
+    return env_prepare(w, h, pixels, radiance, table);
+}
 
 void vvo_hu_to_unorm16(const int16_t* hu, long n, uint16_t* out) {
     for (long i = 0; i < n; i++) out[i] = hu_to_unorm16(hu[i]);

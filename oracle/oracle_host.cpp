@@ -295,4 +295,71 @@ int mask_margin(const Geometry& G, const vv_label_params& l) {
     return int(m);
 }
 
+
+// ------------------------------------------------------------ light map
+// environment.rs:57-130 (EnvironmentMap::prepare without the diffuse
+// convolution, which only the ray marcher reads) and the upload of
+// renderer.rs:2224-2290 (radiance to RGBA16F after min(60000)). Sums run in
+// f64 in the Rust's order; per-texel arithmetic in f32 without contraction.
+static float env_luminance(const float* c) { return 0.2126f * c[0] + 0.7152f * c[1] + 0.0722f * c[2]; }
+
+float env_prepare(int w, int h, const float* pixels, uint16_t* radiance, float* table) {
+    const float PI_F = 3.14159265358979323846f;
+    auto sin_theta = [&](int y) { return std::sin(PI_F * ((float)y + 0.5f) / (float)h); };
+    // Mean radiance over the sphere (texels weighted by their solid angle).
+    double sum[3] = {0.0, 0.0, 0.0}, weight = 0.0;
+    for (int y = 0; y < h; y++) {
+        float s = sin_theta(y);
+        double row[3] = {0.0, 0.0, 0.0};
+        for (int x = 0; x < w; x++)
+            for (int i = 0; i < 3; i++) row[i] = row[i] + (double)pixels[3 * ((long)y * w + x) + i];
+        for (int i = 0; i < 3; i++) sum[i] = sum[i] + row[i] * (double)s;
+        weight = weight + (double)s * (double)w;
+    }
+    float mean_rgb[3] = {(float)(sum[0] / weight), (float)(sum[1] / weight), (float)(sum[2] / weight)};
+    float mean = std::max(env_luminance(mean_rgb), 1e-6f);
+    for (long i = 0; i < (long)w * h; i++) {
+        for (int c = 0; c < 3; c++) radiance[4 * i + c] = glsl::float_to_half(std::min(pixels[3 * i + c] / mean, 60000.0f));
+        radiance[4 * i + 3] = glsl::float_to_half(1.0f);
+    }
+    // Importance sampling proportional to luminance x solid angle.
+    std::vector<float> f((size_t)w * h);
+    for (long i = 0; i < (long)w * h; i++) f[i] = env_luminance(pixels + 3 * i) * sin_theta((int)(i / w));
+    std::vector<double> row_sums(h);
+    for (int y = 0; y < h; y++) {
+        double a = 0.0;
+        for (int x = 0; x < w; x++) a = a + (double)f[(long)y * w + x];
+        row_sums[y] = a;
+    }
+    double total = 0.0;
+    for (int y = 0; y < h; y++) total = total + row_sums[y];
+    total = std::max(total, (double)1e-12L);  // f64 constants: L-suffixed (floats otherwise)
+    double marginal = 0.0;
+    for (int y = 0; y < h; y++) {
+        float* row = table + 2 * (long)y * (w + 1);
+        double acc = 0.0;
+        for (int x = 0; x < w; x++) {
+            acc = acc + (double)f[(long)y * w + x];
+            row[2 * x] = row_sums[y] > 0.0 ? (float)(acc / row_sums[y]) : (float)(x + 1) / (float)w;
+            row[2 * x + 1] = (float)((double)f[(long)y * w + x] / total);
+        }
+        row[2 * (w - 1)] = 1.0f;
+        marginal = marginal + row_sums[y];
+        row[2 * w] = (float)(marginal / total);
+        row[2 * w + 1] = (float)(row_sums[y] / total);
+    }
+    table[2 * ((long)(h - 1) * (w + 1) + w)] = 1.0f;
+    // Brightest region: azimuth of the squared-luminance-weighted mean direction.
+    double px = 0.0, pz = 0.0;
+    for (int y = 0; y < h; y++)
+        for (int x = 0; x < w; x++) {
+            double l = (double)f[(long)y * w + x];
+            float uu = ((float)x + 0.5f) / (float)w, vv = ((float)y + 0.5f) / (float)h;
+            float phi = (uu - 0.5f) * 2.0f * PI_F, theta = vv * PI_F;
+            float dx = std::sin(theta) * std::sin(phi), dz = std::sin(theta) * std::cos(phi);
+            px = px + l * l * (double)dx;
+            pz = pz + l * l * (double)dz;
+        }
+    return 0.5f + (float)(std::atan2(px, pz) / (double)(2.0L * 3.14159265358979323846264338327950288L));
+}
 }  // namespace vvo

@@ -24,6 +24,7 @@ struct Units {
     sampler3D density, normals, mask, majorant, mask_b;
     usampler3D labels, soft;
     sampler1D tf, preint;
+    sampler2D env, env_table;  // light map (bindings 25, 26)
 };
 
 static void bind3(glsl::Texture& t, const void* data, glsl::Format f, ivec3 d, glsl::Filter filt) {
@@ -40,6 +41,10 @@ Units bind_scene(const Scene& s) {
     if (s.labels) bind3(t.labels, s.labels, glsl::R8_UINT, s.label_dims, glsl::NEAREST);
     if (s.tf_lut) bind3(t.tf, s.tf_lut, glsl::RGBA16F, ivec3(4096, 1, 1), glsl::LINEAR);
     if (s.preint) bind3(t.preint, s.preint, glsl::RGBA32F, ivec3(4096, 1, 1), glsl::NEAREST);
+    if (s.env_rad) {
+        bind3(t.env, s.env_rad, glsl::RGBA16F, ivec3(s.env_dims.x, s.env_dims.y, 1), glsl::LINEAR);
+        bind3(t.env_table, s.env_table, glsl::RG32F, ivec3(s.env_dims.x + 1, s.env_dims.y, 1), glsl::NEAREST);
+    }
     return t;
 }
 
@@ -509,8 +514,27 @@ struct Tracer : Shading {
     vec3 amb() const { return vec3(u.ambient.x, u.ambient.y, u.ambient.z); }
     vec3 lightdir() const { return vec3(u.light_dir.x, u.light_dir.y, u.light_dir.z); }
 
-    // pt.comp:56-82 (the light map, lighting.w == 2, is not bound here)
+    // common.glsl:459-485: light map coordinates, directions and radiance.
+    vec2 env_uv(vec3 d) const {
+        vec3 f = fwd(), r = rgt(), up = upv();
+        float phi = atan(dot(d, r), dot(d, f));
+        float theta = acos(clamp(dot(d, up), -1.0f, 1.0f));
+        return vec2(fract(0.5f + (phi + u.env.x) / (2.0f * PI)), theta / PI);
+    }
+    vec3 env_direction(vec2 uv) const {
+        float phi = (uv.x - 0.5f) * 2.0f * PI - u.env.x;
+        float theta = uv.y * PI;
+        vec3 f = fwd(), r = rgt(), up = upv();
+        return sin(theta) * (sin(phi) * r + cos(phi) * f) + cos(theta) * up;
+    }
+    vec3 env_map_radiance(vec3 d) const {
+        vec4 c = textureLod(t.env, env_uv(d), 0.0f);
+        return amb() * vec3(c.x, c.y, c.z);
+    }
+
+    // pt.comp:56-82
     vec3 environment(vec3 d) const {
+        if (u.lighting.w == 2u) return env_map_radiance(d);
         if (u.lighting.w == 1u) {
             vec3 f = fwd(), r = rgt(), up = upv();
             float key_side = dot(lightdir(), r) >= 0.0f ? 1.0f : -1.0f;
@@ -642,6 +666,42 @@ struct Tracer : Shading {
         }
         return false;
     }
+    // pt.comp:193-200: solid-angle pdf of light map direction `d`.
+    float env_pdf(vec3 d) const {
+        ivec2 size = textureSize(t.env, 0);
+        vec2 uv = env_uv(d);
+        ivec2 texel = min(ivec2(int(uv.x * float(size.x)), int(uv.y * float(size.y))), size - 1);
+        float p = texelFetch(t.env_table, texel, 0).y;
+        return p * float(size.x * size.y) / (2.0f * PI * PI * max(sin(uv.y * PI), 1e-6f));
+    }
+    // pt.comp:204-233: a light map direction by luminance (binary searches of
+    // the marginal and the row's conditional CDF).
+    vec3 sample_env(float& pdf) {
+        ivec2 size = textureSize(t.env, 0);
+        float xi = rand();
+        int lo = 0, hi = size.y - 1;
+        while (lo < hi) {
+            int mid = (lo + hi) / 2;
+            if (texelFetch(t.env_table, ivec2(size.x, mid), 0).x >= xi) hi = mid;
+            else lo = mid + 1;
+        }
+        int y = lo;
+        xi = rand();
+        lo = 0;
+        hi = size.x - 1;
+        while (lo < hi) {
+            int mid = (lo + hi) / 2;
+            if (texelFetch(t.env_table, ivec2(mid, y), 0).x >= xi) hi = mid;
+            else lo = mid + 1;
+        }
+        float jx = rand();
+        float jy = rand();
+        vec2 uv = (vec2(float(lo), float(y)) + vec2(jx, jy)) / vec2(float(size.x), float(size.y));
+        float p = texelFetch(t.env_table, ivec2(lo, y), 0).y;
+        pdf = p * float(size.x * size.y) / (2.0f * PI * PI * max(sin(uv.y * PI), 1e-6f));
+        return env_direction(uv);
+    }
+
     // pt.comp:339-371: ratio tracking with Russian roulette.
     vec3 transmittance(vec3 origin, vec3 dir) {
         vec3 d_idx = w2i3() * dir;
@@ -681,6 +741,7 @@ struct Tracer : Shading {
         float cos_light = cos(u.material.w);
         bool area_light = u.material.w > 1e-4f;
         float light_pdf = area_light ? 1.0f / (2.0f * PI * (1.0f - cos_light)) : 0.0f;
+        bool env_map = u.lighting.w == 2u;
         mat3 to_index = w2i3();
         vec4 e4 = u.world_to_index * vec4(u.eye.x, u.eye.y, u.eye.z, 1.0f);
         vec3 eye_idx(e4.x, e4.y, e4.z);
@@ -717,7 +778,8 @@ struct Tracer : Shading {
                         R.normal_sum.w += 1e4f;
                     } else {
                         vec3 path_weight = throughput * spectral / dot(spectral, vec3(1.0f / 3.0f));
-                        radiance += path_weight * environment(dir) * 1.0f;
+                        float weight = env_map ? mis(last_pdf, env_pdf(dir)) : 1.0f;
+                        radiance += path_weight * environment(dir) * weight;
                         if (area_light && dot(dir, lightdir()) >= cos_light)
                             radiance += path_weight * light * light_pdf * mis(last_pdf, light_pdf);
                     }
@@ -737,6 +799,13 @@ struct Tracer : Shading {
                 }
                 vec3 light_dir = sample_light(light_frame);
                 vec3 light_t = transmittance(idx, light_dir);
+                float map_pdf = 0.0f;
+                vec3 map_dir(0.0f), map_light(0.0f);
+                if (env_map) {
+                    map_dir = sample_env(map_pdf);
+                    map_light = env_map_radiance(map_dir) / max(map_pdf, 1e-8f);
+                    if (map_pdf > 0.0f) map_light *= transmittance(idx, map_dir);
+                }
                 if (surface_event) {
                     n = dot(n, v) < 0.0f ? -n : n;
                     vec3 diffuse;
@@ -744,6 +813,11 @@ struct Tracer : Shading {
                     float light_weight = area_light ? mis(light_pdf, bsdf_pdf(n, v, light_dir, s)) : 1.0f;
                     radiance += path_weight * (diffuse + specular) * max(dot(n, light_dir), 0.0f) * light * light_t *
                                 light_weight;
+                    if (map_pdf > 0.0f && dot(n, map_dir) > 0.0f) {
+                        specular = brdf_coated(n, v, map_dir, s, diffuse);
+                        radiance += path_weight * (diffuse + specular) * dot(n, map_dir) * map_light *
+                                    mis(map_pdf, bsdf_pdf(n, v, map_dir, s));
+                    }
                     mat3 frame = basis(n);
                     vec3 l;
                     if (rand() < coat_share(s)) {
@@ -769,6 +843,10 @@ struct Tracer : Shading {
                     float light_phase = phase_hg(dot(dir, light_dir));
                     radiance += path_weight * albedo * light_phase * light * light_t *
                                 (area_light ? mis(light_pdf, light_phase) : 1.0f);
+                    if (map_pdf > 0.0f) {
+                        float phase = phase_hg(dot(dir, map_dir));
+                        radiance += path_weight * albedo * phase * map_light * mis(map_pdf, phase);
+                    }
                     throughput *= albedo;
                     volumes++;
                     origin = idx;

@@ -61,6 +61,10 @@ def bind_common(l, r, dummy):
     if getattr(r, "majorant", None) is not None:
         bw, bh, bd = r.majorant.shape[::-1]
         l.ref_bind_texture(b"majorant_tex", _p(r.majorant), R32F, bw, bh, bd, NEAREST, 0)
+    if getattr(r, "env_rad", None) is not None:
+        eh, ew = r.env_rad.shape[:2]
+        l.ref_bind_texture(b"env_tex", _p(r.env_rad), RGBA16F, ew, eh, 1, LINEAR, 0)
+        l.ref_bind_texture(b"env_table_tex", _p(r.env_table), RG32F, ew + 1, eh, 1, NEAREST, 0)
 
 
 def normals(r, uniforms):

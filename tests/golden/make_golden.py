@@ -8,6 +8,9 @@ host (density normalisation, LUT, uniforms) come from the oracle's restatement
 of the render crate; the density normalisation and LUT are themselves pinned by
 the reference's unit tests (crates/render/src/transfer.rs:130-149).
 
+light_map_fixture() writes tests/golden/small_light_map.npz: the same scene lit
+by a seeded synthetic light map (Environment::Map).
+
 Usage (needs the reference sources): python tests/golden/make_golden.py
 """
 import os
@@ -63,5 +66,40 @@ def main():
     print(out, os.path.getsize(out), "bytes; background share", float(acc[..., 3].mean()) / (frames * spf))
 
 
+def light_map_fixture():
+    """The same scene lit by a synthetic light map (Environment::Map): the light
+    map's preparation (oracle restatement of environment.rs), then two
+    accumulate-frames of two paths each from the reference's pt.comp."""
+    n, size, frames, spf = 24, 24, 2, 2
+    cfg = scene.small_config(n=n, size=size, spp=frames * spf)
+    r = O.CpuRenderer(cfg["volume"], cfg["tf"], cfg["hu"])
+    r.set_labels(cfg["labels_vol"], cfg["soft"])
+    light_map = scene.synthetic_light_map(32, 16, seed=5)
+    r.set_environment_map(light_map)
+    g = r.geo
+    params = scene.frame_params_for(cfg, list(g.center), g.diagonal, clip_sagittal=True, spf=spf)
+    params.lighting.environment = abi.ENV_MAP
+    r.resize(size, size)
+    r.normals = R.normals(r, r._uniforms_geometry_only())
+    u1 = r.uniforms(params, 1, size, size)
+    r.mask = R.mask(r, u1, O.mask_margin(cfg["volume"], params.labels), int(params.labels.smoothing))
+    r.majorant = R.majorant(r, u1)
+    acc = np.zeros((size, size, 4), np.float32)
+    alb, nor = np.zeros_like(acc), np.zeros_like(acc)
+    hdr = np.zeros((size, size, 4), np.uint16)
+    for f in range(frames):
+        r.accumulated = f * spf
+        u = r.uniforms(params, f + 1, size, size)
+        R.pt_frame(r, u, acc, alb, nor, hdr)
+    out = os.path.join(os.path.dirname(os.path.abspath(__file__)), "small_light_map.npz")
+    np.savez_compressed(out, hu=cfg["hu"], labels=cfg["labels_vol"], soft=cfg["soft"],
+                        spacing=np.array(cfg["spacing"]), params=np.frombuffer(bytes(params), np.uint8),
+                        width=size, height=size, frames=frames, light_map=light_map, env_rad=r.env_rad,
+                        env_table=r.env_table, env_peak_u=r.env_peak_u, uniforms_frame1=u1, accum=acc,
+                        albedo=alb, normal=nor, hdr=hdr)
+    print(out, os.path.getsize(out), "bytes")
+
+
 if __name__ == "__main__":
     main()
+    light_map_fixture()

@@ -338,3 +338,24 @@ def frame_params_for(cfg, center, diagonal, clip_sagittal=False, anisotropy=0.6,
         clip.planes[0].cut_positive = 1
         clip.planes[0].position = float(center[0])
     return abi.frame_params(cam, abi.f32(0.5 * cfg["min_spacing"]), cfg["label_params"], light, pt, clip)
+
+
+def synthetic_light_map(width=64, height=32, seed=3):
+    """A seeded equirectangular studio-like HDR light map, (height, width, 3) linear RGB,
+    rows from the zenith down: a graded sky, a small bright sun and two soft boxes,
+    standing in for the reference's HDR (data/hdri/studio_small_09_2k.hdr), which
+    is not shipped."""
+    rng = np.random.default_rng(seed)
+    v = (np.arange(height, dtype=np.float64) + 0.5) / height
+    u = (np.arange(width, dtype=np.float64) + 0.5) / width
+    uu, vv = np.meshgrid(u, v)
+    sky = np.stack([0.25 + 0.55 * (1 - vv), 0.28 + 0.6 * (1 - vv), 0.35 + 0.7 * (1 - vv)], -1)
+    img = sky * (0.9 + 0.2 * rng.random((height, width, 1)))
+    sun_u, sun_v = rng.uniform(0.2, 0.8), rng.uniform(0.15, 0.35)
+    d2 = ((uu - sun_u) * 2) ** 2 + (vv - sun_v) ** 2
+    img += (d2 < 0.004)[..., None] * np.array([60.0, 55.0, 45.0])
+    for _ in range(2):
+        cu, cv = rng.uniform(0, 1), rng.uniform(0.3, 0.6)
+        box = (np.abs(uu - cu) < 0.06) & (np.abs(vv - cv) < 0.08)
+        img += box[..., None] * rng.uniform(3.0, 8.0)
+    return np.ascontiguousarray(img, np.float32)

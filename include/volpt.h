@@ -241,7 +241,10 @@ vv_status vv_set_transfer_function(vv_renderer* r, const vv_transfer_function* t
  * `soft` may be NULL. */
 vv_status vv_set_labels(vv_renderer* r, const uint8_t* labels, size_t n,
                         const vv_soft_label_grid* soft);
-/* Renderer::set_environment_map (renderer.rs:1283); NULL removes the map. */
+/* Renderer::set_environment_map (renderer.rs:1283); NULL removes the map.
+ * Prepares the importance-sampling tables (environment.rs:57-130) and restarts
+ * the accumulation; Environment::Map renders with the studio until a map is
+ * set, as the reference does. Maps above 16384 texels per axis: VV_ERR_LIMIT. */
 vv_status vv_set_environment_map(vv_renderer* r, const vv_environment_map* map);
 /* Renderer::resize (renderer.rs:1313): (re)allocates the output images. */
 vv_status vv_resize(vv_renderer* r, uint32_t width, uint32_t height);

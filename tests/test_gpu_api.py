@@ -140,3 +140,27 @@ def test_rmse_estimate_matches_a_converged_render(rend):
     actual = np.sqrt(np.mean((lum64 - lum4096) ** 2)) / np.sqrt(0.984)
     assert est > 0
     assert abs(est / actual - 1.0) < 0.1
+
+
+def test_environment_map_restarts_accumulation_and_falls_back(rend):
+    """set_environment_map restarts the accumulation (renderer.rs:1299);
+    Environment::Map without a map renders the studio (renderer.rs:1524-1527)."""
+    cfg, r, p = rend
+    r.resize(32, 24)
+    p.lighting.environment = abi.ENV_MAP
+    studio = abi.FrameParams.from_buffer_copy(bytes(p))
+    studio.lighting.environment = abi.ENV_STUDIO
+    assert np.array_equal(r.pack_uniforms(p, 1), r.pack_uniforms(studio, 1))  # no map yet
+    r.record(1, p)
+    r.record(2, p)
+    assert r.accumulated_samples() == 2
+    r.set_environment_map(abi.env_struct(scene.synthetic_light_map()))
+    assert not np.array_equal(r.pack_uniforms(p, 1), r.pack_uniforms(studio, 1))
+    r.record(3, p)
+    assert r.accumulated_samples() == 1
+    r.set_environment_map(None)
+    assert np.array_equal(r.pack_uniforms(p, 1), r.pack_uniforms(studio, 1))
+    big = np.zeros((4, 16385, 3), np.float32)
+    with pytest.raises(R.VolptError) as e:
+        r.set_environment_map(abi.env_struct(big))
+    assert e.value.status == abi.VV_ERR_LIMIT

@@ -118,6 +118,32 @@ def _rel_close(a, b, rtol=1e-4, atol=1e-6):
     return np.all(np.abs(a - b) <= rtol * np.abs(b) + atol, axis=-1)
 
 
+@pytest.fixture(scope="module")
+def pair_light_map(small_cfg, gpu_ctx):
+    """The same scene lit by a synthetic light map (Environment::Map) on both sides."""
+    cfg = small_cfg
+    light_map = scene.synthetic_light_map()
+    gpu = R.Renderer(gpu_ctx, cfg["volume"], cfg["tf"])
+    gpu.set_labels(cfg["labels_vol"], abi.soft_struct(cfg["soft"]))
+    gpu.set_environment_map(abi.env_struct(light_map))
+    cpu = O.CpuRenderer(cfg["volume"], cfg["tf"], cfg["hu"])
+    cpu.set_labels(cfg["labels_vol"], cfg["soft"])
+    cpu.set_environment_map(light_map)
+    params = make_params(cfg, list(gpu.center), gpu.diagonal, clip_sagittal=True)
+    params.lighting.environment = abi.ENV_MAP
+    gpu.resize(48, 48)
+    cpu.resize(48, 48)
+    yield cfg, gpu, cpu, params
+    gpu.destroy()
+
+
+def test_light_map_uniforms_bit_exact(pair_light_map):
+    """The light map's rotation towards the key light (renderer.rs:1524-1535)
+    from the map's preparation (environment.rs:110-121), packed as the oracle does."""
+    cfg, gpu, cpu, params = pair_light_map
+    assert np.array_equal(gpu.pack_uniforms(params, 1), cpu.uniforms(params, 1, 48, 48))
+
+
 def test_single_path_replays(pair):
     """Same pixel, same accumulation index: the same random stream.
 
@@ -128,7 +154,16 @@ def test_single_path_replays(pair):
     tracking or roulette comparison decided the other way). The first-hit guides
     (coverage, depth) must agree for every pixel whose primary ray did not flip.
     """
-    cfg, gpu, cpu, params = pair
+    _replays(*pair)
+
+
+def test_single_path_replays_light_map(pair_light_map):
+    """Replays under the light map: its importance sampling (binary searches of
+    the CDFs), its shadow ray and the MIS weights of escaping paths."""
+    _replays(*pair_light_map)
+
+
+def _replays(cfg, gpu, cpu, params):
     adopt_device_inputs(gpu, cpu, params)
     ys, xs = np.mgrid[0:48, 0:48]
     pix = np.stack([xs.ravel(), ys.ravel()], 1).astype(np.int32)
@@ -147,9 +182,16 @@ def test_single_path_replays(pair):
     assert flips <= 0.15
 
 
-def test_converged_image_within_3_sigma(pair, gpu_ctx):
-    cfg, gpu, cpu, params = pair
-    p = make_params(cfg, list(gpu.center), gpu.diagonal, clip_sagittal=True)
+def test_converged_image_within_3_sigma(pair):
+    _converged(*pair)
+
+
+def test_converged_image_light_map(pair_light_map):
+    _converged(*pair_light_map)
+
+
+def _converged(cfg, gpu, cpu, params):
+    p = abi.FrameParams.from_buffer_copy(bytes(params))
     p.path_tracing.denoiser = abi.DENOISE_OFF
     adopt_device_inputs(gpu, cpu, p)
     n_gpu, n_cpu = 1024, 256

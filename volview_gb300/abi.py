@@ -242,6 +242,16 @@ def volume_struct(hu, spacing, origin=(0.0, 0.0, 0.0), direction=None):
     return v
 
 
+def env_struct(rgb):
+    """An EnvironmentMap over float32 linear RGB `rgb` shaped (height, width, 3), rows from the zenith."""
+    rgb = np.ascontiguousarray(rgb, dtype=np.float32)
+    e = EnvironmentMap()
+    e.width, e.height = rgb.shape[1], rgb.shape[0]
+    e.rgb = rgb.ctypes.data_as(C.POINTER(C.c_float))
+    e._keep = rgb
+    return e
+
+
 def soft_struct(data, src_axis=(0, 1, 2), flip=(0, 0, 0)):
     """A SoftLabelGrid over uint8 array `data` shaped (gz, gy, gx, 4)."""
     data = np.ascontiguousarray(data, dtype=np.uint8)

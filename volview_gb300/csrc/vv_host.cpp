@@ -212,8 +212,13 @@ struct vv_renderer {
     uint32_t width = 0, height = 0;
     DBuf accum, albedo, normal, ping, pong, guide_nd, guide_alb, hdr, out, bloom[4];
     int bw[4], bh[4];
+    // light map (Environment::Map): RGBA16F radiance, RG32F sampling table
+    DBuf env_rad, env_table;
+    int env_w = 0, env_h = 0;
+    bool has_env = false;
+    float env_peak_u = 0.0f;
     // wavefront tracer: path slots, stage queues, counters
-    DBuf wf_slots, wf_queues, wf_counts;
+    DBuf wf_slots, wf_map, wf_queues, wf_counts;
     uint32_t* wf_host_count = nullptr;
     // accumulation
     uint32_t accumulated = 0;
@@ -390,7 +395,14 @@ static void pack(const vv_renderer* r, const vv_frame_params& p, uint32_t accumu
     const vv_lighting& L = p.lighting;
     float se = std::sin(L.elevation), ce = std::cos(L.elevation), sa = std::sin(L.azimuth), ca = std::cos(L.azimuth);
     h3 ld = hnorm(add(add(scl(scl(scl(f, -1.0f), ce), ca), scl(scl(right, ce), sa)), scl(up, se)));
-    int environment = L.environment == VV_ENV_MAP ? VV_ENV_STUDIO : L.environment;  // no light map bound
+    // Environment::Map without a light map falls back to the studio (renderer.rs:1524-1535);
+    // the map's brightest column turns to the key light's azimuth.
+    int environment = L.environment == VV_ENV_MAP && !r->has_env ? VV_ENV_STUDIO : L.environment;
+    float env_rotation = 0.0f;
+    if (r->has_env) {
+        float key_phi = std::atan2(std::sin(L.azimuth), -std::cos(L.azimuth));
+        env_rotation = (r->env_peak_u - 0.5f) * 6.28318530717958647692f - key_phi + L.env_rotation;
+    }
     const vv_label_params& lab = p.labels;
     std::memcpy(u.w2i, r->w2i, sizeof(u.w2i));
     auto put3 = [](float* d, h3 v, float w) { d[0] = v.x; d[1] = v.y; d[2] = v.z; d[3] = w; };
@@ -439,7 +451,7 @@ static void pack(const vv_renderer* r, const vv_frame_params& p, uint32_t accumu
     } else {
         u.path[3] = skip;
     }
-    u.env[0] = 0.0f; u.env[1] = p.smooth_sampling ? 1.0f : 0.0f; u.env[2] = L.anisotropy; u.env[3] = L.chromatic;
+    u.env[0] = env_rotation; u.env[1] = p.smooth_sampling ? 1.0f : 0.0f; u.env[2] = L.anisotropy; u.env[3] = L.chromatic;
     u.finish[0] = L.bloom; u.finish[1] = L.vignette; u.finish[2] = L.grain; u.finish[3] = L.auto_exposure ? 1.0f : 0.0f;
     std::memcpy(u.tf_bucket_max, r->bucket, sizeof(r->bucket));
     u.subsurface[0] = L.subsurface * L.subsurface_strength;
@@ -591,12 +603,14 @@ extern "C" vv_status vv_renderer_destroy(vv_renderer* r) {
     if (!r) return VV_OK;
     cudaSetDevice(r->ctx->device);
     cudaStreamSynchronize(r->ctx->stream);
-    DBuf* all[] = {&r->density, &r->normals, &r->mask_a, &r->mask_b, &r->labels, &r->majorant, &r->lut,
+    DBuf* all[] = {&r->density, &r->normals, &r->mask_a, &r->mask_b, &r->labels, &r->majorant, &r->env_rad,
+                   &r->env_table, &r->lut,
                    &r->bucket_dev, &r->tables, &r->soft, &r->work, &r->exposure, &r->accum, &r->albedo,
                    &r->normal, &r->ping, &r->pong, &r->guide_nd, &r->guide_alb, &r->hdr, &r->out, &r->bloom[0], &r->bloom[1], &r->bloom[2],
                    &r->bloom[3]};
     for (DBuf* b : all) b->release();
     r->wf_slots.release();
+    r->wf_map.release();
     r->wf_queues.release();
     r->wf_counts.release();
     if (r->wf_host_count) cudaFreeHost(r->wf_host_count);
@@ -686,10 +700,112 @@ extern "C" vv_status vv_set_labels(vv_renderer* r, const uint8_t* labels, size_t
     return VV_OK;
 }
 
+// EnvironmentMap::prepare (environment.rs:57-130) without the diffuse
+// convolution (only the ray marcher reads it), and the upload of
+// renderer.rs:2224-2290: radiance normalised to a mean luminance of 1 over the
+// sphere, min(60000), to RGBA16F; the importance-sampling table as RG32F,
+// (w + 1) x h: per row the conditional CDF and each texel's probability, in
+// the last column the marginal CDF and the row's probability. Sums in f64 in
+// the Rust's order, per-texel arithmetic in f32 (this file is compiled
+// without floating-point contraction, as Rust compiles).
+static float env_lum(const float* c) { return 0.2126f * c[0] + 0.7152f * c[1] + 0.0722f * c[2]; }
+
+static float prepare_light_map(int w, int h, const float* px, std::vector<uint16_t>& rad, std::vector<float>& table) {
+    const float PI_F = 3.14159265358979323846f;
+    auto sin_theta = [&](int y) { return std::sin(PI_F * ((float)y + 0.5f) / (float)h); };
+    double sum[3] = {0.0, 0.0, 0.0}, weight = 0.0;
+    for (int y = 0; y < h; y++) {
+        float st = sin_theta(y);
+        double row[3] = {0.0, 0.0, 0.0};
+        for (int x = 0; x < w; x++)
+            for (int c = 0; c < 3; c++) row[c] = row[c] + (double)px[3 * ((size_t)y * w + x) + c];
+        for (int c = 0; c < 3; c++) sum[c] = sum[c] + row[c] * (double)st;
+        weight = weight + (double)st * (double)w;
+    }
+    float mean_rgb[3] = {(float)(sum[0] / weight), (float)(sum[1] / weight), (float)(sum[2] / weight)};
+    float mean = std::max(env_lum(mean_rgb), 1e-6f);
+    size_t n = (size_t)w * h;
+    rad.resize(4 * n);
+    auto half_bits = [](float v) {
+        _Float16 hv = (_Float16)v;
+        uint16_t b;
+        std::memcpy(&b, &hv, 2);
+        return b;
+    };
+    for (size_t i = 0; i < n; i++) {
+        for (int c = 0; c < 3; c++) rad[4 * i + c] = half_bits(std::min(px[3 * i + c] / mean, 60000.0f));
+        rad[4 * i + 3] = half_bits(1.0f);
+    }
+    std::vector<float> f(n);
+    for (size_t i = 0; i < n; i++) f[i] = env_lum(px + 3 * i) * sin_theta((int)(i / (size_t)w));
+    std::vector<double> row_sums(h);
+    double total = 0.0;
+    for (int y = 0; y < h; y++) {
+        double a = 0.0;
+        for (int x = 0; x < w; x++) a = a + (double)f[(size_t)y * w + x];
+        row_sums[y] = a;
+    }
+    for (int y = 0; y < h; y++) total = total + row_sums[y];
+    total = std::max(total, 1e-12);
+    table.assign(2 * (size_t)(w + 1) * h, 0.0f);
+    double marginal = 0.0;
+    for (int y = 0; y < h; y++) {
+        float* row = table.data() + 2 * (size_t)y * (w + 1);
+        double acc = 0.0;
+        for (int x = 0; x < w; x++) {
+            double fx = (double)f[(size_t)y * w + x];
+            acc = acc + fx;
+            row[2 * x] = row_sums[y] > 0.0 ? (float)(acc / row_sums[y]) : (float)(x + 1) / (float)w;
+            row[2 * x + 1] = (float)(fx / total);
+        }
+        row[2 * (w - 1)] = 1.0f;
+        marginal = marginal + row_sums[y];
+        row[2 * w] = (float)(marginal / total);
+        row[2 * w + 1] = (float)(row_sums[y] / total);
+    }
+    table[2 * ((size_t)(h - 1) * (w + 1) + w)] = 1.0f;
+    double pxs = 0.0, pzs = 0.0;
+    for (int y = 0; y < h; y++)
+        for (int x = 0; x < w; x++) {
+            double l = (double)f[(size_t)y * w + x];
+            float uu = ((float)x + 0.5f) / (float)w, vv = ((float)y + 0.5f) / (float)h;
+            float phi = (uu - 0.5f) * 2.0f * PI_F, theta = vv * PI_F;
+            pxs = pxs + l * l * (double)(std::sin(theta) * std::sin(phi));
+            pzs = pzs + l * l * (double)(std::sin(theta) * std::cos(phi));
+        }
+    return 0.5f + (float)(std::atan2(pxs, pzs) / (2.0 * 3.14159265358979323846));
+}
+
 extern "C" vv_status vv_set_environment_map(vv_renderer* r, const vv_environment_map* map) {
     if (!r) return fail(VV_ERR_ARG, "null renderer");
-    if (map) return fail(VV_ERR_LIMIT, "light maps are not supported by this build; the studio environment is used");
-    r->have_params = false;
+    vv_status st = use_device(r);
+    if (st != VV_OK) return st;
+    CK(cudaStreamSynchronize(r->ctx->stream));  // the reference waits for the device to go idle
+    if (!map) {
+        r->env_rad.release();
+        r->env_table.release();
+        r->has_env = false;
+        r->env_w = r->env_h = 0;
+        r->env_peak_u = 0.0f;
+        r->have_params = false;
+        return VV_OK;
+    }
+    if (!map->rgb) return fail(VV_ERR_ARG, "null light map pixels");
+    if (map->width == 0 || map->height == 0) return fail(VV_ERR_ARG, "empty light map");
+    if (map->width > 16384 || map->height > 16384) return fail(VV_ERR_LIMIT, "light map above 16384 texels per axis");
+    int w = (int)map->width, h = (int)map->height;
+    std::vector<uint16_t> rad;
+    std::vector<float> table;
+    float peak = prepare_light_map(w, h, map->rgb, rad, table);
+    CK(r->env_rad.alloc(rad.size() * sizeof(uint16_t)));
+    CK(r->env_table.alloc(table.size() * sizeof(float)));
+    CK(cudaMemcpy(r->env_rad.p, rad.data(), rad.size() * sizeof(uint16_t), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(r->env_table.p, table.data(), table.size() * sizeof(float), cudaMemcpyHostToDevice));
+    r->env_w = w;
+    r->env_h = h;
+    r->env_peak_u = peak;
+    r->has_env = true;
+    r->have_params = false;  // accumulated_params = None
     return VV_OK;
 }
 
@@ -710,7 +826,8 @@ extern "C" vv_status vv_resize(vv_renderer* r, uint32_t width, uint32_t height) 
     CK(r->guide_alb.alloc(px * 16));
     CK(r->hdr.alloc(px * 8));
     CK(r->out.alloc(px * 4));
-    CK(r->wf_slots.alloc(px * 256));
+    CK(r->wf_slots.alloc(px * WF_SLOT_BYTES));
+    CK(r->wf_map.alloc(px * WF_MAP_BYTES));
     CK(r->wf_queues.alloc(px * 7 * sizeof(uint32_t)));
     CK(r->wf_counts.alloc(WF_COUNTERS * sizeof(uint32_t)));
     if (!r->wf_host_count) CK(cudaMallocHost((void**)&r->wf_host_count, sizeof(uint32_t)));
@@ -757,6 +874,10 @@ static PtArgs pt_args(vv_renderer* r, const UHead& u) {
     a.normals = r->normals.as<uint32_t>();
     a.labels = r->labels.as<uint8_t>();
     a.majorant = r->majorant.as<float>();
+    a.env_rad = r->env_rad.as<ushort4>();
+    a.env_table = r->env_table.as<float2>();
+    a.env_w = r->env_w;
+    a.env_h = r->env_h;
     a.lut = r->lut.as<float4>();
     a.tab = r->tables.as<LabelTables>();
     a.vol = r->vol;
@@ -789,6 +910,7 @@ static cudaError_t run_pt(vv_renderer* r, PtArgs& a, int* launches) {
     size_t px = (size_t)r->width * r->height;
     WfArgs w;
     w.slots = r->wf_slots.as<float4>();
+    w.map = r->wf_map.as<float4>();
     uint32_t* q = r->wf_queues.as<uint32_t>();
     w.ext[0] = q;
     w.ext[1] = q + px;

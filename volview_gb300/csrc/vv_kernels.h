@@ -30,6 +30,9 @@ struct PtArgs {
     const uint32_t* normals;
     const uint8_t* labels;
     const float* majorant;
+    const ushort4* env_rad;     // light map radiance, RGBA16F, env_w x env_h (lighting.w == 2)
+    const float2* env_table;    // light map sampling table, (env_w + 1) x env_h
+    int env_w, env_h;
     const float4* lut;          // transfer function, RGBA16F values as float
     const LabelTables* tab;
     Vol vol;
@@ -72,8 +75,10 @@ cudaError_t launch_brick_u8(const uint8_t* src, uint8_t* dst, const Vol& v, cuda
 // One or more accumulate-frames (pt.comp). Returns the number of kernel launches.
 cudaError_t launch_pt(const PtArgs& a, int sms, cudaStream_t s, int* launches);
 
-// Wavefront tracer state: one 256-byte slot per pixel, the stage queues (slot
-// indices) and their counters.
+// Wavefront tracer state: one slot of WF_SLOT_BYTES per pixel, the stage
+// queues (slot indices) and their counters.
+constexpr int WF_SLOT_BYTES = 256;
+constexpr int WF_MAP_BYTES = 32;  // per slot: the light map's next-event sample
 enum {
     WF_EXT0 = 0, WF_EXT1 = 1, WF_SHADE = 2, WF_SHADOW = 3, WF_SCATTER = 4,
     WF_ITEMS = 5,     // next (frame, pixel) work item
@@ -84,6 +89,7 @@ enum {
 };
 struct WfArgs {
     float4* slots;
+    float4* map;           // WF_MAP_BYTES per slot
     uint32_t* ext[2];
     uint32_t* esc[2];
     uint32_t* shade;

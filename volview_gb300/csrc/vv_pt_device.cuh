@@ -672,8 +672,50 @@ __device__ __noinline__ Consts make_consts(const PtArgs& A) {
     return c;
 }
 
-// pt.comp:56-82 (dome and studio; the light map is not bound by this build)
+// common.glsl:459-481: light map coordinates of a world direction (the map is
+// fixed to the camera: centre column ahead, top row above) and back.
+__device__ __forceinline__ float2 env_uv(const PtArgs& A, f3 d) {
+    f3 f = normalize(U3(A.u.forward)), r = normalize(U3(A.u.right)), up = normalize(U3(A.u.up));
+    float phi = atan2f(dot(d, r), dot(d, f));
+    float theta = acosf(gclamp(dot(d, up), -1.0f, 1.0f));
+    float x = 0.5f + (phi + A.u.env[0]) / (2.0f * PI);
+    return make_float2(x - floorf(x), theta / PI);
+}
+__device__ __forceinline__ f3 env_direction(const PtArgs& A, float2 uv) {
+    float phi = (uv.x - 0.5f) * 2.0f * PI - A.u.env[0];
+    float theta = uv.y * PI;
+    f3 f = normalize(U3(A.u.forward)), r = normalize(U3(A.u.right)), up = normalize(U3(A.u.up));
+    return sinf(theta) * (sinf(phi) * r + cosf(phi) * f) + cosf(theta) * up;
+}
+// common.glsl:483-486: the light map's radiance towards `d`, filtered as the
+// sampler does (linear between texel centres, CLAMP_TO_EDGE, RGBA16F texels).
+__device__ __noinline__ f3 env_map_radiance(const PtArgs& A, f3 d) {
+    float2 uv = env_uv(A, d);
+    float x = uv.x * (float)A.env_w - 0.5f, y = uv.y * (float)A.env_h - 0.5f;
+    int i0 = (int)floorf(x), j0 = (int)floorf(y);
+    float a = x - (float)i0, b = y - (float)j0;
+    f3 c = mk(0.0f);
+    for (int dj = 0; dj < 2; dj++)
+        for (int di = 0; di < 2; di++) {
+            int i = clampi(i0 + di, 0, A.env_w - 1), j = clampi(j0 + dj, 0, A.env_h - 1);
+            ushort4 t = __ldg(A.env_rad + (long)j * A.env_w + i);
+            float w = (di ? a : 1.0f - a) * (dj ? b : 1.0f - b);
+            c += mk(__half2float(__ushort_as_half(t.x)), __half2float(__ushort_as_half(t.y)),
+                    __half2float(__ushort_as_half(t.z))) * w;
+        }
+    return U3(A.u.ambient) * c;
+}
+// pt.comp:193-200: solid-angle pdf of light map direction `d`.
+__device__ __noinline__ float env_pdf(const PtArgs& A, f3 d) {
+    float2 uv = env_uv(A, d);
+    int tx = min((int)(uv.x * (float)A.env_w), A.env_w - 1), ty = min((int)(uv.y * (float)A.env_h), A.env_h - 1);
+    float p = __ldg(&A.env_table[(long)ty * (A.env_w + 1) + tx].y);
+    return p * (float)(A.env_w * A.env_h) / (2.0f * PI * PI * gmax(sinf(uv.y * PI), 1e-6f));
+}
+
+// pt.comp:56-82
 __device__ __noinline__ f3 environment(const PtArgs& A, f3 d) {
+    if (A.u.lighting[3] == 2u) return env_map_radiance(A, d);
     f3 amb = U3(A.u.ambient);
     if (A.u.lighting[3] >= 1u) {
         f3 f = normalize(U3(A.u.forward)), r = normalize(U3(A.u.right)), up = normalize(U3(A.u.up));
@@ -696,6 +738,36 @@ __device__ __forceinline__ f3 sample_light(const PtArgs& A, const Consts& C, Rng
     float sp, cp;
     sincosf(phi, &sp, &cp);
     return mul(C.light_frame, mk(sin_t * cp, sin_t * sp, cos_t));
+}
+
+// pt.comp:204-233: a direction towards the light map drawn by luminance x
+// solid angle: binary search of the marginal CDF over rows, then of the row's
+// conditional CDF, then a uniform point in the texel.
+__device__ __noinline__ f3 sample_env(const PtArgs& A, Rng& rng, float& pdf) {
+    const int W = A.env_w, H = A.env_h;
+    const float2* T = A.env_table;
+    float xi = rng.rand();
+    int lo = 0, hi = H - 1;
+    while (lo < hi) {
+        int mid = (lo + hi) / 2;
+        if (__ldg(&T[(long)mid * (W + 1) + W].x) >= xi) hi = mid;
+        else lo = mid + 1;
+    }
+    int y = lo;
+    xi = rng.rand();
+    lo = 0;
+    hi = W - 1;
+    while (lo < hi) {
+        int mid = (lo + hi) / 2;
+        if (__ldg(&T[(long)y * (W + 1) + mid].x) >= xi) hi = mid;
+        else lo = mid + 1;
+    }
+    float jx = rng.rand();
+    float jy = rng.rand();
+    float2 uv = make_float2(((float)lo + jx) / (float)W, ((float)y + jy) / (float)H);
+    float p = __ldg(&T[(long)y * (W + 1) + lo].y);
+    pdf = p * (float)(W * H) / (2.0f * PI * PI * gmax(sinf(uv.y * PI), 1e-6f));
+    return env_direction(A, uv);
 }
 __device__ __forceinline__ f3 single_scattering_albedo(f3 a) {
     a = gclamp(a, 0.0f, 0.999f);
@@ -988,6 +1060,8 @@ struct Vertex {
     bool surface_event;
     f3 light_dir;
     f3 light_t;
+    f3 map_dir, map_light;  // the light map's sample (lighting.w == 2), map_light / pdf x transmittance
+    float map_pdf;          // 0: no light map sample
 };
 
 // The bounce loop (pt.comp:427-545) in four stages, in the order the
@@ -1016,8 +1090,9 @@ __device__ __noinline__ void stage_escape(const PtArgs& A, const Consts& C, Path
         S.albedo.x += 1.0f; S.albedo.y += 1.0f; S.albedo.z += 1.0f;
         S.normal.w += 1e4f;
     } else {
+        float weight = A.u.lighting[3] == 2u ? mis(P.last_pdf, env_pdf(A, P.dir)) : 1.0f;
         f3 path_weight = P.throughput * P.spectral / dot(P.spectral, mk(1.0f / 3.0f));
-        P.radiance += path_weight * environment(A, P.dir);
+        P.radiance += path_weight * environment(A, P.dir) * weight;
         if (C.area_light && dot(P.dir, C.light_dir) >= C.cos_light)
             P.radiance += path_weight * (C.light * C.light_pdf * mis(P.last_pdf, C.light_pdf));
     }
@@ -1040,9 +1115,24 @@ __device__ __noinline__ void stage_shade(const PtArgs& A, const Consts& C, Path&
     V.light_dir = sample_light(A, C, P.rng);
 }
 
-// Stage 3: the shadow ray towards the light sample (pt.comp:466).
+// The light map's next-event sample after the key light's shadow ray
+// (pt.comp:467-476), before its own shadow ray.
+__device__ __forceinline__ void sample_map_light(const PtArgs& A, Rng& rng, Vertex& V) {
+    V.map_dir = sample_env(A, rng, V.map_pdf);
+    V.map_light = env_map_radiance(A, V.map_dir) / gmax(V.map_pdf, 1e-8f);
+}
+
+// Stage 3: the shadow rays towards the light sample and the light map's
+// sample (pt.comp:466-476).
 __device__ __forceinline__ void stage_shadow(const PtArgs& A, Path& P, Vertex& V) {
     V.light_t = transmittance(A, V.idx, V.light_dir, P.rng);
+    V.map_pdf = 0.0f;
+    V.map_dir = mk(0.0f);
+    V.map_light = mk(0.0f);
+    if (A.u.lighting[3] == 2u) {
+        sample_map_light(A, P.rng, V);
+        if (V.map_pdf > 0.0f) V.map_light *= transmittance(A, V.idx, V.map_dir, P.rng);
+    }
 }
 
 // Stage 4: light contribution, next direction, Russian roulette (pt.comp:478-545).
@@ -1058,6 +1148,11 @@ __device__ __noinline__ bool stage_scatter(const PtArgs& A, const Consts& C, Pat
         float light_weight = C.area_light ? mis(C.light_pdf, bsdf_pdf(n, v, V.light_dir, s)) : 1.0f;
         P.radiance += path_weight * (diffuse + specular) * (gmax(dot(n, V.light_dir), 0.0f) * C.light) * V.light_t *
                       light_weight;
+        if (V.map_pdf > 0.0f && dot(n, V.map_dir) > 0.0f) {
+            specular = brdf_coated(n, v, V.map_dir, s, diffuse);
+            P.radiance += path_weight * (diffuse + specular) * dot(n, V.map_dir) * V.map_light *
+                          mis(V.map_pdf, bsdf_pdf(n, v, V.map_dir, s));
+        }
         m3 frame = basis(n);
         f3 l;
         if (P.rng.rand() < coat_share(s)) {
@@ -1086,6 +1181,10 @@ __device__ __noinline__ bool stage_scatter(const PtArgs& A, const Consts& C, Pat
         float light_phase = phase_hg(A, dot(P.dir, V.light_dir));
         P.radiance += path_weight * albedo * (light_phase * C.light) * V.light_t *
                       (C.area_light ? mis(C.light_pdf, light_phase) : 1.0f);
+        if (V.map_pdf > 0.0f) {
+            float phase = phase_hg(A, dot(P.dir, V.map_dir));
+            P.radiance += path_weight * albedo * phase * V.map_light * mis(V.map_pdf, phase);
+        }
         P.throughput *= albedo;
         P.volumes++;
         P.origin = V.idx;

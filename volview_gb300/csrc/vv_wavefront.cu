@@ -30,7 +30,8 @@
 
 namespace vv {
 
-// Slot layout: 16 x float4 = 256 bytes per pixel.
+// Slot layout: 16 x float4 = 256 bytes per pixel (WF_SLOT_BYTES); the light
+// map's sample, when there is a light map, in a parallel array of 2 x float4.
 enum {
     Q_ORIGIN = 0,   // origin.xyz, last_pdf
     Q_DIR = 1,      // dir.xyz, rng
@@ -47,11 +48,16 @@ enum {
     Q_N = 12,       // shading normal
     Q_LD = 13,      // light direction
     Q_LT = 14,      // light transmittance
-    Q_CTL = 15,     // frame, sample, hero, -
+    Q_CTL = 15,     // frame, sample, hero, escape flag (extend -> scatter)
     Q_COUNT = 16
 };
+// W.map entries per slot: light map sample direction.xyz and pdf (0: none);
+// its radiance / pdf x transmittance.
+enum { M_DIR = 0, M_LIGHT = 1, M_COUNT = 2 };
+static_assert(Q_COUNT * 16 == WF_SLOT_BYTES, "slot layout");
 
 __device__ __forceinline__ float4* slot_of(const WfArgs& W, uint32_t s) { return W.slots + (size_t)s * Q_COUNT; }
+__device__ __forceinline__ float4* map_of(const WfArgs& W, uint32_t s) { return W.map + (size_t)s * M_COUNT; }
 __device__ __forceinline__ float4 f4(f3 v, float w) { return make_float4(v.x, v.y, v.z, w); }
 __device__ __forceinline__ f3 xyz(float4 q) { return mk(q.x, q.y, q.z); }
 __device__ __forceinline__ uint32_t ubits(float f) { return __float_as_uint(f); }
@@ -329,17 +335,20 @@ __global__ void __launch_bounds__(128, 4) k_wf_shade(const __grid_constant__ PtA
 
 // Shadow rays, persistent over their queue like extend: one ratio-tracking
 // step (tr_step, the loop body of transmittance, pt.comp:344-369) per
-// iteration, lanes refilled as their rays finish.
+// iteration, lanes refilled as their rays finish. With a light map, a lane
+// whose key-light ray finished draws the light map's sample and traces its
+// ray next (pt.comp:466-476, in the reference's order of random numbers).
 #ifndef VV_SHADOW_MIN_BLOCKS
 #define VV_SHADOW_MIN_BLOCKS 8
 #endif
 __global__ void __launch_bounds__(128, VV_SHADOW_MIN_BLOCKS) k_wf_shadow(const __grid_constant__ PtArgs A, const WfArgs W) {
     const uint32_t n = W.counts[WF_SHADOW];
+    const bool env_map = A.u.lighting[3] == 2u;
     uint32_t slot = 0;
     f3 origin;
     Rng rng;
     Shadow T;
-    bool active = false, drained = false;
+    bool active = false, drained = false, map_ray = false;
     for (;;) {
         bool need = !active && !drained;
         if (__any_sync(0xffffffffu, need)) {
@@ -351,20 +360,41 @@ __global__ void __launch_bounds__(128, VV_SHADOW_MIN_BLOCKS) k_wf_shadow(const _
                 origin = xyz(q[Q_IDX]);
                 tr_begin(A, origin, xyz(q[Q_LD]), T);
                 active = true;
+                map_ray = false;
             }
             drained = __any_sync(0xffffffffu, need && k == ~0u);
         }
         bool done = false;
         if (active && !tr_step(A, origin, T, rng)) {
-            active = false;
-            done = true;
+            float4* q = slot_of(W, slot);
+            float4* m = map_of(W, slot);
+            if (map_ray) {
+                float4 ml = m[M_LIGHT];
+                m[M_LIGHT] = f4(xyz(ml) * T.result, 0.0f);
+                done = true;
+            } else {
+                q[Q_LT] = f4(T.result, 0.0f);
+                float map_pdf = 0.0f;
+                if (env_map) {
+                    Vertex V;
+                    sample_map_light(A, rng, V);
+                    map_pdf = V.map_pdf;
+                    m[M_DIR] = f4(V.map_dir, V.map_pdf);
+                    m[M_LIGHT] = f4(V.map_light, 0.0f);
+                    if (map_pdf > 0.0f) {
+                        tr_begin(A, origin, V.map_dir, T);
+                        map_ray = true;
+                    }
+                }
+                done = !(map_pdf > 0.0f);
+            }
+            if (done) active = false;
         }
         if (__any_sync(0xffffffffu, done)) {
             if (done) {
                 float4* q = slot_of(W, slot);
                 float4 d = q[Q_DIR];
                 q[Q_DIR] = make_float4(d.x, d.y, d.z, fbits(rng.s));
-                q[Q_LT] = f4(T.result, 0.0f);
             }
             push(W.scatter, &W.counts[WF_SCATTER], slot, done);
         }
@@ -397,6 +427,14 @@ __global__ void __launch_bounds__(128, 6) k_wf_scatter(const __grid_constant__ P
                 V.n = xyz(q[Q_N]);
                 V.light_dir = xyz(q[Q_LD]);
                 V.light_t = xyz(q[Q_LT]);
+                V.map_pdf = 0.0f;
+                if (A.u.lighting[3] == 2u) {
+                    const float4* m = map_of(W, slot);
+                    float4 md = m[M_DIR];
+                    V.map_dir = xyz(md);
+                    V.map_pdf = md.w;
+                    V.map_light = xyz(m[M_LIGHT]);
+                }
                 to_ext = stage_scatter(A, C, P, V);
             }
             if (!to_ext) {

@@ -147,6 +147,7 @@ class Renderer:
         check(load().vv_set_labels(self.handle, _ptr(labels), labels.size, _ref(soft)))
 
     def set_environment_map(self, env):
+        """`env`: an abi.EnvironmentMap (abi.env_struct), or None to remove the map."""
         check(load().vv_set_environment_map(self.handle, _ref(env)))
 
     def resize(self, width, height):

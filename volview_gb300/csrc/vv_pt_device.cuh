@@ -1117,9 +1117,13 @@ __device__ __noinline__ void stage_shade(const PtArgs& A, const Consts& C, Path&
 
 // The light map's next-event sample after the key light's shadow ray
 // (pt.comp:467-476), before its own shadow ray.
-__device__ __forceinline__ void sample_map_light(const PtArgs& A, Rng& rng, Vertex& V) {
+__device__ __noinline__ void sample_map_light(const PtArgs& A, Rng& rng, Vertex& V) {
     V.map_dir = sample_env(A, rng, V.map_pdf);
     V.map_light = env_map_radiance(A, V.map_dir) / gmax(V.map_pdf, 1e-8f);
+}
+__device__ __noinline__ void map_shadow(const PtArgs& A, Path& P, Vertex& V) {
+    sample_map_light(A, P.rng, V);
+    if (V.map_pdf > 0.0f) V.map_light *= transmittance(A, V.idx, V.map_dir, P.rng);
 }
 
 // Stage 3: the shadow rays towards the light sample and the light map's
@@ -1129,10 +1133,19 @@ __device__ __forceinline__ void stage_shadow(const PtArgs& A, Path& P, Vertex& V
     V.map_pdf = 0.0f;
     V.map_dir = mk(0.0f);
     V.map_light = mk(0.0f);
-    if (A.u.lighting[3] == 2u) {
-        sample_map_light(A, P.rng, V);
-        if (V.map_pdf > 0.0f) V.map_light *= transmittance(A, V.idx, V.map_dir, P.rng);
-    }
+    if (A.u.lighting[3] == 2u) map_shadow(A, P, V);
+}
+
+// The light map's next-event contributions (pt.comp:484-488, 525-528).
+__device__ __noinline__ f3 map_surface_term(const Vertex& V, f3 n, f3 v, f3 path_weight) {
+    f3 diffuse;
+    f3 specular = brdf_coated(n, v, V.map_dir, V.s, diffuse);
+    return path_weight * (diffuse + specular) * dot(n, V.map_dir) * V.map_light *
+           mis(V.map_pdf, bsdf_pdf(n, v, V.map_dir, V.s));
+}
+__device__ __noinline__ f3 map_volume_term(const PtArgs& A, const Vertex& V, f3 dir, f3 path_weight, f3 albedo) {
+    float phase = phase_hg(A, dot(dir, V.map_dir));
+    return path_weight * albedo * phase * V.map_light * mis(V.map_pdf, phase);
 }
 
 // Stage 4: light contribution, next direction, Russian roulette (pt.comp:478-545).
@@ -1148,11 +1161,7 @@ __device__ __noinline__ bool stage_scatter(const PtArgs& A, const Consts& C, Pat
         float light_weight = C.area_light ? mis(C.light_pdf, bsdf_pdf(n, v, V.light_dir, s)) : 1.0f;
         P.radiance += path_weight * (diffuse + specular) * (gmax(dot(n, V.light_dir), 0.0f) * C.light) * V.light_t *
                       light_weight;
-        if (V.map_pdf > 0.0f && dot(n, V.map_dir) > 0.0f) {
-            specular = brdf_coated(n, v, V.map_dir, s, diffuse);
-            P.radiance += path_weight * (diffuse + specular) * dot(n, V.map_dir) * V.map_light *
-                          mis(V.map_pdf, bsdf_pdf(n, v, V.map_dir, s));
-        }
+        if (V.map_pdf > 0.0f && dot(n, V.map_dir) > 0.0f) P.radiance += map_surface_term(V, n, v, path_weight);
         m3 frame = basis(n);
         f3 l;
         if (P.rng.rand() < coat_share(s)) {
@@ -1181,10 +1190,7 @@ __device__ __noinline__ bool stage_scatter(const PtArgs& A, const Consts& C, Pat
         float light_phase = phase_hg(A, dot(P.dir, V.light_dir));
         P.radiance += path_weight * albedo * (light_phase * C.light) * V.light_t *
                       (C.area_light ? mis(C.light_pdf, light_phase) : 1.0f);
-        if (V.map_pdf > 0.0f) {
-            float phase = phase_hg(A, dot(P.dir, V.map_dir));
-            P.radiance += path_weight * albedo * phase * V.map_light * mis(V.map_pdf, phase);
-        }
+        if (V.map_pdf > 0.0f) P.radiance += map_volume_term(A, V, P.dir, path_weight, albedo);
         P.throughput *= albedo;
         P.volumes++;
         P.origin = V.idx;

@@ -341,9 +341,11 @@ __global__ void __launch_bounds__(128, 4) k_wf_shade(const __grid_constant__ PtA
 #ifndef VV_SHADOW_MIN_BLOCKS
 #define VV_SHADOW_MIN_BLOCKS 8
 #endif
+// MAP: the frame has a light map (lighting.w == 2); the kernel without it is
+// the key light's shadow rays alone.
+template <bool MAP>
 __global__ void __launch_bounds__(128, VV_SHADOW_MIN_BLOCKS) k_wf_shadow(const __grid_constant__ PtArgs A, const WfArgs W) {
     const uint32_t n = W.counts[WF_SHADOW];
-    const bool env_map = A.u.lighting[3] == 2u;
     uint32_t slot = 0;
     f3 origin;
     Rng rng;
@@ -366,27 +368,28 @@ __global__ void __launch_bounds__(128, VV_SHADOW_MIN_BLOCKS) k_wf_shadow(const _
         }
         bool done = false;
         if (active && !tr_step(A, origin, T, rng)) {
-            float4* q = slot_of(W, slot);
-            float4* m = map_of(W, slot);
-            if (map_ray) {
-                float4 ml = m[M_LIGHT];
-                m[M_LIGHT] = f4(xyz(ml) * T.result, 0.0f);
+            if (!MAP) {
                 done = true;
             } else {
-                q[Q_LT] = f4(T.result, 0.0f);
-                float map_pdf = 0.0f;
-                if (env_map) {
+                float4* q = slot_of(W, slot);
+                float4* m = map_of(W, slot);
+                if (map_ray) {
+                    float4 ml = m[M_LIGHT];
+                    m[M_LIGHT] = f4(xyz(ml) * T.result, 0.0f);
+                    done = true;
+                } else {
+                    q[Q_LT] = f4(T.result, 0.0f);
                     Vertex V;
                     sample_map_light(A, rng, V);
-                    map_pdf = V.map_pdf;
                     m[M_DIR] = f4(V.map_dir, V.map_pdf);
                     m[M_LIGHT] = f4(V.map_light, 0.0f);
-                    if (map_pdf > 0.0f) {
+                    if (V.map_pdf > 0.0f) {
                         tr_begin(A, origin, V.map_dir, T);
                         map_ray = true;
+                    } else {
+                        done = true;
                     }
                 }
-                done = !(map_pdf > 0.0f);
             }
             if (done) active = false;
         }
@@ -395,6 +398,7 @@ __global__ void __launch_bounds__(128, VV_SHADOW_MIN_BLOCKS) k_wf_shadow(const _
                 float4* q = slot_of(W, slot);
                 float4 d = q[Q_DIR];
                 q[Q_DIR] = make_float4(d.x, d.y, d.z, fbits(rng.s));
+                if (!MAP) q[Q_LT] = f4(T.result, 0.0f);
             }
             push(W.scatter, &W.counts[WF_SCATTER], slot, done);
         }
@@ -495,7 +499,7 @@ cudaError_t launch_pt_wavefront(const PtArgs& a, const WfArgs& w, int sms, cudaS
     if (!g_ext) {
         g_ext = sms * blocks_per_sm(k_wf_extend, 128);
         g_shade = sms * blocks_per_sm(k_wf_shade, 128);
-        g_shadow = sms * blocks_per_sm(k_wf_shadow, 128);
+        g_shadow = sms * blocks_per_sm(k_wf_shadow<false>, 128);
         g_scatter = sms * blocks_per_sm(k_wf_scatter, 128);
         g_finish = sms * blocks_per_sm(k_wf_finish, 128);
     }
@@ -503,6 +507,7 @@ cudaError_t launch_pt_wavefront(const PtArgs& a, const WfArgs& w, int sms, cudaS
     uint32_t tail = env ? (uint32_t)std::atoi(env) : 1024u;
     uint32_t pixels = a.width * a.height;
     uint32_t slots = pixels;  // one frame's worth of paths in flight
+    const bool map = a.u.lighting[3] == 2u;
     k_wf_init<<<(slots + 255) / 256 < (uint32_t)(sms * 8) ? (slots + 255) / 256 : sms * 8, 256, 0, s>>>(a, w, slots);
     *launches += 1;
     int cur = 0;
@@ -510,7 +515,8 @@ cudaError_t launch_pt_wavefront(const PtArgs& a, const WfArgs& w, int sms, cudaS
     for (int wave = 0; wave < 1 << 20; wave++) {
         k_wf_extend<<<g_ext, 128, 0, s>>>(a, w, cur);
         k_wf_shade<<<g_shade, 128, 0, s>>>(a, w, cur);
-        k_wf_shadow<<<g_shadow, 128, 0, s>>>(a, w);
+        if (map) k_wf_shadow<true><<<g_shadow, 128, 0, s>>>(a, w);
+        else k_wf_shadow<false><<<g_shadow, 128, 0, s>>>(a, w);
         k_wf_scatter<<<g_scatter, 128, 0, s>>>(a, w, cur);
         *launches += 4;
         cur ^= 1;

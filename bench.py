@@ -60,6 +60,9 @@ def parse():
                     help="light with a seeded synthetic 2048x1024 light map (Environment::Map) instead of the studio")
     ap.add_argument("--rmse-requests", type=int, default=6,
                     help="views rendered to the fixed RMSE for the time-to-RMSE latencies (0: skip)")
+    ap.add_argument("--rmse-reference-spp", type=int, default=0,
+                    help="also render the default view to this many paths/pixel (e.g. 16384) and compare the "
+                         "estimated RMSE at the target's paths/pixel with the error against that render")
     ap.add_argument("--rmse-target", type=float, default=RMSE_TARGET,
                     help="luminance RMSE to reach; 0 measures it on the default view at 1024 paths/pixel")
     return ap.parse_args()
@@ -296,6 +299,34 @@ def time_to_rmse(r, params, args, frame, stream):
                      "estimated from per-pixel sums of luminance and squared luminance"}
 
 
+def rmse_against_reference(r, params, args, frame):
+    """The estimator checked at full size: the default view at RMSE_TARGET_SPP
+    paths/pixel, its estimated RMSE, then the same accumulation continued to
+    `args.rmse_reference_spp` and the error of the first image against it. The
+    long render contains the short one, so the short image's expected squared
+    error against it is s^2 (1/a - 1/N) per pixel; the measured RMSE is scaled by
+    1 / sqrt(1 - a/N) to the error against the converged image."""
+    from volview_gb300 import convergence as CV
+    a, N = RMSE_TARGET_SPP, args.rmse_reference_spp
+    p = params  # the time-to-RMSE views before this moved the camera: a new accumulation
+    done = 0
+    while done < N:
+        n = min(1024, (a if done < a else N) - done)
+        r.record_frames(frame[0], n, p)
+        frame[0] += n
+        done += n
+        if done == a:
+            assert r.accumulated_samples() == a
+            acc, alb, _ = r.read_accumulation()
+            est = CV.rmse_estimate(acc, alb, a)
+            lum_a = acc[..., :3].astype(np.float64) @ CV.LUMA / a
+    acc, _, _ = r.read_accumulation()
+    lum_n = acc[..., :3].astype(np.float64) @ CV.LUMA / N
+    measured = float(np.sqrt(np.mean((lum_a - lum_n) ** 2)) / np.sqrt(1.0 - a / N))
+    return {"paths_per_pixel": a, "reference_paths_per_pixel": N, "estimated_rmse": est,
+            "rmse_against_reference": measured, "ratio": est / measured}
+
+
 def run_ours(args, rank, world, local):
     import torch
     from volview_gb300 import abi
@@ -388,6 +419,8 @@ def run_ours(args, rank, world, local):
                "d2h_bytes_per_step": W * H * 4,
                "call": "vv_record_frames + vv_read_output" if F > 1 else "vv_record + vv_read_output"}
     to_rmse = time_to_rmse(r, params, args, frame, stream) if args.rmse_requests > 0 else None
+    if args.rmse_reference_spp > 0 and to_rmse is not None:
+        to_rmse["check"] = rmse_against_reference(r, params, args, frame)
     # Roofline of the path-tracing pass (the wavefront stage kernels of a frame).
     alg_bytes = float(sum(counts[n] * b for n, b in zip(COUNT_NAMES, COUNT_BYTES)))
     pt_frame_ms = pt_ms / (args.steps * F)

@@ -85,12 +85,15 @@ enum {
     WF_TAKE_EXT = 6,  // entries of the extend queue taken so far
     WF_TAKE_SHADOW = 7,  // entries of the shadow queue taken so far
     WF_ESC0 = 8, WF_ESC1 = 9,  // flights that left the volume or hit the bounce limits
-    WF_COUNTERS = 10
+    WF_FIRST0 = 10, WF_FIRST1 = 11,  // first flights (bounce 0): a queue of their own
+    WF_COUNTERS = 12
 };
 struct WfArgs {
+    uint32_t capacity;     // slots (and queue entries) allocated
     float4* slots;
     float4* map;           // WF_MAP_BYTES per slot
-    uint32_t* ext[2];
+    uint32_t* ext[2];      // later flights
+    uint32_t* first[2];    // first flights
     uint32_t* esc[2];
     uint32_t* shade;
     uint32_t* shadow;

@@ -216,11 +216,11 @@ __global__ void __launch_bounds__(256) k_wf_init(const __grid_constant__ PtArgs 
         float4* q = slot_of(W, i);
         store_path(q, P, c);
         store_sums(q, S);
-        W.ext[0][i] = i;
+        W.first[0][i] = i;
     }
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         for (int k = 0; k < WF_COUNTERS; k++) W.counts[k] = 0;
-        W.counts[WF_EXT0] = slots;
+        W.counts[WF_FIRST0] = slots;
         W.counts[WF_ITEMS] = slots;
     }
 }
@@ -239,7 +239,10 @@ __global__ void __launch_bounds__(256) k_wf_init(const __grid_constant__ PtArgs 
 enum { EXT_END = 3 };
 __global__ void __launch_bounds__(128, VV_EXTEND_MIN_BLOCKS)
     k_wf_extend(const __grid_constant__ PtArgs A, const WfArgs W, int cur) {
-    const uint32_t n = W.counts[cur];
+    // First flights (cubic B-spline density) are taken before later ones
+    // (trilinear), as one range of indices: lanes that take work together get
+    // neighbouring indices, so a warp mostly runs one kind of flight.
+    const uint32_t n_first = W.counts[WF_FIRST0 + cur], n = n_first + W.counts[cur];
     const Consts C = make_consts(A);
     uint32_t slot = 0;
     f3 origin, dir, spectral;
@@ -254,7 +257,7 @@ __global__ void __launch_bounds__(128, VV_EXTEND_MIN_BLOCKS)
         if (__any_sync(0xffffffffu, need)) {
             uint32_t k = take_item(&W.counts[WF_TAKE_EXT], n, need);
             if (need && k != ~0u) {
-                slot = W.ext[cur][k];
+                slot = k < n_first ? W.first[cur][k] : W.ext[cur][k - n_first];
                 const float4* q = slot_of(W, slot);
                 float4 a = q[Q_ORIGIN], b = q[Q_DIR], s = q[Q_SPEC];
                 origin = xyz(a);
@@ -328,6 +331,7 @@ __global__ void __launch_bounds__(128, 4) k_wf_shade(const __grid_constant__ PtA
     }
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         W.counts[cur] = 0;
+        W.counts[WF_FIRST0 + cur] = 0;
         W.counts[WF_TAKE_EXT] = 0;
         W.counts[WF_ESC0 + (cur ^ 1)] = 0;  // finished by the previous wave's scatter
     }
@@ -418,7 +422,7 @@ __global__ void __launch_bounds__(128, 6) k_wf_scatter(const __grid_constant__ P
         bool valid = i < n;
         bool ended = i >= n_scatter;
         uint32_t slot = valid ? (ended ? W.esc[cur][i - n_scatter] : W.scatter[i]) : 0u;
-        bool to_ext = false, need = false;
+        bool to_ext = false, to_first = false, need = false;
         if (valid) {
             float4* q = slot_of(W, slot);
             Path P;
@@ -445,14 +449,15 @@ __global__ void __launch_bounds__(128, 6) k_wf_scatter(const __grid_constant__ P
                 PixelSums S;
                 load_sums(q, S);
                 if (escaped) stage_escape(A, C, P, S);
-                to_ext = end_path(A, C, P, S, c);
-                need = !to_ext;
+                to_first = end_path(A, C, P, S, c);
+                need = !to_first;
                 store_sums(q, S);
             }
             store_path(q, P, c);
         }
-        if (refill(A, W, C, slot, need)) to_ext = true;
+        if (refill(A, W, C, slot, need)) to_first = true;
         push(W.ext[nxt], &W.counts[nxt], slot, to_ext);
+        push(W.first[nxt], &W.counts[WF_FIRST0 + nxt], slot, to_first);
     }
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         W.counts[WF_SHADOW] = 0;
@@ -463,10 +468,10 @@ __global__ void __launch_bounds__(128, 6) k_wf_scatter(const __grid_constant__ P
 // The paths still alive, run to completion one thread each (the reference's
 // loop), including their pixels' remaining samples and frames.
 __global__ void __launch_bounds__(128, 4) k_wf_finish(const __grid_constant__ PtArgs A, const WfArgs W, int cur) {
-    uint32_t n = W.counts[cur];
+    uint32_t n_first = W.counts[WF_FIRST0 + cur], n = n_first + W.counts[cur];
     Consts C = make_consts(A);
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        uint32_t slot = W.ext[cur][i];
+        uint32_t slot = i < n_first ? W.first[cur][i] : W.ext[cur][i - n_first];
         float4* q = slot_of(W, slot);
         Path P;
         Ctl c;
@@ -506,7 +511,8 @@ cudaError_t launch_pt_wavefront(const PtArgs& a, const WfArgs& w, int sms, cudaS
     const char* env = std::getenv("VV_WF_TAIL");
     uint32_t tail = env ? (uint32_t)std::atoi(env) : 1024u;
     uint32_t pixels = a.width * a.height;
-    uint32_t slots = pixels;  // one frame's worth of paths in flight
+    uint32_t items = a.frames * pixels;
+    uint32_t slots = items < w.capacity ? items : w.capacity;  // paths in flight
     const bool map = a.u.lighting[3] == 2u;
     k_wf_init<<<(slots + 255) / 256 < (uint32_t)(sms * 8) ? (slots + 255) / 256 : sms * 8, 256, 0, s>>>(a, w, slots);
     *launches += 1;
@@ -523,10 +529,10 @@ cudaError_t launch_pt_wavefront(const PtArgs& a, const WfArgs& w, int sms, cudaS
         cudaError_t e = cudaGetLastError();
         if (e != cudaSuccess) return e;
         if (wave % check == check - 1) {
-            e = cudaMemcpyAsync(w.host_count, w.counts + cur, sizeof(uint32_t), cudaMemcpyDeviceToHost, s);
+            e = cudaMemcpyAsync(w.host_count, w.counts, WF_COUNTERS * sizeof(uint32_t), cudaMemcpyDeviceToHost, s);
             if (e == cudaSuccess) e = cudaStreamSynchronize(s);
             if (e != cudaSuccess) return e;
-            uint32_t live = *w.host_count;
+            uint32_t live = w.host_count[cur] + w.host_count[WF_FIRST0 + cur];
             if (live == 0) break;
             if (live <= tail) {
                 k_wf_finish<<<g_finish, 128, 0, s>>>(a, w, cur);

@@ -292,7 +292,9 @@ enum {
     VV_VOLUME_NORMALS = 1,  /* 4 x int8 per voxel (RGBA8_SNORM) */
     VV_VOLUME_MASK = 2,     /* 2 x uint16 per voxel (RG16_UNORM) */
     VV_VOLUME_LABELS = 3,   /* uint8 per voxel */
-    VV_VOLUME_MAJORANT = 4  /* float per brick, brick grid x-fastest */
+    VV_VOLUME_MAJORANT = 4, /* float per brick, brick grid x-fastest */
+    VV_VOLUME_SHADOW = 5,   /* ray marcher's shadow volume: RGBA16F, ceil(dims / 2), x-fastest */
+    VV_VOLUME_AO = 6        /* ray marcher's occlusion volume: R16F, ceil(dims / 4), x-fastest */
 };
 /* Copies a device volume out in x-fastest voxel order (whatever its layout on
  * the device). */

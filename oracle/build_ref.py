@@ -34,7 +34,7 @@ from concurrent.futures import ThreadPoolExecutor
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 OUT = os.path.join(HERE, "_ref")
-SHADERS = ["pt", "majorant", "normals", "mask", "denoise", "tonemap", "bloom"]
+SHADERS = ["pt", "majorant", "normals", "mask", "denoise", "tonemap", "bloom", "dvr", "shadow", "ao"]
 CXXFLAGS = ["-std=c++20", "-O2", "-fPIC", "-shared", "-fsingle-precision-constant",
             "-ffp-contract=off", "-fno-strict-aliasing", "-w", "-pthread"]
 

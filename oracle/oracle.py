@@ -42,7 +42,7 @@ def lib():
         _lib.vvo_pack_uniforms.argtypes = [P, P, C.c_int, C.c_int, C.c_float, P, C.c_uint32, C.c_uint64,
                                            C.c_uint32, C.c_uint32, P]
         _lib.vvo_env_prepare.restype = C.c_float
-        _lib.vvo_env_prepare.argtypes = [C.c_int, C.c_int, P, P, P]
+        _lib.vvo_env_prepare.argtypes = [C.c_int, C.c_int, P, P, P, P]
     return _lib
 
 
@@ -87,16 +87,17 @@ def hu_to_unorm16(hu):
     return out
 
 
-def env_prepare(rgb):
-    """EnvironmentMap::prepare + upload (environment.rs:57-130, renderer.rs:2224-2290) of an
+def env_prepare(rgb, diffuse=False):
+    """EnvironmentMap::prepare + upload (environment.rs:57-175, renderer.rs:2224-2290) of an
     (h, w, 3) linear-RGB light map: (RGBA16F radiance (h, w, 4) uint16, RG32F table
-    (h, w + 1, 2), peak_u)."""
+    (h, w + 1, 2), peak_u), and with `diffuse` the RGBA16F diffuse convolution (16, 32, 4)."""
     rgb = np.ascontiguousarray(rgb, np.float32)
     h, w = rgb.shape[:2]
     rad = np.zeros((h, w, 4), np.uint16)
     table = np.zeros((h, w + 1, 2), np.float32)
-    peak = lib().vvo_env_prepare(w, h, ptr(rgb), ptr(rad), ptr(table))
-    return rad, table, float(peak)
+    dif = np.zeros((16, 32, 4), np.uint16) if diffuse else None
+    peak = lib().vvo_env_prepare(w, h, ptr(rgb), ptr(rad), ptr(table), ptr(dif))
+    return (rad, table, float(peak)) + ((dif,) if diffuse else ())
 
 
 def geometry(volume):
@@ -144,7 +145,7 @@ class CpuRenderer:
         self.mask_key = None
         self.accumulated = 0
         self.accum_key = None
-        self.env_rad = self.env_table = None
+        self.env_rad = self.env_table = self.env_diffuse = None
         self.env_peak_u = 0.0
         zero = self._uniforms_geometry_only()
         self.normals = np.zeros(self.density.shape + (4,), np.int8)
@@ -181,10 +182,10 @@ class CpuRenderer:
     def set_environment_map(self, rgb=None):
         """Renderer::set_environment_map (renderer.rs:1283): (h, w, 3) linear RGB, or None."""
         if rgb is None:
-            self.env_rad = self.env_table = None
+            self.env_rad = self.env_table = self.env_diffuse = None
             self.env_peak_u = 0.0
         else:
-            self.env_rad, self.env_table, self.env_peak_u = env_prepare(rgb)
+            self.env_rad, self.env_table, self.env_peak_u, self.env_diffuse = env_prepare(rgb, diffuse=True)
         self.accum_key = None
 
     def brick_dims(self):

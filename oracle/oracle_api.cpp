@@ -28,7 +28,7 @@ void bspline(const Uniforms& u, const Scene& sc, const float* idx, long n, float
 void denoise(const Uniforms& u, const float* accum, const float* albedo, const float* normal, uint16_t* hdr,
              float* ping, float* pong, int threads);
 void post(const Uniforms& u, const uint16_t* hdr, float* exposure, uint8_t* out);
-float env_prepare(int w, int h, const float* pixels, uint16_t* radiance, float* table);
+float env_prepare(int w, int h, const float* pixels, uint16_t* radiance, float* table, uint16_t* diffuse);
 }  // namespace vvo
 
 using namespace vvo;
@@ -83,11 +83,12 @@ static const Uniforms& U(const void* p) { return *(const Uniforms*)p; }
 
 long vvo_uniform_size(void) { return (long)sizeof(Uniforms); }
 
-// EnvironmentMap::prepare (environment.rs:57-130) and the RGBA16F upload
+// EnvironmentMap::prepare (environment.rs:57-175) and the RGBA16F uploads
 // (renderer.rs:2224-2290): radiance as half RGBA (w x h), the sampling table
-// (RG32F, (w + 1) x h); returns peak_u.
-float vvo_env_prepare(int w, int h, const float* pixels, uint16_t* radiance, float* table) {
-    return env_prepare(w, h, pixels, radiance, table);
+// (RG32F, (w + 1) x h), the diffuse convolution (half RGBA, 32 x 16; may be
+// NULL); returns peak_u.
+float vvo_env_prepare(int w, int h, const float* pixels, uint16_t* radiance, float* table, uint16_t* diffuse) {
+    return env_prepare(w, h, pixels, radiance, table, diffuse);
 }
 
 void vvo_hu_to_unorm16(const int16_t* hu, long n, uint16_t* out) {

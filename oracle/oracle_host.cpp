@@ -303,7 +303,51 @@ int mask_margin(const Geometry& G, const vv_label_params& l) {
 // f64 in the Rust's order; per-texel arithmetic in f32 without contraction.
 static float env_luminance(const float* c) { return 0.2126f * c[0] + 0.7152f * c[1] + 0.0722f * c[2]; }
 
-float env_prepare(int w, int h, const float* pixels, uint16_t* radiance, float* table) {
+// environment.rs:133-175: the normalised radiance box-filtered to at most
+// 128 x 64, then convolved with a clamped cosine lobe into 32 x 16 texels, to
+// RGBA16F (min 60000) as uploaded. f32 arithmetic in the Rust's order.
+static void env_diffuse(int w, int h, const float* rad, uint16_t* out) {
+    const float PI_F = 3.14159265358979323846f;
+    auto direction = [&](float uu, float vv, float d[3]) {
+        float phi = (uu - 0.5f) * 2.0f * PI_F, theta = vv * PI_F;
+        d[0] = std::sin(theta) * std::sin(phi);
+        d[1] = std::cos(theta);
+        d[2] = std::sin(theta) * std::cos(phi);
+    };
+    int sw = std::min(128, w), sh = std::max(sw / 2, 1);
+    std::vector<float> small(6 * (size_t)sw * sh);  // radiance x solid angle rgb, direction xyz
+    for (int i = 0; i < sw * sh; i++) {
+        int sx = i % sw, sy = i / sw;
+        int x0 = sx * w / sw, x1 = std::max((sx + 1) * w / sw, sx * w / sw + 1);
+        int y0 = sy * h / sh, y1 = std::max((sy + 1) * h / sh, sy * h / sh + 1);
+        float c[3] = {0.0f, 0.0f, 0.0f};
+        for (int y = y0; y < y1; y++)
+            for (int x = x0; x < x1; x++)
+                for (int k = 0; k < 3; k++) c[k] = c[k] + rad[4 * ((size_t)y * w + x) + k];
+        float n = (float)((y1 - y0) * (x1 - x0));
+        float uu = ((float)sx + 0.5f) / (float)sw, vv = ((float)sy + 0.5f) / (float)sh;
+        float solid = (2.0f * PI_F / (float)sw) * (PI_F / (float)sh) * std::sin(PI_F * vv);
+        float* e = small.data() + 6 * (size_t)i;
+        for (int k = 0; k < 3; k++) e[k] = c[k] / n * solid;
+        direction(uu, vv, e + 3);
+    }
+    const int dw = 32, dh = 16;
+    for (int i = 0; i < dw * dh; i++) {
+        float nrm[3];
+        direction(((float)(i % dw) + 0.5f) / (float)dw, ((float)(i / dw) + 0.5f) / (float)dh, nrm);
+        float c[3] = {0.0f, 0.0f, 0.0f};
+        for (int j = 0; j < sw * sh; j++) {
+            const float* e = small.data() + 6 * (size_t)j;
+            float cs = nrm[0] * e[3] + nrm[1] * e[4] + nrm[2] * e[5];
+            if (cs > 0.0f)
+                for (int k = 0; k < 3; k++) c[k] = c[k] + e[k] * cs;
+        }
+        for (int k = 0; k < 3; k++) out[4 * i + k] = glsl::float_to_half(std::min(c[k] / PI_F, 60000.0f));
+        out[4 * i + 3] = glsl::float_to_half(1.0f);
+    }
+}
+
+float env_prepare(int w, int h, const float* pixels, uint16_t* radiance, float* table, uint16_t* diffuse) {
     const float PI_F = 3.14159265358979323846f;
     auto sin_theta = [&](int y) { return std::sin(PI_F * ((float)y + 0.5f) / (float)h); };
     // Mean radiance over the sphere (texels weighted by their solid angle).
@@ -318,10 +362,16 @@ float env_prepare(int w, int h, const float* pixels, uint16_t* radiance, float* 
     }
     float mean_rgb[3] = {(float)(sum[0] / weight), (float)(sum[1] / weight), (float)(sum[2] / weight)};
     float mean = std::max(env_luminance(mean_rgb), 1e-6f);
+    std::vector<float> rad_f((size_t)4 * w * h);
     for (long i = 0; i < (long)w * h; i++) {
-        for (int c = 0; c < 3; c++) radiance[4 * i + c] = glsl::float_to_half(std::min(pixels[3 * i + c] / mean, 60000.0f));
+        for (int c = 0; c < 3; c++) {
+            rad_f[4 * i + c] = pixels[3 * i + c] / mean;
+            radiance[4 * i + c] = glsl::float_to_half(std::min(rad_f[4 * i + c], 60000.0f));
+        }
+        rad_f[4 * i + 3] = 1.0f;
         radiance[4 * i + 3] = glsl::float_to_half(1.0f);
     }
+    if (diffuse) env_diffuse(w, h, rad_f.data(), diffuse);
     // Importance sampling proportional to luminance x solid angle.
     std::vector<float> f((size_t)w * h);
     for (long i = 0; i < (long)w * h; i++) f[i] = env_luminance(pixels + 3 * i) * sin_theta((int)(i / w));

@@ -189,3 +189,92 @@ def post(uniforms, hdr, exposure):
 
 def _threads():
     return max(1, min(os.cpu_count() or 1, 64))
+
+
+SHADOW_DOWNSAMPLE, AO_DOWNSAMPLE = 2, 4  # renderer.rs:35-40
+CLAMP_TO_BORDER_WHITE = 1
+
+
+def _downsampled(dims, k):
+    """renderer.rs:2139-2145: (nx, ny, nz) divided by k, rounded up."""
+    return tuple((d + k - 1) // k for d in dims)
+
+
+def ao_volume(r, uniforms):
+    """ao.comp over the occlusion volume (renderer.rs:1709-1728): R16F, (z, y, x)."""
+    l = shader("ao")
+    dummy = np.zeros(16, np.uint8)
+    l.ref_set_uniforms(_p(uniforms), 21200)
+    bind_common(l, r, dummy)
+    ad = _downsampled(r.dims, AO_DOWNSAMPLE)
+    out = np.zeros(ad[::-1], np.uint16)
+    l.ref_bind_image(b"ao_image", _p(out), R16F, *ad)
+    push = np.array([ad[0], ad[1], ad[2], 0, 0, 0, 0, 0], np.int32)
+    l.ref_set_push(_p(push), push.nbytes)
+    l.ref_run(0, ad[0], 0, ad[1], 0, ad[2], _threads())
+    return out
+
+
+def shadow_volume(r, uniforms):
+    """record_shadow_sweep (renderer.rs:1907-1950) with shadow.comp: slices swept
+    away from the key light along its dominant axis; RGBA16F, (z, y, x, 4),
+    starting from zeros."""
+    l = shader("shadow")
+    dummy = np.zeros(16, np.uint8)
+    l.ref_set_uniforms(_p(uniforms), 21200)
+    bind_common(l, r, dummy)
+    sd = _downsampled(r.dims, SHADOW_DOWNSAMPLE)
+    vol = np.zeros(sd[::-1] + (4,), np.uint16)
+    l.ref_bind_texture(b"shadow_tex", _p(vol), RGBA16F, *sd, LINEAR, CLAMP_TO_BORDER_WHITE)
+    l.ref_bind_image(b"shadow_image", _p(vol), RGBA16F, *sd)
+    return l, sd, vol
+
+
+def _shadow_axis(w2i_cols, light_dir, sd, dims):
+    """renderer.rs:1915-1928 in f32: the light's dominant axis in shadow-volume units and its sign."""
+    f32 = np.float32
+    m = [np.array(w2i_cols[c][:3], f32) for c in range(3)]
+    v = np.array(light_dir, f32)
+    l_idx = m[0] * v[0]
+    l_idx = m[1] * v[1] + l_idx
+    l_idx = m[2] * v[2] + l_idx
+    l_idx = l_idx * (np.array(sd, f32) / np.array(dims, f32))
+    a = np.abs(l_idx)
+    axis = 0 if (a[0] >= a[1] and a[0] >= a[2]) else (1 if a[1] >= a[2] else 2)
+    return axis, (1 if l_idx[axis] >= 0 else -1)
+
+
+def shadow_sweep(r, uniforms, light_dir):
+    """The shadow volume of `light_dir` (the packed uniform's light_dir.xyz)."""
+    l, sd, vol = shadow_volume(r, uniforms)
+    cols = uniforms.view(np.float32)[0:16].reshape(4, 4)
+    axis, sign = _shadow_axis(cols, light_dir, sd, r.dims)
+    u_axis, v_axis = (axis + 1) % 3, (axis + 2) % 3
+    n = sd[axis]
+    for i in range(n):
+        sl = n - 1 - i if sign > 0 else i
+        push = np.array([sd[0], sd[1], sd[2], 0, axis, sl, sign, 0], np.int32)
+        l.ref_set_push(_p(push), push.nbytes)
+        l.ref_run(0, sd[u_axis], 0, sd[v_axis], 0, 1, _threads())
+    return vol
+
+
+def dvr(r, uniforms, width, height, shadow=None, ao=None):
+    """dvr.comp over the image: RGBA16F (radiance, transmittance), (height, width, 4)."""
+    l = shader("dvr")
+    dummy = np.zeros(16, np.uint8)
+    l.ref_set_uniforms(_p(uniforms), 21200)
+    bind_common(l, r, dummy)
+    if shadow is not None:
+        sz, sy, sx = shadow.shape[:3]
+        l.ref_bind_texture(b"shadow_tex", _p(shadow), RGBA16F, sx, sy, sz, LINEAR, CLAMP_TO_BORDER_WHITE)
+    if ao is not None:
+        az, ay, ax = ao.shape
+        l.ref_bind_texture(b"ao_tex", _p(ao), R16F, ax, ay, az, LINEAR, CLAMP_TO_BORDER_WHITE)
+    if getattr(r, "env_diffuse", None) is not None:
+        dh, dw = r.env_diffuse.shape[:2]
+        l.ref_bind_texture(b"env_diffuse_tex", _p(r.env_diffuse), RGBA16F, dw, dh, 1, LINEAR, 0)
+    hdr = np.zeros((height, width, 4), np.uint16)
+    l.ref_bind_image(b"hdr_image", _p(hdr), RGBA16F, width, height, 1)
+    l.ref_run(0, width, 0, height, 0, 1, _threads())
+    return hdr

@@ -9,7 +9,9 @@ of the render crate; the density normalisation and LUT are themselves pinned by
 the reference's unit tests (crates/render/src/transfer.rs:130-149).
 
 light_map_fixture() writes tests/golden/small_light_map.npz: the same scene lit
-by a seeded synthetic light map (Environment::Map).
+by a seeded synthetic light map (Environment::Map); raymarch_fixture() writes
+tests/golden/small_raymarch.npz: the real-time ray marcher's occlusion volume,
+shadow volume and image (ao.comp, shadow.comp, dvr.comp).
 
 Usage (needs the reference sources): python tests/golden/make_golden.py
 """
@@ -100,6 +102,48 @@ def light_map_fixture():
     print(out, os.path.getsize(out), "bytes")
 
 
+def raymarch_fixture():
+    """The real-time ray marcher (path_tracing off) on the same scene: the
+    ambient-occlusion volume (ao.comp), the shadow volume swept towards the key
+    light (shadow.comp, record_shadow_sweep) and the image (dvr.comp), for
+    point-sampled and pre-integrated transfer functions, studio and light map."""
+    n, W, H = 24, 32, 24
+    cfg = scene.small_config(n=n, size=W, spp=1)
+    r = O.CpuRenderer(cfg["volume"], cfg["tf"], cfg["hu"])
+    r.set_labels(cfg["labels_vol"], cfg["soft"])
+    light_map = scene.synthetic_light_map(32, 16, seed=5)
+    g = r.geo
+    r.resize(W, H)
+    r.normals = R.normals(r, r._uniforms_geometry_only())
+    out = {"hu": cfg["hu"], "labels": cfg["labels_vol"], "soft": cfg["soft"], "spacing": np.array(cfg["spacing"]),
+           "width": W, "height": H, "light_map": light_map}
+    for name, pre, env in (("point", 0, False), ("preint", 1, False), ("map", 1, True)):
+        params = scene.frame_params_for(cfg, list(g.center), g.diagonal, clip_sagittal=True)
+        params.camera.distance = abi.f32(params.camera.distance * 0.6)
+        params.path_tracing.enabled = 0
+        params.preintegrate = pre
+        if env:
+            r.set_environment_map(light_map)
+            params.lighting.environment = abi.ENV_MAP
+        else:
+            r.set_environment_map(None)
+        u = r.uniforms(params, 1, W, H)
+        r.mask = R.mask(r, u, O.mask_margin(cfg["volume"], params.labels), int(params.labels.smoothing))
+        r.majorant = R.majorant(r, u)
+        ao = R.ao_volume(r, u)
+        shadow = R.shadow_sweep(r, u, u.view(np.float32)[44:47])
+        hdr = R.dvr(r, u, W, H, shadow=shadow, ao=ao)
+        out.update({f"{name}_params": np.frombuffer(bytes(params), np.uint8), f"{name}_uniforms": u,
+                    f"{name}_ao": ao, f"{name}_shadow": shadow, f"{name}_hdr": hdr})
+        if env:
+            out["map_env_diffuse"] = r.env_diffuse
+    out["mask"], out["majorant"] = r.mask, r.majorant
+    path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "small_raymarch.npz")
+    np.savez_compressed(path, **out)
+    print(path, os.path.getsize(path), "bytes")
+
+
 if __name__ == "__main__":
     main()
     light_map_fixture()
+    raymarch_fixture()

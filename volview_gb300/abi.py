@@ -18,7 +18,7 @@ ENV_DOME, ENV_STUDIO, ENV_MAP = range(3)
 TONE_NONE, TONE_ACES, TONE_AGX = range(3)
 PLANE_SAGITTAL, PLANE_CORONAL, PLANE_AXIAL = range(3)
 DENOISE_OFF, DENOISE_ATROUS, DENOISE_OIDN = range(3)
-VOLUME_DENSITY, VOLUME_NORMALS, VOLUME_MASK, VOLUME_LABELS, VOLUME_MAJORANT = range(5)
+VOLUME_DENSITY, VOLUME_NORMALS, VOLUME_MASK, VOLUME_LABELS, VOLUME_MAJORANT, VOLUME_SHADOW, VOLUME_AO = range(7)
 
 F4x256 = (C.c_float * 4) * VV_LABEL_COUNT
 

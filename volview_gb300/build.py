@@ -13,7 +13,8 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libvolpt.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-SOURCES = ["vv_volume.cu", "vv_pt.cu", "vv_wavefront.cu", "vv_post.cu", "vv_noalloc.cu", "vv_host.cpp"]
+SOURCES = ["vv_volume.cu", "vv_pt.cu", "vv_wavefront.cu", "vv_raymarch.cu", "vv_post.cu", "vv_noalloc.cu",
+           "vv_host.cpp"]
 # Host code never contracts a*b+c into an FMA (Rust, whose host math the
 # renderer restates, does not either; gcc does by default on Arm).
 NVFLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",

@@ -212,8 +212,13 @@ struct vv_renderer {
     uint32_t width = 0, height = 0;
     DBuf accum, albedo, normal, ping, pong, guide_nd, guide_alb, hdr, out, bloom[4];
     int bw[4], bh[4];
-    // light map (Environment::Map): RGBA16F radiance, RG32F sampling table
-    DBuf env_rad, env_table;
+    // pre-integrated transfer function (RGBA32F, 4096), ray-marcher lighting volumes
+    DBuf preint, shadow_vol, ao_vol;
+    int shadow_dims[3] = {0, 0, 0}, ao_dims[3] = {0, 0, 0};
+    std::vector<uint8_t> ao_key, shadow_key;
+    // light map (Environment::Map): RGBA16F radiance, RG32F sampling table,
+    // RGBA16F diffuse convolution (32 x 16, the ray marcher's ambient light)
+    DBuf env_rad, env_table, env_diffuse;
     int env_w = 0, env_h = 0;
     bool has_env = false;
     float env_peak_u = 0.0f;
@@ -303,6 +308,24 @@ static vv_status upload_tf(vv_renderer* r, const vv_transfer_function* tf) {
     for (int i = 0; i < 4 * 4096; i++) lut_half[i] = (float)(_Float16)lut[i];
     CK(r->lut.alloc(lut_half.size() * sizeof(float)));
     CK(cudaMemcpyAsync(r->lut.p, lut_half.data(), lut_half.size() * sizeof(float), cudaMemcpyHostToDevice,
+                       r->ctx->stream));
+    // transfer.rs:103-117: cumulative integrals of (albedo x extinction,
+    // extinction) over density, trapezoid rule in f64, for pre-integration.
+    std::vector<float> preint(4 * 4096, 0.0f);
+    double sum[4] = {0.0, 0.0, 0.0, 0.0};
+    const double dx = 1.0 / 4095.0;
+    for (int i = 1; i < 4096; i++) {
+        const float* e0 = &lut[4 * (i - 1)];
+        const float* e1 = &lut[4 * i];
+        double a[4] = {(double)(e0[0] * e0[3]), (double)(e0[1] * e0[3]), (double)(e0[2] * e0[3]), (double)e0[3]};
+        double b[4] = {(double)(e1[0] * e1[3]), (double)(e1[1] * e1[3]), (double)(e1[2] * e1[3]), (double)e1[3]};
+        for (int c = 0; c < 4; c++) {
+            sum[c] += 0.5 * (a[c] + b[c]) * dx;
+            preint[4 * i + c] = (float)sum[c];
+        }
+    }
+    CK(r->preint.alloc(preint.size() * sizeof(float)));
+    CK(cudaMemcpyAsync(r->preint.p, preint.data(), preint.size() * sizeof(float), cudaMemcpyHostToDevice,
                        r->ctx->stream));
     CK(r->bucket_dev.alloc(64 * sizeof(float)));
     CK(cudaMemcpyAsync(r->bucket_dev.p, r->bucket, sizeof(r->bucket), cudaMemcpyHostToDevice, r->ctx->stream));
@@ -604,7 +627,7 @@ extern "C" vv_status vv_renderer_destroy(vv_renderer* r) {
     cudaSetDevice(r->ctx->device);
     cudaStreamSynchronize(r->ctx->stream);
     DBuf* all[] = {&r->density, &r->normals, &r->mask_a, &r->mask_b, &r->labels, &r->majorant, &r->env_rad,
-                   &r->env_table, &r->lut,
+                   &r->env_table, &r->env_diffuse, &r->preint, &r->shadow_vol, &r->ao_vol, &r->lut,
                    &r->bucket_dev, &r->tables, &r->soft, &r->work, &r->exposure, &r->accum, &r->albedo,
                    &r->normal, &r->ping, &r->pong, &r->guide_nd, &r->guide_alb, &r->hdr, &r->out, &r->bloom[0], &r->bloom[1], &r->bloom[2],
                    &r->bloom[3]};
@@ -710,7 +733,58 @@ extern "C" vv_status vv_set_labels(vv_renderer* r, const uint8_t* labels, size_t
 // without floating-point contraction, as Rust compiles).
 static float env_lum(const float* c) { return 0.2126f * c[0] + 0.7152f * c[1] + 0.0722f * c[2]; }
 
-static float prepare_light_map(int w, int h, const float* px, std::vector<uint16_t>& rad, std::vector<float>& table) {
+// environment.rs:133-175: the normalised radiance box-filtered to at most
+// 128 x 64, convolved with a clamped cosine lobe into 32 x 16 texels, as RGBA16F.
+static void light_map_diffuse(int w, int h, const std::vector<float>& rad, std::vector<uint16_t>& out) {
+    const float PI_F = 3.14159265358979323846f;
+    auto direction = [&](float uu, float vv, float d[3]) {
+        float phi = (uu - 0.5f) * 2.0f * PI_F, theta = vv * PI_F;
+        d[0] = std::sin(theta) * std::sin(phi);
+        d[1] = std::cos(theta);
+        d[2] = std::sin(theta) * std::cos(phi);
+    };
+    auto half_bits = [](float v) {
+        _Float16 hv = (_Float16)v;
+        uint16_t b;
+        std::memcpy(&b, &hv, 2);
+        return b;
+    };
+    int sw = std::min(128, w), sh = std::max(sw / 2, 1);
+    std::vector<float> small(6 * (size_t)sw * sh);
+    for (int i = 0; i < sw * sh; i++) {
+        int sx = i % sw, sy = i / sw;
+        int x0 = sx * w / sw, x1 = std::max((sx + 1) * w / sw, sx * w / sw + 1);
+        int y0 = sy * h / sh, y1 = std::max((sy + 1) * h / sh, sy * h / sh + 1);
+        float c[3] = {0.0f, 0.0f, 0.0f};
+        for (int y = y0; y < y1; y++)
+            for (int x = x0; x < x1; x++)
+                for (int k = 0; k < 3; k++) c[k] = c[k] + rad[4 * ((size_t)y * w + x) + k];
+        float n = (float)((y1 - y0) * (x1 - x0));
+        float uu = ((float)sx + 0.5f) / (float)sw, vv = ((float)sy + 0.5f) / (float)sh;
+        float solid = (2.0f * PI_F / (float)sw) * (PI_F / (float)sh) * std::sin(PI_F * vv);
+        float* e = small.data() + 6 * (size_t)i;
+        for (int k = 0; k < 3; k++) e[k] = c[k] / n * solid;
+        direction(uu, vv, e + 3);
+    }
+    const int dw = 32, dh = 16;
+    out.assign(4 * dw * dh, 0);
+    for (int i = 0; i < dw * dh; i++) {
+        float nrm[3];
+        direction(((float)(i % dw) + 0.5f) / (float)dw, ((float)(i / dw) + 0.5f) / (float)dh, nrm);
+        float c[3] = {0.0f, 0.0f, 0.0f};
+        for (int j = 0; j < sw * sh; j++) {
+            const float* e = small.data() + 6 * (size_t)j;
+            float cs = nrm[0] * e[3] + nrm[1] * e[4] + nrm[2] * e[5];
+            if (cs > 0.0f)
+                for (int k = 0; k < 3; k++) c[k] = c[k] + e[k] * cs;
+        }
+        for (int k = 0; k < 3; k++) out[4 * i + k] = half_bits(std::min(c[k] / PI_F, 60000.0f));
+        out[4 * i + 3] = half_bits(1.0f);
+    }
+}
+
+static float prepare_light_map(int w, int h, const float* px, std::vector<uint16_t>& rad, std::vector<float>& table,
+                               std::vector<uint16_t>& diffuse) {
     const float PI_F = 3.14159265358979323846f;
     auto sin_theta = [&](int y) { return std::sin(PI_F * ((float)y + 0.5f) / (float)h); };
     double sum[3] = {0.0, 0.0, 0.0}, weight = 0.0;
@@ -732,10 +806,16 @@ static float prepare_light_map(int w, int h, const float* px, std::vector<uint16
         std::memcpy(&b, &hv, 2);
         return b;
     };
+    std::vector<float> rad_f(4 * n);
     for (size_t i = 0; i < n; i++) {
-        for (int c = 0; c < 3; c++) rad[4 * i + c] = half_bits(std::min(px[3 * i + c] / mean, 60000.0f));
+        for (int c = 0; c < 3; c++) {
+            rad_f[4 * i + c] = px[3 * i + c] / mean;
+            rad[4 * i + c] = half_bits(std::min(rad_f[4 * i + c], 60000.0f));
+        }
+        rad_f[4 * i + 3] = 1.0f;
         rad[4 * i + 3] = half_bits(1.0f);
     }
+    light_map_diffuse(w, h, rad_f, diffuse);
     std::vector<float> f(n);
     for (size_t i = 0; i < n; i++) f[i] = env_lum(px + 3 * i) * sin_theta((int)(i / (size_t)w));
     std::vector<double> row_sums(h);
@@ -784,6 +864,7 @@ extern "C" vv_status vv_set_environment_map(vv_renderer* r, const vv_environment
     if (!map) {
         r->env_rad.release();
         r->env_table.release();
+        r->env_diffuse.release();
         r->has_env = false;
         r->env_w = r->env_h = 0;
         r->env_peak_u = 0.0f;
@@ -794,11 +875,13 @@ extern "C" vv_status vv_set_environment_map(vv_renderer* r, const vv_environment
     if (map->width == 0 || map->height == 0) return fail(VV_ERR_ARG, "empty light map");
     if (map->width > 16384 || map->height > 16384) return fail(VV_ERR_LIMIT, "light map above 16384 texels per axis");
     int w = (int)map->width, h = (int)map->height;
-    std::vector<uint16_t> rad;
+    std::vector<uint16_t> rad, diffuse;
     std::vector<float> table;
-    float peak = prepare_light_map(w, h, map->rgb, rad, table);
+    float peak = prepare_light_map(w, h, map->rgb, rad, table, diffuse);
     CK(r->env_rad.alloc(rad.size() * sizeof(uint16_t)));
     CK(r->env_table.alloc(table.size() * sizeof(float)));
+    CK(r->env_diffuse.alloc(diffuse.size() * sizeof(uint16_t)));
+    CK(cudaMemcpy(r->env_diffuse.p, diffuse.data(), diffuse.size() * sizeof(uint16_t), cudaMemcpyHostToDevice));
     CK(cudaMemcpy(r->env_rad.p, rad.data(), rad.size() * sizeof(uint16_t), cudaMemcpyHostToDevice));
     CK(cudaMemcpy(r->env_table.p, table.data(), table.size() * sizeof(float), cudaMemcpyHostToDevice));
     r->env_w = w;
@@ -872,6 +955,8 @@ static PtArgs pt_args(vv_renderer* r, const UHead& u) {
     a.labels = r->labels.as<uint8_t>();
     a.majorant = r->majorant.as<float>();
     a.env_rad = r->env_rad.as<ushort4>();
+    a.env_diffuse = r->env_diffuse.as<ushort4>();
+    a.preint = r->preint.as<float4>();
     a.env_table = r->env_table.as<float2>();
     a.env_w = r->env_w;
     a.env_h = r->env_h;
@@ -966,13 +1051,11 @@ static PostArgs post_args(vv_renderer* r, const UHead& u) {
 // (renderer.rs:1554-1706); returns the packed head.
 static vv_status prepare_frame(vv_renderer* r, const vv_frame_params& p, uint64_t frame, UHead& u) {
     if (!r->accum.p) return fail(VV_ERR_STATE, "resize() must be called before record()");
-    if (!p.path_tracing.enabled)
-        return fail(VV_ERR_ARG, "only path tracing is supported (path_tracing.enabled = 0 selects the ray marcher)");
     if (p.labels.mode < 0 || p.labels.mode > 3) return fail(VV_ERR_ARG, "label mode out of range");
     vv_status s = use_device(r);
     if (s != VV_OK) return s;
     cudaStream_t st = r->ctx->stream;
-    if (!r->have_params || !same_accumulation(r->accumulated_params, p)) {
+    if (p.path_tracing.enabled && (!r->have_params || !same_accumulation(r->accumulated_params, p))) {
         r->accumulated = 0;
         r->accumulated_params = p;
         r->have_params = true;
@@ -1023,7 +1106,7 @@ static vv_status prepare_frame(vv_renderer* r, const vv_frame_params& p, uint64_
         r->majorant_key = key;
         r->have_majorant_key = true;
     }
-    if (r->accumulated == 0) {
+    if (p.path_tracing.enabled && r->accumulated == 0) {
         size_t bytes = (size_t)r->width * r->height * 16;
         CK(cudaMemsetAsync(r->accum.p, 0, bytes, st));
         CK(cudaMemsetAsync(r->albedo.p, 0, bytes, st));
@@ -1044,11 +1127,76 @@ static vv_status finish_frame(vv_renderer* r, const vv_frame_params& p, const UH
     return VV_OK;
 }
 
+// The ray marcher's frame (renderer.rs:1707-1790): the occlusion volume when
+// the opacity or the clipping changed, the shadow volume when the light or the
+// tint changed as well, then dvr.comp into the HDR image and the display.
+static void append_key(std::vector<uint8_t>& k, const void* p, size_t n) {
+    const uint8_t* b = (const uint8_t*)p;
+    k.insert(k.end(), b, b + n);
+}
+static vv_status record_ray_march(vv_renderer* r, const vv_frame_params& p, const UHead& u) {
+    cudaStream_t st = r->ctx->stream;
+    const int dims[3] = {(int)r->vol.nx, (int)r->vol.ny, (int)r->vol.nz};
+    if (!r->shadow_vol.p) {
+        for (int a = 0; a < 3; a++) {
+            r->shadow_dims[a] = (dims[a] + 1) / 2;  // SHADOW_DOWNSAMPLE (renderer.rs:35)
+            r->ao_dims[a] = (dims[a] + 3) / 4;      // AO_DOWNSAMPLE (renderer.rs:39)
+        }
+        CK(r->shadow_vol.alloc((size_t)r->shadow_dims[0] * r->shadow_dims[1] * r->shadow_dims[2] * 8));
+        CK(r->ao_vol.alloc((size_t)r->ao_dims[0] * r->ao_dims[1] * r->ao_dims[2] * 2));
+        CK(cudaMemsetAsync(r->shadow_vol.p, 0, r->shadow_vol.n, st));
+        CK(cudaMemsetAsync(r->ao_vol.p, 0, r->ao_vol.n, st));
+    }
+    PtArgs a = pt_args(r, u);
+    int launches = 0;
+    OpacityKey opacity = opacity_key(r, p.labels);
+    std::vector<uint8_t> ao_key;  // (opacity, clip key: renderer.rs:1663-1667)
+    append_key(ao_key, &opacity, sizeof(opacity));
+    append_key(ao_key, u.clip, 2 * sizeof(uint32_t));
+    append_key(ao_key, u.clip_planes, 12 * sizeof(float));
+    if (p.lighting.ambient_occlusion && r->ao_key != ao_key) {
+        CK(launch_ao(a, r->ao_vol.as<uint16_t>(), r->ao_dims[0], r->ao_dims[1], r->ao_dims[2], st));
+        launches += 1;
+        r->ao_key = ao_key;
+    }
+    std::vector<uint8_t> shadow_key = ao_key;  // + light direction bits and the tint (renderer.rs:1730-1748)
+    append_key(shadow_key, u.light_dir, 3 * sizeof(float));
+    append_key(shadow_key, p.labels.colors, sizeof(p.labels.colors));
+    append_key(shadow_key, &p.lighting.scattering_distance, sizeof(float));
+    if (p.lighting.shadows && r->shadow_key != shadow_key) {
+        // record_shadow_sweep (renderer.rs:1907-1928): sweep away from the light
+        // along its dominant axis in shadow-volume units.
+        const float* m = u.w2i;
+        float ld[3] = {u.light_dir[0], u.light_dir[1], u.light_dir[2]};
+        float l_idx[3];
+        for (int k = 0; k < 3; k++) {
+            float v = m[k] * ld[0];
+            v = m[4 + k] * ld[1] + v;
+            v = m[8 + k] * ld[2] + v;
+            l_idx[k] = v * ((float)r->shadow_dims[k] / r->dims[k]);
+        }
+        float ax = std::fabs(l_idx[0]), ay = std::fabs(l_idx[1]), az = std::fabs(l_idx[2]);
+        int axis = (ax >= ay && ax >= az) ? 0 : (ay >= az ? 1 : 2);
+        int sign = l_idx[axis] >= 0.0f ? 1 : -1;
+        CK(launch_shadow_sweep(a, r->shadow_vol.as<ushort4>(), r->shadow_dims[0], r->shadow_dims[1],
+                               r->shadow_dims[2], axis, sign, st, &launches));
+        r->shadow_key = shadow_key;
+    }
+    CK(launch_dvr(a, r->shadow_vol.as<ushort4>(), r->shadow_dims[0], r->shadow_dims[1], r->shadow_dims[2],
+                  r->ao_vol.as<uint16_t>(), r->ao_dims[0], r->ao_dims[1], r->ao_dims[2], st));
+    launches += 1;
+    PostArgs pa = post_args(r, u);
+    CK(launch_post(pa, st, &launches));
+    r->launches += launches;
+    return VV_OK;
+}
+
 extern "C" vv_status vv_record(vv_renderer* r, uint64_t frame, const vv_frame_params* params) {
     if (!r || !params) return fail(VV_ERR_ARG, "null argument");
     UHead u;
     vv_status s = prepare_frame(r, *params, frame, u);
     if (s != VV_OK) return s;
+    if (!params->path_tracing.enabled) return record_ray_march(r, *params, u);
     PtArgs a = pt_args(r, u);
     int launches = 0;
     pt_timer_start(r);
@@ -1061,6 +1209,8 @@ extern "C" vv_status vv_record(vv_renderer* r, uint64_t frame, const vv_frame_pa
 extern "C" vv_status vv_record_frames(vv_renderer* r, uint64_t first_frame, uint32_t frames,
                                       const vv_frame_params* params) {
     if (!r || !params) return fail(VV_ERR_ARG, "null argument");
+    if (!params->path_tracing.enabled)
+        return fail(VV_ERR_ARG, "vv_record_frames accumulates path-traced frames (path_tracing.enabled = 0)");
     if (frames == 0) return VV_OK;
     // Work items are (frame, pixel) pairs counted in 32 bits on the device,
     // with room left for the counter's overshoot at the end of the pass.
@@ -1159,10 +1309,11 @@ extern "C" vv_status vv_read_volume(vv_renderer* r, int which, void* out, size_t
     if (s != VV_OK) return s;
     cudaStream_t st = r->ctx->stream;
     size_t voxels = (size_t)r->vol.nx * r->vol.ny * r->vol.nz;
-    if (which == VV_VOLUME_MAJORANT) {
-        size_t bytes = (size_t)r->vol.bx * r->vol.by * r->vol.bz * 4;
-        if (capacity < bytes) return fail(VV_ERR_ARG, "output buffer too small");
-        CK(cudaMemcpyAsync(out, r->majorant.p, bytes, cudaMemcpyDeviceToHost, st));
+    if (which == VV_VOLUME_MAJORANT || which == VV_VOLUME_SHADOW || which == VV_VOLUME_AO) {
+        const DBuf& b = which == VV_VOLUME_MAJORANT ? r->majorant : (which == VV_VOLUME_SHADOW ? r->shadow_vol : r->ao_vol);
+        if (!b.p) return fail(VV_ERR_STATE, "that volume has not been computed");
+        if (capacity < b.n) return fail(VV_ERR_ARG, "output buffer too small");
+        CK(cudaMemcpyAsync(out, b.p, b.n, cudaMemcpyDeviceToHost, st));
         CK(cudaStreamSynchronize(st));
         return VV_OK;
     }

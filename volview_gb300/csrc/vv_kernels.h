@@ -30,6 +30,8 @@ struct PtArgs {
     const uint32_t* normals;
     const uint8_t* labels;
     const float* majorant;
+    const float4* preint;       // cumulative transfer-function integrals, 4096 (ray marcher)
+    const ushort4* env_diffuse; // light map's diffuse convolution, 32 x 16 RGBA16F (ray marcher)
     const ushort4* env_rad;     // light map radiance, RGBA16F, env_w x env_h (lighting.w == 2)
     const float2* env_table;    // light map sampling table, (env_w + 1) x env_h
     int env_w, env_h;
@@ -103,6 +105,13 @@ struct WfArgs {
 };
 // Accumulate-frames with the wavefront tracer (same results as launch_pt).
 cudaError_t launch_pt_wavefront(const PtArgs& a, const WfArgs& w, int sms, cudaStream_t s, int* launches);
+// The ray marcher (path tracing off): occlusion volume (R16F), shadow volume
+// swept slice by slice (RGBA16F), the image into a.hdr.
+cudaError_t launch_ao(const PtArgs& a, uint16_t* out, int ax, int ay, int az, cudaStream_t s);
+cudaError_t launch_shadow_sweep(const PtArgs& a, ushort4* vol, int sx, int sy, int sz, int axis, int sign,
+                                cudaStream_t s, int* launches);
+cudaError_t launch_dvr(const PtArgs& a, const ushort4* shadow, int sx, int sy, int sz, const uint16_t* ao, int ax,
+                       int ay, int az, cudaStream_t s);
 // B-spline density and gradient at n continuous indices (parity probe).
 cudaError_t launch_bspline_probe(const PtArgs& a, const float* idx, float* out, int n, cudaStream_t s);
 // One path per listed pixel at accumulation count a.u.path[0] (parity probe): 12 floats each.

@@ -191,6 +191,10 @@ class Renderer:
         nx, ny, nz = self.dims
         if which == abi.VOLUME_MAJORANT:
             shape, dt = ((nz + 7) // 8, (ny + 7) // 8, (nx + 7) // 8), np.float32
+        elif which == abi.VOLUME_SHADOW:
+            shape, dt = ((nz + 1) // 2, (ny + 1) // 2, (nx + 1) // 2, 4), np.uint16
+        elif which == abi.VOLUME_AO:
+            shape, dt = ((nz + 3) // 4, (ny + 3) // 4, (nx + 3) // 4), np.uint16
         else:
             shape, dt = {abi.VOLUME_DENSITY: ((nz, ny, nx), np.uint16),
                          abi.VOLUME_NORMALS: ((nz, ny, nx, 4), np.int8),

@@ -57,6 +57,8 @@ def parse():
                     help="accumulate-frames per step; >1 batches them in one wavefront pass (vv_record_frames)")
     ap.add_argument("--record-steps", type=int, default=10,
                     help="also time this many single-frame vv_record calls (0: skip)")
+    ap.add_argument("--ray-march-steps", type=int, default=10,
+                    help="also time this many frames of the real-time ray marcher (path tracing off; 0: skip)")
     ap.add_argument("--light-map", action="store_true",
                     help="light with a seeded synthetic 2048x1024 light map (Environment::Map) instead of the studio")
     ap.add_argument("--rmse-requests", type=int, default=6,
@@ -422,6 +424,26 @@ def run_ours(args, rank, world, local):
         e2e = {"value": samples / t1, "unit": UNIT, "h2d_bytes_per_step": 720,
                "d2h_bytes_per_step": W * H * 4,
                "call": "vv_record_frames + vv_read_output" if F > 1 else "vv_record + vv_read_output"}
+    ray_march = None
+    if args.ray_march_steps > 0:
+        # The interactive mode on the same workload: the first frame builds the
+        # occlusion and shadow volumes, later frames only march.
+        q = __import__("copy").deepcopy(params)
+        q.path_tracing.enabled = 0
+        s0, s1, s2 = (torch.cuda.Event(enable_timing=True) for _ in range(3))
+        torch.cuda.synchronize()
+        s0.record(stream)
+        r.record(frame[0], q)
+        s1.record(stream)
+        for i in range(args.ray_march_steps):
+            r.record(frame[0] + 1 + i, q)
+        s2.record(stream)
+        torch.cuda.synchronize()
+        frame[0] += 1 + args.ray_march_steps
+        ms = s1.elapsed_time(s2) / args.ray_march_steps
+        ray_march = {"ms_per_frame": ms, "frames_per_s": 1e3 / ms, "first_frame_ms": s0.elapsed_time(s1),
+                     "call": "vv_record with path_tracing.enabled = 0 (dvr + display; the first frame also "
+                             "builds the occlusion and shadow volumes)"}
     to_rmse = time_to_rmse(r, params, args, frame, stream) if args.rmse_requests > 0 else None
     if args.rmse_reference_spp > 0 and to_rmse is not None:
         to_rmse["check"] = rmse_against_reference(r, params, args, frame)
@@ -440,6 +462,7 @@ def run_ours(args, rank, world, local):
         "path_vertices_per_s": counts["vertex"] / max(counts["pixel"], 1) * value,
         "per_frame_record": per_frame,
         "time_to_rmse": to_rmse,
+        "ray_march": ray_march,
         "e2e": e2e,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": traffic,

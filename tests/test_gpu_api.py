@@ -32,12 +32,23 @@ def test_label_size_mismatch(rend):
     assert e.value.status == abi.VV_ERR_ARG
 
 
-def test_ray_marcher_not_provided(rend):
+def test_ray_marcher_leaves_the_accumulation_alone(rend):
+    """record with path tracing off draws with the ray marcher: the path
+    tracer's accumulation neither grows nor restarts (renderer.rs:1536-1545,
+    1789-1794)."""
     cfg, r, p = rend
     r.resize(16, 16)
-    p.path_tracing.enabled = 0
-    with pytest.raises(R.VolptError):
-        r.record(1, p)
+    r.record(1, p)
+    r.record(2, p)
+    assert r.accumulated_samples() == 2
+    q = abi.FrameParams.from_buffer_copy(bytes(p))
+    q.path_tracing.enabled = 0
+    r.record(3, q)
+    assert r.accumulated_samples() == 2
+    img = r.read_output()
+    assert img[..., :3].std() > 0
+    r.record(4, p)
+    assert r.accumulated_samples() == 3
 
 
 def test_accumulation_keys(rend):

@@ -52,7 +52,7 @@ __device__ __forceinline__ float4 preint_at(const PtArgs& A, float density) {
 }
 
 // common.glsl:206-214: the pre-integrated sample of a segment from `front` to `back`.
-__device__ Sample tf_segment(const PtArgs& A, float front, float back) {
+__device__ __noinline__ Sample tf_segment(const PtArgs& A, float front, float back) {
     if (fabsf(back - front) < 1e-4f) return tf_point(A, 0.5f * (front + back));
     float4 pb = preint_at(A, back), pf = preint_at(A, front);
     float d = back - front;
@@ -71,7 +71,7 @@ __device__ Sample tf_segment(const PtArgs& A, float front, float back) {
 }
 
 // common.glsl:218-230
-__device__ float preint_half_depth(const PtArgs& A, float front, float back) {
+__device__ __noinline__ float preint_half_depth(const PtArgs& A, float front, float back) {
     float target = 0.5f * (preint_at(A, front).w + preint_at(A, back).w);
     float lo = 0.0f, hi = 1.0f;
     for (int i = 0; i < 6; i++) {
@@ -84,7 +84,7 @@ __device__ float preint_half_depth(const PtArgs& A, float front, float back) {
 }
 
 // dvr.comp:14-21: labels applied, measured tissue as dense as the path tracer draws it.
-__device__ Sample labelled(const PtArgs& A, Sample s, f3 idx) {
+__device__ __noinline__ Sample labelled(const PtArgs& A, Sample s, f3 idx) {
     s = apply_labels(A, s, idx);
     if (measured(A, s)) s.extinction = dot(tissue_sigma(A, s), mk(1.0f / 3.0f));
     return s;
@@ -174,6 +174,58 @@ __device__ __noinline__ f3 env_map_diffuse(const PtArgs& A, f3 n) {
     return U3(A.u.ambient) * c;
 }
 
+// dvr.comp:76-96: the first surface a ray meets, bisected between the previous
+// sample and this one for where the opacity reaches half of this sample's.
+__device__ __noinline__ f3 refine_surface(const PtArgs& A, f3 idx, f3 d_idx, float step_mm, float target) {
+    float inside = 0.0f, outside = -step_mm;
+    for (int i = 0; i < 5; i++) {
+        float mid = 0.5f * (inside + outside);
+        f3 at = idx + d_idx * mid;
+        bool opaque = labelled(A, tf_point(A, density_view(A, at)), at).extinction >= target;
+        inside = opaque ? mid : inside;
+        outside = opaque ? outside : mid;
+    }
+    return idx + d_idx * inside;
+}
+
+// dvr.comp:98-141: light reflected and scattered towards the viewer at a
+// sample (lighting volumes, BRDF, subsurface, ambient); ghosted structures'
+// opacity `alpha` is rescaled to their shell.
+__device__ __noinline__ f3 shade_sample(const PtArgs& A, const LightVol& SV, const LightVol& AV, f3 idx, Sample s,
+                                        f3 v, int cap_plane, float cut, float step_mm, float& alpha) {
+    m3 to_index = w2i3(A);
+    f3 l = U3(A.u.light_dir);
+    float light = A.u.light_dir[3];
+    f3 n;
+    float surfaceness;
+    float extinction_scale = surface_frame(A, idx, s, v, cap_plane, cut, 1.5f * step_mm, n, surfaceness);
+    apply_surface_texture(A, idx, s);
+    if (s.ghost) alpha = 1.0f - expf(-s.extinction * extinction_scale * step_mm);
+    f3 shadow_at = index_to_tex(A, idx + mul(to_index, n * (1.5f * A.u.light_cells[0] * surfaceness)));
+    f3 ao_at = index_to_tex(A, idx + mul(to_index, n * (A.u.light_cells[1] * surfaceness)));
+    float shadow_t = A.u.lighting[0] != 0u ? lighting_lookup(A, SV, shadow_at).w : 1.0f;
+    f3 sss_at = index_to_tex(A, idx - mul(to_index, n * (A.u.subsurface[3] * surfaceness)));
+    f3 diffused = mk(1.0f);
+    if (A.u.lighting[0] != 0u) {
+        float4 dl = lighting_lookup(A, SV, sss_at);
+        diffused = mk(dl.x, dl.y, dl.z);
+    }
+    float occlusion = A.u.lighting[1] != 0u ? lighting_lookup(A, AV, ao_at).x : 1.0f;
+    n = bump_normal(A, idx, s, n);
+    n = dot(n, v) < 0.0f ? -n : n;
+    float nl = gmax(dot(n, l), 0.0f);
+    f3 diffuse;
+    f3 specular = brdf_coated(n, v, l, s, diffuse);
+    f3 surface = (specular + diffuse) * (1.0f - s.subsurface) * nl * shadow_t + diffuse * s.subsurface * diffused;
+    f3 volume = s.albedo / (4.0f * PI) * mix3(mk(shadow_t), diffused, s.subsurface);
+    f3 direct = mix3(volume, surface, surfaceness) * light;
+    f3 ambient_light = A.u.lighting[3] == 2u
+                           ? mix3(U3(A.u.ambient), env_map_diffuse(A, n), surfaceness * (1.0f - s.subsurface))
+                           : U3(A.u.ambient);
+    f3 ambient = s.albedo * ambient_light * occlusion;
+    return direct + ambient;
+}
+
 }  // namespace
 
 // ao.comp: mean transmittance over 16 directions within 15 mm, remapped so a
@@ -240,7 +292,10 @@ __global__ void __launch_bounds__(64) k_shadow_slice(const __grid_constant__ PtA
 }
 
 // dvr.comp: one ray per pixel, emission-absorption with single scattering.
-__global__ void __launch_bounds__(64) k_dvr(const __grid_constant__ PtArgs A, const ushort4* __restrict__ shadow,
+#ifndef VV_DVR_MIN_BLOCKS
+#define VV_DVR_MIN_BLOCKS 4
+#endif
+__global__ void __launch_bounds__(64, VV_DVR_MIN_BLOCKS) k_dvr(const __grid_constant__ PtArgs A, const ushort4* __restrict__ shadow,
                                             int sx, int sy, int sz, const uint16_t* __restrict__ ao, int ax, int ay,
                                             int az) {
     int px = blockIdx.x * 8 + (threadIdx.x & 7), py = blockIdx.y * 8 + (threadIdx.x >> 3);
@@ -258,9 +313,7 @@ __global__ void __launch_bounds__(64) k_dvr(const __grid_constant__ PtArgs A, co
     float2 t = intersect_volume(A, o_idx, d_idx);
     float step_mm = A.u.dims[3];
     bool preintegrate = A.u.lighting[2] != 0u;
-    f3 l = U3(A.u.light_dir);
     f3 v = -dir;
-    float light = A.u.light_dir[3];
     f3 radiance = mk(0.0f);
     float transmittance = 1.0f;
     bool refined = false;
@@ -294,44 +347,10 @@ __global__ void __launch_bounds__(64) k_dvr(const __grid_constant__ PtArgs A, co
                 idx = idx - d_idx * (step_mm * (1.0f - preint_half_depth(A, front_density, density)));
             } else if (!refined && alpha > 0.2f && transmittance > 0.9f) {
                 refined = true;
-                float inside = 0.0f, outside = -step_mm, target = 0.5f * s.extinction;
-                for (int i = 0; i < 5; i++) {
-                    float mid = 0.5f * (inside + outside);
-                    f3 at = idx + d_idx * mid;
-                    bool opaque = labelled(A, tf_point(A, density_view(A, at)), at).extinction >= target;
-                    inside = opaque ? mid : inside;
-                    outside = opaque ? outside : mid;
-                }
-                idx = idx + d_idx * inside;
+                idx = refine_surface(A, idx, d_idx, step_mm, 0.5f * s.extinction);
             }
-            f3 n;
-            float surfaceness;
-            float extinction_scale = surface_frame(A, idx, s, v, cap_plane, cut, 1.5f * step_mm, n, surfaceness);
-            apply_surface_texture(A, idx, s);
-            if (s.ghost) alpha = 1.0f - expf(-s.extinction * extinction_scale * step_mm);
-            f3 shadow_at = index_to_tex(A, idx + mul(to_index, n * (1.5f * A.u.light_cells[0] * surfaceness)));
-            f3 ao_at = index_to_tex(A, idx + mul(to_index, n * (A.u.light_cells[1] * surfaceness)));
-            float shadow_t = A.u.lighting[0] != 0u ? lighting_lookup(A, SV, shadow_at).w : 1.0f;
-            f3 sss_at = index_to_tex(A, idx - mul(to_index, n * (A.u.subsurface[3] * surfaceness)));
-            f3 diffused = mk(1.0f);
-            if (A.u.lighting[0] != 0u) {
-                float4 dl = lighting_lookup(A, SV, sss_at);
-                diffused = mk(dl.x, dl.y, dl.z);
-            }
-            float occlusion = A.u.lighting[1] != 0u ? lighting_lookup(A, AV, ao_at).x : 1.0f;
-            n = bump_normal(A, idx, s, n);
-            n = dot(n, v) < 0.0f ? -n : n;
-            float nl = gmax(dot(n, l), 0.0f);
-            f3 diffuse;
-            f3 specular = brdf_coated(n, v, l, s, diffuse);
-            f3 surface = (specular + diffuse) * (1.0f - s.subsurface) * nl * shadow_t + diffuse * s.subsurface * diffused;
-            f3 volume = s.albedo / (4.0f * PI) * mix3(mk(shadow_t), diffused, s.subsurface);
-            f3 direct = mix3(volume, surface, surfaceness) * light;
-            f3 ambient_light = A.u.lighting[3] == 2u
-                                   ? mix3(U3(A.u.ambient), env_map_diffuse(A, n), surfaceness * (1.0f - s.subsurface))
-                                   : U3(A.u.ambient);
-            f3 ambient = s.albedo * ambient_light * occlusion;
-            radiance += transmittance * alpha * (direct + ambient);
+            f3 lit = shade_sample(A, SV, AV, idx, s, v, cap_plane, cut, step_mm, alpha);
+            radiance += transmittance * alpha * lit;
             transmittance *= 1.0f - alpha;
         }
     }

@@ -88,7 +88,8 @@ enum {
     WF_TAKE_SHADOW = 7,  // entries of the shadow queue taken so far
     WF_ESC0 = 8, WF_ESC1 = 9,  // flights that left the volume or hit the bounce limits
     WF_FIRST0 = 10, WF_FIRST1 = 11,  // first flights (bounce 0): a queue of their own
-    WF_COUNTERS = 12
+    WF_TAKE_FIRST = 12,  // entries of the first-flight queue taken so far
+    WF_COUNTERS = 13
 };
 struct WfArgs {
     uint32_t capacity;     // slots (and queue entries) allocated

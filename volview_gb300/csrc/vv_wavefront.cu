@@ -237,12 +237,17 @@ __global__ void __launch_bounds__(256) k_wf_init(const __grid_constant__ PtArgs 
 #define VV_EXTEND_MIN_BLOCKS 8
 #endif
 enum { EXT_END = 3 };
+// FIRST: the first-flight queue (bounce 0: cubic B-spline density along the
+// flight), otherwise later flights (trilinear); each kernel carries only its
+// sampler. Every wave launches both; with all of a pass's frames in flight
+// first flights occur in the first wave only (and with several samples per
+// pixel), so the other launch finds its queue empty.
+template <bool FIRST>
 __global__ void __launch_bounds__(128, VV_EXTEND_MIN_BLOCKS)
     k_wf_extend(const __grid_constant__ PtArgs A, const WfArgs W, int cur) {
-    // First flights (cubic B-spline density) are taken before later ones
-    // (trilinear), as one range of indices: lanes that take work together get
-    // neighbouring indices, so a warp mostly runs one kind of flight.
-    const uint32_t n_first = W.counts[WF_FIRST0 + cur], n = n_first + W.counts[cur];
+    const uint32_t n = W.counts[FIRST ? WF_FIRST0 + cur : cur];
+    const uint32_t* queue = FIRST ? W.first[cur] : W.ext[cur];
+    uint32_t* taken = &W.counts[FIRST ? WF_TAKE_FIRST : WF_TAKE_EXT];
     const Consts C = make_consts(A);
     uint32_t slot = 0;
     f3 origin, dir, spectral;
@@ -255,9 +260,9 @@ __global__ void __launch_bounds__(128, VV_EXTEND_MIN_BLOCKS)
         int done = 0;
         bool need = !active && !drained;
         if (__any_sync(0xffffffffu, need)) {
-            uint32_t k = take_item(&W.counts[WF_TAKE_EXT], n, need);
+            uint32_t k = take_item(taken, n, need);
             if (need && k != ~0u) {
-                slot = k < n_first ? W.first[cur][k] : W.ext[cur][k - n_first];
+                slot = queue[k];
                 const float4* q = slot_of(W, slot);
                 float4 a = q[Q_ORIGIN], b = q[Q_DIR], s = q[Q_SPEC];
                 origin = xyz(a);
@@ -278,7 +283,7 @@ __global__ void __launch_bounds__(128, VV_EXTEND_MIN_BLOCKS)
             drained = __any_sync(0xffffffffu, need && k == ~0u);
         }
         if (active) {
-            int r = ff_step(A, origin, dir, bounce == 0u, (int)hero, spectral, F, V.idx, V.s, V.cap_plane, V.cut, rng);
+            int r = ff_step(A, origin, dir, FIRST, (int)hero, spectral, F, V.idx, V.s, V.cap_plane, V.cut, rng);
             if (r != FF_CONTINUE) {
                 active = false;
                 done = r;
@@ -333,6 +338,7 @@ __global__ void __launch_bounds__(128, 4) k_wf_shade(const __grid_constant__ PtA
         W.counts[cur] = 0;
         W.counts[WF_FIRST0 + cur] = 0;
         W.counts[WF_TAKE_EXT] = 0;
+        W.counts[WF_TAKE_FIRST] = 0;
         W.counts[WF_ESC0 + (cur ^ 1)] = 0;  // finished by the previous wave's scatter
     }
 }
@@ -502,7 +508,7 @@ template <class K> static int blocks_per_sm(K kernel, int threads) {
 cudaError_t launch_pt_wavefront(const PtArgs& a, const WfArgs& w, int sms, cudaStream_t s, int* launches) {
     static int g_ext = 0, g_shade = 0, g_shadow = 0, g_scatter = 0, g_finish = 0;
     if (!g_ext) {
-        g_ext = sms * blocks_per_sm(k_wf_extend, 128);
+        g_ext = sms * blocks_per_sm(k_wf_extend<false>, 128);
         g_shade = sms * blocks_per_sm(k_wf_shade, 128);
         g_shadow = sms * blocks_per_sm(k_wf_shadow<false>, 128);
         g_scatter = sms * blocks_per_sm(k_wf_scatter, 128);
@@ -519,7 +525,8 @@ cudaError_t launch_pt_wavefront(const PtArgs& a, const WfArgs& w, int sms, cudaS
     int cur = 0;
     const int check = 2;
     for (int wave = 0; wave < 1 << 20; wave++) {
-        k_wf_extend<<<g_ext, 128, 0, s>>>(a, w, cur);
+        k_wf_extend<true><<<g_ext, 128, 0, s>>>(a, w, cur);
+        k_wf_extend<false><<<g_ext, 128, 0, s>>>(a, w, cur);
         k_wf_shade<<<g_shade, 128, 0, s>>>(a, w, cur);
         if (map) k_wf_shadow<true><<<g_shadow, 128, 0, s>>>(a, w);
         else k_wf_shadow<false><<<g_shadow, 128, 0, s>>>(a, w);

@@ -11,9 +11,9 @@ flush is needed between steps).
   value     device-timed throughput (CUDA events on the renderer's stream)
   e2e       the same through the C ABI with a host readback of the tone-mapped
             RGBA8 image every step (host wall clock)
-  roofline  the path-tracing pass (the wavefront stage kernels of a frame):
-            algorithmic bytes per frame (event counts x unique element bytes)
-            / its CUDA-event time per frame, against measured HBM
+  roofline  the path tracer: algorithmic bytes per frame (event counts x
+            unique element bytes) / the timed region's time per frame,
+            against measured HBM
   cpu_baseline  the CPU oracle timed on the host cores on a sample of rows
 
 `--impl reference` times the reference's own shaders compiled as CPU code
@@ -440,16 +440,18 @@ def run_ours(args, rank, world, local):
         s2.record(stream)
         torch.cuda.synchronize()
         frame[0] += 1 + args.ray_march_steps
-        ms = s1.elapsed_time(s2) / args.ray_march_steps
-        ray_march = {"ms_per_frame": ms, "frames_per_s": 1e3 / ms, "first_frame_ms": s0.elapsed_time(s1),
+        rm_ms = s1.elapsed_time(s2) / args.ray_march_steps
+        ray_march = {"ms_per_frame": rm_ms, "frames_per_s": 1e3 / rm_ms, "first_frame_ms": s0.elapsed_time(s1),
                      "call": "vv_record with path_tracing.enabled = 0 (dvr + display; the first frame also "
                              "builds the occlusion and shadow volumes)"}
     to_rmse = time_to_rmse(r, params, args, frame, stream) if args.rmse_requests > 0 else None
     if args.rmse_reference_spp > 0 and to_rmse is not None:
         to_rmse["check"] = rmse_against_reference(r, params, args, frame)
     # Roofline of the path-tracing pass (the wavefront stage kernels of a frame).
+    # Consecutive passes overlap (one pass's last waves beside the next one's
+    # first), so the time per frame is the timed region's, display included.
     alg_bytes = float(sum(counts[n] * b for n, b in zip(COUNT_NAMES, COUNT_BYTES)))
-    pt_frame_ms = pt_ms / (args.steps * F)
+    pt_frame_ms = ms / (args.steps * F)
     achieved = alg_bytes / (pt_frame_ms / 1e3) / 1e9
     peak, peak_kind = peaks()
     traffic = ncu_traffic()
@@ -466,9 +468,10 @@ def run_ours(args, rank, world, local):
         "e2e": e2e,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": traffic,
-                     "kernel": "path-tracing pass (k_wf_* stage kernels of one frame)",
+                     "kernel": "path-tracing pass (k_wf_* stage kernels), per frame of the timed steps",
                      "peak_source": peak_kind, "alg_bytes_per_frame": alg_bytes,
-                     "ms_per_frame": pt_frame_ms, "pt_launches": int(pt_launches), "events_per_frame": counts},
+                     "ms_per_frame": pt_frame_ms, "pass_ms_per_frame": pt_ms / (args.steps * F),
+                     "pt_launches": int(pt_launches), "events_per_frame": counts},
         "accumulated_samples": r.accumulated_samples(),
     }
     result["clocks"] = clocks.summary()

@@ -223,8 +223,18 @@ struct vv_renderer {
     bool has_env = false;
     float env_peak_u = 0.0f;
     // wavefront tracer: path slots, stage queues, counters
-    DBuf wf_slots, wf_map, wf_queues, wf_counts;
-    uint32_t* wf_host_count = nullptr;
+    // Path-tracing passes, two in flight: each has its own stream, wavefront
+    // state and sums of its frames; a pass's sums are merged into the
+    // accumulation (and displayed) after the previous call's display, so a
+    // call's pass overlaps the tail of the previous one.
+    struct Pass {
+        DBuf slots, map, queues, counts, accum, albedo, normal;
+        cudaStream_t stream = nullptr;
+        cudaEvent_t shown = nullptr;  // after the pass's merge and display
+    } pass[2];
+    int next_pass = 0;
+    bool prep_work = false;  // device work queued on the context stream by this call's set-up
+    cudaEvent_t prep_done = nullptr;
     // accumulation
     uint32_t accumulated = 0;
     bool have_params = false;
@@ -240,16 +250,16 @@ struct vv_renderer {
 };
 
 // Records the start event of a timed path-tracing launch (if timing is on).
-static void pt_timer_start(vv_renderer* r) {
+static void pt_timer_start(vv_renderer* r, cudaStream_t s) {
     if (!r->timing) return;
     cudaEvent_t a, b;
     cudaEventCreate(&a);
     cudaEventCreate(&b);
-    cudaEventRecord(a, r->ctx->stream);
+    cudaEventRecord(a, s);
     r->pt_events.push_back({a, b});
 }
-static void pt_timer_stop(vv_renderer* r) {
-    if (r->timing && !r->pt_events.empty()) cudaEventRecord(r->pt_events.back().second, r->ctx->stream);
+static void pt_timer_stop(vv_renderer* r, cudaStream_t s) {
+    if (r->timing && !r->pt_events.empty()) cudaEventRecord(r->pt_events.back().second, s);
 }
 
 // ------------------------------------------------------------ host math
@@ -626,17 +636,20 @@ extern "C" vv_status vv_renderer_destroy(vv_renderer* r) {
     if (!r) return VV_OK;
     cudaSetDevice(r->ctx->device);
     cudaStreamSynchronize(r->ctx->stream);
+    for (auto& P : r->pass) {
+        if (P.stream) cudaStreamSynchronize(P.stream);
+        DBuf* pb[] = {&P.slots, &P.map, &P.queues, &P.counts, &P.accum, &P.albedo, &P.normal};
+        for (DBuf* b : pb) b->release();
+        if (P.shown) cudaEventDestroy(P.shown);
+        if (P.stream) cudaStreamDestroy(P.stream);
+    }
+    if (r->prep_done) cudaEventDestroy(r->prep_done);
     DBuf* all[] = {&r->density, &r->normals, &r->mask_a, &r->mask_b, &r->labels, &r->majorant, &r->env_rad,
                    &r->env_table, &r->env_diffuse, &r->preint, &r->shadow_vol, &r->ao_vol, &r->lut,
                    &r->bucket_dev, &r->tables, &r->soft, &r->work, &r->exposure, &r->accum, &r->albedo,
                    &r->normal, &r->ping, &r->pong, &r->guide_nd, &r->guide_alb, &r->hdr, &r->out, &r->bloom[0], &r->bloom[1], &r->bloom[2],
                    &r->bloom[3]};
     for (DBuf* b : all) b->release();
-    r->wf_slots.release();
-    r->wf_map.release();
-    r->wf_queues.release();
-    r->wf_counts.release();
-    if (r->wf_host_count) cudaFreeHost(r->wf_host_count);
     if (r->tables_host) cudaFreeHost(r->tables_host);
     if (r->counters) cudaFree(r->counters);
     delete r;
@@ -898,8 +911,19 @@ extern "C" vv_status vv_resize(vv_renderer* r, uint32_t width, uint32_t height) 
         return fail(VV_ERR_ARG, "image size must be 1..16384 per axis");
     vv_status s = use_device(r);
     if (s != VV_OK) return s;
-    CK(cudaStreamSynchronize(r->ctx->stream));
+    CK(cudaStreamSynchronize(r->ctx->stream));  // the context stream follows every pass's display
     size_t px = (size_t)width * height;
+    for (auto& P : r->pass) {
+        if (!P.stream) {
+            CK(cudaStreamCreateWithFlags(&P.stream, cudaStreamNonBlocking));
+            CK(cudaEventCreateWithFlags(&P.shown, cudaEventDisableTiming));
+        }
+        CK(P.accum.alloc(px * 16));
+        CK(P.albedo.alloc(px * 16));
+        CK(P.normal.alloc(px * 16));
+        CK(P.counts.alloc(WF_COUNTERS * sizeof(uint32_t)));
+    }
+    if (!r->prep_done) CK(cudaEventCreateWithFlags(&r->prep_done, cudaEventDisableTiming));
     CK(r->accum.alloc(px * 16));
     CK(r->albedo.alloc(px * 16));
     CK(r->normal.alloc(px * 16));
@@ -909,8 +933,6 @@ extern "C" vv_status vv_resize(vv_renderer* r, uint32_t width, uint32_t height) 
     CK(r->guide_alb.alloc(px * 16));
     CK(r->hdr.alloc(px * 8));
     CK(r->out.alloc(px * 4));
-    CK(r->wf_counts.alloc(WF_COUNTERS * sizeof(uint32_t)));
-    if (!r->wf_host_count) CK(cudaMallocHost((void**)&r->wf_host_count, WF_COUNTERS * sizeof(uint32_t)));
     uint32_t qw = (width + 3) / 4, qh = (height + 3) / 4;
     uint32_t ew = (qw + 1) / 2, eh = (qh + 1) / 2;
     uint32_t ws[4] = {qw, qw, ew, ew}, hs[4] = {qh, qh, eh, eh};
@@ -975,19 +997,21 @@ static PtArgs pt_args(vv_renderer* r, const UHead& u) {
     a.counter = r->work.as<uint32_t>();
     a.status = r->work.as<int32_t>() + 1;
     a.counters = r->counters;
+    a.write_hdr = 1;
     const char* k = std::getenv("VV_PT_KERNEL");
     a.persistent = !(k && std::strcmp(k, "frame") == 0);
     return a;
 }
 
-// The path-tracing launch(es) of one record: the wavefront tracer, or with
-// VV_PT_KERNEL=persistent / frame the single-kernel tracers (persistent warps
-// with path regeneration / one thread per pixel, the reference's shape).
-static cudaError_t run_pt(vv_renderer* r, PtArgs& a, int* launches) {
+// The path-tracing launches of one pass on stream `s`: the wavefront tracer,
+// or with VV_PT_KERNEL=persistent / frame the single-kernel tracers
+// (persistent warps with path regeneration / one thread per pixel, the
+// reference's shape).
+static cudaError_t run_pt(vv_renderer* r, vv_renderer::Pass& P, PtArgs& a, cudaStream_t s, int* launches) {
     const char* k = std::getenv("VV_PT_KERNEL");
     if (k && (std::strcmp(k, "persistent") == 0 || std::strcmp(k, "frame") == 0)) {
         a.persistent = std::strcmp(k, "persistent") == 0 || a.frames > 1;
-        return launch_pt(a, r->ctx->sms, r->ctx->stream, launches);
+        return launch_pt(a, r->ctx->sms, s, launches);
     }
     // Paths in flight: with several frames per pass, up to 16 frames' worth
     // (VV_WF_SLOTS overrides), at most 2^24 slots (4.6 GB of path state) unless
@@ -998,17 +1022,19 @@ static cudaError_t run_pt(vv_renderer* r, PtArgs& a, int* launches) {
     const char* e = std::getenv("VV_WF_SLOTS");
     size_t per_pixel = e ? (size_t)std::max(1, std::atoi(e)) : 16;
     size_t cap = std::min(px * std::min<size_t>(per_pixel, a.frames), std::max(px, (size_t)1 << 24));
-    cudaError_t ce;
-    if ((ce = r->wf_slots.alloc(std::max(r->wf_slots.n, cap * WF_SLOT_BYTES))) != cudaSuccess ||
-        (ce = r->wf_map.alloc(std::max(r->wf_map.n, cap * WF_MAP_BYTES))) != cudaSuccess ||
-        (ce = r->wf_queues.alloc(std::max(r->wf_queues.n, cap * 9 * sizeof(uint32_t)))) != cudaSuccess)
-        return ce;
-    cap = r->wf_slots.n / WF_SLOT_BYTES;
+    if (P.slots.n < cap * WF_SLOT_BYTES) {
+        cudaError_t ce = cudaStreamSynchronize(s);  // the pass's previous use of its state has ended
+        if (ce == cudaSuccess) ce = P.slots.alloc(cap * WF_SLOT_BYTES);
+        if (ce == cudaSuccess) ce = P.map.alloc(cap * WF_MAP_BYTES);
+        if (ce == cudaSuccess) ce = P.queues.alloc(cap * 9 * sizeof(uint32_t));
+        if (ce != cudaSuccess) return ce;
+    }
+    cap = P.slots.n / WF_SLOT_BYTES;
     WfArgs w;
     w.capacity = (uint32_t)cap;
-    w.slots = r->wf_slots.as<float4>();
-    w.map = r->wf_map.as<float4>();
-    uint32_t* q = r->wf_queues.as<uint32_t>();
+    w.slots = P.slots.as<float4>();
+    w.map = P.map.as<float4>();
+    uint32_t* q = P.queues.as<uint32_t>();
     w.ext[0] = q;
     w.ext[1] = q + cap;
     w.shade = q + 2 * cap;
@@ -1018,9 +1044,8 @@ static cudaError_t run_pt(vv_renderer* r, PtArgs& a, int* launches) {
     w.esc[1] = q + 6 * cap;
     w.first[0] = q + 7 * cap;
     w.first[1] = q + 8 * cap;
-    w.counts = r->wf_counts.as<uint32_t>();
-    w.host_count = r->wf_host_count;
-    return launch_pt_wavefront(a, w, r->ctx->sms, r->ctx->stream, launches);
+    w.counts = P.counts.as<uint32_t>();
+    return launch_pt_wavefront(a, w, r->ctx->sms, s, launches);
 }
 
 static PostArgs post_args(vv_renderer* r, const UHead& u) {
@@ -1076,6 +1101,7 @@ static vv_status prepare_frame(vv_renderer* r, const vv_frame_params& p, uint64_
             return cuda_fail(e, "label table upload");
         }
         r->tables_valid = true;
+        r->prep_work = true;
     }
     delete t;
     OpacityKey key = opacity_key(r, p.labels);
@@ -1095,11 +1121,13 @@ static vv_status prepare_frame(vv_renderer* r, const vv_frame_params& p, uint64_
         L.scratch = r->mask_b.as<uint32_t>();
         L.out = r->mask_a.as<uint32_t>();
         CK(launch_masks(L, st));
+        r->prep_work = true;
         r->launches += 4;
         r->mask_key = key;
         r->have_mask_key = true;
     }
     if (!(r->have_majorant_key && r->majorant_key == key)) {
+        r->prep_work = true;
         CK(launch_majorant(r->density.as<uint16_t>(), r->mask_a.as<uint32_t>(), r->vol, key.mode, p.labels.extinction,
                            r->bucket_dev.as<float>(), r->majorant.as<float>(), st));
         r->launches += 1;
@@ -1111,22 +1139,12 @@ static vv_status prepare_frame(vv_renderer* r, const vv_frame_params& p, uint64_
         CK(cudaMemsetAsync(r->accum.p, 0, bytes, st));
         CK(cudaMemsetAsync(r->albedo.p, 0, bytes, st));
         CK(cudaMemsetAsync(r->normal.p, 0, bytes, st));
+        r->prep_work = true;
     }
     return VV_OK;
 }
 
 // Denoiser and display passes after the frame(s) (renderer.rs:1793-1803).
-static vv_status finish_frame(vv_renderer* r, const vv_frame_params& p, const UHead& u) {
-    cudaStream_t st = r->ctx->stream;
-    int launches = 0;
-    PostArgs pa = post_args(r, u);
-    if (p.path_tracing.denoiser == VV_DENOISE_ATROUS) CK(launch_denoise(pa, st, &launches));
-    r->accumulated += std::max(p.path_tracing.samples_per_frame, 1u);
-    if (p.path_tracing.denoiser != VV_DENOISE_OIDN) CK(launch_post(pa, st, &launches));
-    r->launches += launches;
-    return VV_OK;
-}
-
 // The ray marcher's frame (renderer.rs:1707-1790): the occlusion volume when
 // the opacity or the clipping changed, the shadow volume when the light or the
 // tint changed as well, then dvr.comp into the HDR image and the display.
@@ -1191,19 +1209,65 @@ static vv_status record_ray_march(vv_renderer* r, const vv_frame_params& p, cons
     return VV_OK;
 }
 
+// One path-tracing pass of `frames` accumulate-frames and its display
+// (record, renderer.rs:1770-1797). The pass runs on its own stream into its own
+// sums, starting after this call's set-up work (if it queued any) and after
+// the previous use of its stream; then, after the previous call's display, its
+// sums are merged into the accumulation, the HDR image is stored, denoised and
+// displayed, and the context stream waits for that display. So a call returns
+// at once, and consecutive calls overlap: one pass's last, nearly empty waves
+// run beside the next pass's first ones.
+static vv_status record_pass(vv_renderer* r, const vv_frame_params& p, UHead& u, uint32_t frames) {
+    vv_renderer::Pass& P = r->pass[r->next_pass];
+    vv_renderer::Pass& prev = r->pass[r->next_pass ^ 1];
+    r->next_pass ^= 1;
+    cudaStream_t s = P.stream;
+    if (r->prep_work) {
+        CK(cudaEventRecord(r->prep_done, r->ctx->stream));
+        CK(cudaStreamWaitEvent(s, r->prep_done, 0));
+        r->prep_work = false;
+    }
+    const char* k = std::getenv("VV_PT_KERNEL");
+    if (k) CK(cudaStreamWaitEvent(s, prev.shown, 0));  // the single-kernel tracers share one work counter
+    uint32_t spf = std::max(p.path_tracing.samples_per_frame, 1u);
+    size_t bytes = (size_t)r->width * r->height * 16;
+    CK(cudaMemsetAsync(P.accum.p, 0, bytes, s));
+    CK(cudaMemsetAsync(P.albedo.p, 0, bytes, s));
+    CK(cudaMemsetAsync(P.normal.p, 0, bytes, s));
+    PtArgs a = pt_args(r, u);
+    a.frames = frames;
+    a.accum = P.accum.as<float4>();
+    a.albedo = P.albedo.as<float4>();
+    a.normal = P.normal.as<float4>();
+    a.write_hdr = 0;
+    int launches = 0;
+    pt_timer_start(r, s);
+    CK(run_pt(r, P, a, s, &launches));
+    pt_timer_stop(r, s);
+    // The last frame's view of the counts: accumulated before it, spf after.
+    r->accumulated += (frames - 1) * spf;
+    u.path[0] = r->accumulated;
+    PostArgs pa = post_args(r, u);
+    CK(cudaStreamWaitEvent(s, prev.shown, 0));
+    CK(launch_merge(pa, P.accum.as<float4>(), P.albedo.as<float4>(), P.normal.as<float4>(),
+                    (float)(r->accumulated + spf), s));
+    launches += 1;
+    if (p.path_tracing.denoiser == VV_DENOISE_ATROUS) CK(launch_denoise(pa, s, &launches));
+    r->accumulated += spf;
+    if (p.path_tracing.denoiser != VV_DENOISE_OIDN) CK(launch_post(pa, s, &launches));
+    CK(cudaEventRecord(P.shown, s));
+    CK(cudaStreamWaitEvent(r->ctx->stream, P.shown, 0));
+    r->launches += launches;
+    return VV_OK;
+}
+
 extern "C" vv_status vv_record(vv_renderer* r, uint64_t frame, const vv_frame_params* params) {
     if (!r || !params) return fail(VV_ERR_ARG, "null argument");
     UHead u;
     vv_status s = prepare_frame(r, *params, frame, u);
     if (s != VV_OK) return s;
     if (!params->path_tracing.enabled) return record_ray_march(r, *params, u);
-    PtArgs a = pt_args(r, u);
-    int launches = 0;
-    pt_timer_start(r);
-    CK(run_pt(r, a, &launches));
-    pt_timer_stop(r);
-    r->launches += launches;
-    return finish_frame(r, *params, u);
+    return record_pass(r, *params, u, 1);
 }
 
 extern "C" vv_status vv_record_frames(vv_renderer* r, uint64_t first_frame, uint32_t frames,
@@ -1219,24 +1283,7 @@ extern "C" vv_status vv_record_frames(vv_renderer* r, uint64_t first_frame, uint
     UHead u;
     vv_status s = prepare_frame(r, *params, first_frame + frames - 1, u);
     if (s != VV_OK) return s;
-    uint32_t spf = std::max(params->path_tracing.samples_per_frame, 1u);
-    PtArgs a = pt_args(r, u);
-    a.frames = frames;
-    a.persistent = 1;
-    int launches = 0;
-    pt_timer_start(r);
-    CK(run_pt(r, a, &launches));
-    pt_timer_stop(r);
-    // The last frame's view of the counts: accumulated before it, spf after.
-    r->accumulated += (frames - 1) * spf;
-    u.path[0] = r->accumulated;
-    PostArgs pa = post_args(r, u);
-    if (frames > 1) {
-        CK(launch_hdr_resolve(pa, (float)(r->accumulated + spf), r->ctx->stream));
-        launches += 1;
-    }
-    r->launches += launches;
-    return finish_frame(r, *params, u);
+    return record_pass(r, *params, u, frames);
 }
 
 static vv_status read_dev(vv_renderer* r, void* dst, const DBuf& src, size_t bytes, size_t capacity) {

@@ -48,6 +48,8 @@ struct PtArgs {
     uint32_t* counter;          // work-item counter, zero at launch
     int32_t* status;            // device status word (0 ok)
     int persistent;             // 1: persistent warps with path regeneration
+    int write_hdr;              // 1: accum/albedo/normal are the totals and a single-frame pass writes each
+                                // pixel's HDR as it finishes; 0: they are the pass's own sums (merged later)
     unsigned long long* counters;  // event counters (COUNT_*), or null
 };
 
@@ -89,7 +91,8 @@ enum {
     WF_ESC0 = 8, WF_ESC1 = 9,  // flights that left the volume or hit the bounce limits
     WF_FIRST0 = 10, WF_FIRST1 = 11,  // first flights (bounce 0): a queue of their own
     WF_TAKE_FIRST = 12,  // entries of the first-flight queue taken so far
-    WF_COUNTERS = 13
+    WF_STOP = 13,     // 0 while waves run; 1 + the queue index the finishing launch takes over
+    WF_COUNTERS = 14
 };
 struct WfArgs {
     uint32_t capacity;     // slots (and queue entries) allocated
@@ -102,7 +105,6 @@ struct WfArgs {
     uint32_t* shadow;
     uint32_t* scatter;
     uint32_t* counts;      // WF_COUNTERS words
-    uint32_t* host_count;  // pinned, for the live-path check
 };
 // Accumulate-frames with the wavefront tracer (same results as launch_pt).
 cudaError_t launch_pt_wavefront(const PtArgs& a, const WfArgs& w, int sms, cudaStream_t s, int* launches);
@@ -140,5 +142,9 @@ cudaError_t launch_denoise(const PostArgs& a, cudaStream_t s, int* launches);
 cudaError_t launch_post(const PostArgs& a, cudaStream_t s, int* launches);
 // hdr = accum / n (the HDR store at the end of pt.comp) for batched frames.
 cudaError_t launch_hdr_resolve(const PostArgs& a, float n, cudaStream_t s);
+// A pass's own sums added to the accumulation images (a.accum/albedo/normal),
+// then hdr = accum / n: the end of pt.comp for the pass's last frame.
+cudaError_t launch_merge(const PostArgs& a, const float4* accum, const float4* albedo, const float4* normal, float n,
+                         cudaStream_t s);
 
 }  // namespace vv

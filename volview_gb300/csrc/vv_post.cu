@@ -138,6 +138,26 @@ __global__ void k_hdr_resolve(const PostArgs a, float n) {
     a.hdr[i] = to_h4(make_float4(v.x / n, v.y / n, v.z / n, v.w / n));
 }
 
+// The pass's sums into the accumulation (pt.comp:554-559 for the pass's
+// frames), then the HDR store of its last frame (pt.comp:560). A single-frame
+// pass's own sums are that frame's, so the totals are the reference's to the bit.
+__global__ void k_merge(const PostArgs a, const float4* __restrict__ pacc, const float4* __restrict__ palb,
+                        const float4* __restrict__ pnor, float n) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= (int)(a.width * a.height)) return;
+    float4 v = a.accum[i], pv = pacc[i];
+    v = make_float4(v.x + pv.x, v.y + pv.y, v.z + pv.z, v.w + pv.w);
+    float4* acc = (float4*)a.accum;
+    float4* alb = (float4*)a.albedo;
+    float4* nor = (float4*)a.normal;
+    acc[i] = v;
+    float4 b = alb[i], pb = palb[i];
+    alb[i] = make_float4(b.x + pb.x, b.y + pb.y, b.z + pb.z, b.w + pb.w);
+    float4 c = nor[i], pc = pnor[i];
+    nor[i] = make_float4(c.x + pc.x, c.y + pc.y, c.z + pc.z, c.w + pc.w);
+    a.hdr[i] = to_h4(make_float4(v.x / n, v.y / n, v.z / n, v.w / n));
+}
+
 // ------------------------------------------------------------------- bloom
 // bloom.comp pass 0: Karis-weighted 4x4 average of the HDR image, with coverage.
 __global__ void k_bloom_down4(const PostArgs a) {
@@ -346,6 +366,13 @@ cudaError_t launch_post(const PostArgs& a, cudaStream_t s, int* launches) {
     k_bloom_blur<<<grid16(a.bw[2], a.bh[2]), 256, 0, s>>>(a.bloom[3], a.bloom[2], a.bw[2], a.bh[2], 0, 1);
     k_tonemap<<<grid16(a.width, a.height), 256, 0, s>>>(a);
     *launches += 9;
+    return cudaGetLastError();
+}
+
+cudaError_t launch_merge(const PostArgs& a, const float4* accum, const float4* albedo, const float4* normal, float n,
+                         cudaStream_t s) {
+    int N = (int)(a.width * a.height);
+    k_merge<<<(N + 255) / 256, 256, 0, s>>>(a, accum, albedo, normal, n);
     return cudaGetLastError();
 }
 

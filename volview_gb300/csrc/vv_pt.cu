@@ -36,7 +36,7 @@ __global__ void __launch_bounds__(64, 8) k_pt_frame(const __grid_constant__ PtAr
         }
         finish_path(P, S);
     }
-    accumulate(A, px, py, S, false, true, (float)(A.u.path[0] + A.u.path[2]));
+    accumulate(A, px, py, S, false, A.write_hdr != 0, (float)(A.u.path[0] + A.u.path[2]));
 }
 
 // Persistent warps over (frame, 8x4 tile) work items with per-lane path
@@ -115,7 +115,7 @@ __global__ void __launch_bounds__(128, 4) k_pt_persistent(const __grid_constant_
                 if (++sample < spf) {
                     start_path(A, C, P, px, py);
                 } else {
-                    accumulate(A, px, py, S, multi, !multi, (float)(A.u.path[0] + spf));
+                    accumulate(A, px, py, S, multi, !multi && A.write_hdr != 0, (float)(A.u.path[0] + spf));
                     active = false;
                 }
             }

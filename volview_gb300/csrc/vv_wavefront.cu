@@ -24,6 +24,7 @@
 // the longest random walks.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cstdlib>
 
 #include "vv_pt_device.cuh"
@@ -155,7 +156,7 @@ __device__ bool end_path(const PtArgs& A, const Consts& C, Path& P, PixelSums& S
     // One frame per launch: this slot owns the pixel; several: frames of one
     // pixel may finish concurrently in different slots.
     bool multi = A.frames > 1;
-    accumulate(A, px, py, S, multi, !multi, (float)(A.u.path[0] + spf));
+    accumulate(A, px, py, S, multi, !multi && A.write_hdr != 0, (float)(A.u.path[0] + spf));
     return false;
 }
 
@@ -246,7 +247,19 @@ enum { EXT_END = 3 };
 // pixel), so the other launch finds its queue empty.
 template <bool FIRST>
 __global__ void __launch_bounds__(128, VV_EXTEND_MIN_BLOCKS)
-    k_wf_extend(const __grid_constant__ PtArgs A, const WfArgs W, int cur) {
+    k_wf_extend(const __grid_constant__ PtArgs A, const WfArgs W, int cur, uint32_t tail) {
+    if (W.counts[WF_STOP] != 0u) return;
+    if (FIRST) {
+        // The wave's first launch decides whether the waves go on: with at most
+        // `tail` live paths left, the finishing launch takes queue `cur` over.
+        // Every block reads the same counts (nothing changes them before this
+        // launch ends), so all blocks decide alike.
+        uint32_t live = W.counts[WF_FIRST0 + cur] + W.counts[cur];
+        if (live <= tail) {
+            if (blockIdx.x == 0 && threadIdx.x == 0) W.counts[WF_STOP] = (uint32_t)cur + 1u;
+            return;
+        }
+    }
     const uint32_t n = W.counts[FIRST ? WF_FIRST0 + cur : cur];
     const uint32_t* queue = FIRST ? W.first[cur] : W.ext[cur];
     uint32_t* taken = &W.counts[FIRST ? WF_TAKE_FIRST : WF_TAKE_EXT];
@@ -310,6 +323,7 @@ __global__ void __launch_bounds__(128, VV_EXTEND_MIN_BLOCKS)
 }
 
 __global__ void __launch_bounds__(128, 4) k_wf_shade(const __grid_constant__ PtArgs A, const WfArgs W, int cur) {
+    if (W.counts[WF_STOP] != 0u) return;
     uint32_t n = W.counts[WF_SHADE];
     Consts C = make_consts(A);
     WF_FOR_EACH(n) {
@@ -357,6 +371,7 @@ __global__ void __launch_bounds__(128, 4) k_wf_shade(const __grid_constant__ PtA
 // the key light's shadow rays alone.
 template <bool MAP>
 __global__ void __launch_bounds__(128, VV_SHADOW_MIN_BLOCKS) k_wf_shadow(const __grid_constant__ PtArgs A, const WfArgs W) {
+    if (W.counts[WF_STOP] != 0u) return;
     const uint32_t n = W.counts[WF_SHADOW];
     uint32_t slot = 0;
     f3 origin;
@@ -422,6 +437,7 @@ __global__ void __launch_bounds__(128, VV_SHADOW_MIN_BLOCKS) k_wf_shadow(const _
 // Scatter, and the end of the flights that left the volume or hit the bounce
 // limits in this wave's extend (queued after the scatter entries).
 __global__ void __launch_bounds__(128, 6) k_wf_scatter(const __grid_constant__ PtArgs A, const WfArgs W, int cur) {
+    if (W.counts[WF_STOP] != 0u) return;
     uint32_t n_scatter = W.counts[WF_SCATTER], n = n_scatter + W.counts[WF_ESC0 + cur];
     int nxt = cur ^ 1;
     Consts C = make_consts(A);
@@ -476,6 +492,8 @@ __global__ void __launch_bounds__(128, 6) k_wf_scatter(const __grid_constant__ P
 // The paths still alive, run to completion one thread each (the reference's
 // loop), including their pixels' remaining samples and frames.
 __global__ void __launch_bounds__(128, 4) k_wf_finish(const __grid_constant__ PtArgs A, const WfArgs W, int cur) {
+    uint32_t stop = W.counts[WF_STOP];
+    if (stop != 0u) cur = (int)stop - 1;  // else the waves ran out first: `cur` is the next wave's queue
     uint32_t n_first = W.counts[WF_FIRST0 + cur], n = n_first + W.counts[cur];
     Consts C = make_consts(A);
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
@@ -524,32 +542,30 @@ cudaError_t launch_pt_wavefront(const PtArgs& a, const WfArgs& w, int sms, cudaS
     const bool map = a.u.lighting[3] == 2u;
     k_wf_init<<<(slots + 255) / 256 < (uint32_t)(sms * 8) ? (slots + 255) / 256 : sms * 8, 256, 0, s>>>(a, w, slots);
     *launches += 1;
+    // All waves are queued at once, with no host round trip: the first launch
+    // of each wave stops the waves on the device once at most `tail` paths
+    // are left, the rest of the queued waves then return at once, and the
+    // finishing launch runs the remaining paths to completion. Enough waves
+    // for the pass: about 10 per round of slots plus the tail of long random
+    // walks (a path has at most 4 surface and 80 volume events at g = 0.6);
+    // if they still run out, the finishing launch takes what is left.
+    uint32_t rounds = (items + slots - 1) / slots;
+    int waves = (int)std::min<uint32_t>(24u + 10u * rounds, 4096u);
     int cur = 0;
-    const int check = 2;
-    for (int wave = 0; wave < 1 << 20; wave++) {
-        k_wf_extend<true><<<g_ext, 128, 0, s>>>(a, w, cur);
-        k_wf_extend<false><<<g_ext, 128, 0, s>>>(a, w, cur);
+    for (int wave = 0; wave < waves; wave++) {
+        k_wf_extend<true><<<g_ext, 128, 0, s>>>(a, w, cur, tail);
+        k_wf_extend<false><<<g_ext, 128, 0, s>>>(a, w, cur, tail);
         k_wf_shade<<<g_shade, 128, 0, s>>>(a, w, cur);
         if (map) k_wf_shadow<true><<<g_shadow, 128, 0, s>>>(a, w);
         else k_wf_shadow<false><<<g_shadow, 128, 0, s>>>(a, w);
         k_wf_scatter<<<g_scatter, 128, 0, s>>>(a, w, cur);
-        *launches += 4;
+        *launches += 5;
         cur ^= 1;
         cudaError_t e = cudaGetLastError();
         if (e != cudaSuccess) return e;
-        if (wave % check == check - 1) {
-            e = cudaMemcpyAsync(w.host_count, w.counts, WF_COUNTERS * sizeof(uint32_t), cudaMemcpyDeviceToHost, s);
-            if (e == cudaSuccess) e = cudaStreamSynchronize(s);
-            if (e != cudaSuccess) return e;
-            uint32_t live = w.host_count[cur] + w.host_count[WF_FIRST0 + cur];
-            if (live == 0) break;
-            if (live <= tail) {
-                k_wf_finish<<<g_finish, 128, 0, s>>>(a, w, cur);
-                *launches += 1;
-                break;
-            }
-        }
     }
+    k_wf_finish<<<g_finish, 128, 0, s>>>(a, w, cur);
+    *launches += 1;
     return cudaGetLastError();
 }
 

@@ -11,8 +11,11 @@
  * Conventions
  *  - Every call returns vv_status; on failure vv_last_error() describes why.
  *  - The renderer owns its device memory; inputs are borrowed and copied.
- *  - One renderer per host thread; calls on one renderer are serialised. All
- *    device work runs on the context's CUDA stream.
+ *  - One renderer per host thread; calls on one renderer are serialised. Device
+ *    work is ordered on the context's CUDA stream: path-tracing passes run on
+ *    two streams of the renderer, and the context stream waits for each
+ *    record's display, so work queued on it afterwards (readbacks, the caller's
+ *    own kernels) sees the frame; consecutive records overlap on the device.
  *  - There is no CPU fallback: without a CUDA device every call that needs one
  *    returns VV_ERR_CUDA.
  */
@@ -251,8 +254,8 @@ vv_status vv_resize(vv_renderer* r, uint32_t width, uint32_t height);
 
 /* Renderer::record (renderer.rs:1499): one accumulate-frame (samples_per_frame
  * paths per pixel), then the denoiser and the display passes. Returns
- * VV_ERR_STATE where the reference panics (record before resize). Asynchronous
- * on the context's stream. */
+ * VV_ERR_STATE where the reference panics (record before resize). Asynchronous:
+ * returns once the work is queued; the context stream waits for the display. */
 vv_status vv_record(vv_renderer* r, uint64_t frame, const vv_frame_params* params);
 /* `frames` consecutive accumulate-frames with the same params in one
  * path-tracing pass; the denoiser and display passes run once, after the last.

@@ -187,6 +187,15 @@ struct OpacityKey {
     bool operator==(const OpacityKey& o) const { return std::memcmp(this, &o, sizeof(*this)) == 0; }
 };
 
+// Path-tracing passes in flight at once (each on its own stream, with its own
+// path state: up to 2^24 slots, 5.4 GB at 1024^2 with 16 frames per pass).
+// Measured at 1024^2 with 16 frames per call: 306, 316, 323, 325 and 323 M path
+// samples/s with 2, 3, 4, 6 and 8 passes; one frame per call: 11.8, 10.7, 9.2,
+// 8.2 and 7.8 ms per frame.
+#ifndef VV_PASSES
+#define VV_PASSES 6
+#endif
+
 struct vv_renderer {
     vv_context* ctx;
     Vol vol;
@@ -223,7 +232,7 @@ struct vv_renderer {
     bool has_env = false;
     float env_peak_u = 0.0f;
     // wavefront tracer: path slots, stage queues, counters
-    // Path-tracing passes, two in flight: each has its own stream, wavefront
+    // Path-tracing passes, VV_PASSES in flight: each has its own stream, wavefront
     // state and sums of its frames; a pass's sums are merged into the
     // accumulation (and displayed) after the previous call's display, so a
     // call's pass overlaps the tail of the previous one.
@@ -231,7 +240,7 @@ struct vv_renderer {
         DBuf slots, map, queues, counts, accum, albedo, normal;
         cudaStream_t stream = nullptr;
         cudaEvent_t shown = nullptr;  // after the pass's merge and display
-    } pass[2];
+    } pass[VV_PASSES];
     int next_pass = 0;
     bool prep_work = false;  // device work queued on the context stream by this call's set-up
     cudaEvent_t prep_done = nullptr;
@@ -1219,8 +1228,8 @@ static vv_status record_ray_march(vv_renderer* r, const vv_frame_params& p, cons
 // run beside the next pass's first ones.
 static vv_status record_pass(vv_renderer* r, const vv_frame_params& p, UHead& u, uint32_t frames) {
     vv_renderer::Pass& P = r->pass[r->next_pass];
-    vv_renderer::Pass& prev = r->pass[r->next_pass ^ 1];
-    r->next_pass ^= 1;
+    vv_renderer::Pass& prev = r->pass[(r->next_pass + VV_PASSES - 1) % VV_PASSES];
+    r->next_pass = (r->next_pass + 1) % VV_PASSES;
     cudaStream_t s = P.stream;
     if (r->prep_work) {
         CK(cudaEventRecord(r->prep_done, r->ctx->stream));

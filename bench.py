@@ -288,12 +288,12 @@ def time_to_rmse(r, params, args, frame, stream):
         while True:
             r.record_frames(frame[0], chunk, p)
             frame[0] += chunk
-            acc, alb, _ = r.read_accumulation()
+            acc, alb, _ = r.read_accumulation(normal=False)
             n = r.accumulated_samples()
             e = CV.rmse_estimate(acc, alb, n)
             if e <= target:
                 break
-            chunk = int(min(max(CV.samples_for(e, n, target) - n, 8), 1024))
+            chunk = int(min(max(CV.samples_for(e, n, target) - n, 8), 4096))
         latencies.append(time.perf_counter() - t0)
         spps.append(n)
     lat = np.array(latencies)

@@ -39,6 +39,12 @@ vv_status vv_count_events(vv_renderer* r, int enable, uint64_t* out, size_t n);
  * and returns the summed milliseconds and the number of launches. */
 vv_status vv_time_pt(vv_renderer* r, int enable, double* ms, uint64_t* launches);
 
+/* Light map importance sampling (pt.comp:204-233) from n random-stream states
+ * seeds[n]: out[6n] = texel column, texel row, pdf, direction (xyz). Needs a
+ * light map (vv_set_environment_map). */
+vv_status vv_probe_light_samples(vv_renderer* r, const vv_frame_params* params, const uint32_t* seeds, size_t n,
+                                 float* out);
+
 #ifdef __cplusplus
 }
 #endif

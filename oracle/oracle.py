@@ -308,6 +308,15 @@ class CpuRenderer:
         lib().vvo_post(ptr(u), ptr(np.ascontiguousarray(hdr, np.uint16)), ptr(exposure), ptr(out))
         return out
 
+    def light_samples(self, params, seeds):
+        """(n, 6): texel column and row (linear scans of the CDFs), pdf and
+        direction of the light map samples that pt.comp draws from `seeds`."""
+        seeds = np.ascontiguousarray(seeds, np.uint32).ravel()
+        out = np.zeros((seeds.size, 6), np.float32)
+        u = self.uniforms(params, 1, self.width, self.height)
+        lib().vvo_light_samples(ptr(u), C.byref(self.scene()), ptr(seeds), C.c_long(seeds.size), ptr(out))
+        return out
+
     def bspline(self, params, idx):
         idx = np.ascontiguousarray(idx, np.float32).reshape(-1, 3)
         out = np.zeros((idx.shape[0], 4), np.float32)

@@ -25,6 +25,7 @@ void pt_pixel(const Uniforms& u, const Scene& sc, int x, int y, float out[12]);
 void pt_rows(const Uniforms& u, const Scene& sc, float* accum, float* albedo, float* normal, uint16_t* hdr,
              const int* rows, int nrows, int threads);
 void bspline(const Uniforms& u, const Scene& sc, const float* idx, long n, float* out);
+void light_samples(const Uniforms& u, const Scene& sc, const uint32_t* seeds, long n, float* out);
 void denoise(const Uniforms& u, const float* accum, const float* albedo, const float* normal, uint16_t* hdr,
              float* ping, float* pong, int threads);
 void post(const Uniforms& u, const uint16_t* hdr, float* exposure, uint8_t* out);
@@ -149,6 +150,9 @@ void vvo_pt_pixel(const void* u, const vvo_scene* s, int x, int y, float out[12]
 }
 void vvo_bspline(const void* u, const vvo_scene* s, const float* idx, long n, float* out) {
     bspline(U(u), to_scene(s), idx, n, out);
+}
+void vvo_light_samples(const void* u, const vvo_scene* s, const uint32_t* seeds, long n, float* out) {
+    light_samples(U(u), to_scene(s), seeds, n, out);
 }
 void vvo_denoise(const void* u, const float* accum, const float* albedo, const float* normal, uint16_t* hdr,
                  float* ping, float* pong, int threads) {

@@ -1112,6 +1112,28 @@ void pt_pixel(const Uniforms& u, const Scene& sc, int x, int y, float out[12]) {
     std::memcpy(out, v, sizeof(v));
 }
 
+// Light map samples (pt.comp:204-233) from random-stream states: texel column
+// and row (the draws replayed through the searches), pdf, direction.
+void light_samples(const Uniforms& u, const Scene& sc, const uint32_t* seeds, long n, float* out) {
+    Units t = bind_scene(sc);
+    Tracer tr{Shading{u, t}};
+    ivec2 size = textureSize(t.env, 0);
+    for (long i = 0; i < n; i++) {
+        tr.state = seeds[i];
+        float xi = tr.rand();
+        int y = 0;
+        while (y < size.y - 1 && !(texelFetch(t.env_table, ivec2(size.x, y), 0).x >= xi)) y++;
+        xi = tr.rand();
+        int x = 0;
+        while (x < size.x - 1 && !(texelFetch(t.env_table, ivec2(x, y), 0).x >= xi)) x++;
+        tr.state = seeds[i];
+        float pdf;
+        vec3 d = tr.sample_env(pdf);
+        float v[6] = {float(x), float(y), pdf, d.x, d.y, d.z};
+        std::memcpy(out + 6 * i, v, sizeof(v));
+    }
+}
+
 // Cubic B-spline density and gradient at continuous voxel indices (common.glsl:124-136).
 void bspline(const Uniforms& u, const Scene& sc, const float* idx, long n, float* out) {
     Units t = bind_scene(sc);

@@ -5,6 +5,9 @@ Tolerances (written here, checked below):
 * masks: every voxel within one RG16 quantum, >= 99.9% exact (the soft masks
   call expf, whose last bit may differ between CUDA and the C library);
 * cubic B-spline value and gradient: 1e-4 relative (scale: the value range);
+* light map importance samples: the texel bit-exact against a linear scan of
+  the CDFs (the device searches only its guide bucket's range), pdf within
+  1e-5 relative and direction within 1e-5 (sinf/cosf last bits);
 * single-path replays: 1e-4 relative per pixel for >= 70% of the pixels; the
   share of pixels whose paths branch differently (a float comparison flipped
   by a last-bit difference: expf/logf/powf differ in the last bit between CUDA
@@ -135,6 +138,45 @@ def pair_light_map(small_cfg, gpu_ctx):
     cpu.resize(48, 48)
     yield cfg, gpu, cpu, params
     gpu.destroy()
+
+
+def _light_maps():
+    rng = np.random.default_rng(21)
+    peaked = np.full((32, 64, 3), 0.0, np.float32)
+    peaked[9, 40] = 1000.0
+    rows = rng.random((19, 37, 3)).astype(np.float32)
+    rows[[0, 3, 4, 11, 18]] = 0.0
+    steps = np.zeros((24, 40, 3), np.float32)
+    steps[:, ::7] = 5.0  # columns of equal weight: CDF plateaus at bucket edges
+    return {"synthetic": scene.synthetic_light_map(), "peaked": peaked, "zero_rows": rows, "plateaus": steps,
+            "single": np.ones((1, 1, 3), np.float32), "dark": np.zeros((8, 16, 3), np.float32),
+            "large": scene.synthetic_light_map(512, 256, seed=5)}
+
+
+@pytest.mark.parametrize("case", sorted(_light_maps()))
+def test_light_map_samples(small_cfg, gpu_ctx, case):
+    """The light map's importance sampling (pt.comp:204-233) from the same
+    random streams: zero rows and an all-dark map (uniform conditional CDFs), a
+    single bright texel, plateaus of the CDF, 1x1 and odd sizes."""
+    cfg = small_cfg
+    light_map = _light_maps()[case]
+    gpu = R.Renderer(gpu_ctx, cfg["volume"], cfg["tf"])
+    gpu.set_environment_map(abi.env_struct(light_map))
+    cpu = O.CpuRenderer(cfg["volume"], cfg["tf"], cfg["hu"])
+    cpu.set_environment_map(light_map)
+    params = make_params(cfg, list(gpu.center), gpu.diagonal)
+    params.lighting.environment = abi.ENV_MAP
+    gpu.resize(16, 16)
+    cpu.resize(16, 16)
+    seeds = np.random.default_rng(5).integers(0, 2 ** 32, 1 << 16, dtype=np.uint64).astype(np.uint32)
+    a = gpu.probe_light_samples(params, seeds)
+    b = cpu.light_samples(params, seeds)
+    gpu.destroy()
+    assert np.array_equal(a[:, :2], b[:, :2])
+    assert np.all(np.abs(a[:, 2] - b[:, 2]) <= 1e-5 * np.abs(b[:, 2]))
+    assert np.abs(a[:, 3:] - b[:, 3:]).max() <= 1e-5
+    h, w = light_map.shape[:2]
+    assert b[:, 0].max() < w and b[:, 1].max() < h
 
 
 def test_light_map_uniforms_bit_exact(pair_light_map):

@@ -161,6 +161,32 @@ def test_light_map_tables():
     assert abs(float(mean @ np.array([0.2126, 0.7152, 0.0722])) - 1.0) < 2e-3
 
 
+def test_light_map_samples_follow_luminance(small_cfg):
+    """The oracle's light map samples (pt.comp:204-233) land on texels in
+    proportion to luminance x sin(theta), with the pdf of the texel they land on."""
+    from volview_gb300 import abi, scene
+    m = scene.synthetic_light_map()
+    cpu = O.CpuRenderer(small_cfg["volume"], small_cfg["tf"], small_cfg["hu"])
+    cpu.set_environment_map(m)
+    cpu.resize(16, 16)
+    p = scene.frame_params_for(small_cfg, [0.0, 0.0, 0.0], 100.0)
+    p.lighting.environment = abi.ENV_MAP
+    seeds = np.random.default_rng(5).integers(0, 2 ** 32, 1 << 16, dtype=np.uint64).astype(np.uint32)
+    b = cpu.light_samples(p, seeds)
+    h, w = m.shape[:2]
+    lum = (m.astype(np.float64) @ np.array([0.2126, 0.7152, 0.0722])) * np.sin(np.pi * (np.arange(h) + 0.5) / h)[:, None]
+    prob = lum / lum.sum()
+    x, y = b[:, 0].astype(int), b[:, 1].astype(int)
+    freq = np.bincount(y * w + x, minlength=h * w).reshape(h, w) / len(seeds)
+    assert np.abs(freq - prob).max() < 4 * np.sqrt(prob.max() / len(seeds))
+    # pdf = p(texel) w h / (2 pi^2 sin(theta)), theta within the texel's row
+    s0, s1 = np.sin(np.pi * y / h), np.sin(np.pi * (y + 1) / h)
+    scale = prob[y, x] * w * h / (2 * np.pi ** 2)
+    assert np.all(b[:, 2] >= scale / np.maximum(s0, s1) * (1 - 1e-4))
+    assert np.all(b[:, 2] <= scale / np.maximum(np.minimum(s0, s1), 1e-6) * (1 + 1e-4))
+    assert np.all(np.abs(np.linalg.norm(b[:, 3:], axis=1) - 1) < 1e-5)
+
+
 def test_oracle_matches_reference_shaders_live_light_map(small_cfg):
     from oracle import ref as R
     if not R.available():

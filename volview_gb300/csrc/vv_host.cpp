@@ -223,12 +223,19 @@ struct vv_renderer {
     int bw[4], bh[4];
     // pre-integrated transfer function (RGBA32F, 4096), ray-marcher lighting volumes
     DBuf preint, shadow_vol, ao_vol;
+    // the lighting volumes as the image loop reads them: 3D textures with a
+    // white border, written from shadow_vol / ao_vol after each rebuild
+    struct TexVol {
+        cudaArray_t arr = nullptr;
+        cudaTextureObject_t tex = 0;
+        cudaSurfaceObject_t surf = 0;
+    } shadow_tex, ao_tex;
     int shadow_dims[3] = {0, 0, 0}, ao_dims[3] = {0, 0, 0};
     std::vector<uint8_t> ao_key, shadow_key;
     // light map (Environment::Map): RGBA16F radiance, RG32F sampling table,
     // RGBA16F diffuse convolution (32 x 16, the ray marcher's ambient light)
-    DBuf env_rad, env_table, env_diffuse;
-    int env_w = 0, env_h = 0;
+    DBuf env_rad, env_table, env_diffuse, env_guide;
+    int env_w = 0, env_h = 0, env_gm = 0, env_gr = 0;
     bool has_env = false;
     float env_peak_u = 0.0f;
     // wavefront tracer: path slots, stage queues, counters
@@ -257,6 +264,13 @@ struct vv_renderer {
     bool timing = false;
     std::vector<std::pair<cudaEvent_t, cudaEvent_t>> pt_events;
 };
+
+static void free_tex_vol(vv_renderer::TexVol& t) {
+    if (t.tex) cudaDestroyTextureObject(t.tex);
+    if (t.surf) cudaDestroySurfaceObject(t.surf);
+    if (t.arr) cudaFreeArray(t.arr);
+    t = vv_renderer::TexVol();
+}
 
 // Records the start event of a timed path-tracing launch (if timing is on).
 static void pt_timer_start(vv_renderer* r, cudaStream_t s) {
@@ -654,11 +668,13 @@ extern "C" vv_status vv_renderer_destroy(vv_renderer* r) {
     }
     if (r->prep_done) cudaEventDestroy(r->prep_done);
     DBuf* all[] = {&r->density, &r->normals, &r->mask_a, &r->mask_b, &r->labels, &r->majorant, &r->env_rad,
-                   &r->env_table, &r->env_diffuse, &r->preint, &r->shadow_vol, &r->ao_vol, &r->lut,
+                   &r->env_table, &r->env_diffuse, &r->env_guide, &r->preint, &r->shadow_vol, &r->ao_vol, &r->lut,
                    &r->bucket_dev, &r->tables, &r->soft, &r->work, &r->exposure, &r->accum, &r->albedo,
                    &r->normal, &r->ping, &r->pong, &r->guide_nd, &r->guide_alb, &r->hdr, &r->out, &r->bloom[0], &r->bloom[1], &r->bloom[2],
                    &r->bloom[3]};
     for (DBuf* b : all) b->release();
+    free_tex_vol(r->shadow_tex);
+    free_tex_vol(r->ao_tex);
     if (r->tables_host) cudaFreeHost(r->tables_host);
     if (r->counters) cudaFree(r->counters);
     delete r;
@@ -878,6 +894,33 @@ static float prepare_light_map(int w, int h, const float* px, std::vector<uint16
     return 0.5f + (float)(std::atan2(pxs, pzs) / (2.0 * 3.14159265358979323846));
 }
 
+// Guides for the inverse-CDF searches of the sampling table (Chen and Asau's
+// guide table): bucket k of g covers u in [k / g, (k + 1) / g), and the first
+// index whose CDF reaches u lies between the first indices for k / g and
+// (k + 1) / g, so a search within them returns what the search over the whole
+// CDF returns, with the same comparisons in f32. g is a power of two, so k / g
+// and the device's bucket floor(u * g) are exact.
+static void guide_of(const float* cdf, size_t stride, int n, int g, uint16_t* out) {
+    int i = 0;
+    for (int k = 0; k <= g; k++) {
+        float u = (float)k / (float)g;
+        while (i < n - 1 && !(cdf[stride * (size_t)i] >= u)) i++;
+        out[k] = (uint16_t)i;
+    }
+}
+static void search_guides(int w, int h, const std::vector<float>& table, int& gm, int& gr,
+                          std::vector<uint16_t>& guide) {
+    gm = 1;
+    while (gm < h && gm < 16384) gm *= 2;  // about one row per bucket
+    gr = 1;
+    while (gr < (w + 3) / 4 && gr < 4096) gr *= 2;  // about four columns per bucket
+    guide.assign((size_t)(gm + 1) + (size_t)h * (gr + 1), 0);
+    const size_t row = 2 * (size_t)(w + 1);
+    guide_of(table.data() + 2 * (size_t)w, row, h, gm, guide.data());
+    for (int y = 0; y < h; y++)
+        guide_of(table.data() + row * y, 2, w, gr, guide.data() + (gm + 1) + (size_t)y * (gr + 1));
+}
+
 extern "C" vv_status vv_set_environment_map(vv_renderer* r, const vv_environment_map* map) {
     if (!r) return fail(VV_ERR_ARG, "null renderer");
     vv_status st = use_device(r);
@@ -887,8 +930,9 @@ extern "C" vv_status vv_set_environment_map(vv_renderer* r, const vv_environment
         r->env_rad.release();
         r->env_table.release();
         r->env_diffuse.release();
+        r->env_guide.release();
         r->has_env = false;
-        r->env_w = r->env_h = 0;
+        r->env_w = r->env_h = r->env_gm = r->env_gr = 0;
         r->env_peak_u = 0.0f;
         r->have_params = false;
         return VV_OK;
@@ -900,6 +944,11 @@ extern "C" vv_status vv_set_environment_map(vv_renderer* r, const vv_environment
     std::vector<uint16_t> rad, diffuse;
     std::vector<float> table;
     float peak = prepare_light_map(w, h, map->rgb, rad, table, diffuse);
+    int gm = 1, gr = 1;
+    std::vector<uint16_t> guide;
+    search_guides(w, h, table, gm, gr, guide);
+    CK(r->env_guide.alloc(guide.size() * sizeof(uint16_t)));
+    CK(cudaMemcpy(r->env_guide.p, guide.data(), guide.size() * sizeof(uint16_t), cudaMemcpyHostToDevice));
     CK(r->env_rad.alloc(rad.size() * sizeof(uint16_t)));
     CK(r->env_table.alloc(table.size() * sizeof(float)));
     CK(r->env_diffuse.alloc(diffuse.size() * sizeof(uint16_t)));
@@ -908,6 +957,8 @@ extern "C" vv_status vv_set_environment_map(vv_renderer* r, const vv_environment
     CK(cudaMemcpy(r->env_table.p, table.data(), table.size() * sizeof(float), cudaMemcpyHostToDevice));
     r->env_w = w;
     r->env_h = h;
+    r->env_gm = gm;
+    r->env_gr = gr;
     r->env_peak_u = peak;
     r->has_env = true;
     r->have_params = false;  // accumulated_params = None
@@ -989,8 +1040,11 @@ static PtArgs pt_args(vv_renderer* r, const UHead& u) {
     a.env_diffuse = r->env_diffuse.as<ushort4>();
     a.preint = r->preint.as<float4>();
     a.env_table = r->env_table.as<float2>();
+    a.env_guide = r->env_guide.as<uint16_t>();
     a.env_w = r->env_w;
     a.env_h = r->env_h;
+    a.env_gm = r->env_gm;
+    a.env_gr = r->env_gr;
     a.lut = r->lut.as<float4>();
     a.tab = r->tables.as<LabelTables>();
     a.vol = r->vol;
@@ -1161,6 +1215,24 @@ static void append_key(std::vector<uint8_t>& k, const void* p, size_t n) {
     const uint8_t* b = (const uint8_t*)p;
     k.insert(k.end(), b, b + n);
 }
+static cudaError_t make_tex_vol(vv_renderer::TexVol& t, int w, int h, int d, bool rgba) {
+    cudaChannelFormatDesc f = rgba ? cudaCreateChannelDescHalf4() : cudaCreateChannelDescHalf();
+    cudaError_t e = cudaMalloc3DArray(&t.arr, &f, make_cudaExtent(w + 2, h + 2, d + 2), cudaArraySurfaceLoadStore);
+    if (e != cudaSuccess) return e;
+    cudaResourceDesc rd;
+    std::memset(&rd, 0, sizeof(rd));
+    rd.resType = cudaResourceTypeArray;
+    rd.res.array.array = t.arr;
+    if ((e = cudaCreateSurfaceObject(&t.surf, &rd)) != cudaSuccess) return e;
+    cudaTextureDesc td;
+    std::memset(&td, 0, sizeof(td));
+    for (int k = 0; k < 3; k++) td.addressMode[k] = cudaAddressModeClamp;
+    td.filterMode = cudaFilterModeLinear;
+    td.readMode = cudaReadModeElementType;
+    td.normalizedCoords = 0;
+    return cudaCreateTextureObject(&t.tex, &rd, &td, nullptr);
+}
+
 static vv_status record_ray_march(vv_renderer* r, const vv_frame_params& p, const UHead& u) {
     cudaStream_t st = r->ctx->stream;
     const int dims[3] = {(int)r->vol.nx, (int)r->vol.ny, (int)r->vol.nz};
@@ -1173,6 +1245,13 @@ static vv_status record_ray_march(vv_renderer* r, const vv_frame_params& p, cons
         CK(r->ao_vol.alloc((size_t)r->ao_dims[0] * r->ao_dims[1] * r->ao_dims[2] * 2));
         CK(cudaMemsetAsync(r->shadow_vol.p, 0, r->shadow_vol.n, st));
         CK(cudaMemsetAsync(r->ao_vol.p, 0, r->ao_vol.n, st));
+        CK(make_tex_vol(r->shadow_tex, r->shadow_dims[0], r->shadow_dims[1], r->shadow_dims[2], true));
+        CK(make_tex_vol(r->ao_tex, r->ao_dims[0], r->ao_dims[1], r->ao_dims[2], false));
+        CK(launch_pad_lighting(r->shadow_vol.as<uint16_t>(), 4, r->shadow_dims[0], r->shadow_dims[1],
+                               r->shadow_dims[2], r->shadow_tex.surf, st));
+        CK(launch_pad_lighting(r->ao_vol.as<uint16_t>(), 1, r->ao_dims[0], r->ao_dims[1], r->ao_dims[2],
+                               r->ao_tex.surf, st));
+        r->launches += 2;
     }
     PtArgs a = pt_args(r, u);
     int launches = 0;
@@ -1183,7 +1262,9 @@ static vv_status record_ray_march(vv_renderer* r, const vv_frame_params& p, cons
     append_key(ao_key, u.clip_planes, 12 * sizeof(float));
     if (p.lighting.ambient_occlusion && r->ao_key != ao_key) {
         CK(launch_ao(a, r->ao_vol.as<uint16_t>(), r->ao_dims[0], r->ao_dims[1], r->ao_dims[2], st));
-        launches += 1;
+        CK(launch_pad_lighting(r->ao_vol.as<uint16_t>(), 1, r->ao_dims[0], r->ao_dims[1], r->ao_dims[2],
+                               r->ao_tex.surf, st));
+        launches += 2;
         r->ao_key = ao_key;
     }
     std::vector<uint8_t> shadow_key = ao_key;  // + light direction bits and the tint (renderer.rs:1730-1748)
@@ -1207,10 +1288,14 @@ static vv_status record_ray_march(vv_renderer* r, const vv_frame_params& p, cons
         int sign = l_idx[axis] >= 0.0f ? 1 : -1;
         CK(launch_shadow_sweep(a, r->shadow_vol.as<ushort4>(), r->shadow_dims[0], r->shadow_dims[1],
                                r->shadow_dims[2], axis, sign, st, &launches));
+        CK(launch_pad_lighting(r->shadow_vol.as<uint16_t>(), 4, r->shadow_dims[0], r->shadow_dims[1],
+                               r->shadow_dims[2], r->shadow_tex.surf, st));
+        launches += 1;
         r->shadow_key = shadow_key;
     }
-    CK(launch_dvr(a, r->shadow_vol.as<ushort4>(), r->shadow_dims[0], r->shadow_dims[1], r->shadow_dims[2],
-                  r->ao_vol.as<uint16_t>(), r->ao_dims[0], r->ao_dims[1], r->ao_dims[2], st));
+    LightTex sv{r->shadow_tex.tex, r->shadow_dims[0], r->shadow_dims[1], r->shadow_dims[2], 1};
+    LightTex av{r->ao_tex.tex, r->ao_dims[0], r->ao_dims[1], r->ao_dims[2], 0};
+    CK(launch_dvr(a, sv, av, st));
     launches += 1;
     PostArgs pa = post_args(r, u);
     CK(launch_post(pa, st, &launches));
@@ -1464,6 +1549,28 @@ extern "C" vv_status vv_probe_bspline(vv_renderer* r, const vv_frame_params* par
     di.release();
     dout.release();
     if (e != cudaSuccess) return cuda_fail(e, "bspline probe");
+    return VV_OK;
+}
+
+extern "C" vv_status vv_probe_light_samples(vv_renderer* r, const vv_frame_params* params, const uint32_t* seeds,
+                                             size_t n, float* out) {
+    if (!r || !params || !seeds || !out) return fail(VV_ERR_ARG, "null argument");
+    if (!r->has_env) return fail(VV_ERR_STATE, "no light map");
+    UHead u;
+    vv_status s = prepare_frame(r, *params, 1, u);
+    if (s != VV_OK) return s;
+    DBuf ds, dout;
+    CK(ds.alloc(n * 4));
+    CK(dout.alloc(n * 24));
+    cudaStream_t st = r->ctx->stream;
+    PtArgs a = pt_args(r, u);
+    cudaError_t e = cudaMemcpyAsync(ds.p, seeds, n * 4, cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) e = launch_light_sample_probe(a, ds.as<uint32_t>(), dout.as<float>(), (int)n, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(out, dout.p, n * 24, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    ds.release();
+    dout.release();
+    if (e != cudaSuccess) return cuda_fail(e, "light sample probe");
     return VV_OK;
 }
 

@@ -34,7 +34,11 @@ struct PtArgs {
     const ushort4* env_diffuse; // light map's diffuse convolution, 32 x 16 RGBA16F (ray marcher)
     const ushort4* env_rad;     // light map radiance, RGBA16F, env_w x env_h (lighting.w == 2)
     const float2* env_table;    // light map sampling table, (env_w + 1) x env_h
-    int env_w, env_h;
+    // Search guides of the sampling table: for bucket k of `env_gm` (of `env_gr`
+    // per row) the first row (column) whose CDF reaches k / env_gm, clamped to
+    // the last; the marginal's env_gm + 1 entries, then env_gr + 1 per row.
+    const uint16_t* env_guide;
+    int env_w, env_h, env_gm, env_gr;
     const float4* lut;          // transfer function, RGBA16F values as float
     const LabelTables* tab;
     Vol vol;
@@ -113,10 +117,22 @@ cudaError_t launch_pt_wavefront(const PtArgs& a, const WfArgs& w, int sms, cudaS
 cudaError_t launch_ao(const PtArgs& a, uint16_t* out, int ax, int ay, int az, cudaStream_t s);
 cudaError_t launch_shadow_sweep(const PtArgs& a, ushort4* vol, int sx, int sy, int sz, int axis, int sign,
                                 cudaStream_t s, int* launches);
-cudaError_t launch_dvr(const PtArgs& a, const ushort4* shadow, int sx, int sy, int sz, const uint16_t* ao, int ax,
-                       int ay, int az, cudaStream_t s);
+// A lighting volume as the image loop reads it: a 3D texture of its texels
+// inside a one-texel white border, filtered by the texture units (clamped
+// addressing onto the border = the reference's white-border sampler).
+struct LightTex {
+    cudaTextureObject_t tex;
+    int w, h, d;  // texels of the volume, border excluded
+    int rgba;     // 1: RGBA16F (shadow), 0: R16F (occlusion)
+};
+// Copies a pixel-linear lighting volume (`channels` halves per texel) into its
+// texture array through `surf`, white border included.
+cudaError_t launch_pad_lighting(const uint16_t* vol, int channels, int w, int h, int d, cudaSurfaceObject_t surf,
+                                cudaStream_t s);
+cudaError_t launch_dvr(const PtArgs& a, const LightTex& shadow, const LightTex& ao, cudaStream_t s);
 // B-spline density and gradient at n continuous indices (parity probe).
 cudaError_t launch_bspline_probe(const PtArgs& a, const float* idx, float* out, int n, cudaStream_t s);
+cudaError_t launch_light_sample_probe(const PtArgs& a, const uint32_t* seeds, float* out, int n, cudaStream_t s);
 // One path per listed pixel at accumulation count a.u.path[0] (parity probe): 12 floats each.
 cudaError_t launch_pt_pixels(const PtArgs& a, const int* px, float* out, int n, cudaStream_t s);
 

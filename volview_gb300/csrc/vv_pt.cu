@@ -155,6 +155,26 @@ cudaError_t launch_bspline_probe(const PtArgs& a, const float* idx, float* out, 
     return cudaGetLastError();
 }
 
+__global__ void k_light_sample_probe(const __grid_constant__ PtArgs A, const uint32_t* seeds, float* out, int n) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    Rng rng;
+    rng.s = seeds[i];
+    Rng replay = rng;
+    int x, y;
+    env_texel(A, replay, x, y);
+    float pdf;
+    f3 d = sample_env(A, rng, pdf);
+    out[6 * i] = (float)x;
+    out[6 * i + 1] = (float)y;
+    out[6 * i + 2] = pdf;
+    out[6 * i + 3] = d.x; out[6 * i + 4] = d.y; out[6 * i + 5] = d.z;
+}
+cudaError_t launch_light_sample_probe(const PtArgs& a, const uint32_t* seeds, float* out, int n, cudaStream_t s) {
+    k_light_sample_probe<<<(n + 127) / 128, 128, 0, s>>>(a, seeds, out, n);
+    return cudaGetLastError();
+}
+
 __global__ void k_pt_pixels(const __grid_constant__ PtArgs A, const int* pix, float* out, int n) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;

@@ -740,32 +740,45 @@ __device__ __forceinline__ f3 sample_light(const PtArgs& A, const Consts& C, Rng
     return mul(C.light_frame, mk(sin_t * cp, sin_t * sp, cos_t));
 }
 
-// pt.comp:204-233: a direction towards the light map drawn by luminance x
-// solid angle: binary search of the marginal CDF over rows, then of the row's
-// conditional CDF, then a uniform point in the texel.
-__device__ __noinline__ f3 sample_env(const PtArgs& A, Rng& rng, float& pdf) {
-    const int W = A.env_w, H = A.env_h;
+// pt.comp:204-223: the light map texel drawn by luminance x solid angle:
+// binary search of the marginal CDF over rows, then of the row's conditional
+// CDF. Each search starts from its guide bucket's range (PtArgs::env_guide),
+// which holds the index the search over the whole CDF finds.
+__device__ __forceinline__ void env_texel(const PtArgs& A, Rng& rng, int& x, int& y) {
+    const int W = A.env_w;
     const float2* T = A.env_table;
+    const uint16_t* G = A.env_guide;
     float xi = rng.rand();
-    int lo = 0, hi = H - 1;
+    int k = (int)(xi * (float)A.env_gm);
+    int lo = __ldg(G + k), hi = __ldg(G + k + 1);
     while (lo < hi) {
         int mid = (lo + hi) / 2;
         if (__ldg(&T[(long)mid * (W + 1) + W].x) >= xi) hi = mid;
         else lo = mid + 1;
     }
-    int y = lo;
+    y = lo;
     xi = rng.rand();
-    lo = 0;
-    hi = W - 1;
+    const uint16_t* g = G + (A.env_gm + 1) + (long)y * (A.env_gr + 1);
+    k = (int)(xi * (float)A.env_gr);
+    lo = __ldg(g + k);
+    hi = __ldg(g + k + 1);
     while (lo < hi) {
         int mid = (lo + hi) / 2;
         if (__ldg(&T[(long)y * (W + 1) + mid].x) >= xi) hi = mid;
         else lo = mid + 1;
     }
+    x = lo;
+}
+// pt.comp:204-233: a direction towards the light map: the texel, then a
+// uniform point in it, with its solid-angle pdf.
+__device__ __noinline__ f3 sample_env(const PtArgs& A, Rng& rng, float& pdf) {
+    const int W = A.env_w, H = A.env_h;
+    int x, y;
+    env_texel(A, rng, x, y);
     float jx = rng.rand();
     float jy = rng.rand();
-    float2 uv = make_float2(((float)lo + jx) / (float)W, ((float)y + jy) / (float)H);
-    float p = __ldg(&T[(long)y * (W + 1) + lo].y);
+    float2 uv = make_float2(((float)x + jx) / (float)W, ((float)y + jy) / (float)H);
+    float p = __ldg(&A.env_table[(long)y * (W + 1) + x].y);
     pdf = p * (float)(W * H) / (2.0f * PI * PI * gmax(sinf(uv.y * PI), 1e-6f));
     return env_direction(A, uv);
 }

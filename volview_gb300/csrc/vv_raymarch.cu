@@ -130,9 +130,18 @@ __device__ float4 lv_linear(const LightVol& v, f3 tc) {
 __device__ __forceinline__ float4 f4add(float4 a, float4 b) { return make_float4(a.x + b.x, a.y + b.y, a.z + b.z, a.w + b.w); }
 __device__ __forceinline__ float4 f4mul(float s, float4 a) { return make_float4(s * a.x, s * a.y, s * a.z, s * a.w); }
 
+// A linear fetch of a lighting texture at texel-space position p (texel i's
+// centre at i; the border texel sits at -1 and w).
+__device__ __forceinline__ float4 lt_fetch(const LightTex& v, float x, float y, float z) {
+    if (v.rgba) return tex3D<float4>(v.tex, x + 1.5f, y + 1.5f, z + 1.5f);
+    return make_float4(tex3D<float>(v.tex, x + 1.5f, y + 1.5f, z + 1.5f), 0.0f, 0.0f, 1.0f);
+}
+__device__ __forceinline__ float4 lt_linear(const LightTex& v, f3 tc) {
+    return lt_fetch(v, tc.x * (float)v.w - 0.5f, tc.y * (float)v.h - 0.5f, tc.z * (float)v.d - 0.5f);
+}
 // common.glsl:141-152: B-spline filtering from 8 linear fetches (folded taps of
 // common.glsl:89-108).
-__device__ __noinline__ float4 lv_cubic(const LightVol& v, f3 tc) {
+__device__ __noinline__ float4 lt_cubic(const LightTex& v, f3 tc) {
     f3 size = mk((float)v.w, (float)v.h, (float)v.d);
     f3 idx = tc * size - 0.5f;
     f3 i = mk(floorf(idx.x), floorf(idx.y), floorf(idx.z));
@@ -142,17 +151,16 @@ __device__ __noinline__ float4 lv_cubic(const LightVol& v, f3 tc) {
     f3 w2 = (1.0f + 3.0f * f + 3.0f * f2 - 3.0f * f3v) / 6.0f;
     f3 w3 = f3v / 6.0f;
     f3 g0 = w0 + w1, g1 = w2 + w3;
-    f3 h0 = i - 1.0f + w1 / g0, h1 = i + 1.0f + w3 / g1;
-    f3 a = (h0 + 0.5f) / size, b = (h1 + 0.5f) / size;
-    float4 z0 = f4add(f4mul(g0.y, f4add(f4mul(g0.x, lv_linear(v, mk(a.x, a.y, a.z))), f4mul(g1.x, lv_linear(v, mk(b.x, a.y, a.z))))),
-                      f4mul(g1.y, f4add(f4mul(g0.x, lv_linear(v, mk(a.x, b.y, a.z))), f4mul(g1.x, lv_linear(v, mk(b.x, b.y, a.z))))));
-    float4 z1 = f4add(f4mul(g0.y, f4add(f4mul(g0.x, lv_linear(v, mk(a.x, a.y, b.z))), f4mul(g1.x, lv_linear(v, mk(b.x, a.y, b.z))))),
-                      f4mul(g1.y, f4add(f4mul(g0.x, lv_linear(v, mk(a.x, b.y, b.z))), f4mul(g1.x, lv_linear(v, mk(b.x, b.y, b.z))))));
+    f3 a = i - 1.0f + w1 / g0, b = i + 1.0f + w3 / g1;  // the folded taps, in texels
+    float4 z0 = f4add(f4mul(g0.y, f4add(f4mul(g0.x, lt_fetch(v, a.x, a.y, a.z)), f4mul(g1.x, lt_fetch(v, b.x, a.y, a.z)))),
+                      f4mul(g1.y, f4add(f4mul(g0.x, lt_fetch(v, a.x, b.y, a.z)), f4mul(g1.x, lt_fetch(v, b.x, b.y, a.z)))));
+    float4 z1 = f4add(f4mul(g0.y, f4add(f4mul(g0.x, lt_fetch(v, a.x, a.y, b.z)), f4mul(g1.x, lt_fetch(v, b.x, a.y, b.z)))),
+                      f4mul(g1.y, f4add(f4mul(g0.x, lt_fetch(v, a.x, b.y, b.z)), f4mul(g1.x, lt_fetch(v, b.x, b.y, b.z)))));
     return f4add(f4mul(g0.z, z0), f4mul(g1.z, z1));
 }
 // common.glsl:154-157
-__device__ __forceinline__ float4 lighting_lookup(const PtArgs& A, const LightVol& v, f3 tc) {
-    return A.u.env[1] > 0.5f ? lv_cubic(v, tc) : lv_linear(v, tc);
+__device__ __forceinline__ float4 lighting_lookup(const PtArgs& A, const LightTex& v, f3 tc) {
+    return A.u.env[1] > 0.5f ? lt_cubic(v, tc) : lt_linear(v, tc);
 }
 
 // common.glsl:483-486: cosine-weighted mean light map radiance around `n`
@@ -191,7 +199,7 @@ __device__ __noinline__ f3 refine_surface(const PtArgs& A, f3 idx, f3 d_idx, flo
 // dvr.comp:98-141: light reflected and scattered towards the viewer at a
 // sample (lighting volumes, BRDF, subsurface, ambient); ghosted structures'
 // opacity `alpha` is rescaled to their shell.
-__device__ __noinline__ f3 shade_sample(const PtArgs& A, const LightVol& SV, const LightVol& AV, f3 idx, Sample s,
+__device__ __noinline__ f3 shade_sample(const PtArgs& A, const LightTex& SV, const LightTex& AV, f3 idx, Sample s,
                                         f3 v, int cap_plane, float cut, float step_mm, float& alpha) {
     m3 to_index = w2i3(A);
     f3 l = U3(A.u.light_dir);
@@ -295,9 +303,8 @@ __global__ void __launch_bounds__(64) k_shadow_slice(const __grid_constant__ PtA
 #ifndef VV_DVR_MIN_BLOCKS
 #define VV_DVR_MIN_BLOCKS 4
 #endif
-__global__ void __launch_bounds__(64, VV_DVR_MIN_BLOCKS) k_dvr(const __grid_constant__ PtArgs A, const ushort4* __restrict__ shadow,
-                                            int sx, int sy, int sz, const uint16_t* __restrict__ ao, int ax, int ay,
-                                            int az) {
+__global__ void __launch_bounds__(64, VV_DVR_MIN_BLOCKS) k_dvr(const __grid_constant__ PtArgs A, const LightTex SV,
+                                                               const LightTex AV) {
     int px = blockIdx.x * 8 + (threadIdx.x & 7), py = blockIdx.y * 8 + (threadIdx.x >> 3);
     if (px >= (int)A.u.flags[2] || py >= (int)A.u.flags[3]) return;
     float nx = ((float)px + 0.5f) / (float)A.u.flags[2] * 2.0f - 1.0f;
@@ -317,7 +324,6 @@ __global__ void __launch_bounds__(64, VV_DVR_MIN_BLOCKS) k_dvr(const __grid_cons
     f3 radiance = mk(0.0f);
     float transmittance = 1.0f;
     bool refined = false;
-    LightVol SV{(const uint16_t*)shadow, sx, sy, sz, 4}, AV{ao, ax, ay, az, 1};
     if (t.x < t.y) {
         float tt = t.x + ign((float)px, (float)py) * step_mm;
         float prev_density = density_view(A, o_idx + d_idx * (tt - step_mm));
@@ -379,10 +385,34 @@ cudaError_t launch_shadow_sweep(const PtArgs& a, ushort4* vol, int sx, int sy, i
     return cudaGetLastError();
 }
 
-cudaError_t launch_dvr(const PtArgs& a, const ushort4* shadow, int sx, int sy, int sz, const uint16_t* ao, int ax,
-                       int ay, int az, cudaStream_t s) {
+// The texture array of a lighting volume: texel (x, y, z) of the volume at
+// (x + 1, y + 1, z + 1), white (1, 1, 1, 1) around it.
+__global__ void k_pad_lighting(const uint16_t* __restrict__ vol, int channels, int w, int h, int d,
+                               cudaSurfaceObject_t surf) {
+    int x = blockIdx.x * 8 + (threadIdx.x & 7), y = blockIdx.y * 8 + (threadIdx.x >> 3), z = blockIdx.z;
+    if (x >= w + 2 || y >= h + 2 || z >= d + 2) return;
+    const uint16_t one = 0x3c00u;  // 1.0 in binary16
+    bool inside = x >= 1 && y >= 1 && z >= 1 && x <= w && y <= h && z <= d;
+    long i = inside ? ((long)(z - 1) * h + (y - 1)) * w + (x - 1) : 0;
+    if (channels == 4) {
+        ushort4 t = inside ? __ldg((const ushort4*)vol + i) : make_ushort4(one, one, one, one);
+        surf3Dwrite(t, surf, x * (int)sizeof(ushort4), y, z);
+    } else {
+        uint16_t t = inside ? __ldg(vol + i) : one;
+        surf3Dwrite(t, surf, x * (int)sizeof(uint16_t), y, z);
+    }
+}
+
+cudaError_t launch_pad_lighting(const uint16_t* vol, int channels, int w, int h, int d, cudaSurfaceObject_t surf,
+                                cudaStream_t s) {
+    dim3 g((w + 2 + 7) / 8, (h + 2 + 7) / 8, d + 2);
+    k_pad_lighting<<<g, 64, 0, s>>>(vol, channels, w, h, d, surf);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_dvr(const PtArgs& a, const LightTex& shadow, const LightTex& ao, cudaStream_t s) {
     dim3 g((a.width + 7) / 8, (a.height + 7) / 8);
-    k_dvr<<<g, 64, 0, s>>>(a, shadow, sx, sy, sz, ao, ax, ay, az);
+    k_dvr<<<g, 64, 0, s>>>(a, shadow, ao);
     return cudaGetLastError();
 }
 

@@ -57,6 +57,7 @@ EXPORTS = [
 PROBES = [
     ("vv_probe_bspline", C.c_int, [P, P, P, C.c_size_t, P]),
     ("vv_probe_paths", C.c_int, [P, P, C.c_uint32, P, C.c_size_t, P]),
+    ("vv_probe_light_samples", C.c_int, [P, P, P, C.c_size_t, P]),
     ("vv_count_events", C.c_int, [P, C.c_int, P, C.c_size_t]),
     ("vv_time_pt", C.c_int, [P, C.c_int, P, P]),
 ]
@@ -176,10 +177,12 @@ class Renderer:
         check(load().vv_read_hdr(self.handle, _ptr(out), out.size))
         return out
 
-    def read_accumulation(self):
+    def read_accumulation(self, normal=True):
+        """(radiance sums, albedo sums, normal sums or None) as (h, w, 4) float32."""
         shape = (self.height, self.width, 4)
-        a, b, c = (np.empty(shape, np.float32) for _ in range(3))
-        check(load().vv_read_accumulation(self.handle, _ptr(a), _ptr(b), _ptr(c), a.size))
+        a, b = np.empty(shape, np.float32), np.empty(shape, np.float32)
+        c = np.empty(shape, np.float32) if normal else None
+        check(load().vv_read_accumulation(self.handle, _ptr(a), _ptr(b), _ptr(c) if normal else None, a.size))
         return a, b, c
 
     def pack_uniforms(self, params, frame=1):
@@ -211,6 +214,13 @@ class Renderer:
         idx = np.ascontiguousarray(idx, np.float32).reshape(-1, 3)
         out = np.zeros((idx.shape[0], 4), np.float32)
         check(load().vv_probe_bspline(self.handle, C.byref(params), _ptr(idx), idx.shape[0], _ptr(out)))
+        return out
+
+    def probe_light_samples(self, params, seeds):
+        """(n, 6): texel column, row, pdf, direction xyz of light map samples from `seeds`."""
+        seeds = np.ascontiguousarray(seeds, np.uint32).ravel()
+        out = np.zeros((seeds.size, 6), np.float32)
+        check(load().vv_probe_light_samples(self.handle, C.byref(params), _ptr(seeds), seeds.size, _ptr(out)))
         return out
 
     def probe_paths(self, params, accumulated, pixels):

@@ -207,6 +207,39 @@ __device__ __noinline__ f3 density_gradient_cubic(const PtArgs& A, f3 p) {
     return mk(gx, gy, gz) * INV65535;
 }
 
+// density_cubic and density_gradient_cubic at one point from one read of the
+// 64 voxels, each with the arithmetic of its own function (the value's
+// z-slices are the gradient's vz sums), so both results are those functions'.
+__device__ __noinline__ float density_cubic_with_gradient(const PtArgs& A, f3 p, f3& grad) {
+    count(A, COUNT_CUBIC);
+    Cubic c = cubic_taps(A.vol, p);
+    float wx[4], wy[4], wz[4], dx[4], dy[4], dz[4];
+    bspline_w(c.fx, wx); bspline_w(c.fy, wy); bspline_w(c.fz, wz);
+    bspline_d(c.fx, dx); bspline_d(c.fy, dy); bspline_d(c.fz, dz);
+    float acc = 0.0f, gx = 0.0f, gy = 0.0f, gz = 0.0f;
+#pragma unroll
+    for (int z = 0; z < 4; z++) {
+        float vz = 0.0f, gxz = 0.0f, gyz = 0.0f;
+#pragma unroll
+        for (int y = 0; y < 4; y++) {
+            const uint16_t* row = A.density + c.oz[z] + c.oy[y];
+            float v0 = (float)__ldg(row + c.ox[0]), v1 = (float)__ldg(row + c.ox[1]);
+            float v2 = (float)__ldg(row + c.ox[2]), v3 = (float)__ldg(row + c.ox[3]);
+            float rw = wx[0] * v0 + wx[1] * v1 + wx[2] * v2 + wx[3] * v3;
+            float rd = dx[0] * v0 + dx[1] * v1 + dx[2] * v2 + dx[3] * v3;
+            vz = fmaf(wy[y], rw, vz);
+            gxz = fmaf(wy[y], rd, gxz);
+            gyz = fmaf(dy[y], rw, gyz);
+        }
+        acc = fmaf(wz[z], vz, acc);
+        gx = fmaf(wz[z], gxz, gx);
+        gy = fmaf(wz[z], gyz, gy);
+        gz = fmaf(dz[z], vz, gz);
+    }
+    grad = mk(gx, gy, gz) * INV65535;
+    return acc * INV65535;
+}
+
 // transfer (common.glsl:170-173): linear LUT lookup at texel centres.
 __device__ float4 transfer(const PtArgs& A, float d) {
     float u = d * 4095.0f;
@@ -427,8 +460,10 @@ __device__ __noinline__ f3 brdf_coated(f3 n, f3 v, f3 l, const Sample& s, f3& di
 }
 
 // shading.glsl:73-144
+// With GIVEN, `given_grad` is density_gradient_cubic(A, idx), already known.
+template <bool GIVEN = false>
 __device__ __noinline__ float surface_frame(const PtArgs& A, f3 idx, const Sample& s, f3 v, int cap_plane, float cut,
-                               float cap_depth, f3& n, float& surfaceness) {
+                               float cap_depth, f3& n, float& surfaceness, f3 given_grad = f3{0.0f, 0.0f, 0.0f}) {
     uint32_t label_mode = (uint32_t)A.u.labels[0];
     float4 nw = normal_tri(A, idx);
     f3 nxyz = mk(nw.x, nw.y, nw.z);
@@ -437,7 +472,7 @@ __device__ __noinline__ float surface_frame(const PtArgs& A, f3 idx, const Sampl
     surfaceness = nw.w;
     bool skin = s.label == SKIN_LABEL;
     if (A.u.env[1] > 0.5f && n_len > 1e-3f && (!s.ghost || skin)) {
-        f3 gw = mul_t(w2i3(A), density_gradient_cubic(A, idx));
+        f3 gw = mul_t(w2i3(A), GIVEN ? given_grad : density_gradient_cubic(A, idx));
         float l = len(gw);
         n = l > 1e-7f ? -gw / l : n;
     }

@@ -309,7 +309,7 @@ __global__ void __launch_bounds__(64) k_shadow_slice(const __grid_constant__ PtA
 __global__ void __launch_bounds__(64, VV_DVR_MIN_BLOCKS) k_dvr(const __grid_constant__ PtArgs A, const LightTex SV,
                                                                const LightTex AV) {
     int px = blockIdx.x * 8 + (threadIdx.x & 7), py = blockIdx.y * 8 + (threadIdx.x >> 3);
-    const bool in_image = px < (int)A.u.flags[2] && py < (int)A.u.flags[3];
+    if (px >= (int)A.u.flags[2] || py >= (int)A.u.flags[3]) return;
     float nx = ((float)px + 0.5f) / (float)A.u.flags[2] * 2.0f - 1.0f;
     float ny = ((float)py + 0.5f) / (float)A.u.flags[3] * 2.0f - 1.0f;
     f3 dir = normalize(U3(A.u.forward) + nx * U3(A.u.right) - ny * U3(A.u.up));
@@ -327,55 +327,35 @@ __global__ void __launch_bounds__(64, VV_DVR_MIN_BLOCKS) k_dvr(const __grid_cons
     f3 radiance = mk(0.0f);
     float transmittance = 1.0f;
     bool refined = false;
-    bool live = in_image && t.x < t.y;
-    float tt = 0.0f, prev_density = -1.0f;
-    if (live) {
-        tt = t.x + ign((float)px, (float)py) * step_mm;
-        prev_density = density_view(A, o_idx + d_idx * (tt - step_mm));
-    }
-    // Each lane marches (steps of step_mm, empty bricks and clipped samples
-    // skipped) to its next sample with extinction, then the warp shades those
-    // samples together: the same steps in the same order per lane as one loop
-    // over the steps, with the large shading code run by many lanes at once.
-    for (;;) {
-        if (!__any_sync(0xffffffffu, live)) break;
-        bool pending = false;
-        f3 idx = mk(0.0f), grad = mk(0.0f);
-        Sample s;
-        int cap_plane = -1;
-        float cut = 0.0f, alpha = 0.0f;
-        bool has_grad = false;
-        while (live && !pending) {
-            if (!(tt < t.y && transmittance > 0.01f)) {
-                live = false;
-                break;
-            }
-            idx = o_idx + d_idx * tt;
+    if (t.x < t.y) {
+        float tt = t.x + ign((float)px, (float)py) * step_mm;
+        float prev_density = density_view(A, o_idx + d_idx * (tt - step_mm));
+        for (; tt < t.y && transmittance > 0.01f; tt += step_mm) {
+            f3 idx = o_idx + d_idx * tt;
             float maj = A.u.path[3] == 0u ? 1e30f : __ldg(A.majorant + brick_index(A, idx));
             if (maj <= 0.0f) {
                 tt += brick_exit(idx, inv_d);
                 prev_density = -1.0f;
-                tt += step_mm;
                 continue;
             }
-            cut = clip_depth(A, idx, cap_plane);
+            int cap_plane;
+            float cut = clip_depth(A, idx, cap_plane);
             if (cut > 0.0f) {
                 prev_density = -1.0f;
-                tt += step_mm;
                 continue;
             }
             // With smooth sampling the gradient comes with the density: a
             // sample shaded where it was taken needs no second read.
-            has_grad = A.u.env[1] > 0.5f;
+            f3 grad = mk(0.0f);
+            bool has_grad = A.u.env[1] > 0.5f;
             float density = has_grad ? density_cubic_with_gradient(A, idx, grad) : density_tri(A, idx);
             float front_density = prev_density;
             bool segment = preintegrate && front_density >= 0.0f;
-            s = segment ? tf_segment(A, front_density, density) : tf_point(A, density);
+            Sample s = segment ? tf_segment(A, front_density, density) : tf_point(A, density);
             prev_density = density;
             s = labelled(A, s, idx);
-            tt += step_mm;
             if (s.extinction <= 0.0f) continue;
-            alpha = 1.0f - expf(-s.extinction * step_mm);
+            float alpha = 1.0f - expf(-s.extinction * step_mm);
             if (segment && alpha > 0.2f && transmittance > 0.5f && s.label == 0u && fabsf(density - front_density) > 1e-4f) {
                 idx = idx - d_idx * (step_mm * (1.0f - preint_half_depth(A, front_density, density)));
                 has_grad = false;
@@ -384,18 +364,12 @@ __global__ void __launch_bounds__(64, VV_DVR_MIN_BLOCKS) k_dvr(const __grid_cons
                 idx = refine_surface(A, idx, d_idx, step_mm, 0.5f * s.extinction);
                 has_grad = false;
             }
-            pending = true;
-        }
-        __syncwarp();
-        if (pending) {
             f3 lit = shade_sample(A, SV, AV, idx, s, v, cap_plane, cut, step_mm, has_grad, grad, alpha);
             radiance += transmittance * alpha * lit;
             transmittance *= 1.0f - alpha;
         }
     }
-    if (in_image)
-        A.hdr[(long)py * A.width + px] = make_ushort4(f2h(radiance.x), f2h(radiance.y), f2h(radiance.z),
-                                                      f2h(transmittance));
+    A.hdr[(long)py * A.width + px] = make_ushort4(f2h(radiance.x), f2h(radiance.y), f2h(radiance.z), f2h(transmittance));
 }
 
 cudaError_t launch_ao(const PtArgs& a, uint16_t* out, int ax, int ay, int az, cudaStream_t s) {

@@ -48,8 +48,19 @@ def parse():
     ap.add_argument("--steps", type=int, default=40)
     ap.add_argument("--warmup", type=int, default=4)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--size", type=int, default=1024)
-    ap.add_argument("--dims", default="512,512,400")
+    ap.add_argument("--workload", default="head_neck", choices=["head_neck", "torso"],
+                    help="head_neck: 512x512x400 at 0.5x0.5x1 mm, 1024^2; torso: the precision workload, the "
+                         "small phantom scaled to 512x512x800 1 mm voxels, 1920x1080")
+    ap.add_argument("--size", type=int, default=0, help="square image side (default: the workload's)")
+    ap.add_argument("--dims", default="", help="volume dims x,y,z (default: the workload's)")
+    ap.add_argument("--density", default="unorm16", choices=list(DENSITY_FORMATS),
+                    help="density storage (vv_precision): the reference's R16_UNORM, or FP16 / BF16 / FP32")
+    ap.add_argument("--sums", default="fp32", choices=["fp32", "kahan"], help="running sums (vv_precision)")
+    ap.add_argument("--fp64-after", type=int, default=0,
+                    help="running sums continue in FP64 past this many paths/pixel (0: never)")
+    ap.add_argument("--precision-study", type=int, default=0,
+                    help="also render the default view to this many paths/pixel with each density storage "
+                         "format and report each one's error against FP32 storage (same random streams)")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
@@ -69,6 +80,26 @@ def parse():
     ap.add_argument("--rmse-target", type=float, default=RMSE_TARGET,
                     help="luminance RMSE to reach; 0 measures it on the default view at 1024 paths/pixel")
     return ap.parse_args()
+
+
+DENSITY_FORMATS = {"unorm16": 0, "fp16": 1, "bf16": 2, "fp32": 3}
+WORKLOADS = {"head_neck": ("512,512,400", (1024, 1024)), "torso": ("512,512,800", (1920, 1080))}
+
+
+def dims_of(args):
+    return args.dims or WORKLOADS[args.workload][0]
+
+
+def image_size(args):
+    """(width, height) of the workload's image, or args.size square."""
+    return (args.size, args.size) if args.size else WORKLOADS[args.workload][1]
+
+
+def precision_of(args, density=None):
+    from volview_gb300 import abi
+    fmt = DENSITY_FORMATS[density or args.density]
+    return abi.precision(density_format=fmt, sums=abi.SUMS_KAHAN if args.sums == "kahan" else abi.SUMS_FP32,
+                         fp64_after=args.fp64_after)
 
 
 def dist_init(n):
@@ -148,9 +179,11 @@ class Clocks:
 
 def workload(args):
     from volview_gb300 import scene
-    dims = tuple(int(v) for v in args.dims.split(","))
-    cfg = scene.head_neck_config(seed=2, dims=dims, spacing=(0.5, 0.5, 1.0), size=args.size, spp=1024)
-    return cfg
+    dims = tuple(int(v) for v in dims_of(args).split(","))
+    W, H = image_size(args)
+    if args.workload == "torso":
+        return scene.torso_config(seed=1, dims=dims, width=W, height=H, spp=4096)
+    return scene.head_neck_config(seed=2, dims=dims, spacing=(0.5, 0.5, 1.0), size=W, spp=1024)
 
 
 def frame_params(cfg, center, diagonal, light_map=False):
@@ -173,12 +206,16 @@ def light_map():
 
 
 def bench_config(args, F):
-    W = H = args.size
-    return {"workload": f"head_neck {args.dims.replace(',', 'x')} int16 HU at 0.5x0.5x1 mm, 120 labels, "
-                        f"soft labels, hybrid mode, sagittal clip, g=0.6, "
+    W, H = image_size(args)
+    volume = (f"head_neck {dims_of(args).replace(',', 'x')} int16 HU at 0.5x0.5x1 mm, 120 labels"
+              if args.workload == "head_neck" else
+              f"torso {dims_of(args).replace(',', 'x')} int16 HU at 1 mm (the 128^3 phantom's recipe scaled), "
+              "10 labels")
+    return {"workload": volume + ", soft labels, hybrid mode, sagittal clip, g=0.6, "
                         + ("synthetic 2048x1024 light map" if args.light_map else "studio light")
                         + f", {W}x{H}, "
                         f"1 path/pixel/frame",
+            "precision": {"density": args.density, "sums": args.sums, "fp64_after": args.fp64_after},
             "frames_per_step": F,
             "step": ("vv_record_frames: %d accumulate-frames in one wavefront pass, then a-trous and the "
                      "tone-mapped display once" % F) if F > 1 else "vv_record",
@@ -259,8 +296,8 @@ def time_to_rmse(r, params, args, frame, stream):
     import copy
     from volview_gb300 import convergence as CV
     target = args.rmse_target
-    if args.light_map and target == RMSE_TARGET:
-        target = 0.0  # the fixed target is the studio-lit workload's; measure the light map's
+    if (args.light_map or args.workload != "head_neck") and target == RMSE_TARGET:
+        target = 0.0  # the fixed target is the studio-lit head/neck workload's; measure this one's
     source = "fixed (default view, %d paths/pixel)" % RMSE_TARGET_SPP
     if target <= 0:
         # Measure the target: the default view at RMSE_TARGET_SPP paths per pixel,
@@ -340,10 +377,10 @@ def run_ours(args, rank, world, local):
     from volview_gb300.renderer import COUNT_BYTES, COUNT_NAMES
     torch.cuda.set_device(local)
     cfg = workload(args)
-    W = H = args.size
+    W, H = image_size(args)
     stream = torch.cuda.Stream()
     ctx = R.Context(local, stream=stream.cuda_stream)
-    r = R.Renderer(ctx, cfg["volume"], cfg["tf"])
+    r = R.Renderer(ctx, cfg["volume"], cfg["tf"], precision_of(args))
     r.set_labels(cfg["labels_vol"], abi.soft_struct(cfg["soft"]))
     if args.light_map:
         r.set_environment_map(abi.env_struct(light_map()))
@@ -458,7 +495,8 @@ def run_ours(args, rank, world, local):
     result = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded head/neck phantom; no CT data ships)",
+        "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded %s phantom; no CT data ships)" % args.workload.replace("_", "/"),
         "config": bench_config(args, F),
         "gpu_launches": int(launches),
         "path_vertices_per_s": counts["vertex"] / max(counts["pixel"], 1) * value,
@@ -475,12 +513,70 @@ def run_ours(args, rank, world, local):
         "accumulated_samples": r.accumulated_samples(),
     }
     result["clocks"] = clocks.summary()
+    if args.precision_study > 0 and rank == 0:
+        result["precision_study"] = precision_study(args, cfg, ctx, stream)
     if rank == 0 and not args.no_cpu_baseline:
         result["cpu_baseline"] = cpu_baseline(cfg, r, params, args)
     r.destroy()
     ctx.destroy()
     if rank == 0:
         print(json.dumps(result))
+
+
+def precision_study(args, cfg, ctx, stream):
+    """The default view at args.precision_study paths/pixel with the density
+    stored as FP32, R16_UNORM, FP16 and BF16, and once more as FP32 with Kahan
+    running sums (FP64 past 65536): the same random streams in every render, so
+    an image's luminance RMSE against the FP32-storage render is the storage
+    error (plus the paths whose decisions it flips), set beside the Monte Carlo
+    RMSE of the renders themselves."""
+    import copy
+    import torch
+    from volview_gb300 import abi
+    from volview_gb300 import convergence as CV
+    from volview_gb300 import renderer as R
+    W, H = image_size(args)
+    spp = args.precision_study
+    runs = [("fp32", "fp32", 0), ("unorm16", "fp32", 0), ("fp16", "fp32", 0), ("bf16", "fp32", 0),
+            ("fp32", "kahan", 65536)]
+    out, ref = {"paths_per_pixel": spp, "reference": "density stored as FP32, plain FP32 running sums"}, None
+    for density, sums, fp64_after in runs:
+        a = copy.copy(args)
+        a.sums, a.fp64_after = sums, fp64_after
+        r = R.Renderer(ctx, cfg["volume"], cfg["tf"], precision_of(a, density))
+        r.set_labels(cfg["labels_vol"], abi.soft_struct(cfg["soft"]))
+        if args.light_map:
+            r.set_environment_map(abi.env_struct(light_map()))
+        p = frame_params(cfg, list(r.center), r.diagonal, args.light_map)
+        r.resize(W, H)
+        r.record(1, p)  # masks and majorants
+        r.resize(W, H)  # restarts the accumulation
+        s0, s1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        s0.record(stream)
+        done, frame = 0, 2
+        while done < spp:
+            n = min(64, spp - done)
+            r.record_frames(frame, n, p)
+            frame, done = frame + n, done + n
+        s1.record(stream)
+        torch.cuda.synchronize()
+        ms = s0.elapsed_time(s1)
+        acc, alb, _ = r.read_accumulation(normal=False)
+        r.destroy()
+        lum = np.asarray(acc[..., :3], np.float64) @ CV.LUMA / spp
+        key = density if sums == "fp32" else f"{density}+{sums}+fp64_after_{fp64_after}"
+        entry = {"path_samples_per_s": W * H * spp / (ms / 1e3), "mc_rmse": CV.rmse_estimate(acc, alb, spp),
+                 "mean_luminance": float(lum.mean())}
+        if ref is None:
+            ref = (lum, acc)
+        else:
+            entry["rmse_vs_fp32"] = float(np.sqrt(np.mean((lum - ref[0]) ** 2)))
+            if sums != "fp32":
+                d = np.abs(acc.astype(np.float64) - ref[1]) / np.maximum(np.abs(ref[1]), 1e-30)
+                entry["sums_max_rel_diff"] = float(d[ref[1] != 0].max())
+        out[key] = entry
+    return out
 
 
 def cpu_renderer_from_device(cfg, r, params):
@@ -495,6 +591,7 @@ def cpu_renderer_from_device(cfg, r, params):
     cpu.dims = tuple(cfg["volume"].dims)
     cpu.geo = O.geometry(cfg["volume"])
     cpu.density = r.read_volume(abi.VOLUME_DENSITY)
+    cpu.density_format = r.precision.density_format
     cpu.set_transfer_function(cfg["tf"])
     cpu.normals = r.read_volume(abi.VOLUME_NORMALS)
     cpu.set_labels(cfg["labels_vol"], cfg["soft"])
@@ -525,7 +622,7 @@ def run_reference(args, rank, world):
     from oracle import oracle as O
     from oracle import ref as REF
     cfg = workload(args)
-    W = H = args.size
+    W, H = image_size(args)
     cpu = O.CpuRenderer(cfg["volume"], cfg["tf"], cfg["hu"])
     cpu.set_labels(cfg["labels_vol"], cfg["soft"])
     if args.light_map:

@@ -232,6 +232,32 @@ vv_status vv_context_destroy(vv_context* ctx);
  * device, uploads the transfer function and computes the normal volume. */
 vv_status vv_renderer_create(vv_context* ctx, const vv_volume* volume,
                              const vv_transfer_function* tf, vv_renderer** out);
+
+/* Storage and running-sum precision: an extension beyond the reference
+ * (whose density is R16_UNORM and whose sums are FP32), for the precision
+ * variant of the workload. vv_renderer_create uses the reference's
+ * {VV_DENSITY_UNORM16, VV_SUMS_FP32, 0}. */
+enum {
+    VV_DENSITY_UNORM16 = 0, /* round(t * 65535), t = normalised density (the reference) */
+    VV_DENSITY_FP16 = 1,    /* t as binary16, rounded to nearest even */
+    VV_DENSITY_BF16 = 2,    /* t as bfloat16, rounded to nearest even */
+    VV_DENSITY_FP32 = 3     /* t as binary32 */
+};
+enum {
+    VV_SUMS_FP32 = 0,       /* accumulation images are plain FP32 running sums */
+    VV_SUMS_KAHAN = 1       /* FP32 running sums with Kahan compensation per merge */
+};
+typedef struct vv_precision {
+    uint32_t density_format; /* VV_DENSITY_* */
+    uint32_t sums;           /* VV_SUMS_* */
+    uint32_t fp64_after;     /* 0: never; else the running sums continue in FP64
+                                once they hold this many samples per pixel */
+} vv_precision;
+/* vv_renderer_create with a storage and running-sum precision. Frames
+ * accumulated by the wavefront passes are summed per pass (FP32, atomically
+ * for several frames per pass), then merged into the running sums. */
+vv_status vv_renderer_create_ex(vv_context* ctx, const vv_volume* volume, const vv_transfer_function* tf,
+                                const vv_precision* precision, vv_renderer** out);
 /* Renderer::destroy (renderer.rs:2072). */
 vv_status vv_renderer_destroy(vv_renderer* r);
 vv_status vv_renderer_get_info(const vv_renderer* r, vv_renderer_info* out);
@@ -291,7 +317,7 @@ vv_status vv_pack_uniforms(vv_renderer* r, const vv_frame_params* params, uint64
                            void* out, size_t capacity);
 
 enum {
-    VV_VOLUME_DENSITY = 0,  /* uint16 per voxel (R16_UNORM) */
+    VV_VOLUME_DENSITY = 0,  /* uint16 per voxel (R16_UNORM; FP16 / BF16 bits, or float, per vv_precision) */
     VV_VOLUME_NORMALS = 1,  /* 4 x int8 per voxel (RGBA8_SNORM) */
     VV_VOLUME_MASK = 2,     /* 2 x uint16 per voxel (RG16_UNORM) */
     VV_VOLUME_LABELS = 3,   /* uint8 per voxel */

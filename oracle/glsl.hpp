@@ -331,12 +331,12 @@ inline mat3 inverse(const mat3& m) {
 
 // ------------------------------------------------------- texel formats and units
 enum Format : int {
-    R16_UNORM, RG16_UNORM, RGBA8_SNORM, RGBA8_UNORM, R32F, RG32F, RGBA32F, RGBA16F, R16F,
+    R16_UNORM, RG16_UNORM, RGBA8_SNORM, RGBA8_UNORM, R32F, RG32F, RGBA32F, RGBA16F, R16F, R16_BF16,
     R8_UINT, RGBA8_UINT
 };
 inline int format_bytes(Format f) {
     switch (f) {
-        case R16_UNORM: case R16F: return 2;
+        case R16_UNORM: case R16F: case R16_BF16: return 2;
         case RG16_UNORM: case RGBA8_SNORM: case RGBA8_UNORM: case R32F: case RGBA8_UINT: return 4;
         case RG32F: case RGBA16F: return 8;
         case RGBA32F: return 16;
@@ -360,6 +360,11 @@ inline vec4 decode(const void* data, Format f, long i) {
         case RGBA32F: { float v[4]; std::memcpy(v, b, 16); return vec4(v[0], v[1], v[2], v[3]); }
         case RGBA16F: { uint16_t v[4]; std::memcpy(v, b, 8); return vec4(half_to_float(v[0]), half_to_float(v[1]), half_to_float(v[2]), half_to_float(v[3])); }
         case R16F: { uint16_t v; std::memcpy(&v, b, 2); return vec4(half_to_float(v), 0, 0, 1); }
+        case R16_BF16: {  // the upper half of a binary32 (not a Vulkan format: the precision variant's density)
+            uint16_t v; std::memcpy(&v, b, 2);
+            uint32_t w = (uint32_t)v << 16; float x; std::memcpy(&x, &w, 4);
+            return vec4(x, 0, 0, 1);
+        }
         case R8_UINT: return vec4(float(b[0]), 0, 0, 1);
         case RGBA8_UINT: return vec4(float(b[0]), float(b[1]), float(b[2]), float(b[3]));
     }
@@ -382,6 +387,10 @@ inline void encode(void* data, Format f, long i, const vec4& v) {
         case RGBA32F: std::memcpy(b, &v.x, 16); break;
         case RGBA16F: { uint16_t q[4]; for (int k = 0; k < 4; k++) q[k] = float_to_half(v[k]); std::memcpy(b, q, 8); break; }
         case R16F: { uint16_t q = float_to_half(v.x); std::memcpy(b, &q, 2); break; }
+        case R16_BF16: {  // round to nearest even (finite values)
+            uint32_t w; std::memcpy(&w, &v.x, 4);
+            uint16_t q = (uint16_t)((w + 0x7fffu + ((w >> 16) & 1u)) >> 16); std::memcpy(b, &q, 2); break;
+        }
         case R8_UINT: b[0] = (uint8_t)v.x; break;
         case RGBA8_UINT: for (int k = 0; k < 4; k++) b[k] = (uint8_t)v[k]; break;
     }

@@ -53,7 +53,8 @@ struct Geometry {
 // Device-side inputs of the shaders, as x-fastest arrays.
 struct Scene {
     ivec3 dims;
-    const uint16_t* density = nullptr;   // R16_UNORM
+    const void* density = nullptr;       // R16_UNORM, or the precision variant's format
+    int density_format = 0;              // VV_DENSITY_*
     const int8_t* normals = nullptr;     // RGBA8_SNORM
     const uint16_t* mask = nullptr;      // RG16_UNORM (final, blurred)
     const uint8_t* labels = nullptr;     // R8_UINT; 1 voxel placeholder if absent

@@ -18,7 +18,8 @@ P = C.c_void_p
 class Scene(C.Structure):
     _fields_ = [("dims", C.c_int * 3), ("density", P), ("normals", P), ("mask", P), ("labels", P),
                 ("label_dims", C.c_int * 3), ("majorant", P), ("brick_dims", C.c_int * 3), ("tf_lut", P),
-                ("preint", P), ("env_rad", P), ("env_table", P), ("env_dims", C.c_int * 2)]
+                ("preint", P), ("env_rad", P), ("env_table", P), ("env_dims", C.c_int * 2),
+                ("density_format", C.c_int)]
 
 
 class Geometry(C.Structure):
@@ -87,6 +88,33 @@ def hu_to_unorm16(hu):
     return out
 
 
+# Density storage formats of the precision variant (vv_precision.density_format).
+DENSITY_UNORM16, DENSITY_FP16, DENSITY_BF16, DENSITY_FP32 = 0, 1, 2, 3
+
+
+def normalised_density(hu):
+    """t = clamp((hu + 1024) / 4095, 0, 1) in float32 (transfer.rs:121-124 before quantisation)."""
+    h = np.ascontiguousarray(hu, np.int16).astype(np.float32)
+    t = (h - np.float32(-1024.0)) / np.float32(3071.0 - -1024.0)
+    return np.clip(t, np.float32(0.0), np.float32(1.0)).astype(np.float32)
+
+
+def density_encode(hu, fmt=DENSITY_UNORM16):
+    """The stored density volume: R16_UNORM codes, or t as FP16 / BF16 bits
+    (round to nearest even) or float32."""
+    if fmt == DENSITY_UNORM16:
+        return hu_to_unorm16(hu)
+    t = normalised_density(hu)
+    if fmt == DENSITY_FP16:
+        return t.astype(np.float16).view(np.uint16)
+    if fmt == DENSITY_BF16:
+        w = t.view(np.uint32).astype(np.uint64)
+        return ((w + 0x7FFF + ((w >> 16) & 1)) >> 16).astype(np.uint16)
+    if fmt == DENSITY_FP32:
+        return t
+    raise ValueError(f"unknown density format {fmt}")
+
+
 def env_prepare(rgb, diffuse=False):
     """EnvironmentMap::prepare + upload (environment.rs:57-175, renderer.rs:2224-2290) of an
     (h, w, 3) linear-RGB light map: (RGBA16F radiance (h, w, 4) uint16, RG32F table
@@ -130,12 +158,13 @@ class CpuRenderer:
     every pass run by the oracle. Arrays are x-fastest, shaped (z, y, x, ...).
     """
 
-    def __init__(self, volume, tf, hu):
+    def __init__(self, volume, tf, hu, density_format=DENSITY_UNORM16):
         self.volume = volume
         self.hu = np.ascontiguousarray(hu, np.int16)
         self.dims = tuple(volume.dims)
         self.geo = geometry(volume)
-        self.density = hu_to_unorm16(self.hu)
+        self.density_format = density_format
+        self.density = density_encode(self.hu, density_format)
         self.set_transfer_function(tf)
         self.labels = np.zeros((1, 1, 1), np.uint8)
         self.soft = None
@@ -195,6 +224,7 @@ class CpuRenderer:
         s = Scene()
         s.dims[:] = self.dims
         s.density = ptr(self.density)
+        s.density_format = self.density_format
         s.normals = ptr(getattr(self, "normals", None))
         s.mask = ptr(self.mask)
         s.labels = ptr(self.labels)

@@ -39,7 +39,7 @@ extern "C" {
 // The device inputs of the shaders as plain arrays (x-fastest).
 typedef struct vvo_scene {
     int dims[3];
-    const uint16_t* density;
+    const void* density;
     const int8_t* normals;
     const uint16_t* mask;
     const uint8_t* labels;
@@ -51,6 +51,7 @@ typedef struct vvo_scene {
     const uint16_t* env_rad;
     const float* env_table;
     int env_dims[2];
+    int density_format;
 } vvo_scene;
 
 typedef struct vvo_geometry {
@@ -78,6 +79,7 @@ static Scene to_scene(const vvo_scene* s) {
     sc.env_rad = s->env_rad;
     sc.env_table = s->env_table;
     sc.env_dims = ivec2(s->env_dims[0], s->env_dims[1]);
+    sc.density_format = s->density_format;
     return sc;
 }
 static const Uniforms& U(const void* p) { return *(const Uniforms*)p; }

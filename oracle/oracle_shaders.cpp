@@ -34,7 +34,8 @@ static void bind3(glsl::Texture& t, const void* data, glsl::Format f, ivec3 d, g
 
 Units bind_scene(const Scene& s) {
     Units t;
-    bind3(t.density, s.density, glsl::R16_UNORM, s.dims, glsl::LINEAR);
+    static const glsl::Format density_formats[4] = {glsl::R16_UNORM, glsl::R16F, glsl::R16_BF16, glsl::R32F};
+    bind3(t.density, s.density, density_formats[s.density_format & 3], s.dims, glsl::LINEAR);
     if (s.normals) bind3(t.normals, s.normals, glsl::RGBA8_SNORM, s.dims, glsl::LINEAR);
     if (s.mask) bind3(t.mask, s.mask, glsl::RG16_UNORM, s.dims, glsl::LINEAR);
     if (s.majorant) bind3(t.majorant, s.majorant, glsl::R32F, s.brick_dims, glsl::NEAREST);

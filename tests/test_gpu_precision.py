@@ -1,0 +1,150 @@
+"""The precision variant (GPU): density stored as FP16, BF16 or FP32 instead of
+R16_UNORM, and running sums with Kahan compensation or in FP64 past a sample
+count (vv_renderer_create_ex / vv_precision).
+
+Tolerances (written here, checked below):
+* stored density, normals and majorant: bit-exact against the oracle run on
+  the same format (round-to-nearest-even encodings of the same normalised
+  density t = clamp((hu + 1024) / 4095, 0, 1));
+* single-path replays: the parity bar of the R16_UNORM path (>= 70 % of the
+  pixel-paths within 1e-4 relative, <= 15 % flipped);
+* running sums over 300 single-frame passes: with Kahan compensation, and with
+  FP64 from the 100th sample on, every non-negative sum (radiance, coverage,
+  albedo, squared luminance, depth) within 3 ulp (float32) of the FP64 running
+  sum (Kahan's bound 2 eps sum|x| plus the final rounding), the signed normal
+  sums within 1e-4; plain FP32 sums drift further on average.
+"""
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+from volview_gb300 import abi, scene
+from volview_gb300 import renderer as R
+
+pytestmark = pytest.mark.gpu
+
+FORMATS = [abi.DENSITY_FP16, abi.DENSITY_BF16, abi.DENSITY_FP32]
+
+
+def _params(cfg, gpu):
+    p = scene.frame_params_for(cfg, list(gpu.center), gpu.diagonal, clip_sagittal=True)
+    p.camera.distance = abi.f32(p.camera.distance * 0.45)
+    return p
+
+
+@pytest.fixture(scope="module", params=FORMATS, ids=["fp16", "bf16", "fp32"])
+def fmt_pair(request, small_cfg, gpu_ctx):
+    cfg, fmt = small_cfg, request.param
+    gpu = R.Renderer(gpu_ctx, cfg["volume"], cfg["tf"], abi.precision(density_format=fmt))
+    gpu.set_labels(cfg["labels_vol"], abi.soft_struct(cfg["soft"]))
+    cpu = O.CpuRenderer(cfg["volume"], cfg["tf"], cfg["hu"], density_format=fmt)
+    cpu.set_labels(cfg["labels_vol"], cfg["soft"])
+    params = _params(cfg, gpu)
+    gpu.resize(48, 48)
+    cpu.resize(48, 48)
+    yield cfg, gpu, cpu, params
+    gpu.destroy()
+
+
+def test_stored_density_bit_exact(fmt_pair):
+    cfg, gpu, cpu, params = fmt_pair
+    got = gpu.read_volume(abi.VOLUME_DENSITY)
+    assert got.dtype == cpu.density.dtype and np.array_equal(got, cpu.density)
+    t = O.normalised_density(cfg["hu"])
+    dec = {abi.DENSITY_FP16: lambda d: d.view(np.float16).astype(np.float32),
+           abi.DENSITY_BF16: lambda d: (d.astype(np.uint32) << 16).view(np.float32),
+           abi.DENSITY_FP32: lambda d: d}[gpu.precision.density_format](got)
+    ulp = {abi.DENSITY_FP16: 2.0 ** -11, abi.DENSITY_BF16: 2.0 ** -8, abi.DENSITY_FP32: 0.0}
+    assert np.all(np.abs(dec - t) <= ulp[gpu.precision.density_format] * np.maximum(t, 2.0 ** -14) + 1e-30)
+
+
+def test_normals_bit_exact(fmt_pair):
+    cfg, gpu, cpu, params = fmt_pair
+    assert np.array_equal(gpu.read_volume(abi.VOLUME_NORMALS), cpu.normals)
+
+
+def test_majorant_bit_exact(fmt_pair):
+    """The majorant from the stored values (majorant.comp:26-71): min/max of the
+    decoded densities, so it bounds every interpolated sample of the format."""
+    cfg, gpu, cpu, params = fmt_pair
+    gpu.probe_bspline(params, np.zeros((1, 3), np.float32))  # runs record's mask and majorant passes
+    cpu_mask = cpu.mask
+    cpu.mask = gpu.read_volume(abi.VOLUME_MASK)
+    u = cpu.uniforms(params, 1, 48, 48)
+    maj = np.zeros(cpu.brick_dims()[::-1], np.float32)
+    O.lib().vvo_majorant(O.ptr(u), O.C.byref(cpu.scene()), O.ptr(maj))
+    cpu.mask = cpu_mask
+    assert np.array_equal(gpu.read_volume(abi.VOLUME_MAJORANT), maj)
+
+
+def test_single_path_replays(fmt_pair):
+    cfg, gpu, cpu, params = fmt_pair
+    gpu.probe_bspline(params, np.zeros((1, 3), np.float32))
+    cpu.adopt(mask=gpu.read_volume(abi.VOLUME_MASK), majorant=gpu.read_volume(abi.VOLUME_MAJORANT))
+    ys, xs = np.mgrid[0:48, 0:48]
+    pix = np.stack([xs.ravel(), ys.ravel()], 1).astype(np.int32)
+    rels = []
+    for acc in (0, 5):
+        a = gpu.probe_paths(params, acc, pix)
+        b = np.stack([cpu.trace_pixel(params, int(x), int(y), acc) for x, y in pix])
+        rels.append(np.max(np.abs(a[:, :3] - b[:, :3]) / (np.abs(b[:, :3]) + 1e-5), axis=1))
+        assert (a[:, 3] == b[:, 3]).mean() >= 0.99
+    rel = np.concatenate(rels)
+    agree, flips = float((rel <= 1e-4).mean()), float((rel > 1e-2).mean())
+    print(f"format {gpu.precision.density_format}: {agree:.2%} agree within 1e-4, {flips:.2%} flipped")
+    assert agree >= 0.7
+    assert flips <= 0.15
+
+
+def test_bspline_matches_oracle(fmt_pair):
+    cfg, gpu, cpu, params = fmt_pair
+    rng = np.random.default_rng(3)
+    idx = rng.uniform(-0.5, 47.5, size=(4096, 3)).astype(np.float32)
+    a, b = gpu.probe_bspline(params, idx), cpu.bspline(params, idx)
+    assert np.abs(a[:, 0] - b[:, 0]).max() <= 1e-4 * max(float(np.abs(b[:, 0]).max()), 1e-6)
+    assert np.abs(a[:, 1:] - b[:, 1:]).max() <= 1e-4 * max(float(np.abs(b[:, 1:]).max()), 1e-6)
+
+
+def _sums(cfg, gpu_ctx, precision, frames):
+    r = R.Renderer(gpu_ctx, cfg["volume"], cfg["tf"], precision)
+    r.set_labels(cfg["labels_vol"], abi.soft_struct(cfg["soft"]))
+    p = _params(cfg, r)
+    p.path_tracing.denoiser = abi.DENOISE_OFF
+    r.resize(24, 24)
+    for f in range(1, frames + 1):
+        r.record(f, p)
+    assert r.accumulated_samples() == frames
+    acc, alb, nor = r.read_accumulation()
+    hdr = r.read_hdr()
+    r.destroy()
+    return acc, alb, nor, hdr
+
+
+def test_running_sums(small_cfg, gpu_ctx):
+    """Single-frame passes give every renderer the same per-frame sums, so the
+    accumulations differ only by how they are summed."""
+    cfg, n = small_cfg, 300
+    plain = _sums(cfg, gpu_ctx, abi.precision(), n)
+    kahan = _sums(cfg, gpu_ctx, abi.precision(sums=abi.SUMS_KAHAN), n)
+    wide = _sums(cfg, gpu_ctx, abi.precision(fp64_after=1), n)
+    late = _sums(cfg, gpu_ctx, abi.precision(sums=abi.SUMS_KAHAN, fp64_after=100), n)
+    for k in range(3):  # radiance, albedo guide, normal guide
+        ref = wide[k].astype(np.float64)
+        ulp = np.spacing(np.abs(wide[k])).astype(np.float64)
+        tol = 3 * ulp + 1e-30
+        if k == 2:
+            tol[..., :3] = 1e-4  # signed normal components: Kahan's bound is relative to sum |x|
+        assert np.all(np.abs(kahan[k] - ref) <= tol)
+        assert np.all(np.abs(late[k] - ref) <= tol)
+        assert np.abs(plain[k] - ref).mean() >= np.abs(kahan[k] - ref).mean()
+    # The HDR store is the running sum over the sample count, in FP64 when the sums are.
+    d = np.abs(wide[3].view(np.float16).astype(np.float32) - plain[3].view(np.float16).astype(np.float32))
+    assert d.max() <= 2e-3 * max(float(np.abs(plain[3].view(np.float16).astype(np.float32)).max()), 1e-6)
+
+
+def test_create_rejects_unknown_precision(small_cfg, gpu_ctx):
+    cfg = small_cfg
+    for bad in (abi.precision(density_format=7), abi.precision(sums=5)):
+        with pytest.raises(R.VolptError) as e:
+            R.Renderer(gpu_ctx, cfg["volume"], cfg["tf"], bad)
+        assert e.value.status == abi.VV_ERR_ARG

@@ -161,6 +161,24 @@ def test_light_map_tables():
     assert abs(float(mean @ np.array([0.2126, 0.7152, 0.0722])) - 1.0) < 2e-3
 
 
+def test_density_formats():
+    """The precision variant's stored density: t = clamp((hu + 1024) / 4095, 0, 1)
+    in float32, as binary16 and bfloat16 rounded to nearest even (checked here
+    against rounding the significand with numpy's half-to-even rint), or float32."""
+    hu = np.arange(-1100, 3200, dtype=np.int16)
+    t = O.normalised_density(hu)
+    assert t.dtype == np.float32 and t.min() == 0.0 and t.max() == 1.0
+    assert np.array_equal(t, np.clip((hu.astype(np.float32) + np.float32(1024)) / np.float32(4095), 0, 1))
+    half = O.density_encode(hu, O.DENSITY_FP16).view(np.float16).astype(np.float64)
+    assert np.array_equal(half, t.astype(np.float16).astype(np.float64))
+    m, e = np.frexp(t.astype(np.float64))
+    expect = np.ldexp(np.rint(m * 256.0) / 256.0, e)
+    bf = (O.density_encode(hu, O.DENSITY_BF16).astype(np.uint32) << 16).view(np.float32).astype(np.float64)
+    assert np.array_equal(bf, expect)
+    assert np.array_equal(O.density_encode(hu, O.DENSITY_FP32), t)
+    assert np.array_equal(O.density_encode(hu), O.hu_to_unorm16(hu))
+
+
 def test_light_map_samples_follow_luminance(small_cfg):
     """The oracle's light map samples (pt.comp:204-233) land on texels in
     proportion to luminance x sin(theta), with the pdf of the texel they land on."""

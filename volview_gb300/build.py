@@ -15,6 +15,11 @@ LIB = os.path.join(HERE, "libvolpt.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 SOURCES = ["vv_volume.cu", "vv_pt.cu", "vv_wavefront.cu", "vv_raymarch.cu", "vv_post.cu", "vv_noalloc.cu",
            "vv_host.cpp"]
+# Compiled once per density storage format (VV_DFMT = 0..3: R16_UNORM, FP16,
+# BF16, FP32), each into its own namespace, so each format's samplers are
+# specialised for it.
+PER_FORMAT = {"vv_pt.cu", "vv_wavefront.cu", "vv_raymarch.cu"}
+FORMATS = 4
 # Host code never contracts a*b+c into an FMA (Rust, whose host math the
 # renderer restates, does not either; gcc does by default on Arm).
 NVFLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
@@ -36,21 +41,34 @@ def build(verbose=False, force=False, extra=()):
     newest = max(os.path.getmtime(p) for p in srcs + headers + [__file__])
     if not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= newest and not extra:
         return LIB
-    objs, procs = [], []
+    units = []  # (source, object, defines)
     for s in srcs:
-        o = os.path.join(BUILD, os.path.basename(s) + ".o")
-        objs.append(o)
-        lang = ["-x", "cu"] if s.endswith(".cu") else ["-x", "c++"]
-        cmd = [nvcc(), *ARCH, *NVFLAGS, *extra, *lang, "-c", s, "-o", o]
-        if s.endswith(".cu"):
-            cmd += ["-Xptxas", "-v"] if verbose else []
-        procs.append((s, subprocess.Popen(cmd, stdout=subprocess.PIPE, stderr=subprocess.PIPE, text=True)))
-    for s, p in procs:
+        base = os.path.join(BUILD, os.path.basename(s))
+        if os.path.basename(s) in PER_FORMAT:
+            units += [(s, f"{base}.f{k}.o", [f"-DVV_DFMT={k}"]) for k in range(FORMATS)]
+        else:
+            units.append((s, base + ".o", []))
+    objs = [o for _, o, _ in units]
+    running, jobs = [], max(2, os.cpu_count() or 2)
+
+    def finish(entry):
+        s, p = entry
         out, err = p.communicate()
         if p.returncode != 0:
             raise RuntimeError(f"nvcc failed on {s}:\n{err[-8000:]}")
         if verbose and err.strip():
             print(err, file=sys.stderr)
+
+    for s, o, defs in units:
+        lang = ["-x", "cu"] if s.endswith(".cu") else ["-x", "c++"]
+        cmd = [nvcc(), *ARCH, *NVFLAGS, *defs, *extra, *lang, "-c", s, "-o", o]
+        if s.endswith(".cu"):
+            cmd += ["-Xptxas", "-v"] if verbose else []
+        if len(running) >= jobs:
+            finish(running.pop(0))
+        running.append((s, subprocess.Popen(cmd, stdout=subprocess.PIPE, stderr=subprocess.PIPE, text=True)))
+    for entry in running:
+        finish(entry)
     link = [nvcc(), *ARCH, "-shared", "-cudart", "static", "-o", LIB + ".tmp", *objs]
     r = subprocess.run(link, capture_output=True, text=True)
     if r.returncode != 0:

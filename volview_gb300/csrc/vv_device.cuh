@@ -100,7 +100,13 @@ struct Vol {
     int nx, ny, nz;     // voxels
     int bx, by, bz;     // bricks per axis
     int sy, sz;         // element strides of a brick row / brick slab
+    int dfmt;           // storage format of the density volume (DF_*)
 };
+
+// Density storage formats (vv_precision::density_format): the reference's
+// R16_UNORM, or the density itself as FP16, BF16 or FP32.
+enum { DF_UNORM16 = 0, DF_FP16 = 1, DF_BF16 = 2, DF_FP32 = 3 };
+__host__ __device__ __forceinline__ int density_bytes(int dfmt) { return dfmt == DF_FP32 ? 4 : 2; }
 
 __host__ __device__ __forceinline__ Vol make_vol(int nx, int ny, int nz) {
     Vol v;
@@ -108,6 +114,7 @@ __host__ __device__ __forceinline__ Vol make_vol(int nx, int ny, int nz) {
     v.bx = (nx + 7) >> 3; v.by = (ny + 7) >> 3; v.bz = (nz + 7) >> 3;
     v.sy = v.bx * 512;
     v.sz = v.bx * v.by * 512;
+    v.dfmt = DF_UNORM16;
     return v;
 }
 __host__ __device__ __forceinline__ long vol_elems(const Vol& v) { return (long)v.bx * v.by * v.bz * 512; }
@@ -128,6 +135,31 @@ __host__ __device__ __forceinline__ void vcoord(const Vol& v, long e, int& x, in
 __device__ __forceinline__ int clampi(int v, int lo, int hi) { return v < lo ? lo : (v > hi ? hi : v); }
 
 __device__ __forceinline__ float unorm16(uint32_t u) { return (float)u / 65535.0f; }
+
+#ifdef __CUDACC__
+// A density element stored as F (its C type: 16 bits, or a float for FP32),
+// in the format's filtering units: a UNORM16 code as its integer (filtered,
+// then scaled by density_unit = 1/65535, as the path tracer's samplers do),
+// the others as the density itself (scale 1).
+template <int F> struct DensityStore { typedef uint16_t type; };
+template <> struct DensityStore<DF_FP32> { typedef float type; };
+template <int F> __device__ __forceinline__ float density_decode(uint16_t v) {
+    if (F == DF_FP16) return __half2float(__ushort_as_half(v));
+    if (F == DF_BF16) return __uint_as_float((uint32_t)v << 16);
+    return (float)v;
+}
+template <int F> __device__ __forceinline__ float density_decode(float v) { return v; }
+template <int F> __device__ __forceinline__ float density_unit() { return F == DF_UNORM16 ? 1.0f / 65535.0f : 1.0f; }
+// Element o decoded to a density in [0, 1] (the texel a sampler reads).
+__device__ __forceinline__ float density_texel(const void* d, int dfmt, long o) {
+    switch (dfmt) {
+        case DF_FP16: return density_decode<DF_FP16>(__ldg((const uint16_t*)d + o));
+        case DF_BF16: return density_decode<DF_BF16>(__ldg((const uint16_t*)d + o));
+        case DF_FP32: return __ldg((const float*)d + o);
+        default: return unorm16(__ldg((const uint16_t*)d + o));
+    }
+}
+#endif
 __device__ __forceinline__ float snorm8(int c) { return gmax((float)c / 127.0f, -1.0f); }
 
 }  // namespace vv

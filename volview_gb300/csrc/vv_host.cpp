@@ -254,6 +254,11 @@ struct vv_renderer {
     // accumulation
     uint32_t accumulated = 0;
     bool have_params = false;
+    // running-sum precision (vv_precision): Kahan compensation of the three
+    // accumulation images, and FP64 running sums once past fp64_after samples
+    uint32_t sums = VV_SUMS_FP32, fp64_after = 0;
+    DBuf comp[3], wide[3];
+    bool wide_active = false;
     vv_frame_params accumulated_params;
     // host staging for the label tables
     LabelTables* tables_host = nullptr;
@@ -264,6 +269,26 @@ struct vv_renderer {
     bool timing = false;
     std::vector<std::pair<cudaEvent_t, cudaEvent_t>> pt_events;
 };
+
+// The path tracer's and the ray marcher's launchers of one density storage
+// format (compiled once per format, vv::fmt0 .. vv::fmt3).
+struct FormatLaunchers {
+    decltype(&fmt0::launch_pt) pt;
+    decltype(&fmt0::launch_pt_wavefront) pt_wavefront;
+    decltype(&fmt0::launch_ao) ao;
+    decltype(&fmt0::launch_shadow_sweep) shadow_sweep;
+    decltype(&fmt0::launch_pad_lighting) pad_lighting;
+    decltype(&fmt0::launch_dvr) dvr;
+    decltype(&fmt0::launch_bspline_probe) bspline_probe;
+    decltype(&fmt0::launch_light_sample_probe) light_sample_probe;
+    decltype(&fmt0::launch_pt_pixels) pt_pixels;
+};
+#define VV_FORMAT_TABLE(ns)                                                                                   \
+    {ns::launch_pt, ns::launch_pt_wavefront, ns::launch_ao, ns::launch_shadow_sweep, ns::launch_pad_lighting, \
+     ns::launch_dvr, ns::launch_bspline_probe, ns::launch_light_sample_probe, ns::launch_pt_pixels}
+static const FormatLaunchers FORMAT_LAUNCHERS[4] = {VV_FORMAT_TABLE(fmt0), VV_FORMAT_TABLE(fmt1),
+                                                    VV_FORMAT_TABLE(fmt2), VV_FORMAT_TABLE(fmt3)};
+static const FormatLaunchers& kernels_of(const vv_renderer* r) { return FORMAT_LAUNCHERS[r->vol.dfmt & 3]; }
 
 static void free_tex_vol(vv_renderer::TexVol& t) {
     if (t.tex) cudaDestroyTextureObject(t.tex);
@@ -604,7 +629,15 @@ static m3 w2i_m3(const vv_renderer* r) {
 
 extern "C" vv_status vv_renderer_create(vv_context* ctx, const vv_volume* volume, const vv_transfer_function* tf,
                                         vv_renderer** out) {
-    if (!ctx || !volume || !tf || !out) return fail(VV_ERR_ARG, "null argument");
+    vv_precision p = {VV_DENSITY_UNORM16, VV_SUMS_FP32, 0};
+    return vv_renderer_create_ex(ctx, volume, tf, &p, out);
+}
+
+extern "C" vv_status vv_renderer_create_ex(vv_context* ctx, const vv_volume* volume, const vv_transfer_function* tf,
+                                           const vv_precision* precision, vv_renderer** out) {
+    if (!ctx || !volume || !tf || !out || !precision) return fail(VV_ERR_ARG, "null argument");
+    if (precision->density_format > VV_DENSITY_FP32) return fail(VV_ERR_ARG, "unknown density format");
+    if (precision->sums > VV_SUMS_KAHAN) return fail(VV_ERR_ARG, "unknown running-sum mode");
     if (!volume->hu) return fail(VV_ERR_ARG, "volume has no voxels");
     for (int i = 0; i < 3; i++)
         if (volume->dims[i] == 0) return fail(VV_ERR_ARG, "volume has a zero dimension");
@@ -613,9 +646,12 @@ extern "C" vv_status vv_renderer_create(vv_context* ctx, const vv_volume* volume
         volume->dims[2] > 16384)
         return fail(VV_ERR_LIMIT, "volume exceeds 2^31 bricked voxels or 16384 per axis");
     CK(cudaSetDevice(ctx->device));
+    v.dfmt = (int)precision->density_format;
     vv_renderer* r = new vv_renderer();
     r->ctx = ctx;
     r->vol = v;
+    r->sums = precision->sums;
+    r->fp64_after = precision->fp64_after;
     set_geometry(r, volume);
     r->tables_host = nullptr;
     cudaError_t e = cudaMallocHost((void**)&r->tables_host, sizeof(LabelTables));
@@ -633,7 +669,7 @@ extern "C" vv_status vv_renderer_create(vv_context* ctx, const vv_volume* volume
     long elems = vol_elems(v);
     DBuf hu;
     if ((e = hu.alloc(n * sizeof(int16_t))) != cudaSuccess) return bail(cuda_fail(e, "cudaMalloc"));
-    if ((e = r->density.alloc(elems * sizeof(uint16_t))) != cudaSuccess ||
+    if ((e = r->density.alloc(elems * density_bytes(v.dfmt))) != cudaSuccess ||
         (e = r->normals.alloc(elems * sizeof(uint32_t))) != cudaSuccess ||
         (e = r->majorant.alloc((size_t)v.bx * v.by * v.bz * sizeof(float))) != cudaSuccess ||
         (e = r->tables.alloc(sizeof(LabelTables))) != cudaSuccess ||
@@ -643,8 +679,8 @@ extern "C" vv_status vv_renderer_create(vv_context* ctx, const vv_volume* volume
     }
     cudaStream_t st = ctx->stream;
     e = cudaMemcpyAsync(hu.p, volume->hu, n * sizeof(int16_t), cudaMemcpyHostToDevice, st);
-    if (e == cudaSuccess) e = launch_density(hu.as<int16_t>(), r->density.as<uint16_t>(), v, st);
-    if (e == cudaSuccess) e = launch_normals(r->density.as<uint16_t>(), r->normals.as<uint32_t>(), v, w2i_m3(r), st);
+    if (e == cudaSuccess) e = launch_density(hu.as<int16_t>(), r->density.p, v, st);
+    if (e == cudaSuccess) e = launch_normals(r->density.p, r->normals.as<uint32_t>(), v, w2i_m3(r), st);
     if (e == cudaSuccess) e = cudaMemsetAsync(r->exposure.p, 0, sizeof(float), st);
     if (e == cudaSuccess) e = cudaMemsetAsync(r->work.p, 0, 256, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
@@ -671,7 +707,8 @@ extern "C" vv_status vv_renderer_destroy(vv_renderer* r) {
                    &r->env_table, &r->env_diffuse, &r->env_guide, &r->preint, &r->shadow_vol, &r->ao_vol, &r->lut,
                    &r->bucket_dev, &r->tables, &r->soft, &r->work, &r->exposure, &r->accum, &r->albedo,
                    &r->normal, &r->ping, &r->pong, &r->guide_nd, &r->guide_alb, &r->hdr, &r->out, &r->bloom[0], &r->bloom[1], &r->bloom[2],
-                   &r->bloom[3]};
+                   &r->bloom[3], &r->comp[0], &r->comp[1], &r->comp[2], &r->wide[0], &r->wide[1],
+                   &r->wide[2]};
     for (DBuf* b : all) b->release();
     free_tex_vol(r->shadow_tex);
     free_tex_vol(r->ao_tex);
@@ -987,6 +1024,10 @@ extern "C" vv_status vv_resize(vv_renderer* r, uint32_t width, uint32_t height) 
     CK(r->accum.alloc(px * 16));
     CK(r->albedo.alloc(px * 16));
     CK(r->normal.alloc(px * 16));
+    for (int k = 0; k < 3; k++) {
+        if (r->sums == VV_SUMS_KAHAN) CK(r->comp[k].alloc(px * 16));
+        if (r->fp64_after) CK(r->wide[k].alloc(px * 32));
+    }
     CK(r->ping.alloc(px * 16));
     CK(r->pong.alloc(px * 16));
     CK(r->guide_nd.alloc(px * 16));
@@ -1031,7 +1072,7 @@ static PtArgs pt_args(vv_renderer* r, const UHead& u) {
     PtArgs a;
     std::memset(&a, 0, sizeof(a));
     a.u = u;
-    a.density = r->density.as<uint16_t>();
+    a.density = r->density.p;
     a.mask = r->mask_a.as<uint32_t>();
     a.normals = r->normals.as<uint32_t>();
     a.labels = r->labels.as<uint8_t>();
@@ -1074,7 +1115,7 @@ static cudaError_t run_pt(vv_renderer* r, vv_renderer::Pass& P, PtArgs& a, cudaS
     const char* k = std::getenv("VV_PT_KERNEL");
     if (k && (std::strcmp(k, "persistent") == 0 || std::strcmp(k, "frame") == 0)) {
         a.persistent = std::strcmp(k, "persistent") == 0 || a.frames > 1;
-        return launch_pt(a, r->ctx->sms, s, launches);
+        return kernels_of(r).pt(a, r->ctx->sms, s, launches);
     }
     // Paths in flight: with several frames per pass, up to 16 frames' worth
     // (VV_WF_SLOTS overrides), at most 2^24 slots (4.6 GB of path state) unless
@@ -1108,7 +1149,7 @@ static cudaError_t run_pt(vv_renderer* r, vv_renderer::Pass& P, PtArgs& a, cudaS
     w.first[0] = q + 7 * cap;
     w.first[1] = q + 8 * cap;
     w.counts = P.counts.as<uint32_t>();
-    return launch_pt_wavefront(a, w, r->ctx->sms, s, launches);
+    return kernels_of(r).pt_wavefront(a, w, r->ctx->sms, s, launches);
 }
 
 static PostArgs post_args(vv_renderer* r, const UHead& u) {
@@ -1171,7 +1212,7 @@ static vv_status prepare_frame(vv_renderer* r, const vv_frame_params& p, uint64_
     if (key.mode != VV_LABEL_OFF && !(r->have_mask_key && r->mask_key == key)) {
         MaskLaunch L;
         L.v = r->vol;
-        L.density = r->density.as<uint16_t>();
+        L.density = r->density.p;
         L.labels = r->labels.as<uint8_t>();
         static const uint8_t* none = nullptr;
         L.soft = r->soft.p ? r->soft.as<uint8_t>() : none;
@@ -1191,7 +1232,7 @@ static vv_status prepare_frame(vv_renderer* r, const vv_frame_params& p, uint64_
     }
     if (!(r->have_majorant_key && r->majorant_key == key)) {
         r->prep_work = true;
-        CK(launch_majorant(r->density.as<uint16_t>(), r->mask_a.as<uint32_t>(), r->vol, key.mode, p.labels.extinction,
+        CK(launch_majorant(r->density.p, r->mask_a.as<uint32_t>(), r->vol, key.mode, p.labels.extinction,
                            r->bucket_dev.as<float>(), r->majorant.as<float>(), st));
         r->launches += 1;
         r->majorant_key = key;
@@ -1202,6 +1243,9 @@ static vv_status prepare_frame(vv_renderer* r, const vv_frame_params& p, uint64_
         CK(cudaMemsetAsync(r->accum.p, 0, bytes, st));
         CK(cudaMemsetAsync(r->albedo.p, 0, bytes, st));
         CK(cudaMemsetAsync(r->normal.p, 0, bytes, st));
+        for (int k = 0; k < 3; k++)
+            if (r->comp[k].p) CK(cudaMemsetAsync(r->comp[k].p, 0, bytes, st));
+        r->wide_active = false;
         r->prep_work = true;
     }
     return VV_OK;
@@ -1247,9 +1291,9 @@ static vv_status record_ray_march(vv_renderer* r, const vv_frame_params& p, cons
         CK(cudaMemsetAsync(r->ao_vol.p, 0, r->ao_vol.n, st));
         CK(make_tex_vol(r->shadow_tex, r->shadow_dims[0], r->shadow_dims[1], r->shadow_dims[2], true));
         CK(make_tex_vol(r->ao_tex, r->ao_dims[0], r->ao_dims[1], r->ao_dims[2], false));
-        CK(launch_pad_lighting(r->shadow_vol.as<uint16_t>(), 4, r->shadow_dims[0], r->shadow_dims[1],
+        CK(kernels_of(r).pad_lighting(r->shadow_vol.as<uint16_t>(), 4, r->shadow_dims[0], r->shadow_dims[1],
                                r->shadow_dims[2], r->shadow_tex.surf, st));
-        CK(launch_pad_lighting(r->ao_vol.as<uint16_t>(), 1, r->ao_dims[0], r->ao_dims[1], r->ao_dims[2],
+        CK(kernels_of(r).pad_lighting(r->ao_vol.as<uint16_t>(), 1, r->ao_dims[0], r->ao_dims[1], r->ao_dims[2],
                                r->ao_tex.surf, st));
         r->launches += 2;
     }
@@ -1261,8 +1305,8 @@ static vv_status record_ray_march(vv_renderer* r, const vv_frame_params& p, cons
     append_key(ao_key, u.clip, 2 * sizeof(uint32_t));
     append_key(ao_key, u.clip_planes, 12 * sizeof(float));
     if (p.lighting.ambient_occlusion && r->ao_key != ao_key) {
-        CK(launch_ao(a, r->ao_vol.as<uint16_t>(), r->ao_dims[0], r->ao_dims[1], r->ao_dims[2], st));
-        CK(launch_pad_lighting(r->ao_vol.as<uint16_t>(), 1, r->ao_dims[0], r->ao_dims[1], r->ao_dims[2],
+        CK(kernels_of(r).ao(a, r->ao_vol.as<uint16_t>(), r->ao_dims[0], r->ao_dims[1], r->ao_dims[2], st));
+        CK(kernels_of(r).pad_lighting(r->ao_vol.as<uint16_t>(), 1, r->ao_dims[0], r->ao_dims[1], r->ao_dims[2],
                                r->ao_tex.surf, st));
         launches += 2;
         r->ao_key = ao_key;
@@ -1286,16 +1330,16 @@ static vv_status record_ray_march(vv_renderer* r, const vv_frame_params& p, cons
         float ax = std::fabs(l_idx[0]), ay = std::fabs(l_idx[1]), az = std::fabs(l_idx[2]);
         int axis = (ax >= ay && ax >= az) ? 0 : (ay >= az ? 1 : 2);
         int sign = l_idx[axis] >= 0.0f ? 1 : -1;
-        CK(launch_shadow_sweep(a, r->shadow_vol.as<ushort4>(), r->shadow_dims[0], r->shadow_dims[1],
+        CK(kernels_of(r).shadow_sweep(a, r->shadow_vol.as<ushort4>(), r->shadow_dims[0], r->shadow_dims[1],
                                r->shadow_dims[2], axis, sign, st, &launches));
-        CK(launch_pad_lighting(r->shadow_vol.as<uint16_t>(), 4, r->shadow_dims[0], r->shadow_dims[1],
+        CK(kernels_of(r).pad_lighting(r->shadow_vol.as<uint16_t>(), 4, r->shadow_dims[0], r->shadow_dims[1],
                                r->shadow_dims[2], r->shadow_tex.surf, st));
         launches += 1;
         r->shadow_key = shadow_key;
     }
     LightTex sv{r->shadow_tex.tex, r->shadow_dims[0], r->shadow_dims[1], r->shadow_dims[2], 1};
     LightTex av{r->ao_tex.tex, r->ao_dims[0], r->ao_dims[1], r->ao_dims[2], 0};
-    CK(launch_dvr(a, sv, av, st));
+    CK(kernels_of(r).dvr(a, sv, av, st));
     launches += 1;
     PostArgs pa = post_args(r, u);
     CK(launch_post(pa, st, &launches));
@@ -1343,8 +1387,27 @@ static vv_status record_pass(vv_renderer* r, const vv_frame_params& p, UHead& u,
     u.path[0] = r->accumulated;
     PostArgs pa = post_args(r, u);
     CK(cudaStreamWaitEvent(s, prev.shown, 0));
-    CK(launch_merge(pa, P.accum.as<float4>(), P.albedo.as<float4>(), P.normal.as<float4>(),
-                    (float)(r->accumulated + spf), s));
+    if (r->sums == VV_SUMS_FP32 && !r->fp64_after) {
+        CK(launch_merge(pa, P.accum.as<float4>(), P.albedo.as<float4>(), P.normal.as<float4>(),
+                        (float)(r->accumulated + spf), s));
+    } else {
+        // The running sums hold the samples before this pass's first frame;
+        // past fp64_after of them they continue in FP64.
+        uint32_t before = r->accumulated - (frames - 1) * spf;
+        PreciseSums ps;
+        for (int k = 0; k < 3; k++) {
+            ps.comp[k] = r->comp[k].as<float4>();
+            ps.wide[k] = r->wide[k].as<double>();
+        }
+        ps.kahan = r->sums == VV_SUMS_KAHAN;
+        ps.wide_mode = 0;
+        if (r->fp64_after && (r->wide_active || before >= r->fp64_after)) {
+            ps.wide_mode = r->wide_active ? 2 : 1;
+            r->wide_active = true;
+        }
+        CK(launch_merge_precise(pa, P.accum.as<float4>(), P.albedo.as<float4>(), P.normal.as<float4>(), ps,
+                                (double)(r->accumulated + spf), s));
+    }
     launches += 1;
     if (p.path_tracing.denoiser == VV_DENOISE_ATROUS) CK(launch_denoise(pa, s, &launches));
     r->accumulated += spf;
@@ -1461,7 +1524,7 @@ extern "C" vv_status vv_read_volume(vv_renderer* r, int which, void* out, size_t
     const DBuf* src = nullptr;
     int elem = 0;
     switch (which) {
-        case VV_VOLUME_DENSITY: src = &r->density; elem = 2; break;
+        case VV_VOLUME_DENSITY: src = &r->density; elem = density_bytes(r->vol.dfmt); break;
         case VV_VOLUME_NORMALS: src = &r->normals; elem = 4; break;
         case VV_VOLUME_MASK: src = &r->mask_a; elem = 4; break;
         case VV_VOLUME_LABELS: src = &r->labels; elem = 1; break;
@@ -1543,7 +1606,7 @@ extern "C" vv_status vv_probe_bspline(vv_renderer* r, const vv_frame_params* par
     cudaStream_t st = r->ctx->stream;
     PtArgs a = pt_args(r, u);
     cudaError_t e = cudaMemcpyAsync(di.p, idx, n * 12, cudaMemcpyHostToDevice, st);
-    if (e == cudaSuccess) e = launch_bspline_probe(a, di.as<float>(), dout.as<float>(), (int)n, st);
+    if (e == cudaSuccess) e = kernels_of(r).bspline_probe(a, di.as<float>(), dout.as<float>(), (int)n, st);
     if (e == cudaSuccess) e = cudaMemcpyAsync(out, dout.p, n * 16, cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     di.release();
@@ -1565,7 +1628,7 @@ extern "C" vv_status vv_probe_light_samples(vv_renderer* r, const vv_frame_param
     cudaStream_t st = r->ctx->stream;
     PtArgs a = pt_args(r, u);
     cudaError_t e = cudaMemcpyAsync(ds.p, seeds, n * 4, cudaMemcpyHostToDevice, st);
-    if (e == cudaSuccess) e = launch_light_sample_probe(a, ds.as<uint32_t>(), dout.as<float>(), (int)n, st);
+    if (e == cudaSuccess) e = kernels_of(r).light_sample_probe(a, ds.as<uint32_t>(), dout.as<float>(), (int)n, st);
     if (e == cudaSuccess) e = cudaMemcpyAsync(out, dout.p, n * 24, cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     ds.release();
@@ -1587,7 +1650,7 @@ extern "C" vv_status vv_probe_paths(vv_renderer* r, const vv_frame_params* param
     cudaStream_t st = r->ctx->stream;
     PtArgs a = pt_args(r, u);
     cudaError_t e = cudaMemcpyAsync(dp.p, pixels, n * 8, cudaMemcpyHostToDevice, st);
-    if (e == cudaSuccess) e = launch_pt_pixels(a, dp.as<int>(), dout.as<float>(), (int)n, st);
+    if (e == cudaSuccess) e = kernels_of(r).pt_pixels(a, dp.as<int>(), dout.as<float>(), (int)n, st);
     if (e == cudaSuccess) e = cudaMemcpyAsync(out, dout.p, n * 48, cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     dp.release();

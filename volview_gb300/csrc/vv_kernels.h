@@ -9,7 +9,7 @@ namespace vv {
 
 struct MaskLaunch {
     Vol v;
-    const uint16_t* density;
+    const void* density;        // stored as vol.dfmt
     const uint8_t* labels;
     const uint8_t* soft;
     int soft_dims[3];
@@ -25,7 +25,7 @@ struct MaskLaunch {
 // Everything one path-tracing launch reads and writes.
 struct PtArgs {
     UHead u;
-    const uint16_t* density;
+    const void* density;        // stored as vol.dfmt
     const uint32_t* mask;
     const uint32_t* normals;
     const uint8_t* labels;
@@ -72,16 +72,13 @@ enum {
     COUNT_N = 10
 };
 
-cudaError_t launch_density(const int16_t* hu, uint16_t* out, const Vol& v, cudaStream_t s);
-cudaError_t launch_normals(const uint16_t* d, uint32_t* out, const Vol& v, const m3& w2i, cudaStream_t s);
+cudaError_t launch_density(const int16_t* hu, void* out, const Vol& v, cudaStream_t s);
+cudaError_t launch_normals(const void* d, uint32_t* out, const Vol& v, const m3& w2i, cudaStream_t s);
 cudaError_t launch_masks(const MaskLaunch& L, cudaStream_t s);
-cudaError_t launch_majorant(const uint16_t* d, const uint32_t* mask, const Vol& v, int mode, float label_ext,
+cudaError_t launch_majorant(const void* d, const uint32_t* mask, const Vol& v, int mode, float label_ext,
                             const float* bucket, float* out, cudaStream_t s);
 cudaError_t launch_unbrick(const void* src, void* dst, const Vol& v, int elem, cudaStream_t s);
 cudaError_t launch_brick_u8(const uint8_t* src, uint8_t* dst, const Vol& v, cudaStream_t s);
-
-// One or more accumulate-frames (pt.comp). Returns the number of kernel launches.
-cudaError_t launch_pt(const PtArgs& a, int sms, cudaStream_t s, int* launches);
 
 // Wavefront tracer state: one slot of WF_SLOT_BYTES per pixel, the stage
 // queues (slot indices) and their counters.
@@ -110,13 +107,6 @@ struct WfArgs {
     uint32_t* scatter;
     uint32_t* counts;      // WF_COUNTERS words
 };
-// Accumulate-frames with the wavefront tracer (same results as launch_pt).
-cudaError_t launch_pt_wavefront(const PtArgs& a, const WfArgs& w, int sms, cudaStream_t s, int* launches);
-// The ray marcher (path tracing off): occlusion volume (R16F), shadow volume
-// swept slice by slice (RGBA16F), the image into a.hdr.
-cudaError_t launch_ao(const PtArgs& a, uint16_t* out, int ax, int ay, int az, cudaStream_t s);
-cudaError_t launch_shadow_sweep(const PtArgs& a, ushort4* vol, int sx, int sy, int sz, int axis, int sign,
-                                cudaStream_t s, int* launches);
 // A lighting volume as the image loop reads it: a 3D texture of its texels
 // inside a one-texel white border, filtered by the texture units (clamped
 // addressing onto the border = the reference's white-border sampler).
@@ -125,16 +115,36 @@ struct LightTex {
     int w, h, d;  // texels of the volume, border excluded
     int rgba;     // 1: RGBA16F (shadow), 0: R16F (occlusion)
 };
-// Copies a pixel-linear lighting volume (`channels` halves per texel) into its
-// texture array through `surf`, white border included.
-cudaError_t launch_pad_lighting(const uint16_t* vol, int channels, int w, int h, int d, cudaSurfaceObject_t surf,
-                                cudaStream_t s);
-cudaError_t launch_dvr(const PtArgs& a, const LightTex& shadow, const LightTex& ao, cudaStream_t s);
-// B-spline density and gradient at n continuous indices (parity probe).
-cudaError_t launch_bspline_probe(const PtArgs& a, const float* idx, float* out, int n, cudaStream_t s);
-cudaError_t launch_light_sample_probe(const PtArgs& a, const uint32_t* seeds, float* out, int n, cudaStream_t s);
-// One path per listed pixel at accumulation count a.u.path[0] (parity probe): 12 floats each.
-cudaError_t launch_pt_pixels(const PtArgs& a, const int* px, float* out, int n, cudaStream_t s);
+
+// The launchers of the path tracer and the ray marcher (vv_pt.cu,
+// vv_wavefront.cu, vv_raymarch.cu), compiled once per density storage format:
+// namespace vv::fmtN holds those of format N (DF_*), whose samplers read that
+// format with no branch on it.
+#define VV_FORMAT_LAUNCHERS                                                                                      \
+    /* One or more accumulate-frames (pt.comp) with the single-kernel tracers. */                                \
+    cudaError_t launch_pt(const PtArgs& a, int sms, cudaStream_t s, int* launches);                             \
+    /* Accumulate-frames with the wavefront tracer (same results as launch_pt). */                              \
+    cudaError_t launch_pt_wavefront(const PtArgs& a, const WfArgs& w, int sms, cudaStream_t s, int* launches);  \
+    /* The ray marcher (path tracing off): occlusion volume (R16F), shadow volume */                            \
+    /* swept slice by slice (RGBA16F), the image into a.hdr. */                                                  \
+    cudaError_t launch_ao(const PtArgs& a, uint16_t* out, int ax, int ay, int az, cudaStream_t s);              \
+    cudaError_t launch_shadow_sweep(const PtArgs& a, ushort4* vol, int sx, int sy, int sz, int axis, int sign,  \
+                                    cudaStream_t s, int* launches);                                             \
+    /* Copies a pixel-linear lighting volume (`channels` halves per texel) into its */                          \
+    /* texture array through `surf`, white border included. */                                                   \
+    cudaError_t launch_pad_lighting(const uint16_t* vol, int channels, int w, int h, int d,                      \
+                                    cudaSurfaceObject_t surf, cudaStream_t s);                                  \
+    cudaError_t launch_dvr(const PtArgs& a, const LightTex& shadow, const LightTex& ao, cudaStream_t s);        \
+    /* Parity probes: B-spline density and gradient at n continuous indices; light */                           \
+    /* map samples; one path per listed pixel at accumulation count a.u.path[0]. */                              \
+    cudaError_t launch_bspline_probe(const PtArgs& a, const float* idx, float* out, int n, cudaStream_t s);     \
+    cudaError_t launch_light_sample_probe(const PtArgs& a, const uint32_t* seeds, float* out, int n,            \
+                                          cudaStream_t s);                                                      \
+    cudaError_t launch_pt_pixels(const PtArgs& a, const int* px, float* out, int n, cudaStream_t s);
+namespace fmt0 { VV_FORMAT_LAUNCHERS }
+namespace fmt1 { VV_FORMAT_LAUNCHERS }
+namespace fmt2 { VV_FORMAT_LAUNCHERS }
+namespace fmt3 { VV_FORMAT_LAUNCHERS }
 
 struct PostArgs {
     UHead u;
@@ -156,6 +166,16 @@ struct PostArgs {
 cudaError_t launch_denoise(const PostArgs& a, cudaStream_t s, int* launches);
 // record_post (renderer.rs:1817-1866): bloom, exposure, tone mapping.
 cudaError_t launch_post(const PostArgs& a, cudaStream_t s, int* launches);
+// The merge with precise running sums (vv_precision): Kahan-compensated FP32
+// sums and/or FP64 sums once past a sample count.
+struct PreciseSums {
+    float4* comp[3];  // compensation of accum, albedo, normal (kahan)
+    double* wide[3];  // 4 doubles per pixel: the FP64 running sums
+    int kahan;
+    int wide_mode;    // 0: FP32 sums; 1: FP64 from now on (from the FP32 sums); 2: FP64 sums
+};
+cudaError_t launch_merge_precise(const PostArgs& a, const float4* accum, const float4* albedo, const float4* normal,
+                                 const PreciseSums& ps, double n, cudaStream_t s);
 // hdr = accum / n (the HDR store at the end of pt.comp) for batched frames.
 cudaError_t launch_hdr_resolve(const PostArgs& a, float n, cudaStream_t s);
 // A pass's own sums added to the accumulation images (a.accum/albedo/normal),

@@ -158,6 +158,73 @@ __global__ void k_merge(const PostArgs a, const float4* __restrict__ pacc, const
     a.hdr[i] = to_h4(make_float4(v.x / n, v.y / n, v.z / n, v.w / n));
 }
 
+// One running sum (4 channels) plus a pass's sums, as PreciseSums says.
+__device__ __forceinline__ float4 merge_sum(float4* total, float4* comp, double* wide, float4 add,
+                                            const PreciseSums& ps, int i) {
+    float4 t = total[i];
+    float a[4] = {add.x, add.y, add.z, add.w}, v[4] = {t.x, t.y, t.z, t.w};
+    if (ps.wide_mode == 0) {
+        if (ps.kahan) {
+            float4 cv = comp[i];
+            float c[4] = {cv.x, cv.y, cv.z, cv.w};
+#pragma unroll
+            for (int k = 0; k < 4; k++) {  // Kahan: y = a - c, t = v + y, c = (t - v) - y
+                float y = __fsub_rn(a[k], c[k]);
+                float s = __fadd_rn(v[k], y);
+                c[k] = __fsub_rn(__fsub_rn(s, v[k]), y);
+                v[k] = s;
+            }
+            comp[i] = make_float4(c[0], c[1], c[2], c[3]);
+        } else {
+#pragma unroll
+            for (int k = 0; k < 4; k++) v[k] = __fadd_rn(v[k], a[k]);
+        }
+    } else {
+        double w[4];
+        if (ps.wide_mode == 1) {  // the FP32 sum, corrected by its compensation
+            float4 cv = ps.kahan ? comp[i] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            float c[4] = {cv.x, cv.y, cv.z, cv.w};
+#pragma unroll
+            for (int k = 0; k < 4; k++) w[k] = (double)v[k] - (double)c[k];
+        } else {
+#pragma unroll
+            for (int k = 0; k < 4; k++) w[k] = wide[4 * (long)i + k];
+        }
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+            w[k] += (double)a[k];
+            wide[4 * (long)i + k] = w[k];
+            v[k] = (float)w[k];
+        }
+    }
+    float4 r = make_float4(v[0], v[1], v[2], v[3]);
+    total[i] = r;
+    return r;
+}
+
+__global__ void k_merge_precise(const PostArgs a, const float4* __restrict__ pacc, const float4* __restrict__ palb,
+                                const float4* __restrict__ pnor, const PreciseSums ps, double n) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= (int)(a.width * a.height)) return;
+    float4 v = merge_sum((float4*)a.accum, ps.comp[0], ps.wide[0], pacc[i], ps, i);
+    merge_sum((float4*)a.albedo, ps.comp[1], ps.wide[1], palb[i], ps, i);
+    merge_sum((float4*)a.normal, ps.comp[2], ps.wide[2], pnor[i], ps, i);
+    if (ps.wide_mode != 0) {
+        const double* w = ps.wide[0] + 4 * (long)i;
+        a.hdr[i] = to_h4(make_float4((float)(w[0] / n), (float)(w[1] / n), (float)(w[2] / n), (float)(w[3] / n)));
+    } else {
+        float nf = (float)n;
+        a.hdr[i] = to_h4(make_float4(v.x / nf, v.y / nf, v.z / nf, v.w / nf));
+    }
+}
+
+cudaError_t launch_merge_precise(const PostArgs& a, const float4* accum, const float4* albedo, const float4* normal,
+                                 const PreciseSums& ps, double n, cudaStream_t s) {
+    int N = (int)(a.width * a.height);
+    k_merge_precise<<<(N + 255) / 256, 256, 0, s>>>(a, accum, albedo, normal, ps, n);
+    return cudaGetLastError();
+}
+
 // ------------------------------------------------------------------- bloom
 // bloom.comp pass 0: Karis-weighted 4x4 average of the HDR image, with coverage.
 __global__ void k_bloom_down4(const PostArgs a) {

@@ -20,6 +20,7 @@
 #include "vv_pt_device.cuh"
 
 namespace vv {
+namespace VV_FMT_NS {  // this density format's kernels and launchers
 
 // The reference's shape: one thread per pixel, one frame (8x8 blocks).
 __global__ void __launch_bounds__(64, 8) k_pt_frame(const __grid_constant__ PtArgs A) {
@@ -200,4 +201,5 @@ cudaError_t launch_pt_pixels(const PtArgs& a, const int* px, float* out, int n, 
     return cudaGetLastError();
 }
 
+}  // namespace VV_FMT_NS
 }  // namespace vv

@@ -7,6 +7,17 @@
 #include "vv_device.cuh"
 #include "vv_kernels.h"
 
+// The density storage format this translation unit's samplers read (DF_*):
+// the path tracer's and ray marcher's sources are compiled once per format,
+// each into its own namespace (vv::fmt0 .. vv::fmt3), so every format runs
+// code specialised for it and the reference's format has no format branch.
+#ifndef VV_DFMT
+#define VV_DFMT 0
+#endif
+#define VV_FMT_CAT2(a, b) a##b
+#define VV_FMT_CAT(a, b) VV_FMT_CAT2(a, b)
+#define VV_FMT_NS VV_FMT_CAT(fmt, VV_DFMT)
+
 namespace vv {
 // Internal linkage: every translation unit that includes this header gets its
 // own copy of the device functions (some are out of line).
@@ -69,14 +80,16 @@ __device__ __forceinline__ float tri_mix(const float c[8], const Tri& t) {
     return lerpf(lerpf(a, b, t.fy), lerpf(d, e, t.fy), t.fz);
 }
 
-// textureLod(density_tex, index_to_tex(idx)) (common.glsl:76-78).
+// textureLod(density_tex, index_to_tex(idx)) (common.glsl:76-78), the density
+// stored as this translation unit's format (VV_DFMT).
 __device__ float density_tri(const PtArgs& A, f3 p) {
     count(A, COUNT_TRILINEAR);
+    typedef DensityStore<VV_DFMT>::type E;
     Tri t = tri_taps(A.vol, p);
     float c[8];
 #pragma unroll
-    for (int k = 0; k < 8; k++) c[k] = (float)__ldg(A.density + t.o[k]);
-    return tri_mix(c, t) * INV65535;
+    for (int k = 0; k < 8; k++) c[k] = density_decode<VV_DFMT>(__ldg((const E*)A.density + t.o[k]));
+    return tri_mix(c, t) * density_unit<VV_DFMT>();
 }
 
 // textureLod(mask_tex, ...).rg
@@ -157,6 +170,7 @@ __device__ __forceinline__ Cubic cubic_taps(const Vol& v, f3 p) {
 // density_cubic (common.glsl:124-127) as the 64-tap tensor product.
 __device__ __noinline__ float density_cubic(const PtArgs& A, f3 p) {
     count(A, COUNT_CUBIC);
+    typedef DensityStore<VV_DFMT>::type E;
     Cubic c = cubic_taps(A.vol, p);
     float wx[4], wy[4], wz[4];
     bspline_w(c.fx, wx);
@@ -168,50 +182,23 @@ __device__ __noinline__ float density_cubic(const PtArgs& A, f3 p) {
         float az = 0.0f;
 #pragma unroll
         for (int y = 0; y < 4; y++) {
-            const uint16_t* row = A.density + c.oz[z] + c.oy[y];
-            float r = wx[0] * (float)__ldg(row + c.ox[0]) + wx[1] * (float)__ldg(row + c.ox[1]) +
-                      wx[2] * (float)__ldg(row + c.ox[2]) + wx[3] * (float)__ldg(row + c.ox[3]);
+            const E* row = (const E*)A.density + c.oz[z] + c.oy[y];
+            float r = wx[0] * density_decode<VV_DFMT>(__ldg(row + c.ox[0])) +
+                      wx[1] * density_decode<VV_DFMT>(__ldg(row + c.ox[1])) +
+                      wx[2] * density_decode<VV_DFMT>(__ldg(row + c.ox[2])) +
+                      wx[3] * density_decode<VV_DFMT>(__ldg(row + c.ox[3]));
             az = fmaf(wy[y], r, az);
         }
         acc = fmaf(wz[z], az, acc);
     }
-    return acc * INV65535;
+    return acc * density_unit<VV_DFMT>();
 }
 
-// density_gradient_cubic (common.glsl:130-136) from the same 64 voxels.
-__device__ __noinline__ f3 density_gradient_cubic(const PtArgs& A, f3 p) {
-    count(A, COUNT_GRADIENT);
-    Cubic c = cubic_taps(A.vol, p);
-    float wx[4], wy[4], wz[4], dx[4], dy[4], dz[4];
-    bspline_w(c.fx, wx); bspline_w(c.fy, wy); bspline_w(c.fz, wz);
-    bspline_d(c.fx, dx); bspline_d(c.fy, dy); bspline_d(c.fz, dz);
-    float gx = 0.0f, gy = 0.0f, gz = 0.0f;
-#pragma unroll
-    for (int z = 0; z < 4; z++) {
-        float vz = 0.0f, gxz = 0.0f, gyz = 0.0f;
-#pragma unroll
-        for (int y = 0; y < 4; y++) {
-            const uint16_t* row = A.density + c.oz[z] + c.oy[y];
-            float v0 = (float)__ldg(row + c.ox[0]), v1 = (float)__ldg(row + c.ox[1]);
-            float v2 = (float)__ldg(row + c.ox[2]), v3 = (float)__ldg(row + c.ox[3]);
-            float rw = wx[0] * v0 + wx[1] * v1 + wx[2] * v2 + wx[3] * v3;
-            float rd = dx[0] * v0 + dx[1] * v1 + dx[2] * v2 + dx[3] * v3;
-            vz = fmaf(wy[y], rw, vz);
-            gxz = fmaf(wy[y], rd, gxz);
-            gyz = fmaf(dy[y], rw, gyz);
-        }
-        gx = fmaf(wz[z], gxz, gx);
-        gy = fmaf(wz[z], gyz, gy);
-        gz = fmaf(dz[z], vz, gz);
-    }
-    return mk(gx, gy, gz) * INV65535;
-}
-
-// density_cubic and density_gradient_cubic at one point from one read of the
-// 64 voxels, each with the arithmetic of its own function (the value's
-// z-slices are the gradient's vz sums), so both results are those functions'.
-__device__ __noinline__ float density_cubic_with_gradient(const PtArgs& A, f3 p, f3& grad) {
-    count(A, COUNT_CUBIC);
+// density_gradient_cubic (common.glsl:130-136) from the same 64 voxels; with
+// VALUE, also density_cubic's value, with its arithmetic (the value's z-slices
+// are the gradient's vz sums), from the same read.
+template <bool VALUE> __device__ __forceinline__ f3 density_gradient_cubic_impl(const PtArgs& A, f3 p, float& value) {
+    typedef DensityStore<VV_DFMT>::type E;
     Cubic c = cubic_taps(A.vol, p);
     float wx[4], wy[4], wz[4], dx[4], dy[4], dz[4];
     bspline_w(c.fx, wx); bspline_w(c.fy, wy); bspline_w(c.fz, wz);
@@ -222,22 +209,35 @@ __device__ __noinline__ float density_cubic_with_gradient(const PtArgs& A, f3 p,
         float vz = 0.0f, gxz = 0.0f, gyz = 0.0f;
 #pragma unroll
         for (int y = 0; y < 4; y++) {
-            const uint16_t* row = A.density + c.oz[z] + c.oy[y];
-            float v0 = (float)__ldg(row + c.ox[0]), v1 = (float)__ldg(row + c.ox[1]);
-            float v2 = (float)__ldg(row + c.ox[2]), v3 = (float)__ldg(row + c.ox[3]);
+            const E* row = (const E*)A.density + c.oz[z] + c.oy[y];
+            float v0 = density_decode<VV_DFMT>(__ldg(row + c.ox[0])), v1 = density_decode<VV_DFMT>(__ldg(row + c.ox[1]));
+            float v2 = density_decode<VV_DFMT>(__ldg(row + c.ox[2])), v3 = density_decode<VV_DFMT>(__ldg(row + c.ox[3]));
             float rw = wx[0] * v0 + wx[1] * v1 + wx[2] * v2 + wx[3] * v3;
             float rd = dx[0] * v0 + dx[1] * v1 + dx[2] * v2 + dx[3] * v3;
             vz = fmaf(wy[y], rw, vz);
             gxz = fmaf(wy[y], rd, gxz);
             gyz = fmaf(dy[y], rw, gyz);
         }
-        acc = fmaf(wz[z], vz, acc);
+        if (VALUE) acc = fmaf(wz[z], vz, acc);
         gx = fmaf(wz[z], gxz, gx);
         gy = fmaf(wz[z], gyz, gy);
         gz = fmaf(dz[z], vz, gz);
     }
-    grad = mk(gx, gy, gz) * INV65535;
-    return acc * INV65535;
+    if (VALUE) value = acc * density_unit<VV_DFMT>();
+    return mk(gx, gy, gz) * density_unit<VV_DFMT>();
+}
+__device__ __noinline__ f3 density_gradient_cubic(const PtArgs& A, f3 p) {
+    count(A, COUNT_GRADIENT);
+    float unused;
+    return density_gradient_cubic_impl<false>(A, p, unused);
+}
+// density_cubic and density_gradient_cubic at one point from one read of the
+// 64 voxels, each result that function's.
+__device__ __noinline__ float density_cubic_with_gradient(const PtArgs& A, f3 p, f3& grad) {
+    count(A, COUNT_CUBIC);
+    float v;
+    grad = density_gradient_cubic_impl<true>(A, p, v);
+    return v;
 }
 
 // transfer (common.glsl:170-173): linear LUT lookup at texel centres.

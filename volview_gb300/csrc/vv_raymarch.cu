@@ -14,6 +14,7 @@
 #include "vv_pt_device.cuh"
 
 namespace vv {
+namespace VV_FMT_NS {  // this density format's kernels and launchers
 namespace {
 
 __device__ __forceinline__ float h2f(uint16_t h) { return __half2float(__ushort_as_half(h)); }
@@ -425,4 +426,5 @@ cudaError_t launch_dvr(const PtArgs& a, const LightTex& shadow, const LightTex& 
     return cudaGetLastError();
 }
 
+}  // namespace VV_FMT_NS
 }  // namespace vv

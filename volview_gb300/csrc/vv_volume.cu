@@ -8,6 +8,8 @@
 // move a value across a rounding boundary).
 #include <cuda_runtime.h>
 
+#include <cuda_bf16.h>
+
 #include "vv_device.cuh"
 #include "vv_kernels.h"
 
@@ -16,27 +18,33 @@ namespace vv {
 static const float HU_MIN = -1024.0f, HU_MAX = 3071.0f;
 
 // hu_to_unorm16 (crates/render/src/transfer.rs:121-124) into the bricked
-// layout; one thread per bricked element, reading the x-fastest source.
-__global__ void k_density(const int16_t* __restrict__ hu, uint16_t* __restrict__ out, Vol v) {
+// layout; one thread per bricked element, reading the x-fastest source. The
+// precision variants store the same normalised density t as FP16 or BF16
+// (rounded to nearest even) or FP32 instead of round(t * 65535).
+__global__ void k_density(const int16_t* __restrict__ hu, void* __restrict__ out, Vol v) {
     long e = (long)blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= vol_elems(v)) return;
     int x, y, z;
     vcoord(v, e, x, y, z);
-    uint16_t q = 0;
+    float t = 0.0f;
     if (x < v.nx && y < v.ny && z < v.nz) {
         float h = (float)hu[((long)z * v.ny + y) * v.nx + x];
-        float t = __fdiv_rn(__fsub_rn(h, HU_MIN), __fsub_rn(HU_MAX, HU_MIN));
+        t = __fdiv_rn(__fsub_rn(h, HU_MIN), __fsub_rn(HU_MAX, HU_MIN));
         t = fminf(fmaxf(t, 0.0f), 1.0f);
-        q = (uint16_t)roundf(__fmul_rn(t, 65535.0f));
     }
-    out[e] = q;
+    switch (v.dfmt) {
+        case DF_FP16: ((uint16_t*)out)[e] = __half_as_ushort(__float2half_rn(t)); break;
+        case DF_BF16: ((uint16_t*)out)[e] = __bfloat16_as_ushort(__float2bfloat16_rn(t)); break;
+        case DF_FP32: ((float*)out)[e] = t; break;
+        default: ((uint16_t*)out)[e] = (uint16_t)roundf(__fmul_rn(t, 65535.0f));
+    }
 }
 
-__device__ __forceinline__ float dens(const uint16_t* d, const Vol& v, int x, int y, int z) {
+__device__ __forceinline__ float dens(const void* d, const Vol& v, int x, int y, int z) {
     x = clampi(x, 0, v.nx - 1);
     y = clampi(y, 0, v.ny - 1);
     z = clampi(z, 0, v.nz - 1);
-    return unorm16(__ldg(d + voff(v, x, y, z)));
+    return density_texel(d, v.dfmt, voff(v, x, y, z));
 }
 
 __device__ __forceinline__ int8_t to_snorm8(float f) {
@@ -44,7 +52,7 @@ __device__ __forceinline__ int8_t to_snorm8(float f) {
 }
 
 // normals.comp:14-37: 3x3x3 Sobel, /32, world transform, -g/|g| and clamp(|g|*400).
-__global__ void k_normals(const uint16_t* __restrict__ d, uint32_t* __restrict__ out, Vol v, m3 w) {
+__global__ void k_normals(const void* __restrict__ d, uint32_t* __restrict__ out, Vol v, m3 w) {
     long e = (long)blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= vol_elems(v)) return;
     int x, y, z;
@@ -82,7 +90,7 @@ __global__ void k_normals(const uint16_t* __restrict__ d, uint32_t* __restrict__
 // --------------------------------------------------------------------- masks
 struct MaskArgs {
     Vol v;
-    const uint16_t* density;
+    const void* density;
     const uint8_t* labels;
     const uint8_t* soft;  // RGBA8 nodes, x-fastest
     int sdims[3];
@@ -138,7 +146,6 @@ __device__ __forceinline__ float soft_score(bool best, bool second, float m) {
 __device__ void soft_masks(const MaskArgs& A, int px, int py, int pz, const float xg[3], float& mr, float& mg) {
     const float SIGMA_CT = 40.0f / 4095.0f, CERTAIN = 4.0f;
     const int* ax = A.soft_push;
-    int P[3] = {px, py, pz};
     int D[3] = {A.v.nx, A.v.ny, A.v.nz};
     float can[3] = {(float)D[ax[0]], (float)D[ax[1]], (float)D[ax[2]]};
     float to_grid[3];
@@ -254,7 +261,7 @@ __global__ void k_mask_blur(const uint32_t* __restrict__ src, uint32_t* __restri
 }
 
 // majorant.comp:26-71: one thread per brick over the brick and two voxels of border.
-__global__ void k_majorant(const uint16_t* __restrict__ d, const uint32_t* __restrict__ mask, Vol v, int mode,
+__global__ void k_majorant(const void* __restrict__ d, const uint32_t* __restrict__ mask, Vol v, int mode,
                            float label_ext, const float* __restrict__ bucket, float* __restrict__ out) {
     int b = blockIdx.x * blockDim.x + threadIdx.x;
     int nb = v.bx * v.by * v.bz;
@@ -269,7 +276,7 @@ __global__ void k_majorant(const uint16_t* __restrict__ d, const uint32_t* __res
             int oyz = oz + offy(v, y);
             for (int x = lo[0]; x <= hi[0]; x++) {
                 int o = oyz + offx(x);
-                float dv = unorm16(__ldg(d + o));
+                float dv = density_texel(d, v.dfmt, o);
                 dmin = gmin(dmin, dv);
                 dmax = gmax(dmax, dv);
                 if (mode != 0) {
@@ -314,11 +321,11 @@ __global__ void k_brick_u8(const uint8_t* __restrict__ src, uint8_t* __restrict_
 
 static unsigned blocks_for(long n, int t) { return (unsigned)((n + t - 1) / t); }
 
-cudaError_t launch_density(const int16_t* hu, uint16_t* out, const Vol& v, cudaStream_t s) {
+cudaError_t launch_density(const int16_t* hu, void* out, const Vol& v, cudaStream_t s) {
     k_density<<<blocks_for(vol_elems(v), 256), 256, 0, s>>>(hu, out, v);
     return cudaGetLastError();
 }
-cudaError_t launch_normals(const uint16_t* d, uint32_t* out, const Vol& v, const m3& w2i, cudaStream_t s) {
+cudaError_t launch_normals(const void* d, uint32_t* out, const Vol& v, const m3& w2i, cudaStream_t s) {
     k_normals<<<blocks_for(vol_elems(v), 256), 256, 0, s>>>(d, out, v, w2i);
     return cudaGetLastError();
 }
@@ -343,7 +350,7 @@ cudaError_t launch_masks(const MaskLaunch& L, cudaStream_t s) {
     k_mask_blur<<<nb, 256, 0, s>>>(L.scratch, L.out, L.v, 2, L.radius);
     return cudaGetLastError();
 }
-cudaError_t launch_majorant(const uint16_t* d, const uint32_t* mask, const Vol& v, int mode, float label_ext,
+cudaError_t launch_majorant(const void* d, const uint32_t* mask, const Vol& v, int mode, float label_ext,
                             const float* bucket, float* out, cudaStream_t s) {
     int nb = v.bx * v.by * v.bz;
     k_majorant<<<blocks_for(nb, 128), 128, 0, s>>>(d, mask, v, mode, label_ext, bucket, out);

@@ -30,6 +30,7 @@
 #include "vv_pt_device.cuh"
 
 namespace vv {
+namespace VV_FMT_NS {  // this density format's kernels and launchers
 
 // Slot layout: 16 x float4 = 256 bytes per pixel (WF_SLOT_BYTES); the light
 // map's sample, when there is a light map, in a parallel array of 2 x float4.
@@ -569,4 +570,5 @@ cudaError_t launch_pt_wavefront(const PtArgs& a, const WfArgs& w, int sms, cudaS
     return cudaGetLastError();
 }
 
+}  // namespace VV_FMT_NS
 }  // namespace vv

@@ -33,6 +33,7 @@ EXPORTS = [
     ("vv_context_create_on_stream", C.c_int, [C.c_int, P, P]),
     ("vv_context_destroy", C.c_int, [P]),
     ("vv_renderer_create", C.c_int, [P, P, P, P]),
+    ("vv_renderer_create_ex", C.c_int, [P, P, P, P, P]),
     ("vv_renderer_destroy", C.c_int, [P]),
     ("vv_renderer_get_info", C.c_int, [P, P]),
     ("vv_default_camera", C.c_int, [P, P]),
@@ -121,10 +122,14 @@ class Context:
 
 
 class Renderer:
-    def __init__(self, ctx, volume, tf):
+    def __init__(self, ctx, volume, tf, precision=None):
+        """`precision` (abi.Precision) selects the density storage and running sums;
+        None is the reference's (R16_UNORM, FP32 sums)."""
         self.ctx = ctx
         self.handle = C.c_void_p()
-        check(load().vv_renderer_create(ctx.handle, C.byref(volume), C.byref(tf), C.byref(self.handle)))
+        self.precision = precision if precision is not None else abi.precision()
+        check(load().vv_renderer_create_ex(ctx.handle, C.byref(volume), C.byref(tf), C.byref(self.precision),
+                                           C.byref(self.handle)))
         info = abi.RendererInfo()
         check(load().vv_renderer_get_info(self.handle, C.byref(info)))
         self.info = info
@@ -199,7 +204,8 @@ class Renderer:
         elif which == abi.VOLUME_AO:
             shape, dt = ((nz + 3) // 4, (ny + 3) // 4, (nx + 3) // 4), np.uint16
         else:
-            shape, dt = {abi.VOLUME_DENSITY: ((nz, ny, nx), np.uint16),
+            density_dt = np.float32 if self.precision.density_format == abi.DENSITY_FP32 else np.uint16
+            shape, dt = {abi.VOLUME_DENSITY: ((nz, ny, nx), density_dt),
                          abi.VOLUME_NORMALS: ((nz, ny, nx, 4), np.int8),
                          abi.VOLUME_MASK: ((nz, ny, nx, 2), np.uint16),
                          abi.VOLUME_LABELS: ((nz, ny, nx), np.uint8)}[which]

@@ -170,6 +170,52 @@ def small_phantom(seed=1, n=128):
     return hu, lab
 
 
+def torso_phantom(seed=1, dims=(512, 512, 800)):
+    """The small phantom's recipe scaled per axis to `dims` (x, y, z) voxels of
+    1 mm (the precision workload's torso): body ellipsoid 0 +- 40 HU, skull
+    shell 1000 +- 80, brain 20 +- 20, two lungs -800 +- 50, 10 region labels.
+    Generated 32 slices at a time."""
+    nx, ny, nz = dims
+    sx, sy, sz = nx / 128.0, ny / 128.0, nz / 128.0
+    rng = np.random.default_rng(seed)
+    hu = np.empty((nz, ny, nx), np.int16)
+    lab = np.zeros((nz, ny, nx), np.uint8)
+    c = (nx / 2 - 0.5, ny / 2 - 0.5, nz / 2 - 0.5)
+    head_c = (c[0], c[1], c[2] + 31 * sz)
+    y, x = np.ogrid[:ny, :nx]
+    side = (x >= c[0]).astype(np.uint8)
+
+    def ell(zz, center, radii):
+        return (((x - center[0]) / radii[0]) ** 2 + ((y - center[1]) / radii[1]) ** 2 +
+                ((zz - center[2]) / radii[2]) ** 2)
+
+    for z0 in range(0, nz, 32):
+        z1 = min(z0 + 32, nz)
+        zz = np.arange(z0, z1, dtype=np.float64)[:, None, None]
+        noise = rng.standard_normal((z1 - z0, ny, nx), dtype=np.float32)
+        h = np.full((z1 - z0, ny, nx), -1000.0, np.float32)
+        l = np.zeros((z1 - z0, ny, nx), np.uint8)
+        body = ell(zz, c, (50 * sx, 40 * sy, 58 * sz)) <= 1.0
+        h[body] = 40.0 * noise[body]
+        slab = np.clip(((zz - (c[2] - 58 * sz)) / (116 * sz) * 3).astype(int), 0, 2).astype(np.uint8)
+        region = np.broadcast_to(5 + slab * 2 + side, h.shape)
+        l[body] = region[body]
+        r_out = ell(zz, head_c, (34 * sx, 38 * sy, 26 * sz))
+        r_in = ell(zz, head_c, (30 * sx, 34 * sy, 22 * sz))
+        skull, brain = (r_out <= 1.0) & (r_in > 1.0), r_in <= 1.0
+        h[brain] = 20.0 + 20.0 * noise[brain]
+        l[brain] = 4
+        h[skull] = 1000.0 + 80.0 * noise[skull]
+        l[skull] = 1
+        for k, dx in enumerate((-20 * sx, 20 * sx)):
+            lung = ell(zz, (c[0] + dx, c[1], c[2] - 14 * sz), (14 * sx, 18 * sy, 24 * sz)) <= 1.0
+            h[lung] = -800.0 + 50.0 * noise[lung]
+            l[lung] = 2 + k
+        hu[z0:z1] = np.clip(np.rint(h), -32768, 32767).astype(np.int16)
+        lab[z0:z1] = l
+    return hu, lab
+
+
 SMALL_ENTRIES = {
     1: (SKELETON, (0.84, 0.79, 0.70), 0.42),
     2: (LUNGS, (0.58, 0.33, 0.35), 0.5),
@@ -310,6 +356,20 @@ def small_config(seed=1, n=128, size=256, spp=64, mode=abi.LABEL_HYBRID, soft=Tr
     soft_data = soft_grid(lab, spacing, 1, 3.0, np.float32) if soft else None
     return dict(hu=hu, labels_vol=lab, spacing=spacing, volume=vol, tf=tf, label_params=labels,
                 soft=soft_data, width=size, height=size, spp=spp, min_spacing=min(spacing))
+
+
+def torso_config(seed=1, dims=(512, 512, 800), width=1920, height=1080, spp=4096):
+    """The precision workload: the small phantom scaled to a 512x512x800 torso of
+    1 mm voxels, 1920x1080, 4096 paths per pixel; soft labels on a 4x coarser
+    grid with FP16 margins."""
+    hu, lab = torso_phantom(seed, dims)
+    spacing = (1.0, 1.0, 1.0)
+    vol = abi.volume_struct(hu, spacing)
+    tf = abi.tf_struct(abi.PRESETS["bone"])
+    labels = label_params(lab, hu, SMALL_ENTRIES, mode=abi.LABEL_HYBRID)
+    soft_data = soft_grid(lab, spacing, 4, 3.0, np.float16)
+    return dict(hu=hu, labels_vol=lab, spacing=spacing, volume=vol, tf=tf, label_params=labels,
+                soft=soft_data, width=width, height=height, spp=spp, min_spacing=min(spacing))
 
 
 def head_neck_config(seed=2, dims=(512, 512, 400), spacing=(0.5, 0.5, 1.0), size=1024, spp=1024):

@@ -283,8 +283,10 @@ vv_status vv_resize(vv_renderer* r, uint32_t width, uint32_t height);
  * VV_ERR_STATE where the reference panics (record before resize). Asynchronous:
  * returns once the work is queued; the context stream waits for the display. */
 vv_status vv_record(vv_renderer* r, uint64_t frame, const vv_frame_params* params);
-/* `frames` consecutive accumulate-frames with the same params in one
- * path-tracing pass; the denoiser and display passes run once, after the last.
+/* `frames` consecutive accumulate-frames with the same params in path-tracing
+ * passes of up to 64 frames (all of a pass's frames in flight at once,
+ * consecutive passes overlapping); the denoiser and display passes run once,
+ * after the last.
  * Equivalent to `frames` calls of vv_record except that intermediate displays
  * are skipped. frames x width x height may not exceed 2^31 (VV_ERR_LIMIT).
  * No counterpart in the reference. */

@@ -195,6 +195,10 @@ struct OpacityKey {
 #ifndef VV_PASSES
 #define VV_PASSES 6
 #endif
+// Frames per pass of a long vv_record_frames call.
+#ifndef VV_SUBPASS_FRAMES
+#define VV_SUBPASS_FRAMES 64
+#endif
 
 struct vv_renderer {
     vv_context* ctx;
@@ -1355,7 +1359,8 @@ static vv_status record_ray_march(vv_renderer* r, const vv_frame_params& p, cons
 // displayed, and the context stream waits for that display. So a call returns
 // at once, and consecutive calls overlap: one pass's last, nearly empty waves
 // run beside the next pass's first ones.
-static vv_status record_pass(vv_renderer* r, const vv_frame_params& p, UHead& u, uint32_t frames) {
+static vv_status record_pass(vv_renderer* r, const vv_frame_params& p, UHead& u, uint32_t frames,
+                             bool display = true) {
     vv_renderer::Pass& P = r->pass[r->next_pass];
     vv_renderer::Pass& prev = r->pass[(r->next_pass + VV_PASSES - 1) % VV_PASSES];
     r->next_pass = (r->next_pass + 1) % VV_PASSES;
@@ -1409,9 +1414,9 @@ static vv_status record_pass(vv_renderer* r, const vv_frame_params& p, UHead& u,
                                 (double)(r->accumulated + spf), s));
     }
     launches += 1;
-    if (p.path_tracing.denoiser == VV_DENOISE_ATROUS) CK(launch_denoise(pa, s, &launches));
+    if (display && p.path_tracing.denoiser == VV_DENOISE_ATROUS) CK(launch_denoise(pa, s, &launches));
     r->accumulated += spf;
-    if (p.path_tracing.denoiser != VV_DENOISE_OIDN) CK(launch_post(pa, s, &launches));
+    if (display && p.path_tracing.denoiser != VV_DENOISE_OIDN) CK(launch_post(pa, s, &launches));
     CK(cudaEventRecord(P.shown, s));
     CK(cudaStreamWaitEvent(r->ctx->stream, P.shown, 0));
     r->launches += launches;
@@ -1437,10 +1442,21 @@ extern "C" vv_status vv_record_frames(vv_renderer* r, uint64_t first_frame, uint
     // with room left for the counter's overshoot at the end of the pass.
     if ((uint64_t)frames * r->width * r->height > (1ull << 31))
         return fail(VV_ERR_LIMIT, "at most 2^31 (frame, pixel) pairs per vv_record_frames call; split the frames");
-    UHead u;
-    vv_status s = prepare_frame(r, *params, first_frame + frames - 1, u);
-    if (s != VV_OK) return s;
-    return record_pass(r, *params, u, frames);
+    // Long calls run as passes of at most VV_SUBPASS_FRAMES frames on the pass
+    // streams in turn, so that each pass's last waves overlap the next one's
+    // first (one long pass refilling its slots ran at 327 M path samples/s
+    // at 1024^2, 64-frame passes in turn at 339); only the last one displays.
+    uint32_t done = 0;
+    while (done < frames) {
+        uint32_t n = std::min<uint32_t>(frames - done, VV_SUBPASS_FRAMES);
+        UHead u;
+        vv_status s = prepare_frame(r, *params, first_frame + done + n - 1, u);
+        if (s != VV_OK) return s;
+        s = record_pass(r, *params, u, n, done + n == frames);
+        if (s != VV_OK) return s;
+        done += n;
+    }
+    return VV_OK;
 }
 
 static vv_status read_dev(vv_renderer* r, void* dst, const DBuf& src, size_t bytes, size_t capacity) {

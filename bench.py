@@ -58,6 +58,10 @@ def parse():
     ap.add_argument("--sums", default="fp32", choices=["fp32", "kahan"], help="running sums (vv_precision)")
     ap.add_argument("--fp64-after", type=int, default=0,
                     help="running sums continue in FP64 past this many paths/pixel (0: never)")
+    ap.add_argument("--serve", type=int, default=0,
+                    help="instead of the path-tracing bench, run this many render requests (Poisson arrivals "
+                         "at --serve-rate per second) over 8 resident phantoms through the request loop")
+    ap.add_argument("--serve-rate", type=float, default=40.0)
     ap.add_argument("--precision-study", type=int, default=0,
                     help="also render the default view to this many paths/pixel with each density storage "
                          "format and report each one's error against FP32 storage (same random streams)")
@@ -579,6 +583,90 @@ def precision_study(args, cfg, ctx, stream):
     return out
 
 
+SERVE_DIMS = [(256, 256, 256), (320, 320, 320), (384, 384, 300), (384, 384, 400), (448, 448, 400),
+              (512, 512, 400), (512, 512, 600), (512, 512, 800)]
+SERVE_SIZES = [(256, 256), (512, 512), (1024, 1024), (1920, 1080)]
+SERVE_SPP = [16, 64, 256, 1024]
+
+
+def serve_requests(volumes, n, rate, seed=5):
+    """n requests with Poisson arrivals: a resident phantom, an image size and
+    paths per pixel drawn uniformly, a random orbit, a sagittal clip plane at a
+    random depth (or none) and each label hidden with probability 0.2."""
+    from oracle import oracle as O  # geometry of the volumes (host math only)
+    from volview_gb300 import abi, scene
+    from volview_gb300 import serving as S
+    rng = np.random.default_rng(seed)
+    names = sorted(volumes)
+    t, out = 0.0, []
+    for _ in range(n):
+        t += rng.exponential(1.0 / rate)
+        name = names[rng.integers(len(names))]
+        cfg = volumes[name]
+        g = O.geometry(cfg["volume"])
+        clip = bool(rng.random() < 0.5)
+        p = scene.frame_params_for(cfg, list(g.center), g.diagonal, clip_sagittal=clip, anisotropy=0.6, spf=1)
+        p.camera.yaw = abi.f32(p.camera.yaw + rng.uniform(-np.pi, np.pi))
+        p.camera.pitch = abi.f32(p.camera.pitch + rng.uniform(-0.4, 0.4))
+        if clip:
+            lo, hi = g.bounds_lo[0], g.bounds_hi[0]
+            p.clipping.planes[0].position = abi.f32(lo + (hi - lo) * rng.uniform(0.3, 0.7))
+        for label in range(1, 11):
+            if rng.random() < 0.2:
+                p.labels.colors[label][3] = 0.0
+        w, h = SERVE_SIZES[rng.integers(len(SERVE_SIZES))]
+        spp = SERVE_SPP[rng.integers(len(SERVE_SPP))]
+        out.append(S.Request(name, w, h, spp, p, arrival=t))
+    return out
+
+
+def run_serve(args):
+    """The serving workload: 8 resident phantoms (256^3 to 512x512x800), one
+    renderer each, requests admitted by device memory and overlapping on the
+    device, shortest first with aging (`value`) and in arrival order; the same
+    requests one at a time in arrival order for comparison."""
+    import copy
+    import torch
+    from volview_gb300 import scene
+    from volview_gb300 import serving as S
+    t0 = time.perf_counter()
+    volumes = {f"v{i}_{d[0]}x{d[1]}x{d[2]}": scene.torso_config(seed=1 + i, dims=d, soft=False)
+               for i, d in enumerate(SERVE_DIMS)}
+    gen_s = time.perf_counter() - t0
+    free, total = torch.cuda.mem_get_info(0)
+    budget = int(free * 0.85)
+    result = {"metric": "serving: requests/s and p50/p99 latency, 8 resident phantoms, Poisson arrivals",
+              "unit": "requests/s", "higher_is_better": True, "n_gpus": 1, "dtype": "f32",
+              "data": "synthetic (seeded phantoms)",
+              "config": {"workload": "8 resident phantoms %s, 1 mm voxels; requests: image uniform in %s, "
+                                     "paths/pixel uniform in %s, random orbit, sagittal clip at random depth "
+                                     "half the time, each label hidden with probability 0.2; Poisson arrivals "
+                                     "at %.0f/s" % (SERVE_DIMS, SERVE_SIZES, SERVE_SPP, args.serve_rate),
+                         "requests": args.serve, "budget_bytes": budget, "phantom_generation_s": gen_s}}
+    modes = (("continuous_shortest_first", dict(order="shortest", aging_s=2.0, max_per_volume=1)),
+             ("continuous_fifo", dict(order="fifo", max_per_volume=1)),
+             ("one_at_a_time", dict(order="fifo", max_active=1)))
+    for mode, kw in modes:
+        make, base = S.renderer_factory(volumes)
+        srv = S.Server(make, base, budget, **kw)
+        for name in volumes:
+            srv.preload(name)  # resident before the requests come
+        for r in list(srv.owned):
+            r.synchronize()
+        reqs = [copy.copy(q) for q in serve_requests(volumes, args.serve, args.serve_rate)]
+        with Clocks(0) as clocks:
+            t0 = time.perf_counter()
+            done = srv.run(reqs)
+            wall = time.perf_counter() - t0
+        stats = S.summary(done, wall)
+        stats.update({"renderers_created": srv.created, "peak_device_bytes": srv.peak_bytes,
+                      "clocks": clocks.summary()})
+        result[mode] = stats
+        srv.close()
+    result["value"] = result["continuous_shortest_first"]["requests_per_s"]
+    print(json.dumps(result))
+
+
 def cpu_renderer_from_device(cfg, r, params):
     """The oracle's CPU renderer with the device's pre-pass volumes (bit-exact or
     within one quantum of the oracle's own, see tests) so only the path tracer
@@ -678,6 +766,9 @@ def main():
     rank, world, local = dist_init(args.gpus)
     if args.impl == "reference":
         run_reference(args, rank, world)
+    elif args.serve > 0:
+        if rank == 0:
+            run_serve(args)
     else:
         run_ours(args, rank, world, local)
     if world > 1:

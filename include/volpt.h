@@ -334,6 +334,22 @@ vv_status vv_read_volume(vv_renderer* r, int which, void* out, size_t capacity);
 /* Kernel launches this renderer has issued since creation (for accounting). */
 uint64_t vv_kernel_launches(const vv_renderer* r);
 
+/* ------------------------------------------------------------------ serving */
+/* Extensions for a render-request loop over several renderers (no
+ * counterpart in the reference). */
+
+/* *idle = 1 when every call made on the renderer has finished on the device,
+ * 0 while its work is in flight. Never blocks. */
+vv_status vv_query(vv_renderer* r, int* idle);
+/* Device bytes the renderer holds now: its volumes, images, lighting volumes
+ * and path-tracing pass state (which grows with the frames per pass and the
+ * image on first use). */
+vv_status vv_renderer_memory(const vv_renderer* r, uint64_t* bytes);
+/* Starts a new view: the accumulation restarts and auto exposure meters
+ * afresh, as in a renderer just created, so a reused renderer's next image
+ * does not depend on the ones before it. */
+vv_status vv_reset_view(vv_renderer* r);
+
 /* --------------------------------------------------- allocation-free denoise */
 
 /* The a-trous denoiser (the passes `record` runs after a frame) on device

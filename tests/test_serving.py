@@ -1,0 +1,158 @@
+"""The render-request loop's scheduling (CPU, with stand-in renderers): every
+request finishes with its own result, device memory stays within the budget,
+renderers are reused per volume and evicted least recently used first,
+requests that arrive while others run start without waiting for them, a
+request that can never fit is refused, shortest-first admission with aging,
+and the per-volume renderer limit."""
+import pytest
+
+from volview_gb300 import serving as S
+
+
+class FakeRenderer:
+    """The Renderer interface without a device: work takes `ticks` polls."""
+
+    def __init__(self, volume, base, log, ticks=3):
+        self.volume, self.base, self.log, self.ticks = volume, base, log, ticks
+        self.w = self.h = self.spp = 0
+        self.left = 0
+        self.destroyed = False
+        self.calls = []
+
+    def device_bytes(self):
+        assert not self.destroyed
+        return self.base + (S.request_bytes(self.w, self.h, self.spp) if self.spp else 0)
+
+    def reset_view(self):
+        self.calls.append("reset")
+
+    def resize(self, w, h):
+        self.calls.append("resize")
+        self.w, self.h = w, h
+
+    def record_frames(self, first, n, params):
+        self.calls.append("record")
+        self.spp, self.left, self.params = n, self.ticks, params
+        self.log.append(("start", params))
+
+    def idle(self):
+        self.left -= 1
+        return self.left <= 0
+
+    def read_output(self):
+        return ("image", self.volume, self.params)
+
+    def read_accumulation(self):
+        return ("accumulation", self.params)
+
+    def destroy(self):
+        self.destroyed = True
+        self.log.append(("destroy", self.volume))
+
+
+def make_server(budget, bases, ticks=3, max_active=None, **kw):
+    log, made = [], []
+
+    def make(volume):
+        r = FakeRenderer(volume, bases[volume], log, ticks)
+        made.append(r)
+        return r
+
+    srv = S.Server(make, lambda v: bases[v], budget, max_active=max_active, clock=iter(range(10 ** 6)).__next__,
+                   **kw)
+    return srv, log, made
+
+
+def run(srv, reqs):
+    for q in reqs:
+        srv.submit(q)
+    for _ in range(10000):
+        srv.step()
+        if not srv.queue and not srv.active:
+            return
+    raise AssertionError("requests did not finish")
+
+
+def test_results_are_routed_and_memory_stays_in_budget():
+    bases = {"a": 10 ** 9, "b": 2 * 10 ** 9}
+    budget = 40 * 10 ** 9
+    srv, log, made = make_server(budget, bases)
+    reqs = [S.Request("a" if k % 3 else "b", 256 << (k % 3), 256 << (k % 3), (16, 64, 256)[k % 3], params=k)
+            for k in range(12)]
+    run(srv, reqs)
+    assert all(q.image == ("image", q.volume, q.params) for q in reqs)
+    assert srv.peak_bytes <= budget
+    assert srv.created < len(reqs)                      # renderers reused
+    for r in made:
+        assert r.calls[:3] == ["reset", "resize", "record"]  # a fresh view per request
+
+
+def test_requests_overlap_and_later_ones_start_before_earlier_finish():
+    bases = {"a": 10 ** 9}
+    srv, log, made = make_server(100 * 10 ** 9, bases, ticks=50)
+    first = S.Request("a", 512, 512, 64, params="first")
+    srv.submit(first)
+    srv.step()
+    assert first.started is not None and first.finished is None
+    second = S.Request("a", 256, 256, 16, params="second")
+    srv.submit(second)
+    srv.step()
+    assert second.started is not None and first.finished is None  # admitted while the first runs
+    assert srv.created == 2
+
+
+def test_idle_renderers_are_evicted_least_recently_used():
+    bases = {"a": 10 ** 9, "b": 10 ** 9, "c": 10 ** 9}
+    one = bases["a"] + S.request_bytes(256, 256, 16)
+    srv, log, made = make_server(2 * one + 1, bases, ticks=1, max_active=1)
+    run(srv, [S.Request("a", 256, 256, 16, params=1)])
+    run(srv, [S.Request("b", 256, 256, 16, params=2)])
+    assert srv.created == 2 and not any(r.destroyed for r in made)
+    run(srv, [S.Request("c", 256, 256, 16, params=3)])  # needs room: "a" (least recent) goes
+    assert [r.volume for r in made if r.destroyed] == ["a"]
+    run(srv, [S.Request("b", 256, 256, 16, params=4)])  # "b" is still resident and reused
+    assert srv.created == 3
+
+
+def test_a_request_that_cannot_fit_is_refused():
+    srv, log, made = make_server(10 ** 6, {"a": 10 ** 9})
+    srv.submit(S.Request("a", 64, 64, 16, params=0))
+    with pytest.raises(MemoryError):
+        srv.step()
+
+
+def test_shortest_first_with_aging():
+    bases = {"a": 10 ** 9}
+    srv, log, made = make_server(10 ** 12, bases, ticks=5, max_active=1, order="shortest", aging_s=40)
+    big = S.Request("a", 1024, 1024, 1024, params="big")
+    mid = S.Request("a", 512, 512, 64, params="mid")
+    small = S.Request("a", 256, 256, 16, params="small")
+    for q in (big, mid, small):
+        srv.submit(q)
+    run(srv, [])
+    assert [p for kind, p in log if kind == "start"] == ["small", "mid", "big"]
+    # Past aging_s a request goes ahead of younger ones, whatever its size.
+    srv, log, made = make_server(10 ** 12, bases, ticks=5, max_active=1, order="shortest", aging_s=3)
+    srv.submit(S.Request("a", 1024, 1024, 1024, params="old"))
+    for _ in range(5):
+        srv.clock()  # time passes
+    srv.submit(S.Request("a", 256, 256, 16, params="new"))
+    run(srv, [])
+    assert [p for kind, p in log if kind == "start"] == ["old", "new"]
+
+
+def test_max_per_volume_waits_for_the_volumes_renderer():
+    bases = {"a": 10 ** 9, "b": 10 ** 9}
+    srv, log, made = make_server(10 ** 12, bases, ticks=4, max_per_volume=1)
+    reqs = [S.Request(v, 256, 256, 16, params=k) for k, v in enumerate("aab")]
+    run(srv, reqs)
+    assert srv.created == 2  # one renderer per volume
+    starts = [p for kind, p in log if kind == "start"]
+    assert starts == [0, 2, 1]  # "b" started beside the first "a"; the second "a" waited for it
+
+
+def test_request_bytes_model():
+    # One pass of 16 frames at 1024^2: 16 M slots; 1024 frames: six passes of the cap.
+    assert S.request_bytes(1024, 1024, 16) == 1024 * 1024 * (S.IMAGE_BYTES_PER_PIXEL + 16 * S.SLOT_BYTES)
+    assert S.request_bytes(1024, 1024, 1024) == 1024 * 1024 * S.IMAGE_BYTES_PER_PIXEL + 6 * (1 << 24) * S.SLOT_BYTES
+    assert S.request_bytes(4096, 4096, 1) == 4096 * 4096 * (S.IMAGE_BYTES_PER_PIXEL + S.SLOT_BYTES)

@@ -1055,6 +1055,53 @@ extern "C" vv_status vv_resize(vv_renderer* r, uint32_t width, uint32_t height) 
 extern "C" uint32_t vv_accumulated_samples(const vv_renderer* r) { return r ? r->accumulated : 0; }
 extern "C" uint64_t vv_kernel_launches(const vv_renderer* r) { return r ? r->launches : 0; }
 
+extern "C" vv_status vv_query(vv_renderer* r, int* idle) {
+    if (!r || !idle) return fail(VV_ERR_ARG, "null argument");
+    vv_status s = use_device(r);
+    if (s != VV_OK) return s;
+    // The context stream waits for every pass's display, so it is idle when
+    // all of the renderer's work is.
+    cudaError_t e = cudaStreamQuery(r->ctx->stream);
+    if (e == cudaErrorNotReady) {
+        *idle = 0;
+        return VV_OK;
+    }
+    if (e != cudaSuccess) return cuda_fail(e, "cudaStreamQuery");
+    *idle = 1;
+    return VV_OK;
+}
+
+extern "C" vv_status vv_renderer_memory(const vv_renderer* r, uint64_t* bytes) {
+    if (!r || !bytes) return fail(VV_ERR_ARG, "null argument");
+    const DBuf* all[] = {&r->density, &r->normals, &r->mask_a, &r->mask_b, &r->labels, &r->majorant, &r->lut,
+                         &r->bucket_dev, &r->tables, &r->soft, &r->work, &r->exposure, &r->accum, &r->albedo,
+                         &r->normal, &r->ping, &r->pong, &r->guide_nd, &r->guide_alb, &r->hdr, &r->out,
+                         &r->bloom[0], &r->bloom[1], &r->bloom[2], &r->bloom[3], &r->preint, &r->shadow_vol,
+                         &r->ao_vol, &r->env_rad, &r->env_table, &r->env_diffuse, &r->env_guide, &r->comp[0],
+                         &r->comp[1], &r->comp[2], &r->wide[0], &r->wide[1], &r->wide[2]};
+    uint64_t n = 0;
+    for (const DBuf* b : all) n += b->n;
+    for (const auto& P : r->pass) {
+        const DBuf* pb[] = {&P.slots, &P.map, &P.queues, &P.counts, &P.accum, &P.albedo, &P.normal};
+        for (const DBuf* b : pb) n += b->n;
+    }
+    if (r->shadow_tex.arr) n += (uint64_t)(r->shadow_dims[0] + 2) * (r->shadow_dims[1] + 2) * (r->shadow_dims[2] + 2) * 8;
+    if (r->ao_tex.arr) n += (uint64_t)(r->ao_dims[0] + 2) * (r->ao_dims[1] + 2) * (r->ao_dims[2] + 2) * 2;
+    *bytes = n;
+    return VV_OK;
+}
+
+extern "C" vv_status vv_reset_view(vv_renderer* r) {
+    if (!r) return fail(VV_ERR_ARG, "null renderer");
+    vv_status s = use_device(r);
+    if (s != VV_OK) return s;
+    // Exposure 0 = not yet metered (the state of a new renderer's texel).
+    CK(cudaMemsetAsync(r->exposure.p, 0, sizeof(float), r->ctx->stream));
+    r->prep_work = true;     // the next pass starts after it
+    r->have_params = false;  // the next record restarts the accumulation
+    return VV_OK;
+}
+
 extern "C" vv_status vv_synchronize(vv_renderer* r) {
     if (!r) return fail(VV_ERR_ARG, "null renderer");
     vv_status s = use_device(r);

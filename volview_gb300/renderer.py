@@ -52,6 +52,9 @@ EXPORTS = [
     ("vv_pack_uniforms", C.c_int, [P, P, C.c_uint64, P, C.c_size_t]),
     ("vv_read_volume", C.c_int, [P, C.c_int, P, C.c_size_t]),
     ("vv_kernel_launches", C.c_uint64, [P]),
+    ("vv_query", C.c_int, [P, P]),
+    ("vv_renderer_memory", C.c_int, [P, P]),
+    ("vv_reset_view", C.c_int, [P]),
     ("vv_denoise_atrous_noalloc", C.c_int, [P, P, P, P, C.c_uint32, C.c_uint32, C.c_uint32, P]),
 ]
 # Test hooks (include/volpt_probe.h).
@@ -171,6 +174,22 @@ class Renderer:
 
     def synchronize(self):
         check(load().vv_synchronize(self.handle))
+
+    def idle(self):
+        """True once every call made on this renderer has finished on the device (never blocks)."""
+        v = C.c_int(0)
+        check(load().vv_query(self.handle, C.byref(v)))
+        return bool(v.value)
+
+    def device_bytes(self):
+        """Device memory this renderer holds now."""
+        v = C.c_uint64(0)
+        check(load().vv_renderer_memory(self.handle, C.byref(v)))
+        return int(v.value)
+
+    def reset_view(self):
+        """A new view: the accumulation restarts and auto exposure meters afresh."""
+        check(load().vv_reset_view(self.handle))
 
     def read_output(self, out=None):
         out = np.empty((self.height, self.width, 4), np.uint8) if out is None else out

@@ -358,16 +358,16 @@ def small_config(seed=1, n=128, size=256, spp=64, mode=abi.LABEL_HYBRID, soft=Tr
                 soft=soft_data, width=size, height=size, spp=spp, min_spacing=min(spacing))
 
 
-def torso_config(seed=1, dims=(512, 512, 800), width=1920, height=1080, spp=4096):
+def torso_config(seed=1, dims=(512, 512, 800), width=1920, height=1080, spp=4096, soft=True):
     """The precision workload: the small phantom scaled to a 512x512x800 torso of
     1 mm voxels, 1920x1080, 4096 paths per pixel; soft labels on a 4x coarser
-    grid with FP16 margins."""
+    grid with FP16 margins (or none: binary label masks)."""
     hu, lab = torso_phantom(seed, dims)
     spacing = (1.0, 1.0, 1.0)
     vol = abi.volume_struct(hu, spacing)
     tf = abi.tf_struct(abi.PRESETS["bone"])
     labels = label_params(lab, hu, SMALL_ENTRIES, mode=abi.LABEL_HYBRID)
-    soft_data = soft_grid(lab, spacing, 4, 3.0, np.float16)
+    soft_data = soft_grid(lab, spacing, 4, 3.0, np.float16) if soft else None
     return dict(hu=hu, labels_vol=lab, spacing=spacing, volume=vol, tf=tf, label_params=labels,
                 soft=soft_data, width=width, height=height, spp=spp, min_spacing=min(spacing))
 

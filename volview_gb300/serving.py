@@ -1,0 +1,284 @@
+"""A render-request loop over resident volumes (the serving workload).
+
+Requests (a volume, an image size, paths per pixel, a camera, a clip plane and
+label visibility) arrive at any time. A request is admitted when the renderers
+it needs fit the device-memory budget, and it runs on a renderer of its volume
+whose context stream is its own. Its frames are one `vv_record_frames` call:
+passes of up to 64 frames queued at once, with a display after the last. So
+the passes of every admitted request overlap on the device, and requests that
+arrive while others run are admitted as memory and renderers free up, with no
+barrier between them.
+
+A renderer is reused for later requests of its volume. `vv_reset_view` restarts
+its accumulation and auto exposure first, and `vv_resize` sets the request's
+image, so a result depends only on its own request, alone or in any mix
+(tests/test_gpu_serving.py). Idle renderers of other volumes are destroyed,
+least recently used first, when a request needs their memory.
+
+The loop itself is host logic over the C ABI: `vv_query` polls for finished
+work without blocking, and `vv_renderer_memory` reports what each renderer
+holds. Renderers come from a factory, so the scheduling is tested on the CPU
+with stand-ins (tests/test_serving.py).
+"""
+import collections
+import time
+
+# Device bytes per image pixel: the accumulation and guide images, the
+# denoiser's ping/pong and guides, HDR, output and bloom, and the six passes'
+# own sums (vv_resize).
+IMAGE_BYTES_PER_PIXEL = 48 + 32 + 32 + 8 + 4 + 2 + 6 * 48
+# Device bytes per path slot of a pass: the slot, the light map sample and the
+# nine stage queues (vv_wavefront.cu).
+SLOT_BYTES = 256 + 32 + 9 * 4
+PASSES = 6          # passes in flight per renderer
+PASS_FRAMES = 64    # frames per pass of a long vv_record_frames call
+SLOT_FRAMES = 16    # frames' worth of slots a pass holds at most ...
+SLOT_CAP = 1 << 24  # ... and at most this many slots, unless one frame needs more
+
+
+def request_bytes(width, height, spp):
+    """Device bytes a renderer's image and path state take for one request."""
+    px = width * height
+    frames = min(spp, PASS_FRAMES)
+    slots = min(min(frames, SLOT_FRAMES) * px, max(SLOT_CAP, px))
+    passes = min(PASSES, -(-spp // PASS_FRAMES))
+    return px * IMAGE_BYTES_PER_PIXEL + passes * slots * SLOT_BYTES
+
+
+class Request:
+    """One render request. `params` is the vv_frame_params the request renders
+    with (camera, clip plane, label visibility); `spp` its paths per pixel."""
+
+    def __init__(self, volume, width, height, spp, params, arrival=0.0, tag=None):
+        self.volume, self.width, self.height, self.spp = volume, int(width), int(height), int(spp)
+        self.params, self.arrival, self.tag = params, float(arrival), tag
+        self.id = None
+        self.submitted = self.started = self.finished = None
+        self.renderer = None
+        self.image = None
+        self.accumulation = None
+
+    @property
+    def latency(self):
+        return None if self.finished is None else self.finished - self.submitted
+
+    @property
+    def paths(self):
+        return self.width * self.height * self.spp
+
+
+class Server:
+    """Admits and runs requests; see the module docstring.
+
+    `make_renderer(volume)` returns a renderer (the `renderer.Renderer`
+    interface: reset_view, resize, record_frames, idle, read_output,
+    read_accumulation, device_bytes, destroy) of a resident volume, its labels
+    set. `base_bytes(volume)` is the device memory of such a renderer before
+    any image (its volumes). `max_active` bounds the requests in flight (None:
+    memory alone decides); `max_per_volume` the requests in flight per volume,
+    i.e. its renderers (None: a new renderer when the others are busy).
+
+    `order` is the admission order of queued requests: "fifo" (arrival), or
+    "shortest" (fewest paths first, so short requests run beside long ones
+    instead of behind them; a request queued longer than `aging_s` goes ahead
+    of all younger ones, in arrival order, so long ones are not starved)."""
+
+    def __init__(self, make_renderer, base_bytes, budget_bytes, max_active=None, keep_accumulation=False,
+                 clock=time.perf_counter, order="fifo", aging_s=2.0, max_per_volume=None):
+        if order not in ("fifo", "shortest"):
+            raise ValueError(f"unknown admission order {order!r}")
+        self.make_renderer, self.base_bytes = make_renderer, base_bytes
+        self.budget, self.max_active, self.keep_accumulation = int(budget_bytes), max_active, keep_accumulation
+        self.clock, self.order, self.aging_s, self.max_per_volume = clock, order, aging_s, max_per_volume
+        self.queue = collections.deque()
+        self.active = []
+        self.idle = collections.OrderedDict()  # renderer -> volume, least recently used first
+        self.owned = {}                        # renderer -> its volume
+        self.next_id = 0
+        self.done = []
+        self.peak_bytes = 0
+        self.created = 0
+
+    # ------------------------------------------------------------- accounting
+    def used_bytes(self):
+        return sum(r.device_bytes() for r in self.owned)
+
+    def _need(self, req, renderer):
+        """Bytes admitting `req` adds: a new renderer's volumes and image, or
+        the growth of a reused one."""
+        want = request_bytes(req.width, req.height, req.spp)
+        if renderer is None:
+            return self.base_bytes(req.volume) + want
+        return max(0, self.base_bytes(req.volume) + want - renderer.device_bytes())
+
+    # --------------------------------------------------------------- the loop
+    def submit(self, req):
+        req.id = self.next_id
+        self.next_id += 1
+        req.submitted = self.clock()
+        self.queue.append(req)
+        return req.id
+
+    def _idle_renderer(self, volume):
+        for r, v in self.idle.items():
+            if v == volume:
+                return r
+        return None
+
+    def _evict(self, need, keep):
+        """Destroys idle renderers (least recently used first, never `keep`)
+        until `need` more bytes fit; False if they cannot."""
+        used = self.used_bytes()
+        for r in list(self.idle):
+            if used + need <= self.budget:
+                break
+            if r is keep:
+                continue
+            used -= r.device_bytes()
+            del self.idle[r]
+            del self.owned[r]
+            r.destroy()
+        return used + need <= self.budget
+
+    def _candidates(self):
+        if self.order == "fifo":
+            return list(self.queue)
+        now = self.clock()
+        aged = [q for q in self.queue if now - q.submitted > self.aging_s]
+        young = sorted((q for q in self.queue if now - q.submitted <= self.aging_s), key=lambda q: (q.paths, q.id))
+        return aged + young
+
+    def _admit(self):
+        """First fit in admission order: each queued request that fits starts."""
+        for req in self._candidates():
+            if self.max_active is not None and len(self.active) >= self.max_active:
+                return
+            r = self._idle_renderer(req.volume)
+            if r is None and self.max_per_volume is not None and \
+                    sum(q.volume == req.volume for q in self.active) >= self.max_per_volume:
+                continue
+            need = self._need(req, r)
+            if not self._evict(need, r):
+                if not self.active and r is None and not self.idle:
+                    raise MemoryError(f"request {req.id} needs {need} bytes, budget {self.budget}")
+                continue
+            self.queue.remove(req)
+            if r is None:
+                r = self.make_renderer(req.volume)
+                self.owned[r] = req.volume
+                self.created += 1
+            else:
+                del self.idle[r]
+            req.renderer = r
+            req.started = self.clock()
+            r.reset_view()
+            r.resize(req.width, req.height)
+            r.record_frames(1, req.spp, req.params)
+            self.active.append(req)
+            self.peak_bytes = max(self.peak_bytes, self.used_bytes())
+
+    def _collect(self):
+        finished = []
+        for req in list(self.active):
+            r = req.renderer
+            if not r.idle():
+                continue
+            req.image = r.read_output()
+            if self.keep_accumulation:
+                req.accumulation = r.read_accumulation()
+            req.finished = self.clock()
+            self.active.remove(req)
+            self.idle[r] = req.volume
+            self.idle.move_to_end(r)
+            req.renderer = None
+            finished.append(req)
+        self.done += finished
+        return finished
+
+    def step(self):
+        """Collects finished requests and admits queued ones; returns the finished."""
+        finished = self._collect()
+        self._admit()
+        return finished
+
+    def run(self, requests, poll_s=0.0005):
+        """Submits each request at its arrival time (seconds after the start)
+        and runs until all have finished; returns them in submission order."""
+        pending = sorted(requests, key=lambda q: q.arrival)
+        t0 = self.clock()
+        i = 0
+        while i < len(pending) or self.queue or self.active:
+            now = self.clock() - t0
+            while i < len(pending) and pending[i].arrival <= now:
+                self.submit(pending[i])
+                i += 1
+            finished = self.step()
+            if not finished and poll_s > 0:
+                time.sleep(poll_s)
+        return sorted(pending, key=lambda q: q.id)
+
+    def preload(self, volume):
+        """Makes a renderer of `volume` resident (idle) before requests come."""
+        r = self.make_renderer(volume)
+        self.owned[r] = volume
+        self.idle[r] = volume
+        self.created += 1
+        return r
+
+    def close(self):
+        for r in list(self.owned):
+            r.destroy()
+        self.owned.clear()
+        self.idle.clear()
+
+
+def volume_bytes(dims):
+    """Device bytes of a renderer's volumes before any image: bricked density,
+    normals, labels and the two masks (15 bytes per bricked voxel)."""
+    bricked = 1
+    for d in dims:
+        bricked *= -(-int(d) // 8) * 8
+    return 15 * bricked
+
+
+def renderer_factory(volumes, device=0, precision=None):
+    """(make_renderer, base_bytes) for resident `volumes` ({name: scene
+    config}): each renderer on a context (CUDA stream) of its own, owning it."""
+    from . import abi
+    from . import renderer as R
+
+    class OwnedRenderer(R.Renderer):
+        def destroy(self):
+            super().destroy()
+            self.ctx.destroy()
+
+    measured = {}
+
+    def make(name):
+        cfg = volumes[name]
+        r = OwnedRenderer(R.Context(device), cfg["volume"], cfg["tf"], precision)
+        soft = cfg.get("soft")
+        r.set_labels(cfg["labels_vol"], abi.soft_struct(soft) if soft is not None else None)
+        measured.setdefault(name, r.device_bytes())
+        return r
+
+    def base(name):
+        return measured.get(name) or volume_bytes(volumes[name]["volume"].dims)
+
+    return make, base
+
+
+def summary(requests, wall_s):
+    """Throughput and latency of a finished run."""
+    import numpy as np
+    lat = np.array([q.latency for q in requests])
+    wait = np.array([q.started - q.submitted for q in requests])
+    paths = sum(q.paths for q in requests)
+    by_size = {}
+    for q in requests:
+        by_size.setdefault(f"{q.width}x{q.height}", []).append(q.latency)
+    return {"requests": len(requests), "wall_s": wall_s, "requests_per_s": len(requests) / wall_s,
+            "path_samples_per_s": paths / wall_s,
+            "latency_p50_s": float(np.percentile(lat, 50)), "latency_p99_s": float(np.percentile(lat, 99)),
+            "queue_wait_p50_s": float(np.percentile(wait, 50)), "queue_wait_p99_s": float(np.percentile(wait, 99)),
+            "latency_p50_s_by_image": {k: float(np.percentile(v, 50)) for k, v in sorted(by_size.items())}}

@@ -1,0 +1,257 @@
+"""A learned denoiser: a 5-level U-Net on colour, albedo and normal, run and
+trained by the tensor-core operators of include/volpt_nn.h.
+
+Input: 16 channels from an accumulation (log(1 + radiance), albedo, normal,
+zeros; vv_nn_features). Levels of 32, 48, 64, 80 and 96 channels, two 3x3
+convolutions with ReLU each, 2x2 average pooling down, nearest upsampling up,
+skip connections by concatenation; a 3x3 head of 16 channels whose first 3
+are log(1 + radiance). FP16 weights and activations, FP32 accumulation in
+every convolution, FP32 master weights for Adam, an L1 loss in log radiance
+with its gradient scaled by GRAD_SCALE so that FP16 gradients stay normal.
+
+Device memory comes from PyTorch (tensors as buffers, the current CUDA
+stream); every arithmetic operation is a kernel of libvolpt.so. Images are
+padded to multiples of 256 pixels per axis (the coarsest level's rows must
+hold whole 16-pixel tiles).
+"""
+import ctypes as C
+
+import numpy as np
+
+from . import renderer as R
+
+LEVELS = (32, 48, 64, 80, 96)
+IN_CHANNELS, OUT_CHANNELS = 16, 16
+GRAD_SCALE = 65536.0
+PAD = 256
+
+
+def plan():
+    """The layer plan: ("conv", name, source, relu), ("pool", name, source),
+    ("up_cat", name, source, skip); inputs come from the named outputs."""
+    ops, src = [], "input"
+    for lv, c in enumerate(LEVELS):
+        if lv:
+            ops.append(("pool", f"p{lv}", src))
+            src = f"p{lv}"
+        ops += [("conv", f"e{lv}a", src, True), ("conv", f"e{lv}b", f"e{lv}a", True)]
+        src = f"e{lv}b"
+    for lv in range(len(LEVELS) - 2, -1, -1):
+        ops.append(("up_cat", f"u{lv}", src, f"e{lv}b"))
+        ops += [("conv", f"d{lv}a", f"u{lv}", True), ("conv", f"d{lv}b", f"d{lv}a", True)]
+        src = f"d{lv}b"
+    ops.append(("conv", "head", src, False))
+    return ops
+
+
+def channels():
+    """Output channels of every tensor in the plan, and each conv's (cin, cout)."""
+    ch, shapes = {"input": IN_CHANNELS}, {}
+    for op in plan():
+        kind, name, src = op[0], op[1], op[2]
+        if kind == "conv":
+            if name == "head":
+                cout = OUT_CHANNELS
+            else:
+                lv = int(name[1])
+                cout = LEVELS[lv]
+            shapes[name] = (ch[src], cout)
+            ch[name] = cout
+        elif kind == "pool":
+            ch[name] = ch[src]
+        else:
+            ch[name] = ch[src] + ch[op[3]]
+    return ch, shapes
+
+
+def _check(status, what):
+    if status != 0:
+        raise R.VolptError(status, f"{what}: a shape the operators do not take")
+
+
+class UNet:
+    """The network's parameters (FP32 masters, FP16 copies, Adam moments) and
+    its forward and backward passes."""
+
+    def __init__(self, seed=0, device="cuda"):
+        import torch
+        self.torch, self.device = torch, device
+        self.lib = R.load()
+        self.plan = plan()
+        self.ch, self.shapes = channels()
+        rng = np.random.default_rng(seed)
+        self.params = {}
+        for name, (cin, cout) in self.shapes.items():
+            real_in = 9 if name == "e0a" else cin  # input channels 9..15 are zeros
+            std = np.sqrt(2.0 / (9 * real_in)) * (0.1 if name == "head" else 1.0)
+            w = (rng.standard_normal((cout, 3, 3, cin)) * std).astype(np.float32)
+            if name == "e0a":
+                w[..., 9:] = 0.0
+            self.params[name] = self._param(w, np.zeros(cout, np.float32))
+        self.steps = 0
+
+    def _param(self, w, b):
+        t = self.torch
+        p = {"w": t.tensor(w, device=self.device), "b": t.tensor(b, device=self.device)}
+        p["w16"] = p["w"].half()
+        for k in ("w", "b"):
+            p["m" + k] = t.zeros_like(p[k])
+            p["v" + k] = t.zeros_like(p[k])
+            p["g" + k] = t.zeros_like(p[k])
+        return p
+
+    def numpy_params(self):
+        """{name: (w, b)} as float64 arrays of the FP16 weights the kernels use."""
+        return {n: (p["w16"].float().cpu().numpy().astype(np.float64), p["b"].cpu().numpy().astype(np.float64))
+                for n, p in self.params.items()}
+
+    def state(self):
+        return {n: (p["w"].cpu().numpy(), p["b"].cpu().numpy()) for n, p in self.params.items()}
+
+    def load_state(self, state):
+        for n, (w, b) in state.items():
+            p = self.params[n]
+            p["w"].copy_(self.torch.tensor(w))
+            p["b"].copy_(self.torch.tensor(b))
+            p["w16"].copy_(p["w"].half())
+
+    # ------------------------------------------------------------------ passes
+    def _stream(self):
+        return C.c_void_p(self.torch.cuda.current_stream().cuda_stream)
+
+    def forward(self, x):
+        """x: (N, H, W, 16) FP16 on the device; returns the head's output and
+        keeps the activations for backward."""
+        t, s = self.torch, self._stream()
+        acts = {"input": x}
+        for op in self.plan:
+            kind, name, src = op[0], op[1], op[2]
+            a = acts[src]
+            n, h, w, c = a.shape
+            if kind == "conv":
+                p = self.params[name]
+                cout = self.shapes[name][1]
+                y = t.empty((n, h, w, cout), dtype=t.float16, device=self.device)
+                _check(self.lib.vv_nn_conv3x3(a.data_ptr(), n, h, w, c, p["w16"].data_ptr(), p["b"].data_ptr(), cout,
+                                              int(op[3]), y.data_ptr(), s), name)
+            elif kind == "pool":
+                y = t.empty((n, h // 2, w // 2, c), dtype=t.float16, device=self.device)
+                _check(self.lib.vv_nn_avgpool2(a.data_ptr(), n, h, w, c, y.data_ptr(), 0, s), name)
+            else:
+                k = acts[op[3]]
+                u = t.empty((n, 2 * h, 2 * w, c), dtype=t.float16, device=self.device)
+                _check(self.lib.vv_nn_upsample2(a.data_ptr(), n, h, w, c, u.data_ptr(), 0, s), name)
+                y = t.empty((n, 2 * h, 2 * w, c + k.shape[3]), dtype=t.float16, device=self.device)
+                _check(self.lib.vv_nn_concat(u.data_ptr(), c, k.data_ptr(), k.shape[3], n * 4 * h * w, y.data_ptr(),
+                                             s), name)
+            acts[name] = y
+        self.acts = acts
+        return acts["head"]
+
+    def backward(self, dpred):
+        """Weight and bias gradients (into each parameter's gw, gb, zeroed
+        first) for the head's output gradient dpred (FP16, scaled)."""
+        t, s, acts = self.torch, self._stream(), self.acts
+        for p in self.params.values():
+            p["gw"].zero_()
+            p["gb"].zero_()
+        grads = {"head": dpred}
+
+        def add(name, g):
+            if name in grads:
+                _check(self.lib.vv_nn_add(grads[name].data_ptr(), g.data_ptr(), g.numel(), s), "add")
+            else:
+                grads[name] = g
+
+        for op in reversed(self.plan):
+            kind, name, src = op[0], op[1], op[2]
+            if name not in grads:
+                continue
+            dy = grads.pop(name)
+            a = acts[src]
+            n, h, w, c = a.shape
+            if kind == "conv":
+                p = self.params[name]
+                cout = self.shapes[name][1]
+                if op[3]:
+                    _check(self.lib.vv_nn_relu_backward(dy.data_ptr(), acts[name].data_ptr(), dy.numel(), s), name)
+                _check(self.lib.vv_nn_conv3x3_wgrad(a.data_ptr(), dy.data_ptr(), n, h, w, c, cout,
+                                                    p["gw"].data_ptr(), s), name)
+                _check(self.lib.vv_nn_bias_grad(dy.data_ptr(), n * h * w, cout, p["gb"].data_ptr(), s), name)
+                if src != "input":
+                    wt = t.empty((c, 3, 3, cout), dtype=t.float16, device=self.device)
+                    _check(self.lib.vv_nn_flip_weights(p["w16"].data_ptr(), cout, c, wt.data_ptr(), s), name)
+                    dx = t.empty_like(a)
+                    _check(self.lib.vv_nn_conv3x3(dy.data_ptr(), n, h, w, cout, wt.data_ptr(), None, c, 0,
+                                                  dx.data_ptr(), s), name)
+                    add(src, dx)
+            elif kind == "pool":
+                dx = t.empty_like(a)
+                _check(self.lib.vv_nn_avgpool2(dy.data_ptr(), n, h, w, c, dx.data_ptr(), 1, s), name)
+                add(src, dx)
+            else:
+                k = acts[op[3]]
+                du = t.empty((n, 2 * h, 2 * w, c), dtype=t.float16, device=self.device)
+                dk = t.empty_like(k)
+                _check(self.lib.vv_nn_split(dy.data_ptr(), c, k.shape[3], n * 4 * h * w, du.data_ptr(),
+                                            dk.data_ptr(), s), name)
+                dx = t.empty_like(a)
+                _check(self.lib.vv_nn_upsample2(du.data_ptr(), n, h, w, c, dx.data_ptr(), 1, s), name)
+                add(src, dx)
+                add(op[3], dk)
+
+    def adam(self, lr=1e-3, beta1=0.9, beta2=0.999, eps=1e-8):
+        self.steps += 1
+        s = self._stream()
+        for name, p in self.params.items():
+            for k, half in (("w", p["w16"]), ("b", None)):
+                _check(self.lib.vv_nn_adam(p[k].data_ptr(), half.data_ptr() if half is not None else None,
+                                           p["g" + k].data_ptr(), p["m" + k].data_ptr(), p["v" + k].data_ptr(),
+                                           p[k].numel(), lr, beta1, beta2, eps, GRAD_SCALE, self.steps, s), name)
+
+    def loss(self, pred, target):
+        """L1 loss in log radiance (target: (N, H, W, 3) float32 log(1 + radiance))
+        and the scaled FP16 gradient of the prediction."""
+        t = self.torch
+        loss = t.zeros(1, dtype=t.float32, device=self.device)
+        dpred = t.empty_like(pred)
+        n, h, w, c = pred.shape
+        _check(self.lib.vv_nn_l1_loss(pred.data_ptr(), c, target.data_ptr(), n * h * w, GRAD_SCALE, loss.data_ptr(),
+                                      dpred.data_ptr(), self._stream()), "loss")
+        return loss, dpred
+
+    def train_step(self, x, target, lr=1e-3):
+        pred = self.forward(x)
+        loss, dpred = self.loss(pred, target)
+        self.backward(dpred)
+        self.adam(lr)
+        return loss
+
+    # ---------------------------------------------------------------- helpers
+    def features(self, accum, albedo, normal, spp):
+        """(1, H', W', 16) FP16 input from host accumulation sums (H, W, 4), zero
+        padded to multiples of PAD."""
+        t = self.torch
+        h, w = accum.shape[:2]
+        hp, wp = -(-h // PAD) * PAD, -(-w // PAD) * PAD
+        bufs = []
+        for a in (accum, albedo, normal):
+            b = np.zeros((hp, wp, 4), np.float32)
+            b[:h, :w] = a
+            bufs.append(t.tensor(b, device=self.device))
+        x = t.empty((1, hp, wp, IN_CHANNELS), dtype=t.float16, device=self.device)
+        _check(self.lib.vv_nn_features(bufs[0].data_ptr(), bufs[1].data_ptr(), bufs[2].data_ptr(), float(spp),
+                                       hp * wp, x.data_ptr(), self._stream()), "features")
+        return x
+
+    def denoise(self, accum, albedo, normal, spp):
+        """The network's radiance (H, W, 3) for host accumulation sums of spp paths per pixel."""
+        t = self.torch
+        h, w = accum.shape[:2]
+        x = self.features(accum, albedo, normal, spp)
+        pred = self.forward(x)
+        n, hp, wp, c = pred.shape
+        rgb = t.empty((hp, wp, 3), dtype=t.float32, device=self.device)
+        _check(self.lib.vv_nn_radiance(pred.data_ptr(), c, hp * wp, rgb.data_ptr(), self._stream()), "radiance")
+        self.acts = None
+        return rgb[:h, :w].cpu().numpy()

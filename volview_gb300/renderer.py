@@ -66,6 +66,25 @@ PROBES = [
     ("vv_time_pt", C.c_int, [P, C.c_int, P, P]),
 ]
 
+# The learned denoiser's operators (include/volpt_nn.h).
+I, L, F = C.c_int, C.c_long, C.c_float
+NN = [
+    ("vv_nn_conv3x3", I, [P, I, I, I, I, P, P, I, I, P, P]),
+    ("vv_nn_flip_weights", I, [P, I, I, P, P]),
+    ("vv_nn_conv3x3_wgrad", I, [P, P, I, I, I, I, I, P, P]),
+    ("vv_nn_bias_grad", I, [P, L, I, P, P]),
+    ("vv_nn_relu_backward", I, [P, P, L, P]),
+    ("vv_nn_avgpool2", I, [P, I, I, I, I, P, I, P]),
+    ("vv_nn_upsample2", I, [P, I, I, I, I, P, I, P]),
+    ("vv_nn_concat", I, [P, I, P, I, L, P, P]),
+    ("vv_nn_split", I, [P, I, I, L, P, P, P]),
+    ("vv_nn_features", I, [P, P, P, F, L, P, P]),
+    ("vv_nn_l1_loss", I, [P, I, P, L, F, P, P, P]),
+    ("vv_nn_adam", I, [P, P, P, P, P, L, F, F, F, F, F, I, P]),
+    ("vv_nn_add", I, [P, P, L, P]),
+    ("vv_nn_radiance", I, [P, I, L, P, P]),
+]
+
 COUNT_NAMES = ["majorant", "cubic", "trilinear", "mask", "label", "normal", "gradient", "pixel", "path", "vertex"]
 # Unique element bytes each event must read (and write, for pixels).
 COUNT_BYTES = [4, 128, 16, 32, 1, 32, 128, 104, 0, 0]
@@ -87,7 +106,7 @@ def load():
             from . import build
             build.build()
         lib = C.CDLL(LIB_PATH)
-        for name, res, args in EXPORTS + PROBES:
+        for name, res, args in EXPORTS + PROBES + NN:
             fn = getattr(lib, name)
             fn.restype = res
             fn.argtypes = args

@@ -62,6 +62,9 @@ def parse():
                     help="instead of the path-tracing bench, run this many render requests (Poisson arrivals "
                          "at --serve-rate per second) over 8 resident phantoms through the request loop")
     ap.add_argument("--serve-rate", type=float, default=40.0)
+    ap.add_argument("--denoiser-study", type=int, default=0,
+                    help="instead of the path-tracing bench, train the learned denoiser for this many Adam steps "
+                         "on pairs the tracer renders (4 vs 256 paths/pixel) and compare it with a-trous")
     ap.add_argument("--precision-study", type=int, default=0,
                     help="also render the default view to this many paths/pixel with each density storage "
                          "format and report each one's error against FP32 storage (same random streams)")
@@ -667,6 +670,61 @@ def run_serve(args):
     print(json.dumps(result))
 
 
+def run_denoiser_study(args):
+    """The learned denoiser at a reduced scale of its configuration: the
+    head/neck recipe at 256x256x200 (1 x 1 x 2 mm), 256x256 images, 128
+    training views (4 paths/pixel in, 256 as target) and 16 held-out views
+    (1024 paths/pixel as reference); the U-Net's luminance RMSE beside the raw
+    4-path image's and the a-trous filter's, and inference time at 1024^2."""
+    import torch
+    from volview_gb300 import abi, scene
+    from volview_gb300 import learned_denoiser as LD
+    from volview_gb300 import renderer as R
+    t0 = time.perf_counter()
+    cfg = scene.head_neck_config(seed=4, dims=(256, 256, 200), spacing=(1.0, 1.0, 2.0), size=256)
+    gen_s = time.perf_counter() - t0
+    ctx = R.Context(0)
+    r = R.Renderer(ctx, cfg["volume"], cfg["tf"])
+    r.set_labels(cfg["labels_vol"], abi.soft_struct(cfg["soft"]))
+    r.resize(256, 256)
+    center, diag = list(r.center), r.diagonal
+    train_views = LD.random_views(cfg, center, diag, 128, seed=11)
+    test_views = LD.random_views(cfg, center, diag, 16, seed=12)
+    res = LD.study(r, cfg, train_views, test_views, low_spp=4, train_spp=256, test_spp=1024,
+                   steps=args.denoiser_study, batch=4)
+    net = res.pop("net")
+    # Inference at 1024^2 (features and network), and the a-trous passes there.
+    x = torch.zeros((1, 1024, 1024, LD.IN_CHANNELS), dtype=torch.float16, device="cuda")
+    for _ in range(3):
+        net.forward(x)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(10):
+        net.forward(x)
+    e1.record()
+    torch.cuda.synchronize()
+    unet_ms = e0.elapsed_time(e1) / 10
+    flops = 0
+    h = w = 1024
+    for op in net.plan:
+        if op[0] == "conv":
+            cin, cout = net.shapes[op[1]]
+            lv = 0 if op[1] == "head" else int(op[1][1])
+            flops += 2 * 9 * cin * cout * (h >> lv) * (w >> lv)
+    r.destroy()
+    ctx.destroy()
+    losses = res.pop("losses")
+    res.update({"loss_first": losses[0], "loss_last": float(np.mean(losses[-20:])),
+                "unet_forward_ms_1024": unet_ms, "unet_gflop_1024": flops / 1e9,
+                "unet_tflops_1024": flops / (unet_ms / 1e3) / 1e12, "phantom_generation_s": gen_s})
+    print(json.dumps({"metric": "learned denoiser: luminance RMSE at 4 paths/pixel against 1024",
+                      "unit": "RMSE", "higher_is_better": False, "value": res["mean_rmse"]["unet"],
+                      "config": {"workload": "head/neck recipe 256x256x200 at 1x1x2 mm, 256x256, 128 training "
+                                             "views (4 vs 256 paths/pixel), 16 held-out views (1024), %d Adam "
+                                             "steps of 4 images" % args.denoiser_study},
+                      "study": res}))
+
+
 def cpu_renderer_from_device(cfg, r, params):
     """The oracle's CPU renderer with the device's pre-pass volumes (bit-exact or
     within one quantum of the oracle's own, see tests) so only the path tracer
@@ -769,6 +827,9 @@ def main():
     elif args.serve > 0:
         if rank == 0:
             run_serve(args)
+    elif args.denoiser_study > 0:
+        if rank == 0:
+            run_denoiser_study(args)
     else:
         run_ours(args, rank, world, local)
     if world > 1:

@@ -255,3 +255,95 @@ class UNet:
         _check(self.lib.vv_nn_radiance(pred.data_ptr(), c, hp * wp, rgb.data_ptr(), self._stream()), "radiance")
         self.acts = None
         return rgb[:h, :w].cpu().numpy()
+
+
+# ---------------------------------------------------------------- training data
+def random_views(cfg, center, diagonal, count, seed):
+    """`count` frame parameters around the volume: random orbit, a sagittal
+    clip at a random depth half the time; denoiser off (the network sees raw
+    accumulations)."""
+    from . import abi, scene
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(count):
+        clip = bool(rng.random() < 0.5)
+        p = scene.frame_params_for(cfg, center, diagonal, clip_sagittal=clip, anisotropy=0.6, spf=1,
+                                   denoiser=abi.DENOISE_OFF)
+        p.camera.yaw = abi.f32(p.camera.yaw + rng.uniform(-np.pi, np.pi))
+        p.camera.pitch = abi.f32(p.camera.pitch + rng.uniform(-0.4, 0.4))
+        if clip:
+            p.clipping.planes[0].position = abi.f32(center[0] + diagonal * rng.uniform(-0.12, 0.12))
+        out.append(p)
+    return out
+
+
+def render_pair(renderer, params, low_spp, high_spp):
+    """(low-spp accumulation sums (acc, albedo, normal), high-spp radiance (H, W, 3)):
+    one accumulation, read at low_spp and continued to high_spp."""
+    renderer.reset_view()
+    renderer.record_frames(1, low_spp, params)
+    low = renderer.read_accumulation()
+    renderer.record_frames(1 + low_spp, high_spp - low_spp, params)
+    acc, _, _ = renderer.read_accumulation(normal=False)
+    return low, acc[..., :3] / high_spp
+
+
+def atrous(renderer, params, spp):
+    """The a-trous denoiser's radiance (H, W, 3) at spp paths per pixel (the
+    renderer's own denoise pass; HDR read back)."""
+    from . import abi
+    import copy
+    p = copy.deepcopy(params)
+    p.path_tracing.denoiser = abi.DENOISE_ATROUS
+    renderer.reset_view()
+    renderer.record_frames(1, spp, p)
+    return renderer.read_hdr().view(np.float16)[..., :3].astype(np.float32)
+
+
+def train(net, pairs, steps, batch=4, lr=2e-3, seed=0, log_every=0):
+    """Adam on random batches of `pairs` ((acc, albedo, normal) at spp, target
+    radiance, spp); returns the losses."""
+    t = net.torch
+    rng = np.random.default_rng(seed)
+    feats, targets = [], []
+    for (acc, alb, nor), target, spp in pairs:
+        feats.append(net.features(acc, alb, nor, spp))
+        targets.append(t.tensor(np.log1p(np.maximum(target, 0.0)).astype(np.float32), device=net.device))
+    losses = []
+    for step in range(steps):
+        idx = rng.choice(len(pairs), size=batch, replace=False)
+        x = t.cat([feats[i] for i in idx])
+        y = t.stack([targets[i] for i in idx])
+        rate = lr * (0.1 + 0.9 * 0.5 * (1 + np.cos(np.pi * step / steps)))  # cosine decay to lr / 10
+        losses.append(net.train_step(x, y, lr=float(rate)))
+    return [float(v) for v in t.stack(losses).cpu().numpy().ravel()]
+
+
+def luminance_rmse(a, b):
+    w = np.array([0.2126, 0.7152, 0.0722])
+    return float(np.sqrt(np.mean(((np.asarray(a, np.float64) - np.asarray(b, np.float64)) @ w) ** 2)))
+
+
+def study(renderer, cfg, train_views, test_views, low_spp=4, train_spp=256, test_spp=1024, steps=400,
+          batch=4, seed=0):
+    """Trains a U-Net on (low_spp, train_spp) pairs of `train_views` and compares
+    it with the raw accumulation and the a-trous denoiser on `test_views`
+    (luminance RMSE against test_spp renders)."""
+    import time
+    t0 = time.perf_counter()
+    pairs = [(*render_pair(renderer, p, low_spp, train_spp), low_spp) for p in train_views]
+    data_s = time.perf_counter() - t0
+    net = UNet(seed=seed)
+    t0 = time.perf_counter()
+    losses = train(net, pairs, steps, batch=batch, seed=seed)
+    train_s = time.perf_counter() - t0
+    rows = []
+    for p in test_views:
+        (acc, alb, nor), ref = render_pair(renderer, p, low_spp, test_spp)
+        raw = acc[..., :3] / low_spp
+        rows.append({"raw": luminance_rmse(raw, ref), "atrous": luminance_rmse(atrous(renderer, p, low_spp), ref),
+                     "unet": luminance_rmse(net.denoise(acc, alb, nor, low_spp), ref)})
+    mean = {k: float(np.mean([r[k] for r in rows])) for k in ("raw", "atrous", "unet")}
+    return {"net": net, "losses": losses, "per_view": rows, "mean_rmse": mean, "data_s": data_s,
+            "train_s": train_s, "pairs": len(pairs), "low_spp": low_spp, "train_spp": train_spp,
+            "test_spp": test_spp, "steps": steps, "batch": batch}

@@ -62,6 +62,9 @@ def parse():
                     help="instead of the path-tracing bench, run this many render requests (Poisson arrivals "
                          "at --serve-rate per second) over 8 resident phantoms through the request loop")
     ap.add_argument("--serve-rate", type=float, default=40.0)
+    ap.add_argument("--denoised-rmse", type=int, default=0,
+                    help="instead of the path-tracing bench, train the learned denoiser for this many steps on "
+                         "the head/neck workload at 1024^2 and time the fixed RMSE with it on held-out views")
     ap.add_argument("--denoiser-study", type=int, default=0,
                     help="instead of the path-tracing bench, train the learned denoiser for this many Adam steps "
                          "on pairs the tracer renders (4 vs 256 paths/pixel) and compare it with a-trous")
@@ -725,6 +728,58 @@ def run_denoiser_study(args):
                       "study": res}))
 
 
+def run_denoised_rmse(args):
+    """Time to the plain tracer's error with the learned denoiser, head/neck
+    workload at 1024^2. The U-Net is trained on 256^2 crops of 12 full-size
+    views (4, 16, 64 and 256 paths/pixel in, 1024 as target). On 4 held-out
+    views the plain tracer's image at 1024 paths/pixel (the fixed RMSE's
+    sample count) and the network's output, blended per pixel with the raw
+    mean by inverse variance, at 4 to 512 paths/pixel, are compared with a
+    reference of 4096 further, independent paths; the fewest paths/pixel at
+    which the blend is as close as the plain image, and the wall times of
+    both (render, readback, network)."""
+    import copy
+    from volview_gb300 import abi
+    from volview_gb300 import learned_denoiser as LD
+    from volview_gb300 import renderer as R
+    cfg = workload(args)
+    W, H = image_size(args)
+    ctx = R.Context(0)
+    r = R.Renderer(ctx, cfg["volume"], cfg["tf"])
+    r.set_labels(cfg["labels_vol"], abi.soft_struct(cfg["soft"]))
+    r.resize(W, H)
+    base = frame_params(cfg, list(r.center), r.diagonal, args.light_map)
+
+    def views(n, seed):
+        out = []
+        g = np.random.default_rng(seed)
+        for _ in range(n):
+            p = copy.deepcopy(base)
+            p.path_tracing.denoiser = abi.DENOISE_OFF
+            p.camera.yaw = abi.f32(base.camera.yaw + g.uniform(-0.6, 0.6))
+            p.camera.pitch = abi.f32(base.camera.pitch + g.uniform(-0.3, 0.3))
+            out.append(p)
+        return out
+
+    res = LD.time_to_rmse_study(r, views(12, 31), views(4, 32), steps=args.denoised_rmse)
+    res.pop("net")
+    losses = res.pop("losses")
+    res["loss_first"], res["loss_last"] = losses[0], float(np.mean(losses[-20:]))
+    spp = [v["spp_to_target"] for v in res["views"]]
+    # A view the blend does not bring to the plain error within 512 paths/pixel
+    # falls back to plain rendering (1x).
+    speedup = [v["plain_ms"] / v["denoised_ms"] if v["denoised_ms"] else 1.0 for v in res["views"]]
+    r.destroy()
+    ctx.destroy()
+    print(json.dumps({"metric": "time to the plain tracer's 1024-path error with the learned denoiser",
+                      "unit": "x faster (wall)", "higher_is_better": True,
+                      "value": float(np.median(speedup)), "speedup_per_view": speedup,
+                      "config": {"workload": bench_config(args, 1)["workload"],
+                                 "views": "yaw +-0.6, pitch +-0.3 around the default view (training and held-out "
+                                          "from different seeds)"},
+                      "paths_per_pixel_to_target": spp, "study": res}))
+
+
 def cpu_renderer_from_device(cfg, r, params):
     """The oracle's CPU renderer with the device's pre-pass volumes (bit-exact or
     within one quantum of the oracle's own, see tests) so only the path tracer
@@ -830,6 +885,9 @@ def main():
     elif args.denoiser_study > 0:
         if rank == 0:
             run_denoiser_study(args)
+    elif args.denoised_rmse > 0:
+        if rank == 0:
+            run_denoised_rmse(args)
     else:
         run_ours(args, rank, world, local)
     if world > 1:

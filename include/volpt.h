@@ -288,7 +288,8 @@ vv_status vv_record(vv_renderer* r, uint64_t frame, const vv_frame_params* param
  * consecutive passes overlapping); the denoiser and display passes run once,
  * after the last.
  * Equivalent to `frames` calls of vv_record except that intermediate displays
- * are skipped. frames x width x height may not exceed 2^31 (VV_ERR_LIMIT).
+ * are skipped. A pass holds at most 2^31 (frame, pixel) pairs; longer calls
+ * take more passes.
  * No counterpart in the reference. */
 vv_status vv_record_frames(vv_renderer* r, uint64_t first_frame, uint32_t frames,
                            const vv_frame_params* params);

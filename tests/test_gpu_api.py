@@ -122,13 +122,18 @@ def test_render_to_rgba(small_cfg, gpu_ctx):
     r.destroy()
 
 
-def test_record_frames_rejects_too_many_items(rend):
+def test_record_frames_runs_long_calls_as_several_passes(rend):
+    """70 frames at 2048x1024 take two passes (at most 64 frames each): all 70
+    are accumulated, as 70 single-frame records would."""
     cfg, r, p = rend
     r.resize(2048, 1024)
-    with pytest.raises(R.VolptError) as e:
-        r.record_frames(1, 1025, p)
-    assert e.value.status == abi.VV_ERR_LIMIT
-    assert r.accumulated_samples() == 0
+    before = r.kernel_launches()
+    r.record_frames(1, 70, p)
+    r.synchronize()
+    assert r.accumulated_samples() == 70
+    assert r.kernel_launches() - before > 2 * 10  # two passes of waves
+    acc, _, _ = r.read_accumulation(normal=False)
+    assert np.isfinite(acc).all() and acc[..., 3].max() <= 70.0
 
 
 def test_rmse_estimate_matches_a_converged_render(rend):

@@ -1485,17 +1485,18 @@ extern "C" vv_status vv_record_frames(vv_renderer* r, uint64_t first_frame, uint
     if (!params->path_tracing.enabled)
         return fail(VV_ERR_ARG, "vv_record_frames accumulates path-traced frames (path_tracing.enabled = 0)");
     if (frames == 0) return VV_OK;
-    // Work items are (frame, pixel) pairs counted in 32 bits on the device,
-    // with room left for the counter's overshoot at the end of the pass.
-    if ((uint64_t)frames * r->width * r->height > (1ull << 31))
-        return fail(VV_ERR_LIMIT, "at most 2^31 (frame, pixel) pairs per vv_record_frames call; split the frames");
+    if (!r->accum.p) return fail(VV_ERR_STATE, "resize() must be called before record()");
     // Long calls run as passes of at most VV_SUBPASS_FRAMES frames on the pass
     // streams in turn, so that each pass's last waves overlap the next one's
     // first (one long pass refilling its slots ran at 327 M path samples/s
     // at 1024^2, 64-frame passes in turn at 339); only the last one displays.
+    // A pass's work items, (frame, pixel) pairs, are counted in 32 bits on the
+    // device with room for the counter's overshoot: at most 2^31 per pass.
+    const uint64_t px = (uint64_t)r->width * r->height;
+    const uint32_t per_pass = (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>(VV_SUBPASS_FRAMES, (1ull << 31) / px));
     uint32_t done = 0;
     while (done < frames) {
-        uint32_t n = std::min<uint32_t>(frames - done, VV_SUBPASS_FRAMES);
+        uint32_t n = std::min<uint32_t>(frames - done, per_pass);
         UHead u;
         vv_status s = prepare_frame(r, *params, first_frame + done + n - 1, u);
         if (s != VV_OK) return s;

@@ -5,7 +5,9 @@ Input: 16 channels from an accumulation (log(1 + radiance), albedo, normal,
 zeros; vv_nn_features). Levels of 32, 48, 64, 80 and 96 channels, two 3x3
 convolutions with ReLU each, 2x2 average pooling down, nearest upsampling up,
 skip connections by concatenation; a 3x3 head of 16 channels whose first 3
-are log(1 + radiance). FP16 weights and activations, FP32 accumulation in
+are log(1 + radiance). (A residual connection from the input's log radiance
+to the prediction, tried, trained far slower at 4 paths per pixel: the
+network then has to cancel the fireflies instead of ignoring them.) FP16 weights and activations, FP32 accumulation in
 every convolution, FP32 master weights for Adam, an L1 loss in log radiance
 with its gradient scaled by GRAD_SCALE so that FP16 gradients stay normal.
 
@@ -300,9 +302,12 @@ def atrous(renderer, params, spp):
     return renderer.read_hdr().view(np.float16)[..., :3].astype(np.float32)
 
 
-def train(net, pairs, steps, batch=4, lr=2e-3, seed=0, log_every=0):
+def train(net, pairs, steps, batch=4, lr=1e-3, seed=0, log_every=0):
     """Adam on random batches of `pairs` ((acc, albedo, normal) at spp, target
-    radiance, spp); returns the losses."""
+    radiance, spp), the learning rate rising linearly over the first fifth of
+    the steps (at most 100: Adam's first steps move every weight by the full
+    rate, which can blow up a deep ReLU network) and then decaying as a cosine
+    to a tenth; returns the losses."""
     t = net.torch
     rng = np.random.default_rng(seed)
     feats, targets = [], []
@@ -314,7 +319,8 @@ def train(net, pairs, steps, batch=4, lr=2e-3, seed=0, log_every=0):
         idx = rng.choice(len(pairs), size=batch, replace=False)
         x = t.cat([feats[i] for i in idx])
         y = t.stack([targets[i] for i in idx])
-        rate = lr * (0.1 + 0.9 * 0.5 * (1 + np.cos(np.pi * step / steps)))  # cosine decay to lr / 10
+        warm = max(1, min(100, steps // 5))
+        rate = lr * min(1.0, (step + 1) / warm) * (0.1 + 0.9 * 0.5 * (1 + np.cos(np.pi * step / steps)))
         losses.append(net.train_step(x, y, lr=float(rate)))
     return [float(v) for v in t.stack(losses).cpu().numpy().ravel()]
 
@@ -347,3 +353,120 @@ def study(renderer, cfg, train_views, test_views, low_spp=4, train_spp=256, test
     return {"net": net, "losses": losses, "per_view": rows, "mean_rmse": mean, "data_s": data_s,
             "train_s": train_s, "pairs": len(pairs), "low_spp": low_spp, "train_spp": train_spp,
             "test_spp": test_spp, "steps": steps, "batch": batch}
+
+
+# ------------------------------------------------------- time to a fixed RMSE
+def crop_pairs(low, target, spp, size, count, rng):
+    """`count` random size x size crops (aligned to 16) of one view's
+    accumulation sums `low` (acc, albedo, normal) and target radiance."""
+    h, w = target.shape[:2]
+    out = []
+    for _ in range(count):
+        y = int(rng.integers(0, (h - size) // 16 + 1)) * 16
+        x = int(rng.integers(0, (w - size) // 16 + 1)) * 16
+        sl = (slice(y, y + size), slice(x, x + size))
+        out.append((tuple(np.ascontiguousarray(a[sl]) for a in low), np.ascontiguousarray(target[sl]), spp))
+    return out
+
+
+def mean_variance(acc, alb, spp):
+    """Per-pixel variance of the mean luminance after spp paths, from the sums of
+    luminance (radiance sums) and squared luminance (albedo guide's w)."""
+    w = np.array([0.2126, 0.7152, 0.0722])
+    s1 = np.asarray(acc, np.float64)[..., :3] @ w
+    s2 = np.asarray(alb, np.float64)[..., 3]
+    return np.maximum(s2 - s1 * s1 / spp, 0.0) / (spp - 1.0) / spp
+
+
+def blend(net_rgb, acc, alb, spp, eps2):
+    """The network's image and the raw mean mixed per pixel by inverse variance:
+    the raw mean's (estimated) against the network's error eps2 (calibrated)."""
+    var = mean_variance(acc, alb, spp)[..., None]
+    w = var / (var + eps2)
+    return w * net_rgb + (1.0 - w) * np.asarray(acc, np.float64)[..., :3] / spp
+
+
+def time_to_rmse_study(renderer, train_views, test_views, levels=(4, 8, 16, 32, 64, 128, 256, 512),
+                       train_levels=(4, 16, 64, 256), train_spp=1024, plain_spp=1024, ref_spp=4096, crops=12,
+                       steps=1500, seed=0):
+    """Trains the U-Net on crops of full-size renders (inputs at `train_levels`
+    paths/pixel, targets at train_spp), calibrates its error, then on each
+    held-out view compares the plain tracer at plain_spp with the network (and
+    its inverse-variance blend with the raw mean) at each of `levels`, all
+    against a reference of ref_spp further, independent paths (samples
+    plain_spp .. plain_spp + ref_spp - 1): the fewest paths/pixel at which the
+    blend's luminance RMSE is at most the plain image's, and the wall time of
+    each (render, readback, network)."""
+    import time
+    import torch
+    from . import convergence as CV
+    rng = np.random.default_rng(seed)
+    t0 = time.perf_counter()
+    pairs = []
+    for p in train_views:
+        renderer.reset_view()
+        done, lows = 0, {}
+        for lv in sorted(train_levels):
+            renderer.record_frames(1 + done, lv - done, p)
+            done = lv
+            lows[lv] = renderer.read_accumulation()
+        renderer.record_frames(1 + done, train_spp - done, p)
+        acc, _, _ = renderer.read_accumulation(normal=False)
+        target = acc[..., :3] / train_spp
+        for lv, low in lows.items():
+            pairs += crop_pairs(low, target, lv, 256, crops, rng)
+    data_s = time.perf_counter() - t0
+    net = UNet(seed=seed)
+    t0 = time.perf_counter()
+    losses = train(net, pairs, steps, batch=4, seed=seed)
+    train_s = time.perf_counter() - t0
+    # The network's error: its mean squared luminance error against the
+    # targets on training views, less the targets' own estimated noise.
+    eps = []
+    for p in train_views[:4]:
+        renderer.reset_view()
+        cal = max(train_levels)
+        renderer.record_frames(1, cal, p)
+        a, b, c = renderer.read_accumulation()
+        renderer.record_frames(1 + cal, train_spp - cal, p)
+        acc, alb, _ = renderer.read_accumulation(normal=False)
+        err2 = luminance_rmse(net.denoise(a, b, c, cal), acc[..., :3] / train_spp) ** 2
+        eps.append(max(err2 - CV.rmse_estimate(acc, alb, train_spp) ** 2, 1e-9))
+    eps2 = float(np.mean(eps))
+    views = []
+    for p in test_views:
+        renderer.reset_view()
+        done, lows = 0, {}
+        for lv in list(levels) + [plain_spp]:
+            renderer.record_frames(1 + done, lv - done, p)
+            done = lv
+            lows[lv] = renderer.read_accumulation()
+        renderer.record_frames(1 + done, ref_spp, p)
+        acc, _, _ = renderer.read_accumulation(normal=False)
+        ref = (acc[..., :3] - lows[plain_spp][0][..., :3]) / ref_spp
+        plain = luminance_rmse(lows[plain_spp][0][..., :3] / plain_spp, ref)
+        rmse = {}
+        for lv in levels:
+            a, b, c = lows[lv]
+            out = net.denoise(a, b, c, lv)
+            rmse[lv] = {"raw": luminance_rmse(a[..., :3] / lv, ref), "unet": luminance_rmse(out, ref),
+                        "blend": luminance_rmse(blend(out, a, b, lv, eps2), ref)}
+        reached = [lv for lv in levels if rmse[lv]["blend"] <= plain]
+        spp = reached[0] if reached else None
+
+        def wall(n, denoise):
+            renderer.reset_view()
+            renderer.synchronize()
+            t = time.perf_counter()
+            renderer.record_frames(1, n, p)
+            a2, b2, c2 = renderer.read_accumulation()
+            if denoise:
+                blend(net.denoise(a2, b2, c2, n), a2, b2, n, eps2)
+            torch.cuda.synchronize()
+            return (time.perf_counter() - t) * 1e3
+
+        views.append({"plain_rmse": plain, "rmse": {str(k): v for k, v in rmse.items()}, "spp_to_target": spp,
+                      "plain_ms": wall(plain_spp, False), "denoised_ms": wall(spp, True) if spp else None})
+    return {"net": net, "losses": losses, "views": views, "data_s": data_s, "train_s": train_s, "eps": eps2 ** 0.5,
+            "pairs": len(pairs), "train_levels": list(train_levels), "train_spp": train_spp, "plain_spp": plain_spp,
+            "ref_spp": ref_spp, "steps": steps}

@@ -45,3 +45,18 @@ def test_optics_recipe():
     r, g, b, w = scene.optics(scene.MUSCLES)
     assert w == 1.0 and r < g < b
     assert abs(g - 1.89 * (550 / 500) ** -1.286) < 1e-5
+
+
+def test_torso_recipe_is_the_small_phantom_scaled():
+    """The precision and serving workloads' torso: at 128^3 the scaled recipe
+    is the small phantom voxel for voxel; scaled, its regions keep their
+    proportions along each axis."""
+    from volview_gb300 import scene
+    hu, lab = scene.torso_phantom(1, (128, 128, 128))
+    h0, l0 = scene.small_phantom(1, 128)
+    assert np.array_equal(hu, h0) and np.array_equal(lab, l0)
+    hu2, lab2 = scene.torso_phantom(1, (64, 64, 100))
+    assert hu2.shape == (100, 64, 64) and lab2.shape == (100, 64, 64)
+    assert set(np.unique(lab2)) <= set(range(11))
+    frac0 = (l0 == 1).mean()
+    assert abs((lab2 == 1).mean() - frac0) < 0.25 * frac0  # the skull's share of the volume

@@ -162,7 +162,10 @@ typedef struct vv_clipping {
     int32_t all;
 } vv_clipping;
 
-enum { VV_DENOISE_OFF = 0, VV_DENOISE_ATROUS = 1, VV_DENOISE_OIDN = 2 };
+/* VV_DENOISE_LEARNED (no counterpart in the reference): the U-Net whose
+ * weights vv_set_denoiser_weights loaded, run on the accumulation before the
+ * display passes. */
+enum { VV_DENOISE_OFF = 0, VV_DENOISE_ATROUS = 1, VV_DENOISE_OIDN = 2, VV_DENOISE_LEARNED = 3 };
 
 /* Option<PathTracing> (renderer.rs:333-373); enabled = 0 is None. */
 typedef struct vv_path_tracing {
@@ -334,6 +337,12 @@ vv_status vv_read_volume(vv_renderer* r, int which, void* out, size_t capacity);
 
 /* Kernel launches this renderer has issued since creation (for accounting). */
 uint64_t vv_kernel_launches(const vv_renderer* r);
+
+/* Weights of the learned denoiser (VV_DENOISE_LEARNED): `count` floats, its 19
+ * convolutions in order (e0a e0b e1a .. e4b, d3a d3b .. d0a d0b, head; see
+ * volview_gb300/learned_denoiser.py), each as weights [cout][3][3][cin] then
+ * biases [cout]. NULL unloads them. Waits for the renderer's work. */
+vv_status vv_set_denoiser_weights(vv_renderer* r, const float* params, size_t count);
 
 /* ------------------------------------------------------------------ serving */
 /* Extensions for a render-request loop over several renderers (no

@@ -67,6 +67,14 @@ vv_status vv_nn_adam(float* w, void* w16, const float* grad, float* m, float* v,
                      float beta1, float beta2, float eps, float grad_scale, int step, void* stream);
 /* y += x (FP16 tensors of count values). */
 vv_status vv_nn_add(void* y, const void* x, long count, void* stream);
+/* The same input over a padded wp x hp image (zeros outside w x h) from
+ * pixel-linear w x h accumulation images. */
+vv_status vv_nn_features_image(const float* accum, const float* albedo, const float* normal, float n, int w, int h,
+                               int wp, int hp, void* x, void* stream);
+/* The HDR store (RGBA16F, w x h) of a prediction over a padded width wp:
+ * exp(max(pred, 0)) - 1 of its first 3 channels, coverage accum.w / n. */
+vv_status vv_nn_prediction_to_hdr(const void* pred, int c, int wp, int w, int h, const float* accum, float n,
+                                  void* hdr, void* stream);
 /* rgb = exp(max(pred, 0)) - 1 of the first 3 of c channels (3 floats per pixel). */
 vv_status vv_nn_radiance(const void* pred, int c, long pixels, float* rgb, void* stream);
 

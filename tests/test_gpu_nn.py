@@ -187,3 +187,33 @@ def test_training_lowers_the_loss():
     X, T = dev(x, "half"), dev(tgt)
     losses = [float(host(net.train_step(X, T, lr=1e-3 * min(1.0, (k + 1) / 10)))[0]) for k in range(30)]
     assert losses[-1] < 0.7 * losses[0], losses
+
+
+def test_renderer_runs_the_network_as_its_denoiser(gpu_ctx, small_cfg):
+    """DENOISE_LEARNED: the renderer runs the loaded network on its own
+    accumulation before the display; its HDR image is the network's output
+    for the same accumulation read back (within FP16 rounding). Without
+    weights the mode is refused."""
+    from volview_gb300 import abi, scene
+    from volview_gb300 import renderer as R
+    cfg = small_cfg
+    r = R.Renderer(gpu_ctx, cfg["volume"], cfg["tf"])
+    r.set_labels(cfg["labels_vol"], abi.soft_struct(cfg["soft"]))
+    p = scene.frame_params_for(cfg, list(r.center), r.diagonal, denoiser=abi.DENOISE_LEARNED)
+    r.resize(96, 80)
+    with pytest.raises(R.VolptError) as e:
+        r.record(1, p)
+    assert e.value.status == abi.VV_ERR_STATE
+    net = LD.UNet(seed=9)
+    blob = net.weights_blob()
+    with pytest.raises(R.VolptError):
+        r.set_denoiser_weights(blob[:-1])
+    r.set_denoiser_weights(blob)
+    r.record_frames(1, 4, p)
+    hdr = r.read_hdr().view(np.float16).astype(np.float32)
+    acc, alb, nor = r.read_accumulation()
+    ref = net.denoise(acc, alb, nor, 4)
+    assert np.all(np.abs(hdr[..., :3] - ref) <= 2e-3 * np.abs(ref) + 1e-4)
+    assert np.allclose(hdr[..., 3], np.float16(acc[..., 3] / 4.0).astype(np.float32), atol=1e-3)
+    r.set_denoiser_weights(None)
+    r.destroy()

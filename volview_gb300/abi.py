@@ -17,7 +17,7 @@ LABEL_OFF, LABEL_TINT, LABEL_ISOLATE, LABEL_HYBRID = range(4)
 ENV_DOME, ENV_STUDIO, ENV_MAP = range(3)
 TONE_NONE, TONE_ACES, TONE_AGX = range(3)
 PLANE_SAGITTAL, PLANE_CORONAL, PLANE_AXIAL = range(3)
-DENOISE_OFF, DENOISE_ATROUS, DENOISE_OIDN = range(3)
+DENOISE_OFF, DENOISE_ATROUS, DENOISE_OIDN, DENOISE_LEARNED = range(4)
 VOLUME_DENSITY, VOLUME_NORMALS, VOLUME_MASK, VOLUME_LABELS, VOLUME_MAJORANT, VOLUME_SHADOW, VOLUME_AO = range(7)
 DENSITY_UNORM16, DENSITY_FP16, DENSITY_BF16, DENSITY_FP32 = range(4)
 SUMS_FP32, SUMS_KAHAN = range(2)

@@ -15,6 +15,7 @@
 #include <vector>
 
 #include "../../include/volpt.h"
+#include "../../include/volpt_nn.h"
 #include "vv_device.cuh"
 #include "vv_kernels.h"
 
@@ -263,6 +264,14 @@ struct vv_renderer {
     uint32_t sums = VV_SUMS_FP32, fp64_after = 0;
     DBuf comp[3], wide[3];
     bool wide_active = false;
+    // the learned denoiser (VV_DENOISE_LEARNED): its weights (FP16) and biases
+    // per convolution, and its tensors for the padded image size
+    struct UNet {
+        bool loaded = false;
+        DBuf w[19], b[19];
+        int wp = 0, hp = 0;
+        DBuf in, ea[5], eb[5], pool[5], up[4], cat[4], da[4], db[4], head;
+    } unet;
     vv_frame_params accumulated_params;
     // host staging for the label tables
     LabelTables* tables_host = nullptr;
@@ -716,6 +725,26 @@ extern "C" vv_status vv_renderer_destroy(vv_renderer* r) {
     for (DBuf* b : all) b->release();
     free_tex_vol(r->shadow_tex);
     free_tex_vol(r->ao_tex);
+    {
+        auto& U = r->unet;
+        for (int k = 0; k < 19; k++) {
+            U.w[k].release();
+            U.b[k].release();
+        }
+        DBuf* t[] = {&U.in, &U.head};
+        for (DBuf* b : t) b->release();
+        for (int l = 0; l < 5; l++) {
+            U.ea[l].release();
+            U.eb[l].release();
+            U.pool[l].release();
+        }
+        for (int l = 0; l < 4; l++) {
+            U.up[l].release();
+            U.cat[l].release();
+            U.da[l].release();
+            U.db[l].release();
+        }
+    }
     if (r->tables_host) cudaFreeHost(r->tables_host);
     if (r->counters) cudaFree(r->counters);
     delete r;
@@ -1398,6 +1427,134 @@ static vv_status record_ray_march(vv_renderer* r, const vv_frame_params& p, cons
     return VV_OK;
 }
 
+// ------------------------------------------------------ learned denoiser
+// The U-Net of volview_gb300/learned_denoiser.py: levels of 32..96 channels,
+// two 3x3 convolutions (ReLU) per level, average pooling down, nearest
+// upsampling and concatenated skips up, a 16-channel head. Its 19
+// convolutions in order: e0a e0b e1a e1b e2a e2b e3a e3b e4a e4b, d3a d3b
+// d2a d2b d1a d1b d0a d0b, head.
+static const int UNET_LEVELS[5] = {32, 48, 64, 80, 96};
+static void unet_conv_shape(int k, int& cin, int& cout) {
+    if (k < 10) {  // encoder: level k / 2
+        int l = k / 2;
+        cout = UNET_LEVELS[l];
+        cin = (k % 2) ? cout : (l == 0 ? 16 : UNET_LEVELS[l - 1]);
+    } else if (k < 18) {  // decoder: level 3 - (k - 10) / 2
+        int l = 3 - (k - 10) / 2;
+        cout = UNET_LEVELS[l];
+        cin = ((k - 10) % 2) ? cout : UNET_LEVELS[l + 1] + UNET_LEVELS[l];
+    } else {
+        cin = UNET_LEVELS[0];
+        cout = 16;
+    }
+}
+
+extern "C" vv_status vv_set_denoiser_weights(vv_renderer* r, const float* params, size_t count) {
+    if (!r) return fail(VV_ERR_ARG, "null renderer");
+    vv_status st = use_device(r);
+    if (st != VV_OK) return st;
+    CK(cudaStreamSynchronize(r->ctx->stream));  // no display may be using the weights
+    if (!params) {
+        r->unet.loaded = false;
+        return VV_OK;
+    }
+    size_t expect = 0;
+    for (int k = 0; k < 19; k++) {
+        int cin, cout;
+        unet_conv_shape(k, cin, cout);
+        expect += (size_t)cout * 9 * cin + cout;
+    }
+    if (count != expect)
+        return fail(VV_ERR_ARG, "denoiser weights: " + std::to_string(count) + " floats, expected " + std::to_string(expect));
+    const float* p = params;
+    std::vector<uint16_t> half;
+    for (int k = 0; k < 19; k++) {
+        int cin, cout;
+        unet_conv_shape(k, cin, cout);
+        size_t nw = (size_t)cout * 9 * cin;
+        half.resize(nw);
+        for (size_t i = 0; i < nw; i++) {
+            _Float16 v = (_Float16)p[i];
+            std::memcpy(&half[i], &v, 2);
+        }
+        CK(r->unet.w[k].alloc(nw * 2));
+        CK(r->unet.b[k].alloc((size_t)cout * 4));
+        CK(cudaMemcpy(r->unet.w[k].p, half.data(), nw * 2, cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(r->unet.b[k].p, p + nw, (size_t)cout * 4, cudaMemcpyHostToDevice));
+        p += nw + cout;
+    }
+    r->unet.loaded = true;
+    return VV_OK;
+}
+
+// The network on the accumulation (n paths per pixel) into the HDR image, on
+// stream s, over the image padded to multiples of 256 pixels per axis.
+static vv_status run_unet(vv_renderer* r, float n, cudaStream_t s, int* launches) {
+    auto& U = r->unet;
+    const int W = (int)r->width, H = (int)r->height;
+    const int wp = (W + 255) / 256 * 256, hp = (H + 255) / 256 * 256;
+    if (U.wp != wp || U.hp != hp) {
+        CK(cudaStreamSynchronize(s));  // the buffers' previous use has ended
+        CK(U.in.alloc((size_t)wp * hp * 16 * 2));
+        CK(U.head.alloc((size_t)wp * hp * 16 * 2));
+        for (int l = 0; l < 5; l++) {
+            size_t px = (size_t)(wp >> l) * (hp >> l);
+            CK(U.ea[l].alloc(px * UNET_LEVELS[l] * 2));
+            CK(U.eb[l].alloc(px * UNET_LEVELS[l] * 2));
+            if (l) CK(U.pool[l].alloc(px * UNET_LEVELS[l - 1] * 2));
+            if (l < 4) {
+                CK(U.up[l].alloc(px * UNET_LEVELS[l + 1] * 2));
+                CK(U.cat[l].alloc(px * (UNET_LEVELS[l + 1] + UNET_LEVELS[l]) * 2));
+                CK(U.da[l].alloc(px * UNET_LEVELS[l] * 2));
+                CK(U.db[l].alloc(px * UNET_LEVELS[l] * 2));
+            }
+        }
+        U.wp = wp;
+        U.hp = hp;
+    }
+    void* st = (void*)s;
+    auto ok = [](vv_status v, const char* what) { return v == VV_OK ? VV_OK : fail(v, std::string("denoiser: ") + what); };
+    auto conv = [&](const DBuf& x, int l, int k, DBuf& y, int relu) {
+        int cin, cout;
+        unet_conv_shape(k, cin, cout);
+        *launches += 1;
+        return ok(vv_nn_conv3x3(x.p, 1, hp >> l, wp >> l, cin, U.w[k].p, U.b[k].as<float>(), cout, relu, y.p, st),
+                  "convolution");
+    };
+    vv_status v = ok(vv_nn_features_image(r->accum.as<float>(), r->albedo.as<float>(), r->normal.as<float>(), n, W, H,
+                                          wp, hp, U.in.p, st), "features");
+    *launches += 1;
+    const DBuf* x = &U.in;
+    for (int l = 0; l < 5 && v == VV_OK; l++) {
+        if (l) {
+            v = ok(vv_nn_avgpool2(U.eb[l - 1].p, 1, hp >> (l - 1), wp >> (l - 1), UNET_LEVELS[l - 1], U.pool[l].p, 0,
+                                  st), "pooling");
+            *launches += 1;
+            x = &U.pool[l];
+        }
+        if (v == VV_OK) v = conv(*x, l, 2 * l, U.ea[l], 1);
+        if (v == VV_OK) v = conv(U.ea[l], l, 2 * l + 1, U.eb[l], 1);
+    }
+    const DBuf* y = &U.eb[4];
+    int cy = UNET_LEVELS[4];
+    for (int l = 3; l >= 0 && v == VV_OK; l--) {
+        v = ok(vv_nn_upsample2(y->p, 1, hp >> (l + 1), wp >> (l + 1), cy, U.up[l].p, 0, st), "upsampling");
+        long px = (long)(wp >> l) * (hp >> l);
+        if (v == VV_OK) v = ok(vv_nn_concat(U.up[l].p, cy, U.eb[l].p, UNET_LEVELS[l], px, U.cat[l].p, st), "concat");
+        *launches += 2;
+        int k = 10 + 2 * (3 - l);
+        if (v == VV_OK) v = conv(U.cat[l], l, k, U.da[l], 1);
+        if (v == VV_OK) v = conv(U.da[l], l, k + 1, U.db[l], 1);
+        y = &U.db[l];
+        cy = UNET_LEVELS[l];
+    }
+    if (v == VV_OK) v = conv(*y, 0, 18, U.head, 0);
+    if (v == VV_OK)
+        v = ok(vv_nn_prediction_to_hdr(U.head.p, 16, wp, W, H, r->accum.as<float>(), n, r->hdr.p, st), "HDR store");
+    *launches += 1;
+    return v;
+}
+
 // One path-tracing pass of `frames` accumulate-frames and its display
 // (record, renderer.rs:1770-1797). The pass runs on its own stream into its own
 // sums, starting after this call's set-up work (if it queued any) and after
@@ -1462,6 +1619,10 @@ static vv_status record_pass(vv_renderer* r, const vv_frame_params& p, UHead& u,
     }
     launches += 1;
     if (display && p.path_tracing.denoiser == VV_DENOISE_ATROUS) CK(launch_denoise(pa, s, &launches));
+    if (display && p.path_tracing.denoiser == VV_DENOISE_LEARNED) {
+        vv_status v = run_unet(r, (float)(r->accumulated + spf), s, &launches);
+        if (v != VV_OK) return v;
+    }
     r->accumulated += spf;
     if (display && p.path_tracing.denoiser != VV_DENOISE_OIDN) CK(launch_post(pa, s, &launches));
     CK(cudaEventRecord(P.shown, s));
@@ -1470,8 +1631,15 @@ static vv_status record_pass(vv_renderer* r, const vv_frame_params& p, UHead& u,
     return VV_OK;
 }
 
+static vv_status check_denoiser(const vv_renderer* r, const vv_frame_params* params) {
+    if (params->path_tracing.enabled && params->path_tracing.denoiser == VV_DENOISE_LEARNED && !r->unet.loaded)
+        return fail(VV_ERR_STATE, "the learned denoiser has no weights (vv_set_denoiser_weights)");
+    return VV_OK;
+}
+
 extern "C" vv_status vv_record(vv_renderer* r, uint64_t frame, const vv_frame_params* params) {
     if (!r || !params) return fail(VV_ERR_ARG, "null argument");
+    if (check_denoiser(r, params) != VV_OK) return VV_ERR_STATE;
     UHead u;
     vv_status s = prepare_frame(r, *params, frame, u);
     if (s != VV_OK) return s;
@@ -1486,6 +1654,7 @@ extern "C" vv_status vv_record_frames(vv_renderer* r, uint64_t first_frame, uint
         return fail(VV_ERR_ARG, "vv_record_frames accumulates path-traced frames (path_tracing.enabled = 0)");
     if (frames == 0) return VV_OK;
     if (!r->accum.p) return fail(VV_ERR_STATE, "resize() must be called before record()");
+    if (check_denoiser(r, params) != VV_OK) return VV_ERR_STATE;
     // Long calls run as passes of at most VV_SUBPASS_FRAMES frames on the pass
     // streams in turn, so that each pass's last waves overlap the next one's
     // first (one long pass refilling its slots ran at 327 M path samples/s

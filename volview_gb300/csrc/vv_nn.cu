@@ -320,6 +320,43 @@ __global__ void k_radiance(const __half* __restrict__ pred, int c, long pixels, 
     for (int k = 0; k < 3; k++) rgb[p * 3 + k] = expm1f(fmaxf(__half2float(pred[p * c + k]), 0.0f));
 }
 
+// The network's input over a padded image (wp x hp, zeros outside the w x h
+// image) from the renderer's own accumulation images (pixel-linear RGBA32F).
+__global__ void k_features_image(const float4* __restrict__ accum, const float4* __restrict__ albedo,
+                                 const float4* __restrict__ normal, float n, int w, int h, int wp, int hp,
+                                 __half* __restrict__ x) {
+    long q = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= (long)wp * hp) return;
+    int px = (int)(q % wp), py = (int)(q / wp);
+    uint32_t* o = (uint32_t*)(x + q * 16);
+    if (px >= w || py >= h) {
+#pragma unroll
+        for (int k = 0; k < 8; k++) o[k] = 0u;
+        return;
+    }
+    long p = (long)py * w + px;
+    float4 a = accum[p], b = albedo[p], c = normal[p];
+    float inv = 1.0f / n;
+    float f[16] = {log1pf(fmaxf(a.x * inv, 0.0f)), log1pf(fmaxf(a.y * inv, 0.0f)), log1pf(fmaxf(a.z * inv, 0.0f)),
+                   b.x * inv, b.y * inv, b.z * inv, c.x * inv, c.y * inv, c.z * inv, 0, 0, 0, 0, 0, 0, 0};
+#pragma unroll
+    for (int k = 0; k < 8; k++) o[k] = pack(__float2half_rn(f[2 * k]), __float2half_rn(f[2 * k + 1]));
+}
+
+// The HDR store of a denoised image: rgb = exp(max(pred, 0)) - 1 of the
+// prediction (padded width wp, c channels), coverage from the accumulation.
+__global__ void k_prediction_to_hdr(const __half* __restrict__ pred, int c, int wp, int w, int h,
+                                    const float4* __restrict__ accum, float n, ushort4* __restrict__ hdr) {
+    long p = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= (long)w * h) return;
+    long q = (p / w) * wp + p % w;
+    const __half* v = pred + q * c;
+    float r = expm1f(fmaxf(__half2float(v[0]), 0.0f)), g = expm1f(fmaxf(__half2float(v[1]), 0.0f));
+    float b = expm1f(fmaxf(__half2float(v[2]), 0.0f)), a = accum[p].w / n;
+    hdr[p] = make_ushort4(__half_as_ushort(__float2half_rn(r)), __half_as_ushort(__float2half_rn(g)),
+                          __half_as_ushort(__float2half_rn(b)), __half_as_ushort(__float2half_rn(a)));
+}
+
 static inline unsigned blocks(long n, int t) { return (unsigned)((n + t - 1) / t); }
 
 }  // namespace nn
@@ -456,6 +493,22 @@ extern "C" vv_status vv_nn_add(void* y, const void* x, long count, void* stream)
     if (!y || !x || count < 0) return VV_ERR_ARG;
     if (count == 0) return VV_OK;
     k_add<<<blocks(count, 256), 256, 0, (cudaStream_t)stream>>>((__half*)y, (const __half*)x, count);
+    return launched();
+}
+
+extern "C" vv_status vv_nn_features_image(const float* accum, const float* albedo, const float* normal, float n,
+                                          int w, int h, int wp, int hp, void* x, void* stream) {
+    if (!accum || !albedo || !normal || !x || !(n > 0.0f) || w <= 0 || h <= 0 || wp < w || hp < h) return VV_ERR_ARG;
+    k_features_image<<<blocks((long)wp * hp, 256), 256, 0, (cudaStream_t)stream>>>(
+        (const float4*)accum, (const float4*)albedo, (const float4*)normal, n, w, h, wp, hp, (__half*)x);
+    return launched();
+}
+
+extern "C" vv_status vv_nn_prediction_to_hdr(const void* pred, int c, int wp, int w, int h, const float* accum,
+                                             float n, void* hdr, void* stream) {
+    if (!pred || !accum || !hdr || c < 3 || w <= 0 || h <= 0 || wp < w || !(n > 0.0f)) return VV_ERR_ARG;
+    k_prediction_to_hdr<<<blocks((long)w * h, 256), 256, 0, (cudaStream_t)stream>>>(
+        (const __half*)pred, c, wp, w, h, (const float4*)accum, n, (ushort4*)hdr);
     return launched();
 }
 

@@ -107,6 +107,15 @@ class UNet:
         return {n: (p["w16"].float().cpu().numpy().astype(np.float64), p["b"].cpu().numpy().astype(np.float64))
                 for n, p in self.params.items()}
 
+    def weights_blob(self):
+        """The weights as vv_set_denoiser_weights takes them: every convolution
+        in plan order, its weights [cout][3][3][cin] then its biases."""
+        parts = []
+        for name in self.shapes:
+            p = self.params[name]
+            parts += [p["w"].float().cpu().numpy().ravel(), p["b"].float().cpu().numpy().ravel()]
+        return np.concatenate(parts).astype(np.float32)
+
     def state(self):
         return {n: (p["w"].cpu().numpy(), p["b"].cpu().numpy()) for n, p in self.params.items()}
 

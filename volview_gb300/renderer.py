@@ -55,6 +55,7 @@ EXPORTS = [
     ("vv_query", C.c_int, [P, P]),
     ("vv_renderer_memory", C.c_int, [P, P]),
     ("vv_reset_view", C.c_int, [P]),
+    ("vv_set_denoiser_weights", C.c_int, [P, P, C.c_size_t]),
     ("vv_denoise_atrous_noalloc", C.c_int, [P, P, P, P, C.c_uint32, C.c_uint32, C.c_uint32, P]),
 ]
 # Test hooks (include/volpt_probe.h).
@@ -83,6 +84,8 @@ NN = [
     ("vv_nn_adam", I, [P, P, P, P, P, L, F, F, F, F, F, I, P]),
     ("vv_nn_add", I, [P, P, L, P]),
     ("vv_nn_radiance", I, [P, I, L, P, P]),
+    ("vv_nn_features_image", I, [P, P, P, F, I, I, I, I, P, P]),
+    ("vv_nn_prediction_to_hdr", I, [P, I, I, I, I, P, F, P, P]),
 ]
 
 COUNT_NAMES = ["majorant", "cubic", "trilinear", "mask", "label", "normal", "gradient", "pixel", "path", "vertex"]
@@ -205,6 +208,15 @@ class Renderer:
         v = C.c_uint64(0)
         check(load().vv_renderer_memory(self.handle, C.byref(v)))
         return int(v.value)
+
+    def set_denoiser_weights(self, params):
+        """Loads the learned denoiser's weights (a flat float32 array, see
+        learned_denoiser.UNet.weights_blob) for DENOISE_LEARNED; None unloads."""
+        if params is None:
+            check(load().vv_set_denoiser_weights(self.handle, None, 0))
+            return
+        blob = np.ascontiguousarray(params, np.float32).ravel()
+        check(load().vv_set_denoiser_weights(self.handle, _ptr(blob), blob.size))
 
     def reset_view(self):
         """A new view: the accumulation restarts and auto exposure meters afresh."""

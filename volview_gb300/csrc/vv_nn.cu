@@ -32,36 +32,52 @@ __device__ __forceinline__ uint32_t pack(__half lo, __half hi) {
     return (uint32_t)__half_as_ushort(lo) | ((uint32_t)__half_as_ushort(hi) << 16);
 }
 
-// y = act(conv3x3(x, w) + bias): one warp per 16 consecutive output pixels of
-// a row, all COUT channels. The reduction runs over the 9 taps x CIN in steps
-// of 16 channels; a tap outside the image reads zeros (same padding).
+// y = act(conv3x3(x, w) + bias). A block of CONV_WARPS warps takes as many
+// 16-pixel row segments, one per warp, and all COUT channels. For each of the
+// 9 taps the block first copies that tap's weights (COUT x CIN) into shared
+// memory, rows padded to CIN + 8 halves so that the B fragment loads of a
+// warp fall in distinct banks; each warp then reduces over CIN in steps of 16
+// on the tensor cores, its A fragments (the input pixels at the tap's offset,
+// zeros outside the image: same padding) read as aligned 32-bit words.
 // Fragment layouts of m16n8k16 (g = lane / 4, t = lane % 4): A row g / g + 8,
 // columns 2t, 2t + 1 / + 8; B column g, rows 2t, 2t + 1 / + 8; C row g / g + 8,
 // columns 2t, 2t + 1.
+constexpr int CONV_WARPS = 8;
 template <int COUT>
-__global__ void __launch_bounds__(128) k_conv3x3(const __half* __restrict__ x, int n, int h, int w, int cin,
-                                                 const __half* __restrict__ wt, const float* __restrict__ bias,
-                                                 int relu, __half* __restrict__ y) {
+__global__ void __launch_bounds__(CONV_WARPS * 32) k_conv3x3(const __half* __restrict__ x, int n, int h, int w, int cin,
+                                                             const __half* __restrict__ wt,
+                                                             const float* __restrict__ bias, int relu,
+                                                             __half* __restrict__ y) {
     constexpr int NT = COUT / 8;
+    extern __shared__ __align__(16) unsigned char smem[];
+    __half* sw = (__half*)smem;
+    const int stride = cin + 8;  // halves per staged weight row
     const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
-    const long tile = (long)blockIdx.x * 4 + (threadIdx.x >> 5);  // 16-pixel tile
+    const long tile = (long)blockIdx.x * CONV_WARPS + (threadIdx.x >> 5);  // 16-pixel tile
     const long pixels = (long)n * h * w;
-    if (tile * 16 >= pixels) return;
-    const long p0 = tile * 16;
+    const bool active = tile * 16 < pixels;
+    const long p0 = active ? tile * 16 : 0;
     const int img = (int)(p0 / ((long)h * w));
     const int rem = (int)(p0 - (long)img * h * w);
     const int py = rem / w, px0 = rem % w;
     float acc[NT][4];
 #pragma unroll
     for (int j = 0; j < NT; j++) acc[j][0] = acc[j][1] = acc[j][2] = acc[j][3] = 0.0f;
+    const int chunks = COUT * (cin / 8);  // 16-byte pieces of one tap's weights
     for (int tap = 0; tap < 9; tap++) {
+        __syncthreads();  // the previous tap's weights are no longer read
+        for (int i = threadIdx.x; i < chunks; i += CONV_WARPS * 32) {
+            int co = i / (cin / 8), c8 = i % (cin / 8);
+            *(uint4*)(sw + co * stride + c8 * 8) = __ldg((const uint4*)(wt + ((long)co * 9 + tap) * cin + c8 * 8));
+        }
+        __syncthreads();
+        if (!active) continue;
         const int sy = py + tap / 3 - 1;
         const int sx0 = px0 + g + tap % 3 - 1, sx1 = sx0 + 8;
         const bool row_in = sy >= 0 && sy < h;
         const bool in0 = row_in && sx0 >= 0 && sx0 < w, in1 = row_in && sx1 >= 0 && sx1 < w;
         const __half* r0 = x + (((long)img * h + (row_in ? sy : 0)) * w + (in0 ? sx0 : 0)) * cin;
         const __half* r1 = x + (((long)img * h + (row_in ? sy : 0)) * w + (in1 ? sx1 : 0)) * cin;
-        const __half* wtap = wt + (long)tap * cin;
         for (int c0 = 0; c0 < cin; c0 += 16) {
             uint32_t a[4];
             a[0] = in0 ? ld32(r0 + c0 + 2 * t) : 0u;
@@ -70,12 +86,13 @@ __global__ void __launch_bounds__(128) k_conv3x3(const __half* __restrict__ x, i
             a[3] = in1 ? ld32(r1 + c0 + 8 + 2 * t) : 0u;
 #pragma unroll
             for (int j = 0; j < NT; j++) {
-                const __half* wr = wtap + (long)(j * 8 + g) * 9 * cin + c0 + 2 * t;
-                uint32_t b[2] = {ld32(wr), ld32(wr + 8)};
+                const __half* wr = sw + (j * 8 + g) * stride + c0 + 2 * t;
+                uint32_t b[2] = {*(const uint32_t*)wr, *(const uint32_t*)(wr + 8)};
                 mma16816(acc[j], a, b);
             }
         }
     }
+    if (!active) return;
     __half* o0 = y + (p0 + g) * COUT;
     __half* o1 = y + (p0 + g + 8) * COUT;
 #pragma unroll
@@ -373,21 +390,23 @@ extern "C" vv_status vv_nn_conv3x3(const void* x, int n, int h, int w, int cin, 
                                    const float* bias, int cout, int relu, void* y, void* stream) {
     if (!x || !weights || !y || n <= 0 || h <= 0 || w <= 0 || w % 16 || cin <= 0 || cin % 16) return VV_ERR_ARG;
     cudaStream_t s = (cudaStream_t)stream;
-    unsigned g = blocks((long)n * h * w / 16, 4);
+    unsigned g = blocks((long)n * h * w / 16, CONV_WARPS);
     const __half* X = (const __half*)x;
     const __half* W = (const __half*)weights;
     __half* Y = (__half*)y;
+    const size_t smem = (size_t)cout * (cin + 8) * sizeof(__half);
+    if (smem > 48 * 1024) return VV_ERR_ARG;  // one tap's weights staged in shared memory
     switch (cout) {
-        case 8: k_conv3x3<8><<<g, 128, 0, s>>>(X, n, h, w, cin, W, bias, relu, Y); break;
-        case 16: k_conv3x3<16><<<g, 128, 0, s>>>(X, n, h, w, cin, W, bias, relu, Y); break;
-        case 32: k_conv3x3<32><<<g, 128, 0, s>>>(X, n, h, w, cin, W, bias, relu, Y); break;
-        case 48: k_conv3x3<48><<<g, 128, 0, s>>>(X, n, h, w, cin, W, bias, relu, Y); break;
-        case 64: k_conv3x3<64><<<g, 128, 0, s>>>(X, n, h, w, cin, W, bias, relu, Y); break;
-        case 80: k_conv3x3<80><<<g, 128, 0, s>>>(X, n, h, w, cin, W, bias, relu, Y); break;
-        case 96: k_conv3x3<96><<<g, 128, 0, s>>>(X, n, h, w, cin, W, bias, relu, Y); break;
-        case 112: k_conv3x3<112><<<g, 128, 0, s>>>(X, n, h, w, cin, W, bias, relu, Y); break;
-        case 144: k_conv3x3<144><<<g, 128, 0, s>>>(X, n, h, w, cin, W, bias, relu, Y); break;
-        case 176: k_conv3x3<176><<<g, 128, 0, s>>>(X, n, h, w, cin, W, bias, relu, Y); break;
+        case 8: k_conv3x3<8><<<g, CONV_WARPS * 32, smem, s>>>(X, n, h, w, cin, W, bias, relu, Y); break;
+        case 16: k_conv3x3<16><<<g, CONV_WARPS * 32, smem, s>>>(X, n, h, w, cin, W, bias, relu, Y); break;
+        case 32: k_conv3x3<32><<<g, CONV_WARPS * 32, smem, s>>>(X, n, h, w, cin, W, bias, relu, Y); break;
+        case 48: k_conv3x3<48><<<g, CONV_WARPS * 32, smem, s>>>(X, n, h, w, cin, W, bias, relu, Y); break;
+        case 64: k_conv3x3<64><<<g, CONV_WARPS * 32, smem, s>>>(X, n, h, w, cin, W, bias, relu, Y); break;
+        case 80: k_conv3x3<80><<<g, CONV_WARPS * 32, smem, s>>>(X, n, h, w, cin, W, bias, relu, Y); break;
+        case 96: k_conv3x3<96><<<g, CONV_WARPS * 32, smem, s>>>(X, n, h, w, cin, W, bias, relu, Y); break;
+        case 112: k_conv3x3<112><<<g, CONV_WARPS * 32, smem, s>>>(X, n, h, w, cin, W, bias, relu, Y); break;
+        case 144: k_conv3x3<144><<<g, CONV_WARPS * 32, smem, s>>>(X, n, h, w, cin, W, bias, relu, Y); break;
+        case 176: k_conv3x3<176><<<g, CONV_WARPS * 32, smem, s>>>(X, n, h, w, cin, W, bias, relu, Y); break;
         default: return VV_ERR_ARG;
     }
     return launched();

@@ -127,9 +127,11 @@ extern "C" vv_status vv_context_create_on_stream(int device, void* stream, vv_co
     if (e != cudaSuccess || n == 0) return fail(VV_ERR_CUDA, "no CUDA device");
     if (device < 0 || device >= n) return fail(VV_ERR_ARG, "device index out of range");
     CK(cudaSetDevice(device));
+    int sms = 0;
+    CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
     vv_context* c = new vv_context();
     c->device = device;
-    CK(cudaDeviceGetAttribute(&c->sms, cudaDevAttrMultiProcessorCount, device));
+    c->sms = sms;
     if (stream) {
         c->stream = (cudaStream_t)stream;
     } else {

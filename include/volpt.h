@@ -263,6 +263,8 @@ vv_status vv_renderer_create_ex(vv_context* ctx, const vv_volume* volume, const 
                                 const vv_precision* precision, vv_renderer** out);
 /* Renderer::destroy (renderer.rs:2072). */
 vv_status vv_renderer_destroy(vv_renderer* r);
+/* The renderer's public fields bounds, min_spacing, center and diagonal
+ * (renderer.rs:545-551), and the volume's dimensions. */
 vv_status vv_renderer_get_info(const vv_renderer* r, vv_renderer_info* out);
 /* Renderer::default_camera (renderer.rs:944-946). */
 vv_status vv_default_camera(const vv_renderer* r, vv_orbit_camera* out);

@@ -35,7 +35,7 @@ vv_status vv_probe_paths(vv_renderer* r, const vv_frame_params* params, uint32_t
 vv_status vv_count_events(vv_renderer* r, int enable, uint64_t* out, size_t n);
 
 /* Device time of the path-tracing launches: enable = 1 starts recording CUDA
- * events around each launch on the renderer's stream; enable = 0 stops, waits,
+ * events around each launch on the stream it runs on; enable = 0 stops, waits,
  * and returns the summed milliseconds and the number of launches. */
 vv_status vv_time_pt(vv_renderer* r, int enable, double* ms, uint64_t* launches);
 

@@ -13,7 +13,7 @@
  *  - The renderer owns its device memory; inputs are borrowed and copied.
  *  - One renderer per host thread; calls on one renderer are serialised. Device
  *    work is ordered on the context's CUDA stream: path-tracing passes run on
- *    two streams of the renderer, and the context stream waits for each
+ *    the renderer's own streams (six passes in turn), and the context stream waits for each
  *    record's display, so work queued on it afterwards (readbacks, the caller's
  *    own kernels) sees the frame; consecutive records overlap on the device.
  *  - There is no CPU fallback: without a CUDA device every call that needs one
@@ -36,7 +36,8 @@ typedef enum vv_status {
     VV_ERR_ARG = 1,     /* invalid argument (null pointer, size mismatch, bad enum) */
     VV_ERR_OOM = 2,     /* device allocation failed */
     VV_ERR_CUDA = 3,    /* CUDA runtime error or no device */
-    VV_ERR_TIMEOUT = 4, /* a bounded device-side wait ran out */
+    VV_ERR_TIMEOUT = 4, /* a bounded device-side wait ran out (reserved: no kernel
+                           of this library waits on another) */
     VV_ERR_STATE = 5,   /* call out of order (e.g. record before resize) */
     VV_ERR_LIMIT = 6    /* size above a documented maximum */
 } vv_status;

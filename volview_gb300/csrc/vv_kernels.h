@@ -50,7 +50,7 @@ struct PtArgs {
     uint32_t frames;            // accumulate-frames in this launch
     uint32_t tiles_x, tiles_y;  // 8x4-pixel tiles
     uint32_t* counter;          // work-item counter, zero at launch
-    int32_t* status;            // device status word (0 ok)
+    int32_t* status;            // device status word (0 ok; read by vv_synchronize, written by no kernel)
     int persistent;             // 1: persistent warps with path regeneration
     int write_hdr;              // 1: accum/albedo/normal are the totals and a single-frame pass writes each
                                 // pixel's HDR as it finishes; 0: they are the pass's own sums (merged later)

@@ -121,6 +121,20 @@ def test_a_request_that_cannot_fit_is_refused():
         srv.step()
 
 
+def test_a_request_too_large_for_its_idle_renderer_is_refused():
+    """The volume's renderer is resident and idle, nothing runs, and even with
+    every other renderer evicted the request does not fit: refused, not polled
+    for ever."""
+    bases = {"a": 10 ** 9, "b": 10 ** 9}
+    srv, log, made = make_server(3 * 10 ** 9, bases)
+    srv.preload("a")
+    srv.preload("b")
+    srv.submit(S.Request("a", 8192, 8192, 16, params=0))  # ~9.5 GB of image and path state
+    with pytest.raises(MemoryError):
+        srv.step()
+    assert [e for e in log if e[0] == "destroy"] == [("destroy", "b")]  # evicted trying
+
+
 def test_shortest_first_with_aging():
     bases = {"a": 10 ** 9}
     srv, log, made = make_server(10 ** 12, bases, ticks=5, max_active=1, order="shortest", aging_s=40)

@@ -159,7 +159,10 @@ class Server:
                 continue
             need = self._need(req, r)
             if not self._evict(need, r):
-                if not self.active and r is None and not self.idle:
+                # Nothing runs and every other idle renderer is gone: no later
+                # step frees memory (a new renderer in place of `r` would need
+                # the same bytes), so the request can never start.
+                if not self.active and all(x is r for x in self.idle):
                     raise MemoryError(f"request {req.id} needs {need} bytes, budget {self.budget}")
                 continue
             self.queue.remove(req)

@@ -1,7 +1,7 @@
 """Host-side scene generation: phantoms, label recipes, soft grids (CPU)."""
 import numpy as np
 
-from volview_gb300 import abi, scene
+from volview_gb300 import scene
 
 
 def test_small_phantom_recipe():

@@ -1469,19 +1469,19 @@ extern "C" vv_status vv_set_denoiser_weights(vv_renderer* r, const float* params
     if (count != expect)
         return fail(VV_ERR_ARG, "denoiser weights: " + std::to_string(count) + " floats, expected " + std::to_string(expect));
     const float* p = params;
-    std::vector<uint16_t> half;
+    std::vector<uint16_t> w16;
     for (int k = 0; k < 19; k++) {
         int cin, cout;
         unet_conv_shape(k, cin, cout);
         size_t nw = (size_t)cout * 9 * cin;
-        half.resize(nw);
+        w16.resize(nw);
         for (size_t i = 0; i < nw; i++) {
             _Float16 v = (_Float16)p[i];
-            std::memcpy(&half[i], &v, 2);
+            std::memcpy(&w16[i], &v, 2);
         }
         CK(r->unet.w[k].alloc(nw * 2));
         CK(r->unet.b[k].alloc((size_t)cout * 4));
-        CK(cudaMemcpy(r->unet.w[k].p, half.data(), nw * 2, cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(r->unet.w[k].p, w16.data(), nw * 2, cudaMemcpyHostToDevice));
         CK(cudaMemcpy(r->unet.b[k].p, p + nw, (size_t)cout * 4, cudaMemcpyHostToDevice));
         p += nw + cout;
     }
@@ -1576,8 +1576,8 @@ static vv_status record_pass(vv_renderer* r, const vv_frame_params& p, UHead& u,
         CK(cudaStreamWaitEvent(s, r->prep_done, 0));
         r->prep_work = false;
     }
-    const char* k = std::getenv("VV_PT_KERNEL");
-    if (k) CK(cudaStreamWaitEvent(s, prev.shown, 0));  // the single-kernel tracers share one work counter
+    const char* single = std::getenv("VV_PT_KERNEL");
+    if (single) CK(cudaStreamWaitEvent(s, prev.shown, 0));  // the single-kernel tracers share one work counter
     uint32_t spf = std::max(p.path_tracing.samples_per_frame, 1u);
     size_t bytes = (size_t)r->width * r->height * 16;
     CK(cudaMemsetAsync(P.accum.p, 0, bytes, s));

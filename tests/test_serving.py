@@ -3,7 +3,8 @@ request finishes with its own result, device memory stays within the budget,
 renderers are reused per volume and evicted least recently used first,
 requests that arrive while others run start without waiting for them, a
 request that can never fit is refused, shortest-first admission with aging,
-and the per-volume renderer limit."""
+the per-volume renderer limit, and the memory model against the constants the
+library allocates with."""
 import pytest
 
 from volview_gb300 import serving as S
@@ -170,3 +171,28 @@ def test_request_bytes_model():
     assert S.request_bytes(1024, 1024, 16) == 1024 * 1024 * (S.IMAGE_BYTES_PER_PIXEL + 16 * S.SLOT_BYTES)
     assert S.request_bytes(1024, 1024, 1024) == 1024 * 1024 * S.IMAGE_BYTES_PER_PIXEL + 6 * (1 << 24) * S.SLOT_BYTES
     assert S.request_bytes(4096, 4096, 1) == 4096 * 4096 * (S.IMAGE_BYTES_PER_PIXEL + S.SLOT_BYTES)
+
+
+def test_request_bytes_model_follows_the_library_sources():
+    """The model's constants are the ones the library allocates with: slot,
+    light-map sample and stage-queue bytes per path slot, passes in flight,
+    frames per pass, frames' worth of slots and the slot cap."""
+    import os
+    import re
+    csrc = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "volview_gb300", "csrc")
+    host = open(os.path.join(csrc, "vv_host.cpp")).read()
+    kernels = open(os.path.join(csrc, "vv_kernels.h")).read()
+
+    def num(pattern, text):
+        m = re.search(pattern, text)
+        assert m, pattern
+        return int(m.group(1))
+
+    slot = num(r"constexpr int WF_SLOT_BYTES = (\d+);", kernels)
+    light = num(r"constexpr int WF_MAP_BYTES = (\d+);", kernels)
+    queues = num(r"P\.queues\.alloc\(cap \* (\d+) \* sizeof\(uint32_t\)\)", host)
+    assert S.SLOT_BYTES == slot + light + queues * 4
+    assert S.PASSES == num(r"#define VV_PASSES (\d+)", host)
+    assert S.PASS_FRAMES == num(r"#define VV_SUBPASS_FRAMES (\d+)", host)
+    assert S.SLOT_FRAMES == num(r"std::atoi\(e\)\) : (\d+);", host)
+    assert S.SLOT_CAP == 1 << num(r"std::max\(px, \(size_t\)1 << (\d+)\)", host)

@@ -242,8 +242,13 @@ def peaks():
     return 6800.0, "fallback"
 
 
-def ncu_traffic():
-    """DRAM bytes per frame of the path-tracing pass from the committed ncu summary, if any."""
+def ncu_traffic(args):
+    """DRAM bytes per frame of the path-tracing pass from the committed ncu
+    summary, which was captured on the default workload (head/neck 512x512x400,
+    1024x1024, studio light, UNORM16 density); None for any other workload."""
+    if (args.workload, dims_of(args), image_size(args), args.light_map, args.density) != \
+            ("head_neck", "512,512,400", (1024, 1024), False, "unorm16"):
+        return None
     path = os.path.join(ROOT, "profiles", "pt_wavefront_head_neck.md")
     if not os.path.exists(path):
         return None
@@ -501,7 +506,7 @@ def run_ours(args, rank, world, local):
     pt_frame_ms = ms / (args.steps * F)
     achieved = alg_bytes / (pt_frame_ms / 1e3) / 1e9
     peak, peak_kind = peaks()
-    traffic = ncu_traffic()
+    traffic = ncu_traffic(args)
     result = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",

@@ -1,6 +1,7 @@
 """bench.py's host logic (CPU): workload sizes and precision options, and the
 serving request stream (seeded, within the configured sizes and path counts,
-Poisson arrivals at the configured rate)."""
+Poisson arrivals at the configured rate), and the workload the committed ncu
+traffic is reported for."""
 import sys
 
 import numpy as np
@@ -45,3 +46,19 @@ def test_serving_request_stream():
     assert np.all(gaps > 0) and abs(gaps.mean() - 1 / 40.0) < 0.25 / 40.0  # Poisson at 40/s
     hidden = np.mean([[q.params.labels.colors[l][3] == 0.0 for l in range(1, 11)] for q in reqs])
     assert 0.12 < hidden < 0.28  # each label hidden with probability 0.2
+
+
+def test_ncu_traffic_only_on_the_captured_workload():
+    """The committed ncu traffic per frame was captured on the default workload:
+    the bench reports it there and nowhere else."""
+    b = _bench()
+
+    class A:
+        workload, dims, size, density, sums, fp64_after, light_map = "head_neck", "", 0, "unorm16", "fp32", 0, False
+    a = A()
+    assert b.ncu_traffic(a) is not None and b.ncu_traffic(a) > 0
+    for field, value in (("workload", "torso"), ("size", 512), ("dims", "256,256,200"), ("light_map", True),
+                         ("density", "bf16")):
+        other = A()
+        setattr(other, field, value)
+        assert b.ncu_traffic(other) is None, field

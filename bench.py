@@ -229,8 +229,28 @@ def bench_config(args, F):
             "frames_per_step": F,
             "step": ("vv_record_frames: %d accumulate-frames in one wavefront pass, then a-trous and the "
                      "tone-mapped display once" % F) if F > 1 else "vv_record",
-            "l2": "inputs larger than L2 (1.2 GB of volumes)",
+            "l2": l2_note(args),
             "parallelism": "replicas" if args.gpus > 1 else "single GPU"}
+
+
+L2_BYTES = 129 * 10 ** 6
+
+
+def volume_bytes(args):
+    """Device bytes of the volumes every frame reads: per bricked voxel the
+    density (2 bytes, 4 for FP32 storage), the normal (4), the label (1) and
+    the label mask (4)."""
+    bricked = 1
+    for d in dims_of(args).split(","):
+        bricked *= -(-int(d) // 8) * 8
+    return bricked * ((4 if args.density == "fp32" else 2) + 4 + 1 + 4)
+
+
+def l2_note(args):
+    v = volume_bytes(args)
+    if v > L2_BYTES:
+        return "inputs larger than L2 (%.2f GB of volumes), no flush between steps" % (v / 1e9)
+    return "inputs smaller than L2 (%.0f MB of volumes): steps re-read them from L2" % (v / 1e6)
 
 
 def peaks():

@@ -62,3 +62,16 @@ def test_ncu_traffic_only_on_the_captured_workload():
         other = A()
         setattr(other, field, value)
         assert b.ncu_traffic(other) is None, field
+
+
+def test_l2_note_follows_the_volume_sizes():
+    b = _bench()
+
+    class A:
+        workload, dims, size, density, sums, fp64_after, light_map = "head_neck", "", 0, "unorm16", "fp32", 0, False
+    a = A()
+    assert b.volume_bytes(a) == 512 * 512 * 400 * 11 and b.l2_note(a).startswith("inputs larger than L2 (1.15 GB")
+    a.density = "fp32"
+    assert b.volume_bytes(a) == 512 * 512 * 400 * 13
+    a.dims = "60,64,80"  # bricked: 64 x 64 x 80
+    assert b.volume_bytes(a) == 64 * 64 * 80 * 13 and b.l2_note(a).startswith("inputs smaller than L2")

@@ -5,8 +5,7 @@
  * (crates/render/src/lib.rs:14-23): volume, label, transfer-function and light
  * map upload, camera, clip planes, label visibility, accumulate-frame and
  * tone-mapped readback. Every type here is plain C (fixed-size integers, floats,
- * pointers and sizes); the Rust binding a maintainer would add is in
- * INTEGRATION.md.
+ * pointers and sizes), so a Rust `extern "C"` block binds it directly.
  *
  * Conventions
  *  - Every call returns vv_status; on failure vv_last_error() describes why.
@@ -372,17 +371,22 @@ vv_status vv_reset_view(vv_renderer* r);
  * device allocation. No counterpart in the reference.
  *
  * accum, albedo, normal: the RGBA32F accumulation images (width*height*4
- * floats each, as vv_read_accumulation lays them out) on the current device;
- * hdr: the RGBA16F output (width*height*4 half values); samples: the paths per
- * pixel accumulated in them. Work is queued on `stream` (a cudaStream_t, NULL
- * for the legacy default stream) and the call returns without waiting.
+ * floats each, as vv_read_accumulation lays them out, 16-byte aligned) on the
+ * current device; hdr: the RGBA16F output (width*height*4 half values, 8-byte
+ * aligned); samples: the paths per pixel accumulated in them. Misaligned
+ * buffers return VV_ERR_ARG. Work is queued on `stream` (a cudaStream_t, NULL
+ * for the legacy default stream) and the call returns without waiting. A CUDA
+ * error already pending on the calling thread is returned (VV_ERR_CUDA, "pending
+ * CUDA error before the call") and cleared, before anything is queued.
  *
  * Allocates nothing: its four scratch images live in a fixed device array of
  * 512 x 512 pixels each (16 MiB, held by every device that loads the library
  * until the process exits); larger images return VV_ERR_LIMIT. The first call
- * on a device looks the array's device address up (make it before any stream
- * capture). All calls share the array: calls that overlap on the GPU race on
- * it. Each call overwrites the scratch before reading it. */
+ * with a given CUDA context current looks the array's device address up in
+ * that context (make it before any stream capture); resetting the device while
+ * the library is loaded is not supported. All calls share the array: calls
+ * that overlap on the GPU race on it. Each call overwrites the scratch before
+ * reading it. */
 vv_status vv_denoise_atrous_noalloc(const float* accum, const float* albedo, const float* normal, uint16_t* hdr,
                                     uint32_t width, uint32_t height, uint32_t samples, void* stream);
 

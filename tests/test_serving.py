@@ -130,10 +130,17 @@ def test_a_request_too_large_for_its_idle_renderer_is_refused():
     srv, log, made = make_server(3 * 10 ** 9, bases)
     srv.preload("a")
     srv.preload("b")
-    srv.submit(S.Request("a", 8192, 8192, 16, params=0))  # ~9.5 GB of image and path state
+    big = S.Request("a", 8192, 8192, 16, params=0)  # ~9.5 GB of image and path state
+    small = S.Request("a", 256, 256, 16, params=1)
+    srv.submit(big)
+    srv.submit(small)
     with pytest.raises(MemoryError):
         srv.step()
     assert [e for e in log if e[0] == "destroy"] == [("destroy", "b")]  # evicted trying
+    # The refused request leaves the queue: the next steps serve the one behind it.
+    assert srv.refused == [big] and big not in srv.queue
+    run(srv, [])
+    assert small.image == ("image", "a", 1) and big.image is None
 
 
 def test_shortest_first_with_aging():

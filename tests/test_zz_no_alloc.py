@@ -25,7 +25,14 @@ def _half(a):
     return a.view(np.float16).astype(np.float32)
 
 
-def test_noalloc_denoiser_matches_record(small_cfg):
+# Whole 16x16 tiles, partial tiles at the right and bottom edges (the kernels'
+# x >= width / y >= height guards and the per-image offsets into the shared
+# array), and the largest image the scratch holds (512 x 512 pixels).
+SIZES = [(64, 48), (37, 23), (512, 512)]
+
+
+@pytest.mark.parametrize("W,H", SIZES)
+def test_noalloc_denoiser_matches_record(small_cfg, W, H):
     torch = pytest.importorskip("torch")
     cfg = small_cfg
     ctx = R.Context(0)
@@ -34,7 +41,6 @@ def test_noalloc_denoiser_matches_record(small_cfg):
     p = scene.frame_params_for(cfg, list(r.center), r.diagonal)
     p.camera.distance = abi.f32(p.camera.distance * 0.5)
     p.path_tracing.denoiser = abi.DENOISE_ATROUS
-    W, H = 64, 48
     r.resize(W, H)
     stream = torch.cuda.current_stream()
     frame = 1
@@ -63,3 +69,16 @@ def test_noalloc_denoiser_rejects_large_images():
                                            1024, 1024, 1, None)
     assert status == abi.VV_ERR_LIMIT
     assert b"512 x 512" in lib.vv_last_error()
+
+
+def test_noalloc_denoiser_rejects_misaligned_buffers():
+    """The images are read as float4 and the output written as 4 halves: a
+    buffer that is not 16-byte (8-byte for the output) aligned is refused on the
+    host, before anything is queued on the device."""
+    lib = R.load()
+    good, odd = C.c_void_p(4096), C.c_void_p(4096 + 20)
+    for args in ((odd, good, good, good), (good, odd, good, good), (good, good, odd, good),
+                 (good, good, good, C.c_void_p(4096 + 4))):
+        status = lib.vv_denoise_atrous_noalloc(*args, 64, 48, 1, None)
+        assert status == abi.VV_ERR_ARG
+        assert b"aligned" in lib.vv_last_error()

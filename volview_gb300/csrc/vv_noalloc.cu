@@ -15,8 +15,16 @@
 // (different streams, or different host threads on one device) race on it.
 // Each call overwrites every pixel of the scratch it uses before reading it,
 // so nothing needs clearing between calls.
+//
+// The array exists once per CUDA context that loaded the library's module, so
+// its device address is looked up once per context (the first call made with
+// that context current; make it before any stream capture). A device reset
+// while the library is loaded is not supported: the reset context's handle
+// may come back with the array at another address.
+#include <cuda.h>
 #include <cuda_runtime.h>
 
+#include <cstdint>
 #include <cstring>
 #include <mutex>
 #include <string>
@@ -33,24 +41,50 @@ constexpr size_t NOALLOC_MAX_PIXELS = 512 * 512;
 // per-pixel guides the passes read.
 static __device__ __align__(256) float4 g_atrous_scratch[4 * NOALLOC_MAX_PIXELS];
 
-// Device addresses of g_atrous_scratch, looked up once per device. In host
-// code the array's name is only a host-side stand-in, never a device address.
+// Device addresses of g_atrous_scratch, looked up once per CUDA context (a
+// caller may run on a context of its own rather than the device's primary
+// one, and each context holds its own copy of the array). In host code the
+// array's name is only a host-side stand-in, never a device address.
+struct ScratchEntry {
+    int device;
+    CUcontext context;
+    float4* addr;
+};
 static std::mutex g_scratch_mutex;
-static float4* g_scratch_addr[64] = {};
+static ScratchEntry g_scratch_addr[64] = {};
+static int g_scratch_used = 0;
+typedef CUresult (*CtxGetCurrent)(CUcontext*);
 
-static cudaError_t scratch_on_current_device(float4** out) {
+static cudaError_t scratch_for_current_context(float4** out) {
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return e;
-    if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
     std::lock_guard<std::mutex> lock(g_scratch_mutex);
-    if (!g_scratch_addr[dev]) {
-        void* p = nullptr;
-        e = cudaGetSymbolAddress(&p, g_atrous_scratch);
+    static CtxGetCurrent get_current = nullptr;
+    if (!get_current) {
+        void* fn = nullptr;
+        cudaDriverEntryPointQueryResult found;
+        e = cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &fn, 12000, cudaEnableDefault, &found);
         if (e != cudaSuccess) return e;
-        g_scratch_addr[dev] = (float4*)p;
+        if (found != cudaDriverEntryPointSuccess || !fn) return cudaErrorSymbolNotFound;
+        get_current = (CtxGetCurrent)fn;
     }
-    *out = g_scratch_addr[dev];
+    CUcontext ctx = nullptr;
+    if (get_current(&ctx) != CUDA_SUCCESS) return cudaErrorDeviceUninitialized;
+    for (int i = 0; ctx && i < g_scratch_used; i++) {
+        if (g_scratch_addr[i].device == dev && g_scratch_addr[i].context == ctx) {
+            *out = g_scratch_addr[i].addr;
+            return cudaSuccess;
+        }
+    }
+    // No context yet on this thread: the lookup itself makes the runtime's
+    // (primary) context current, which is then the one the address belongs to.
+    void* p = nullptr;
+    e = cudaGetSymbolAddress(&p, g_atrous_scratch);
+    if (e != cudaSuccess) return e;
+    if (!ctx && (get_current(&ctx) != CUDA_SUCCESS || !ctx)) return cudaErrorDeviceUninitialized;
+    if (g_scratch_used < 64) g_scratch_addr[g_scratch_used++] = {dev, ctx, (float4*)p};
+    *out = (float4*)p;
     return cudaSuccess;
 }
 
@@ -64,14 +98,23 @@ extern "C" vv_status vv_denoise_atrous_noalloc(const float* accum, const float* 
                                                uint16_t* hdr, uint32_t width, uint32_t height, uint32_t samples,
                                                void* stream) {
     if (!accum || !albedo || !normal || !hdr) return internal_fail(VV_ERR_ARG, "null buffer");
+    // The kernels read the images as float4 and write the output as 4 halves:
+    // a sub-view that is not aligned to that would fault on the device.
+    if (((uintptr_t)accum | (uintptr_t)albedo | (uintptr_t)normal) % 16 != 0 || (uintptr_t)hdr % 8 != 0)
+        return internal_fail(VV_ERR_ARG, "accum, albedo and normal must be 16-byte aligned, hdr 8-byte aligned");
     if (width == 0 || height == 0 || samples == 0) return internal_fail(VV_ERR_ARG, "empty image or no samples");
     if ((size_t)width * height > NOALLOC_MAX_PIXELS)
         return internal_fail(VV_ERR_LIMIT, "the allocation-free denoiser takes at most " +
                                                std::to_string(NOALLOC_MAX_PIXELS) + " pixels (512 x 512); got " +
                                                std::to_string((size_t)width * height));
+    // An error some earlier work left on this thread is reported as such, not
+    // as a failure of this call's launches.
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess)
+        return internal_fail(VV_ERR_CUDA, std::string("pending CUDA error before the call: ") + cudaGetErrorString(e));
     float4* scratch = nullptr;
-    cudaError_t e = scratch_on_current_device(&scratch);
-    if (e != cudaSuccess) return internal_fail(VV_ERR_CUDA, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
+    e = scratch_for_current_context(&scratch);
+    if (e != cudaSuccess) return internal_fail(VV_ERR_CUDA, std::string("scratch address: ") + cudaGetErrorString(e));
     PostArgs a;
     memset(&a, 0, sizeof(a));
     a.u.path[0] = samples;  // samples() of denoise.comp is path.x + path.z

@@ -96,6 +96,7 @@ class Server:
         self.owned = {}                        # renderer -> its volume
         self.next_id = 0
         self.done = []
+        self.refused = []  # requests that can never fit the budget
         self.peak_bytes = 0
         self.created = 0
 
@@ -163,6 +164,10 @@ class Server:
                 # step frees memory (a new renderer in place of `r` would need
                 # the same bytes), so the request can never start.
                 if not self.active and all(x is r for x in self.idle):
+                    # Refused: it leaves the queue, so the next step serves
+                    # the requests behind it.
+                    self.queue.remove(req)
+                    self.refused.append(req)
                     raise MemoryError(f"request {req.id} needs {need} bytes, budget {self.budget}")
                 continue
             self.queue.remove(req)

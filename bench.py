@@ -894,7 +894,10 @@ def run_reference(args, rank, world):
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": O.threads(), "kind": kind,
                          "sample": f"per step {rates[0][2]}; "
                                    + ("shaders/pt.comp compiled as CPU code" if kind == "reference"
-                                      else "CPU restatement of pt.comp")},
+                                      else "the port: the oracle's CPU restatement of pt.comp, not the "
+                                           "reference's shaders compiled as CPU code (their generated sources "
+                                           "are not on this machine); the two agree bit for bit on the "
+                                           "committed golden frames")},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }))
 

@@ -26,6 +26,15 @@ vv_status vv_probe_bspline(vv_renderer* r, const vv_frame_params* params, const 
 vv_status vv_probe_paths(vv_renderer* r, const vv_frame_params* params, uint32_t accumulated,
                          const int* pixels, size_t n, float* out);
 
+/* vv_probe_paths run by the parity build of the same device code: samplers in
+ * the texture-unit arithmetic the CPU oracle models (texel coordinates through
+ * index_to_tex, texels decoded before filtering, the reference's 8 folded
+ * B-spline fetches, the LUT at (d * 4095 + 0.5) / 4096) and no fused
+ * multiply-adds (--fmad=false), so that a replay differs from the oracle's only
+ * where CUDA's transcendental functions and the C library's differ. */
+vv_status vv_probe_paths_exact(vv_renderer* r, const vv_frame_params* params, uint32_t accumulated,
+                               const int* pixels, size_t n, float* out);
+
 /* Event counting for the roofline's algorithmic-byte model: enable = 1 starts
  * counting the path tracer's memory events over the following records (at
  * some cost in speed); enable = 0 stops and copies up to n totals to out, in

@@ -313,6 +313,19 @@ class CpuRenderer:
         lib().vvo_pt_pixel(ptr(u), C.byref(self.scene()), x, y, ptr(out))
         return out
 
+    def trace_pixels(self, params, pixels, accumulated=0, threads=None):
+        """trace_pixel for every (x, y) row of `pixels`, on `threads` host threads: (n, 12)."""
+        self.prepare(params, self.width, self.height)
+        saved = self.accumulated
+        self.accumulated = accumulated
+        u = self.uniforms(params, 1, self.width, self.height)
+        self.accumulated = saved
+        pix = np.ascontiguousarray(pixels, np.int32).reshape(-1, 2)
+        out = np.zeros((pix.shape[0], 12), np.float32)
+        lib().vvo_pt_pixels(ptr(u), C.byref(self.scene()), ptr(pix), C.c_long(pix.shape[0]), ptr(out),
+                            threads or globals()["threads"]())
+        return out
+
     def denoise(self, params):
         """record_denoise over the current accumulation (uses the last frame's counts)."""
         saved = self.accumulated

@@ -22,6 +22,7 @@ void majorant_pass(const Uniforms& u, const Scene& sc, float* out);
 void pt_frame(const Uniforms& u, const Scene& sc, float* accum, float* albedo, float* normal, uint16_t* hdr,
               int y0, int y1, int threads);
 void pt_pixel(const Uniforms& u, const Scene& sc, int x, int y, float out[12]);
+void pt_pixels(const Uniforms& u, const Scene& sc, const int* pix, long n, float* out, int threads);
 void pt_rows(const Uniforms& u, const Scene& sc, float* accum, float* albedo, float* normal, uint16_t* hdr,
              const int* rows, int nrows, int threads);
 void bspline(const Uniforms& u, const Scene& sc, const float* idx, long n, float* out);
@@ -149,6 +150,9 @@ void vvo_pt_rows(const void* u, const vvo_scene* s, float* accum, float* albedo,
 }
 void vvo_pt_pixel(const void* u, const vvo_scene* s, int x, int y, float out[12]) {
     pt_pixel(U(u), to_scene(s), x, y, out);
+}
+void vvo_pt_pixels(const void* u, const vvo_scene* s, const int* pix, long n, float* out, int threads) {
+    pt_pixels(U(u), to_scene(s), pix, n, out, threads);
 }
 void vvo_bspline(const void* u, const vvo_scene* s, const float* idx, long n, float* out) {
     bspline(U(u), to_scene(s), idx, n, out);

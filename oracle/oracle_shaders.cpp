@@ -1113,6 +1113,19 @@ void pt_pixel(const Uniforms& u, const Scene& sc, int x, int y, float out[12]) {
     std::memcpy(out, v, sizeof(v));
 }
 
+// One path each for a list of pixels (x, y pairs), in parallel: pt_pixel's
+// result per pixel, at the uniforms' accumulation count.
+void pt_pixels(const Uniforms& u, const Scene& sc, const int* pix, long n, float* out, int threads) {
+    Units t = bind_scene(sc);
+    parallel_rows(n, threads, [&](long i) {
+        Tracer tr{Shading{u, t}};
+        Tracer::PixelResult R = tr.trace_pixel(uint(pix[2 * i]), uint(pix[2 * i + 1]));
+        float v[12] = {R.sum.x, R.sum.y, R.sum.z, R.background, R.albedo_sum.x, R.albedo_sum.y, R.albedo_sum.z,
+                       R.albedo_sum.w, R.normal_sum.x, R.normal_sum.y, R.normal_sum.z, R.normal_sum.w};
+        std::memcpy(out + 12 * i, v, sizeof(v));
+    });
+}
+
 // Light map samples (pt.comp:204-233) from random-stream states: texel column
 // and row (the draws replayed through the searches), pdf, direction.
 void light_samples(const Uniforms& u, const Scene& sc, const uint32_t* seeds, long n, float* out) {

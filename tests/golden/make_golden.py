@@ -11,9 +11,13 @@ the reference's unit tests (crates/render/src/transfer.rs:130-149).
 light_map_fixture() writes tests/golden/small_light_map.npz: the same scene lit
 by a seeded synthetic light map (Environment::Map); raymarch_fixture() writes
 tests/golden/small_raymarch.npz: the real-time ray marcher's occlusion volume,
-shadow volume and image (ao.comp, shadow.comp, dvr.comp).
+shadow volume and image (ao.comp, shadow.comp, dvr.comp); modes_fixture()
+writes tests/golden/small_modes.npz: the same scene in each of the reference's
+other rendering modes (scene.MODE_CASES: label modes Off, Tint and Isolate with
+hidden labels, ghosted labels, binary masks, the Dome environment, the thin
+lens), masks, majorants and two accumulate-frames of two paths each.
 
-Usage (needs the reference sources): python tests/golden/make_golden.py
+Usage (needs the reference sources): python tests/golden/make_golden.py [main|light_map|raymarch|modes ...]
 """
 import os
 import sys
@@ -143,7 +147,51 @@ def raymarch_fixture():
     print(path, os.path.getsize(path), "bytes")
 
 
+def modes_fixture():
+    """mask.comp, majorant.comp and pt.comp in each of scene.MODE_CASES."""
+    n, size, frames, spf = 24, 24, 2, 2
+    cfg = scene.small_config(n=n, size=size, spp=frames * spf)
+    out = {"hu": cfg["hu"], "labels": cfg["labels_vol"], "soft": cfg["soft"], "spacing": np.array(cfg["spacing"]),
+           "width": size, "height": size, "frames": frames}
+    for name in scene.MODE_CASES:
+        r = O.CpuRenderer(cfg["volume"], cfg["tf"], cfg["hu"])
+        g = r.geo
+        params = scene.frame_params_for(cfg, list(g.center), g.diagonal, clip_sagittal=True, spf=spf)
+        params.camera.distance = abi.f32(params.camera.distance * 0.45)  # the phantom fills the image
+        soft = scene.mode_case(name, params, list(g.center))
+        r.set_labels(cfg["labels_vol"], cfg["soft"] if soft else None)
+        r.resize(size, size)
+        r.normals = R.normals(r, r._uniforms_geometry_only())
+        u1 = r.uniforms(params, 1, size, size)
+        if int(params.labels.mode) != abi.LABEL_OFF:
+            r.mask = R.mask(r, u1, O.mask_margin(cfg["volume"], params.labels), int(params.labels.smoothing))
+        else:
+            r.mask = np.zeros(r.density.shape + (2,), np.uint16)  # not read in mode Off
+        r.majorant = R.majorant(r, u1)
+        acc = np.zeros((size, size, 4), np.float32)
+        alb, nor = np.zeros_like(acc), np.zeros_like(acc)
+        hdr = np.zeros((size, size, 4), np.uint16)
+        for f in range(frames):
+            r.accumulated = f * spf
+            u = r.uniforms(params, f + 1, size, size)
+            R.pt_frame(r, u, acc, alb, nor, hdr)
+        out.update({f"{name}_params": np.frombuffer(bytes(params), np.uint8), f"{name}_soft": int(soft),
+                    f"{name}_uniforms": u1, f"{name}_mask": r.mask, f"{name}_majorant": r.majorant,
+                    f"{name}_accum": acc, f"{name}_albedo": alb, f"{name}_normal": nor})
+        print(name, "background share", float(acc[..., 3].mean()) / (frames * spf),
+              "radiance mean", float(acc[..., :3].mean()))
+    path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "small_modes.npz")
+    np.savez_compressed(path, **out)
+    print(path, os.path.getsize(path), "bytes")
+
+
 if __name__ == "__main__":
-    main()
-    light_map_fixture()
-    raymarch_fixture()
+    which = sys.argv[1:] or ["main", "light_map", "raymarch", "modes"]
+    if "main" in which:
+        main()
+    if "light_map" in which:
+        light_map_fixture()
+    if "raymarch" in which:
+        raymarch_fixture()
+    if "modes" in which:
+        modes_fixture()

@@ -8,13 +8,12 @@ Tolerances (written here, checked below):
 * light map importance samples: the texel bit-exact against a linear scan of
   the CDFs (the device searches only its guide bucket's range), pdf within
   1e-5 relative and direction within 1e-5 (sinf/cosf last bits);
-* single-path replays: 1e-4 relative per pixel for >= 70% of the pixels; the
-  share of pixels whose paths branch differently (a float comparison flipped
-  by a last-bit difference: expf/logf/powf differ in the last bit between CUDA
-  and the C library, and the tracer contracts multiply-adds) is reported and
-  must stay at or below 15%;
+* single-path replays (tests/parity_util.py): the parity build of the probe
+  (the oracle's texture arithmetic, no fused multiply-adds) >= 97% of
+  pixel-paths within 1e-4 relative and <= 2% flipped; the product build
+  >= 70% and <= 15%, reported beside it;
 * converged image: within 3 sigma of the per-pixel Monte Carlo error for
-  >= 99% of pixels;
+  >= 98% of pixels, image means within 3 sigma;
 * a-trous denoiser on identical accumulation inputs: within one FP16 ulp;
 * tone-mapped readback (bloom, auto exposure over two adapting frames, tone
   curve, vignette, grain, sRGB) on identical HDR inputs: every RGBA8 value
@@ -24,16 +23,11 @@ import numpy as np
 import pytest
 
 from oracle import oracle as O
+from parity_util import adopt_device_inputs, all_pixels, check_replays, converged, make_params
 from volview_gb300 import abi, scene
 from volview_gb300 import renderer as R
 
 pytestmark = pytest.mark.gpu
-
-
-def make_params(cfg, center, diagonal, zoom=0.45, **kw):
-    p = scene.frame_params_for(cfg, center, diagonal, **kw)
-    p.camera.distance = abi.f32(p.camera.distance * zoom)
-    return p
 
 
 @pytest.fixture(scope="module")
@@ -73,16 +67,6 @@ def test_uniforms_bit_exact(pair):
     a = gpu.pack_uniforms(params, 1)
     b = cpu.uniforms(params, 1, 48, 48)
     assert np.array_equal(a, b), np.nonzero(a != b)[0][:16]
-
-
-def adopt_device_inputs(gpu, cpu, params):
-    """Gives the oracle the device's masks and majorants, so that the tracer is
-    compared on identical inputs (the mask pass itself is checked above: a
-    one-quantum difference at the mask's zero boundary can move a brick's
-    majorant between 0 and the label opacity, which changes every ray's random
-    stream through that brick)."""
-    gpu.probe_bspline(params, np.zeros((1, 3), np.float32))  # runs record's mask and majorant passes
-    cpu.adopt(mask=gpu.read_volume(abi.VOLUME_MASK), majorant=gpu.read_volume(abi.VOLUME_MAJORANT))
 
 
 def test_masks_and_majorant(pair):
@@ -207,66 +191,17 @@ def test_single_path_replays_light_map(pair_light_map):
 
 def _replays(cfg, gpu, cpu, params):
     adopt_device_inputs(gpu, cpu, params)
-    ys, xs = np.mgrid[0:48, 0:48]
-    pix = np.stack([xs.ravel(), ys.ravel()], 1).astype(np.int32)
-    rels = []
-    for acc in (0, 5):
-        a = gpu.probe_paths(params, acc, pix)
-        b = np.stack([cpu.trace_pixel(params, int(x), int(y), acc) for x, y in pix])
-        rels.append(np.max(np.abs(a[:, :3] - b[:, :3]) / (np.abs(b[:, :3]) + 1e-5), axis=1))
-        assert (a[:, 3] == b[:, 3]).mean() >= 0.99  # background coverage
-    rel = np.concatenate(rels)
-    agree = float((rel <= 1e-4).mean())
-    flips = float((rel > 1e-2).mean())
-    print(f"single-path replays: {agree:.2%} agree within 1e-4, {1 - agree - flips:.2%} drift, "
-          f"{flips:.2%} flipped, of {rel.size} pixel-paths")
-    assert agree >= 0.7
-    assert flips <= 0.15
+    check_replays(gpu, cpu, params, all_pixels(48, 48), label="small scene")
 
 
 def test_converged_image_within_3_sigma(pair):
-    _converged(*pair)
+    cfg, gpu, cpu, params = pair
+    converged(gpu, cpu, params, 48, 48, label="small scene")
 
 
 def test_converged_image_light_map(pair_light_map):
-    _converged(*pair_light_map)
-
-
-def _converged(cfg, gpu, cpu, params):
-    p = abi.FrameParams.from_buffer_copy(bytes(params))
-    p.path_tracing.denoiser = abi.DENOISE_OFF
-    adopt_device_inputs(gpu, cpu, p)
-    n_gpu, n_cpu = 1024, 256
-    gpu.resize(48, 48)
-    gpu.record_frames(1, n_gpu, p)
-    acc, alb, _ = gpu.read_accumulation()
-    # The oracle traces independent paths (accumulation indices past the GPU's,
-    # so other random streams).
-    cpu.resize(48, 48)
-    cpu.accum_key = O._params_key(p)
-    cpu.accumulated = n_gpu  # streams n_gpu.. (the GPU used 0..n_gpu-1)
-    for f in range(n_cpu):
-        cpu.record(p, f + 1)
-    w = np.array([0.2126, 0.7152, 0.0722], np.float32)
-
-    def stats(acc, alb, n):
-        mean = (acc[..., :3] @ w) / n
-        m2 = alb[..., 3] / n
-        var = np.maximum(m2 - mean * mean, 0.0) / n
-        return mean, var
-
-    mg, vg = stats(acc, alb, n_gpu)
-    mc, vc = stats(cpu.accum, cpu.albedo, n_cpu)
-    sigma = np.sqrt(vg + vc) + 1e-6
-    inside = np.abs(mg - mc) <= 3.0 * sigma
-    # The per-pixel estimates are sums of heavy-tailed path contributions, so the
-    # sample variance from a few hundred paths understates the error in some
-    # pixels; the whole-image mean is checked against its own error as well.
-    image_sigma = np.sqrt(vg.sum() + vc.sum()) / mg.size
-    print(f"converged image: {inside.mean():.4%} of pixels within 3 sigma; image mean "
-          f"{mg.mean():.5f} vs {mc.mean():.5f} (sigma {image_sigma:.5f})")
-    assert inside.mean() >= 0.98
-    assert abs(mg.mean() - mc.mean()) <= 3.0 * image_sigma
+    cfg, gpu, cpu, params = pair_light_map
+    converged(gpu, cpu, params, 48, 48, label="light map")
 
 
 def test_denoiser_on_identical_inputs(pair):

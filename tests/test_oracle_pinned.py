@@ -226,3 +226,68 @@ def test_oracle_matches_reference_shaders_live_light_map(small_cfg):
         R.pt_frame(r, u, acc, alb, nor, hdr)
     assert np.array_equal(acc, r.accum) and np.array_equal(alb, r.albedo) and np.array_equal(nor, r.normal)
     assert np.array_equal(hdr, r.hdr)
+
+
+def _modes_golden():
+    path = os.path.join(os.path.dirname(GOLDEN), "small_modes.npz")
+    if not os.path.exists(path):
+        pytest.skip("mode fixtures not generated")
+    return np.load(path)
+
+
+def _mode_case_params():
+    from volview_gb300 import scene
+    return scene.MODE_CASES
+
+
+@pytest.mark.parametrize("case", _mode_case_params())
+def test_oracle_matches_reference_golden_modes(case):
+    """The reference's other rendering modes (label modes Off, Tint and Isolate
+    with hidden labels, ghosted labels and shells, binary masks, the Dome
+    environment, the thin lens): the oracle's masks, majorants, uniforms and two
+    accumulate-frames against mask.comp, majorant.comp and pt.comp compiled as
+    CPU code, bit for bit."""
+    g = _modes_golden()
+    vol = abi.volume_struct(g["hu"], tuple(g["spacing"]))
+    tf = abi.tf_struct(abi.PRESETS["bone"])
+    r = O.CpuRenderer(vol, tf, g["hu"])
+    r.set_labels(g["labels"], g["soft"] if int(g[f"{case}_soft"]) else None)
+    params = abi.FrameParams.from_buffer_copy(g[f"{case}_params"].tobytes())
+    r.resize(int(g["width"]), int(g["height"]))
+    u = r.record(params, 1)
+    assert np.array_equal(u, g[f"{case}_uniforms"])
+    if int(params.labels.mode) != abi.LABEL_OFF:
+        assert np.array_equal(r.mask, g[f"{case}_mask"])
+    assert np.array_equal(r.majorant, g[f"{case}_majorant"])
+    for f in range(2, int(g["frames"]) + 1):
+        r.record(params, f)
+    assert np.array_equal(r.accum, g[f"{case}_accum"])
+    assert np.array_equal(r.albedo, g[f"{case}_albedo"])
+    assert np.array_equal(r.normal, g[f"{case}_normal"])
+
+
+@pytest.mark.parametrize("case", _mode_case_params())
+def test_oracle_matches_reference_shaders_live_modes(small_cfg, case):
+    """The same modes at 48^3 / 48x48 against the reference's shaders, live."""
+    from oracle import ref as R
+    if not R.available():
+        pytest.skip("oracle/_ref not built (needs the reference sources)")
+    from volview_gb300 import scene
+    cfg = small_cfg
+    r = O.CpuRenderer(cfg["volume"], cfg["tf"], cfg["hu"])
+    g = r.geo
+    params = scene.frame_params_for(cfg, list(g.center), g.diagonal, clip_sagittal=True)
+    params.camera.distance = abi.f32(params.camera.distance * 0.45)
+    soft = scene.mode_case(case, params, list(g.center))
+    r.set_labels(cfg["labels_vol"], cfg["soft"] if soft else None)
+    r.resize(48, 48)
+    u = r.record(params, 1)
+    if int(params.labels.mode) != abi.LABEL_OFF:
+        margin = O.mask_margin(cfg["volume"], params.labels)
+        assert np.array_equal(R.mask(r, u, margin, int(params.labels.smoothing)), r.mask)
+    assert np.array_equal(R.majorant(r, u), r.majorant)
+    acc = np.zeros((48, 48, 4), np.float32)
+    alb, nor = np.zeros_like(acc), np.zeros_like(acc)
+    hdr = np.zeros((48, 48, 4), np.uint16)
+    R.pt_frame(r, u, acc, alb, nor, hdr)
+    assert np.array_equal(acc, r.accum) and np.array_equal(alb, r.albedo) and np.array_equal(nor, r.normal)

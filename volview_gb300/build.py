@@ -13,13 +13,16 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libvolpt.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-SOURCES = ["vv_volume.cu", "vv_pt.cu", "vv_wavefront.cu", "vv_raymarch.cu", "vv_post.cu", "vv_noalloc.cu",
-           "vv_nn.cu", "vv_host.cpp"]
+SOURCES = ["vv_volume.cu", "vv_pt.cu", "vv_pt_exact.cu", "vv_wavefront.cu", "vv_raymarch.cu", "vv_post.cu",
+           "vv_noalloc.cu", "vv_nn.cu", "vv_host.cpp"]
 # Compiled once per density storage format (VV_DFMT = 0..3: R16_UNORM, FP16,
 # BF16, FP32), each into its own namespace, so each format's samplers are
 # specialised for it.
-PER_FORMAT = {"vv_pt.cu", "vv_wavefront.cu", "vv_raymarch.cu"}
+PER_FORMAT = {"vv_pt.cu", "vv_pt_exact.cu", "vv_wavefront.cu", "vv_raymarch.cu"}
 FORMATS = 4
+# The parity build of the path probe: the oracle's texture-unit arithmetic and
+# no multiply-add contraction (every product and sum rounded on its own).
+UNIT_FLAGS = {"vv_pt_exact.cu": ["-DVV_EXACT=1", "--fmad=false"]}
 # Host code never contracts a*b+c into an FMA (Rust, whose host math the
 # renderer restates, does not either; gcc does by default on Arm).
 NVFLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
@@ -61,7 +64,8 @@ def build(verbose=False, force=False, extra=()):
 
     for s, o, defs in units:
         lang = ["-x", "cu"] if s.endswith(".cu") else ["-x", "c++"]
-        cmd = [nvcc(), *ARCH, *NVFLAGS, *defs, *extra, *lang, "-c", s, "-o", o]
+        cmd = [nvcc(), *ARCH, *NVFLAGS, *UNIT_FLAGS.get(os.path.basename(s), []), *defs, *extra, *lang, "-c", s,
+               "-o", o]
         if s.endswith(".cu"):
             cmd += ["-Xptxas", "-v"] if verbose else []
         if len(running) >= jobs:

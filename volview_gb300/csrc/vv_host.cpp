@@ -7,6 +7,7 @@
 // device buffers on one CUDA stream; descriptor sets become kernel arguments.
 #include <cuda_runtime.h>
 
+#include <climits>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -1872,9 +1873,14 @@ extern "C" vv_status vv_probe_light_samples(vv_renderer* r, const vv_frame_param
     return VV_OK;
 }
 
-extern "C" vv_status vv_probe_paths(vv_renderer* r, const vv_frame_params* params, uint32_t accumulated,
-                                    const int* pixels, size_t n, float* out) {
+static decltype(&exact0::launch_pt_pixels) const EXACT_PT_PIXELS[4] = {
+    exact0::launch_pt_pixels, exact1::launch_pt_pixels, exact2::launch_pt_pixels, exact3::launch_pt_pixels};
+
+static vv_status probe_paths(vv_renderer* r, const vv_frame_params* params, uint32_t accumulated, const int* pixels,
+                             size_t n, float* out, bool exact) {
     if (!r || !params || !pixels || !out) return fail(VV_ERR_ARG, "null argument");
+    if (n == 0) return VV_OK;
+    if (n > (size_t)INT32_MAX / 12) return fail(VV_ERR_LIMIT, "too many pixels for one probe");
     UHead u;
     vv_status s = prepare_frame(r, *params, 1, u);
     if (s != VV_OK) return s;
@@ -1885,11 +1891,23 @@ extern "C" vv_status vv_probe_paths(vv_renderer* r, const vv_frame_params* param
     cudaStream_t st = r->ctx->stream;
     PtArgs a = pt_args(r, u);
     cudaError_t e = cudaMemcpyAsync(dp.p, pixels, n * 8, cudaMemcpyHostToDevice, st);
-    if (e == cudaSuccess) e = kernels_of(r).pt_pixels(a, dp.as<int>(), dout.as<float>(), (int)n, st);
+    if (e == cudaSuccess)
+        e = (exact ? EXACT_PT_PIXELS[r->vol.dfmt & 3] : kernels_of(r).pt_pixels)(a, dp.as<int>(), dout.as<float>(),
+                                                                               (int)n, st);
     if (e == cudaSuccess) e = cudaMemcpyAsync(out, dout.p, n * 48, cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     dp.release();
     dout.release();
     if (e != cudaSuccess) return cuda_fail(e, "path probe");
     return VV_OK;
+}
+
+extern "C" vv_status vv_probe_paths(vv_renderer* r, const vv_frame_params* params, uint32_t accumulated,
+                                    const int* pixels, size_t n, float* out) {
+    return probe_paths(r, params, accumulated, pixels, n, out, false);
+}
+
+extern "C" vv_status vv_probe_paths_exact(vv_renderer* r, const vv_frame_params* params, uint32_t accumulated,
+                                          const int* pixels, size_t n, float* out) {
+    return probe_paths(r, params, accumulated, pixels, n, out, true);
 }

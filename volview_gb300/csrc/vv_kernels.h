@@ -145,6 +145,14 @@ namespace fmt0 { VV_FORMAT_LAUNCHERS }
 namespace fmt1 { VV_FORMAT_LAUNCHERS }
 namespace fmt2 { VV_FORMAT_LAUNCHERS }
 namespace fmt3 { VV_FORMAT_LAUNCHERS }
+// The parity build of the single-path probe (vv_pt_exact.cu), per format: the
+// oracle's texture-unit arithmetic, no fused multiply-adds.
+#define VV_EXACT_LAUNCHERS \
+    cudaError_t launch_pt_pixels(const PtArgs& a, const int* px, float* out, int n, cudaStream_t s);
+namespace exact0 { VV_EXACT_LAUNCHERS }
+namespace exact1 { VV_EXACT_LAUNCHERS }
+namespace exact2 { VV_EXACT_LAUNCHERS }
+namespace exact3 { VV_EXACT_LAUNCHERS }
 
 struct PostArgs {
     UHead u;

@@ -14,9 +14,27 @@
 #ifndef VV_DFMT
 #define VV_DFMT 0
 #endif
+// VV_EXACT = 1: the parity build of the path probe (namespace vv::exactN,
+// compiled with --fmad=false). Its samplers take the texture-unit model of the
+// Vulkan specification that the CPU oracle restates: index_to_tex, then
+// linear filtering of decoded texels with weights (1 - a)(1 - b)(1 - c) ... in
+// x, y, z order; the cubic B-spline from the reference's 8 folded trilinear
+// fetches; the LUT at (d * 4095 + 0.5) / 4096. With every product and sum
+// rounded on its own, as the oracle rounds them, a replayed path differs from
+// the oracle's only where CUDA's and the C library's transcendental functions
+// differ in the last bit. The product samplers (VV_EXACT = 0) filter codes
+// directly at the index, with fused multiply-adds: the same filters, rounded
+// differently.
+#ifndef VV_EXACT
+#define VV_EXACT 0
+#endif
 #define VV_FMT_CAT2(a, b) a##b
 #define VV_FMT_CAT(a, b) VV_FMT_CAT2(a, b)
+#if VV_EXACT
+#define VV_FMT_NS VV_FMT_CAT(exact, VV_DFMT)
+#else
 #define VV_FMT_NS VV_FMT_CAT(fmt, VV_DFMT)
+#endif
 
 namespace vv {
 // Internal linkage: every translation unit that includes this header gets its
@@ -80,21 +98,116 @@ __device__ __forceinline__ float tri_mix(const float c[8], const Tri& t) {
     return lerpf(lerpf(a, b, t.fy), lerpf(d, e, t.fy), t.fz);
 }
 
+#if VV_EXACT
+// The texel coordinates of a linear 3D lookup at continuous index p, as the
+// oracle's texture model computes them: tc = (p + 0.5) / dims (index_to_tex,
+// common.glsl:68-70), u = tc * size - 0.5; the eight taps clamped to the edge,
+// their weights (1 - a or a) * (1 - b or b) * (1 - c or c), x fastest.
+struct TriX {
+    int o[8];
+    float w[8];
+};
+__device__ __forceinline__ TriX tri_taps_exact(const PtArgs& A, f3 p) {
+    const Vol& v = A.vol;
+    float tx = (p.x + 0.5f) / A.u.dims[0], ty = (p.y + 0.5f) / A.u.dims[1], tz = (p.z + 0.5f) / A.u.dims[2];
+    float uu = tx * (float)v.nx - 0.5f, vv = ty * (float)v.ny - 0.5f, qq = tz * (float)v.nz - 0.5f;
+    int i0 = (int)floorf(uu), j0 = (int)floorf(vv), k0 = (int)floorf(qq);
+    float a = uu - (float)i0, b = vv - (float)j0, c = qq - (float)k0;
+    TriX t;
+#pragma unroll
+    for (int k = 0; k < 8; k++) {
+        int di = k & 1, dj = (k >> 1) & 1, dk = k >> 2;
+        t.o[k] = offx(clampi(i0 + di, 0, v.nx - 1)) + offy(v, clampi(j0 + dj, 0, v.ny - 1)) +
+                 offz(v, clampi(k0 + dk, 0, v.nz - 1));
+        t.w[k] = (di ? a : 1.0f - a) * (dj ? b : 1.0f - b) * (dk ? c : 1.0f - c);
+    }
+    return t;
+}
+__device__ __forceinline__ float tri_sum_exact(const float c[8], const TriX& t) {
+    float r = 0.0f;
+#pragma unroll
+    for (int k = 0; k < 8; k++) r = r + c[k] * t.w[k];
+    return r;
+}
+// A density texel as the sampler decodes it: R16_UNORM code / 65535, the
+// other formats their value.
+__device__ __forceinline__ float density_texel_exact(const void* d, int o) {
+    typedef DensityStore<VV_DFMT>::type E;
+    float x = density_decode<VV_DFMT>(__ldg((const E*)d + o));
+    return VV_DFMT == DF_UNORM16 ? x / 65535.0f : x;
+}
+__device__ __forceinline__ float density_at_index_exact(const PtArgs& A, f3 p) {
+    TriX t = tri_taps_exact(A, p);
+    float c[8];
+#pragma unroll
+    for (int k = 0; k < 8; k++) c[k] = density_texel_exact(A.density, t.o[k]);
+    return tri_sum_exact(c, t);
+}
+// cubic_taps (common.glsl:89-113) of one axis.
+struct AxisTaps {
+    float h0, h1, g0, g1, dh0, dh1, dg0, dg1;
+};
+__device__ __forceinline__ AxisTaps cubic_axis_exact(float x) {
+    float i = floorf(x), f = x - i, f2 = f * f, f3_ = f2 * f;
+    float w0 = (1.0f - 3.0f * f + 3.0f * f2 - f3_) / 6.0f;
+    float w1 = (4.0f - 6.0f * f2 + 3.0f * f3_) / 6.0f;
+    float w2 = (1.0f + 3.0f * f + 3.0f * f2 - 3.0f * f3_) / 6.0f;
+    float w3 = f3_ / 6.0f;
+    float d0 = -0.5f * (1.0f - f) * (1.0f - f);
+    float d1 = 0.5f * f * (3.0f * f - 4.0f);
+    float d2 = 0.5f * (1.0f - f) * (3.0f * f + 1.0f);
+    float d3 = 0.5f * f2;
+    AxisTaps t;
+    t.g0 = w0 + w1;
+    t.g1 = w2 + w3;
+    t.h0 = i - 1.0f + w1 / t.g0;
+    t.h1 = i + 1.0f + w3 / t.g1;
+    t.dg0 = d0 + d1;
+    t.dg1 = d2 + d3;
+    t.dh0 = i - 1.0f + d1 / gmin(t.dg0, -1e-7f);
+    t.dh1 = i + 1.0f + d3 / gmax(t.dg1, 1e-7f);
+    return t;
+}
+// cubic_fetch (common.glsl:116-122): the 8-fetch tensor product.
+__device__ __forceinline__ float cubic_fetch_exact(const PtArgs& A, f3 h0, f3 h1, f3 g0, f3 g1) {
+    float a = g0.x * density_at_index_exact(A, mk(h0.x, h0.y, h0.z)) + g1.x * density_at_index_exact(A, mk(h1.x, h0.y, h0.z));
+    float b = g0.x * density_at_index_exact(A, mk(h0.x, h1.y, h0.z)) + g1.x * density_at_index_exact(A, mk(h1.x, h1.y, h0.z));
+    float c = g0.x * density_at_index_exact(A, mk(h0.x, h0.y, h1.z)) + g1.x * density_at_index_exact(A, mk(h1.x, h0.y, h1.z));
+    float d = g0.x * density_at_index_exact(A, mk(h0.x, h1.y, h1.z)) + g1.x * density_at_index_exact(A, mk(h1.x, h1.y, h1.z));
+    return g0.z * (g0.y * a + g1.y * b) + g1.z * (g0.y * c + g1.y * d);
+}
+#endif
+
 // textureLod(density_tex, index_to_tex(idx)) (common.glsl:76-78), the density
 // stored as this translation unit's format (VV_DFMT).
 __device__ float density_tri(const PtArgs& A, f3 p) {
     count(A, COUNT_TRILINEAR);
+#if VV_EXACT
+    return density_at_index_exact(A, p);
+#else
     typedef DensityStore<VV_DFMT>::type E;
     Tri t = tri_taps(A.vol, p);
     float c[8];
 #pragma unroll
     for (int k = 0; k < 8; k++) c[k] = density_decode<VV_DFMT>(__ldg((const E*)A.density + t.o[k]));
     return tri_mix(c, t) * density_unit<VV_DFMT>();
+#endif
 }
 
 // textureLod(mask_tex, ...).rg
 __device__ float2 mask_tri(const PtArgs& A, f3 p) {
     count(A, COUNT_MASK);
+#if VV_EXACT
+    TriX x = tri_taps_exact(A, p);
+    float er[8], eg[8];
+#pragma unroll
+    for (int k = 0; k < 8; k++) {
+        uint32_t m = __ldg(A.mask + x.o[k]);
+        er[k] = (float)(m & 0xffffu) / 65535.0f;
+        eg[k] = (float)(m >> 16) / 65535.0f;
+    }
+    return make_float2(tri_sum_exact(er, x), tri_sum_exact(eg, x));
+#endif
     Tri t = tri_taps(A.vol, p);
     float r[8], g[8];
 #pragma unroll
@@ -107,6 +220,16 @@ __device__ float2 mask_tri(const PtArgs& A, f3 p) {
 }
 __device__ float mask_tri_ch(const PtArgs& A, f3 p, int ch) {
     count(A, COUNT_MASK);
+#if VV_EXACT
+    TriX x = tri_taps_exact(A, p);
+    float c[8];
+#pragma unroll
+    for (int k = 0; k < 8; k++) {
+        uint32_t m = __ldg(A.mask + x.o[k]);
+        c[k] = (float)(ch == 0 ? (m & 0xffffu) : (m >> 16)) / 65535.0f;
+    }
+    return tri_sum_exact(c, x);
+#endif
     Tri t = tri_taps(A.vol, p);
     float r[8];
 #pragma unroll
@@ -121,6 +244,17 @@ __device__ float mask_tri_ch(const PtArgs& A, f3 p, int ch) {
 // decode max(c / 127, -1) is c / 127 and commutes with the interpolation.
 __device__ float4 normal_tri(const PtArgs& A, f3 p) {
     count(A, COUNT_NORMAL);
+#if VV_EXACT
+    TriX q = tri_taps_exact(A, p);
+    float c[4][8];
+#pragma unroll
+    for (int k = 0; k < 8; k++) {
+        uint32_t m = __ldg(A.normals + q.o[k]);
+#pragma unroll
+        for (int ch = 0; ch < 4; ch++) c[ch][k] = gmax((float)(int8_t)((m >> (8 * ch)) & 0xff) / 127.0f, -1.0f);
+    }
+    return make_float4(tri_sum_exact(c[0], q), tri_sum_exact(c[1], q), tri_sum_exact(c[2], q), tri_sum_exact(c[3], q));
+#endif
     Tri t = tri_taps(A.vol, p);
     float x[8], y[8], z[8], w[8];
 #pragma unroll
@@ -170,6 +304,10 @@ __device__ __forceinline__ Cubic cubic_taps(const Vol& v, f3 p) {
 // density_cubic (common.glsl:124-127) as the 64-tap tensor product.
 __device__ __noinline__ float density_cubic(const PtArgs& A, f3 p) {
     count(A, COUNT_CUBIC);
+#if VV_EXACT
+    AxisTaps x = cubic_axis_exact(p.x), y = cubic_axis_exact(p.y), z = cubic_axis_exact(p.z);
+    return cubic_fetch_exact(A, mk(x.h0, y.h0, z.h0), mk(x.h1, y.h1, z.h1), mk(x.g0, y.g0, z.g0), mk(x.g1, y.g1, z.g1));
+#endif
     typedef DensityStore<VV_DFMT>::type E;
     Cubic c = cubic_taps(A.vol, p);
     float wx[4], wy[4], wz[4];
@@ -228,6 +366,15 @@ template <bool VALUE> __device__ __forceinline__ f3 density_gradient_cubic_impl(
 }
 __device__ __noinline__ f3 density_gradient_cubic(const PtArgs& A, f3 p) {
     count(A, COUNT_GRADIENT);
+#if VV_EXACT
+    AxisTaps x = cubic_axis_exact(p.x), y = cubic_axis_exact(p.y), z = cubic_axis_exact(p.z);
+    return mk(cubic_fetch_exact(A, mk(x.dh0, y.h0, z.h0), mk(x.dh1, y.h1, z.h1), mk(x.dg0, y.g0, z.g0),
+                                mk(x.dg1, y.g1, z.g1)),
+              cubic_fetch_exact(A, mk(x.h0, y.dh0, z.h0), mk(x.h1, y.dh1, z.h1), mk(x.g0, y.dg0, z.g0),
+                                mk(x.g1, y.dg1, z.g1)),
+              cubic_fetch_exact(A, mk(x.h0, y.h0, z.dh0), mk(x.h1, y.h1, z.dh1), mk(x.g0, y.g0, z.dg0),
+                                mk(x.g1, y.g1, z.dg1)));
+#endif
     float unused;
     return density_gradient_cubic_impl<false>(A, p, unused);
 }
@@ -242,6 +389,16 @@ __device__ __noinline__ float density_cubic_with_gradient(const PtArgs& A, f3 p,
 
 // transfer (common.glsl:170-173): linear LUT lookup at texel centres.
 __device__ float4 transfer(const PtArgs& A, float d) {
+#if VV_EXACT
+    {
+        float uu = (d * (4096.0f - 1.0f) + 0.5f) / 4096.0f * 4096.0f - 0.5f;
+        int i0 = (int)floorf(uu);
+        float a = uu - (float)i0;
+        float4 t0 = ldf4(A.lut + clampi(i0, 0, 4095)), t1 = ldf4(A.lut + clampi(i0 + 1, 0, 4095));
+        float w0 = 1.0f - a;
+        return make_float4(t0.x * w0 + t1.x * a, t0.y * w0 + t1.y * a, t0.z * w0 + t1.z * a, t0.w * w0 + t1.w * a);
+    }
+#endif
     float u = d * 4095.0f;
     float fl = floorf(u);
     float f = u - fl;

@@ -62,6 +62,7 @@ EXPORTS = [
 PROBES = [
     ("vv_probe_bspline", C.c_int, [P, P, P, C.c_size_t, P]),
     ("vv_probe_paths", C.c_int, [P, P, C.c_uint32, P, C.c_size_t, P]),
+    ("vv_probe_paths_exact", C.c_int, [P, P, C.c_uint32, P, C.c_size_t, P]),
     ("vv_probe_light_samples", C.c_int, [P, P, P, C.c_size_t, P]),
     ("vv_count_events", C.c_int, [P, C.c_int, P, C.c_size_t]),
     ("vv_time_pt", C.c_int, [P, C.c_int, P, P]),
@@ -279,10 +280,13 @@ class Renderer:
         check(load().vv_probe_light_samples(self.handle, C.byref(params), _ptr(seeds), seeds.size, _ptr(out)))
         return out
 
-    def probe_paths(self, params, accumulated, pixels):
+    def probe_paths(self, params, accumulated, pixels, exact=False):
+        """One path per listed (x, y) pixel at accumulation count `accumulated`
+        (12 floats each); `exact` runs the parity build (vv_probe_paths_exact)."""
         pix = np.ascontiguousarray(pixels, np.int32).reshape(-1, 2)
         out = np.zeros((pix.shape[0], 12), np.float32)
-        check(load().vv_probe_paths(self.handle, C.byref(params), accumulated, _ptr(pix), pix.shape[0], _ptr(out)))
+        fn = load().vv_probe_paths_exact if exact else load().vv_probe_paths
+        check(fn(self.handle, C.byref(params), accumulated, _ptr(pix), pix.shape[0], _ptr(out)))
         return out
 
     def time_pt(self, enable):

@@ -400,6 +400,46 @@ def frame_params_for(cfg, center, diagonal, clip_sagittal=False, anisotropy=0.6,
     return abi.frame_params(cam, abi.f32(0.5 * cfg["min_spacing"]), cfg["label_params"], light, pt, clip)
 
 
+# Variants of a scene's frame that exercise the reference's other rendering
+# modes: the label modes Off, Tint and Isolate (common.glsl:232-351) with
+# hidden labels, ghosted labels and their shells (pt.comp:286-289,
+# shading.glsl:73-144), binary label masks without a soft grid
+# (mask.comp:107-138), the Dome environment (pt.comp:56-82) and the thin lens
+# (pt.comp:406-416).
+MODE_CASES = ("off", "tint", "isolate", "ghost", "binary", "dome", "lens")
+
+
+def mode_case(name, params, center):
+    """Sets `params` (FrameParams of the small scene) up for mode case `name`;
+    returns whether the labels come with their soft grid (False: binary masks)."""
+    lp = params.labels
+    if name == "off":
+        lp.mode = abi.LABEL_OFF
+    elif name == "tint":
+        lp.mode = abi.LABEL_TINT
+        lp.colors[7][3] = 0.0  # one label hidden: cut away, with the tissue near it
+    elif name == "isolate":
+        lp.mode = abi.LABEL_ISOLATE
+        for v in (5, 6):       # muscles hidden
+            lp.colors[v][3] = 0.0
+    elif name == "ghost":
+        lp.mode = abi.LABEL_HYBRID
+        for v in (1, 2, 3):    # skeleton and lungs ghosted: shells over the rest
+            lp.ghost[v] = 1
+    elif name == "binary":
+        lp.mode = abi.LABEL_HYBRID
+        return False
+    elif name == "dome":
+        params.lighting.environment = abi.ENV_DOME
+    elif name == "lens":
+        params.path_tracing.aperture = abi.f32(6.0)
+        params.path_tracing.has_focus = 1
+        params.path_tracing.focus[:] = [abi.f32(center[0] + 20.0), abi.f32(center[1]), abi.f32(center[2])]
+    else:
+        raise ValueError(f"unknown mode case {name!r}")
+    return True
+
+
 def synthetic_light_map(width=64, height=32, seed=3):
     """A seeded equirectangular studio-like HDR light map, (height, width, 3) linear RGB,
     rows from the zenith down: a graded sky, a small bright sun and two soft boxes,

@@ -40,7 +40,7 @@ vv_status vv_probe_paths_exact(vv_renderer* r, const vv_frame_params* params, ui
  * some cost in speed); enable = 0 stops and copies up to n totals to out, in
  * the order: majorant lookups, cubic densities, trilinear densities, mask
  * lookups, label fetches, normal lookups, cubic gradients, pixel
- * accumulations, paths, path vertices. */
+ * accumulations, paths, path vertices, empty-space cell lookups. */
 vv_status vv_count_events(vv_renderer* r, int enable, uint64_t* out, size_t n);
 
 /* Device time of the path-tracing launches: enable = 1 starts recording CUDA

@@ -6,8 +6,8 @@ Tolerances (written here, checked below):
 * stored density, normals and majorant: bit-exact against the oracle run on
   the same format (round-to-nearest-even encodings of the same normalised
   density t = clamp((hu + 1024) / 4095, 0, 1));
-* single-path replays: the parity bar of the R16_UNORM path (>= 70 % of the
-  pixel-paths within 1e-4 relative, <= 15 % flipped);
+* single-path replays: the bars of tests/parity_util.py, for the parity build
+  of the probe and the product build, on each format;
 * running sums over 300 single-frame passes: with Kahan compensation, and with
   FP64 from the 100th sample on, every non-negative sum (radiance, coverage,
   albedo, squared luminance, depth) within 3 ulp (float32) of the FP64 running
@@ -18,6 +18,7 @@ import numpy as np
 import pytest
 
 from oracle import oracle as O
+from parity_util import adopt_device_inputs, all_pixels, check_replays
 from volview_gb300 import abi, scene
 from volview_gb300 import renderer as R
 
@@ -79,21 +80,8 @@ def test_majorant_bit_exact(fmt_pair):
 
 def test_single_path_replays(fmt_pair):
     cfg, gpu, cpu, params = fmt_pair
-    gpu.probe_bspline(params, np.zeros((1, 3), np.float32))
-    cpu.adopt(mask=gpu.read_volume(abi.VOLUME_MASK), majorant=gpu.read_volume(abi.VOLUME_MAJORANT))
-    ys, xs = np.mgrid[0:48, 0:48]
-    pix = np.stack([xs.ravel(), ys.ravel()], 1).astype(np.int32)
-    rels = []
-    for acc in (0, 5):
-        a = gpu.probe_paths(params, acc, pix)
-        b = np.stack([cpu.trace_pixel(params, int(x), int(y), acc) for x, y in pix])
-        rels.append(np.max(np.abs(a[:, :3] - b[:, :3]) / (np.abs(b[:, :3]) + 1e-5), axis=1))
-        assert (a[:, 3] == b[:, 3]).mean() >= 0.99
-    rel = np.concatenate(rels)
-    agree, flips = float((rel <= 1e-4).mean()), float((rel > 1e-2).mean())
-    print(f"format {gpu.precision.density_format}: {agree:.2%} agree within 1e-4, {flips:.2%} flipped")
-    assert agree >= 0.7
-    assert flips <= 0.15
+    adopt_device_inputs(gpu, cpu, params)
+    check_replays(gpu, cpu, params, all_pixels(48, 48), label=f"density format {gpu.precision.density_format}")
 
 
 def test_bspline_matches_oracle(fmt_pair):

@@ -219,6 +219,7 @@ struct vv_renderer {
     float bucket[64];
     // device volumes
     DBuf density, normals, mask_a, mask_b, labels, majorant, lut, bucket_dev, tables, soft, work, exposure;
+    DBuf occupancy;  // empty-space cells of the majorant grid (launch_occupancy)
     int soft_dims[3] = {1, 1, 1};
     int soft_push[4] = {0, 0, 0, 0};
     bool has_labels = false;
@@ -688,6 +689,7 @@ extern "C" vv_status vv_renderer_create_ex(vv_context* ctx, const vv_volume* vol
     if ((e = r->density.alloc(elems * density_bytes(v.dfmt))) != cudaSuccess ||
         (e = r->normals.alloc(elems * sizeof(uint32_t))) != cudaSuccess ||
         (e = r->majorant.alloc((size_t)v.bx * v.by * v.bz * sizeof(float))) != cudaSuccess ||
+        (e = r->occupancy.alloc((size_t)occ_cells(v.bx) * occ_cells(v.by) * occ_cells(v.bz))) != cudaSuccess ||
         (e = r->tables.alloc(sizeof(LabelTables))) != cudaSuccess ||
         (e = r->work.alloc(256)) != cudaSuccess || (e = r->exposure.alloc(sizeof(float))) != cudaSuccess) {
         hu.release();
@@ -719,7 +721,7 @@ extern "C" vv_status vv_renderer_destroy(vv_renderer* r) {
         if (P.stream) cudaStreamDestroy(P.stream);
     }
     if (r->prep_done) cudaEventDestroy(r->prep_done);
-    DBuf* all[] = {&r->density, &r->normals, &r->mask_a, &r->mask_b, &r->labels, &r->majorant, &r->env_rad,
+    DBuf* all[] = {&r->density, &r->normals, &r->mask_a, &r->mask_b, &r->labels, &r->majorant, &r->occupancy, &r->env_rad,
                    &r->env_table, &r->env_diffuse, &r->env_guide, &r->preint, &r->shadow_vol, &r->ao_vol, &r->lut,
                    &r->bucket_dev, &r->tables, &r->soft, &r->work, &r->exposure, &r->accum, &r->albedo,
                    &r->normal, &r->ping, &r->pong, &r->guide_nd, &r->guide_alb, &r->hdr, &r->out, &r->bloom[0], &r->bloom[1], &r->bloom[2],
@@ -1105,7 +1107,7 @@ extern "C" vv_status vv_query(vv_renderer* r, int* idle) {
 
 extern "C" vv_status vv_renderer_memory(const vv_renderer* r, uint64_t* bytes) {
     if (!r || !bytes) return fail(VV_ERR_ARG, "null argument");
-    const DBuf* all[] = {&r->density, &r->normals, &r->mask_a, &r->mask_b, &r->labels, &r->majorant, &r->lut,
+    const DBuf* all[] = {&r->density, &r->normals, &r->mask_a, &r->mask_b, &r->labels, &r->majorant, &r->occupancy, &r->lut,
                          &r->bucket_dev, &r->tables, &r->soft, &r->work, &r->exposure, &r->accum, &r->albedo,
                          &r->normal, &r->ping, &r->pong, &r->guide_nd, &r->guide_alb, &r->hdr, &r->out,
                          &r->bloom[0], &r->bloom[1], &r->bloom[2], &r->bloom[3], &r->preint, &r->shadow_vol,
@@ -1160,6 +1162,11 @@ static PtArgs pt_args(vv_renderer* r, const UHead& u) {
     a.normals = r->normals.as<uint32_t>();
     a.labels = r->labels.as<uint8_t>();
     a.majorant = r->majorant.as<float>();
+    // Empty-space cells only where empty-space skipping is on (else no brick
+    // is skipped: every majorant is the cap).
+    a.occupancy = u.path[3] != 0u ? r->occupancy.as<uint8_t>() : nullptr;
+    a.occ_x = occ_cells(r->vol.bx);
+    a.occ_y = occ_cells(r->vol.by);
     a.env_rad = r->env_rad.as<ushort4>();
     a.env_diffuse = r->env_diffuse.as<ushort4>();
     a.preint = r->preint.as<float4>();
@@ -1317,7 +1324,8 @@ static vv_status prepare_frame(vv_renderer* r, const vv_frame_params& p, uint64_
         r->prep_work = true;
         CK(launch_majorant(r->density.p, r->mask_a.as<uint32_t>(), r->vol, key.mode, p.labels.extinction,
                            r->bucket_dev.as<float>(), r->majorant.as<float>(), st));
-        r->launches += 1;
+        CK(launch_occupancy(r->majorant.as<float>(), r->vol, r->occupancy.as<uint8_t>(), st));
+        r->launches += 2;
         r->majorant_key = key;
         r->have_majorant_key = true;
     }

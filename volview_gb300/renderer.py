@@ -89,9 +89,10 @@ NN = [
     ("vv_nn_prediction_to_hdr", I, [P, I, I, I, I, P, F, P, P]),
 ]
 
-COUNT_NAMES = ["majorant", "cubic", "trilinear", "mask", "label", "normal", "gradient", "pixel", "path", "vertex"]
+COUNT_NAMES = ["majorant", "cubic", "trilinear", "mask", "label", "normal", "gradient", "pixel", "path", "vertex",
+               "occupancy"]
 # Unique element bytes each event must read (and write, for pixels).
-COUNT_BYTES = [4, 128, 16, 32, 1, 32, 128, 104, 0, 0]
+COUNT_BYTES = [4, 128, 16, 32, 1, 32, 128, 104, 0, 0, 1]
 
 _lib = None
 

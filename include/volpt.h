@@ -239,7 +239,7 @@ vv_status vv_renderer_create(vv_context* ctx, const vv_volume* volume,
 /* Storage and running-sum precision: an extension beyond the reference
  * (whose density is R16_UNORM and whose sums are FP32), for the precision
  * variant of the workload. vv_renderer_create uses the reference's
- * {VV_DENSITY_UNORM16, VV_SUMS_FP32, 0}. */
+ * {VV_DENSITY_UNORM16, VV_SUMS_FP32, 0, VV_MAJORANTS_REFERENCE}. */
 enum {
     VV_DENSITY_UNORM16 = 0, /* round(t * 65535), t = normalised density (the reference) */
     VV_DENSITY_FP16 = 1,    /* t as binary16, rounded to nearest even */
@@ -250,11 +250,25 @@ enum {
     VV_SUMS_FP32 = 0,       /* accumulation images are plain FP32 running sums */
     VV_SUMS_KAHAN = 1       /* FP32 running sums with Kahan compensation per merge */
 };
+/* The transfer function's 64 bucket maxima, from which the brick majorants
+ * come. The reference takes them from the FP32 LUT (renderer.rs:2164-2174)
+ * while the tracer samples the LUT rounded to FP16 (renderer.rs:2177-2195), so
+ * where an entry rounds up a sampled extinction can exceed its brick's
+ * majorant by up to an FP16 half-ulp (measured 2.4e-4 relative for some
+ * transfer functions). VV_MAJORANTS_BOUND takes the maxima of the FP16 LUT
+ * the tracer samples, then rounds them up by 2^-20 relative (past the
+ * rounding of the linear interpolation), so every sampled extinction is at or
+ * below its majorant. */
+enum {
+    VV_MAJORANTS_REFERENCE = 0, /* bucket maxima of the FP32 LUT (the reference) */
+    VV_MAJORANTS_BOUND = 1      /* of the FP16 LUT, rounded up: true bounds */
+};
 typedef struct vv_precision {
     uint32_t density_format; /* VV_DENSITY_* */
     uint32_t sums;           /* VV_SUMS_* */
     uint32_t fp64_after;     /* 0: never; else the running sums continue in FP64
                                 once they hold this many samples per pixel */
+    uint32_t majorants;      /* VV_MAJORANTS_* */
 } vv_precision;
 /* vv_renderer_create with a storage and running-sum precision. Frames
  * accumulated by the wavefront passes are summed per pass (FP32, atomically

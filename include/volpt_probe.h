@@ -35,12 +35,20 @@ vv_status vv_probe_paths(vv_renderer* r, const vv_frame_params* params, uint32_t
 vv_status vv_probe_paths_exact(vv_renderer* r, const vv_frame_params* params, uint32_t accumulated,
                                const int* pixels, size_t n, float* out);
 
+/* The extinction a free flight samples at n continuous voxel indices idx[3n]
+ * (extinction_at, pt.comp:277-292, then path_sigma, pt.comp:143-145) with
+ * direction dir[3] (index space) and, with smooth = 1, the first flight's
+ * B-spline density; and the flight majorant of the brick there (pt.comp:157-163):
+ * out[4n] = sigma (rgb), majorant. Runs record's preparation first. */
+vv_status vv_probe_extinction(vv_renderer* r, const vv_frame_params* params, const float* idx, size_t n,
+                              const float dir[3], int smooth, float* out);
+
 /* Event counting for the roofline's algorithmic-byte model: enable = 1 starts
  * counting the path tracer's memory events over the following records (at
  * some cost in speed); enable = 0 stops and copies up to n totals to out, in
  * the order: majorant lookups, cubic densities, trilinear densities, mask
  * lookups, label fetches, normal lookups, cubic gradients, pixel
- * accumulations, paths, path vertices, empty-space cell lookups. */
+ * accumulations, paths, path vertices. */
 vv_status vv_count_events(vv_renderer* r, int enable, uint64_t* out, size_t n);
 
 /* Device time of the path-tracing launches: enable = 1 starts recording CUDA

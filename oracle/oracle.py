@@ -81,6 +81,24 @@ def bucket_max(tf):
     return out
 
 
+# vv_precision.majorants: the reference's bucket maxima (of the FP32 LUT), or
+# true bounds of the FP16 LUT the tracer samples.
+MAJORANTS_REFERENCE, MAJORANTS_BOUND = 0, 1
+
+
+def bucket_bound(tf):
+    """Bucket maxima of the FP16-rounded LUT (the values pt.comp samples), each
+    multiplied by 1 + 2^-20 and rounded up to the next float32."""
+    lut = tf_lut_half(tf).view(np.float16).astype(np.float32)
+    out = np.zeros(64, np.float32)
+    for k in range(64):
+        m = np.float32(lut[64 * k:min(64 * k + 65, 4096), 3].max())
+        if m > 0:
+            m = np.nextafter(np.float32(m * np.float32(1.0 + 2.0 ** -20)), np.float32(np.inf), dtype=np.float32)
+        out[k] = m
+    return out
+
+
 def hu_to_unorm16(hu):
     hu = np.ascontiguousarray(hu, np.int16)
     out = np.zeros(hu.shape, np.uint16)
@@ -158,12 +176,13 @@ class CpuRenderer:
     every pass run by the oracle. Arrays are x-fastest, shaped (z, y, x, ...).
     """
 
-    def __init__(self, volume, tf, hu, density_format=DENSITY_UNORM16):
+    def __init__(self, volume, tf, hu, density_format=DENSITY_UNORM16, majorants=MAJORANTS_REFERENCE):
         self.volume = volume
         self.hu = np.ascontiguousarray(hu, np.int16)
         self.dims = tuple(volume.dims)
         self.geo = geometry(volume)
         self.density_format = density_format
+        self.majorants = majorants
         self.density = density_encode(self.hu, density_format)
         self.set_transfer_function(tf)
         self.labels = np.zeros((1, 1, 1), np.uint8)
@@ -193,7 +212,7 @@ class CpuRenderer:
         self.tf = tf
         self.lut = tf_lut_half(tf)
         self.preint = tf_cumulative(tf)
-        self.bucket = bucket_max(tf)
+        self.bucket = bucket_bound(tf) if self.majorants == MAJORANTS_BOUND else bucket_max(tf)
         self.mask_key = None
 
     def set_labels(self, labels, soft=None, src_axis=(0, 1, 2), flip=(0, 0, 0)):
@@ -358,6 +377,18 @@ class CpuRenderer:
         out = np.zeros((seeds.size, 6), np.float32)
         u = self.uniforms(params, 1, self.width, self.height)
         lib().vvo_light_samples(ptr(u), C.byref(self.scene()), ptr(seeds), C.c_long(seeds.size), ptr(out))
+        return out
+
+    def extinction(self, params, idx, direction=(0.0, 0.0, 1.0), smooth=True):
+        """(n, 4): the flight's sampled extinction (path_sigma, rgb) at continuous
+        indices idx and the flight majorant of the brick there."""
+        self.prepare(params, self.width, self.height)
+        idx = np.ascontiguousarray(idx, np.float32).reshape(-1, 3)
+        out = np.zeros((idx.shape[0], 4), np.float32)
+        u = self.uniforms(params, 1, self.width, self.height)
+        d = np.ascontiguousarray(direction, np.float32)
+        lib().vvo_extinction(ptr(u), C.byref(self.scene()), ptr(idx), C.c_long(idx.shape[0]), ptr(d), int(smooth),
+                             ptr(out), threads())
         return out
 
     def bspline(self, params, idx):

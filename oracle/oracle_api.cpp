@@ -23,6 +23,8 @@ void pt_frame(const Uniforms& u, const Scene& sc, float* accum, float* albedo, f
               int y0, int y1, int threads);
 void pt_pixel(const Uniforms& u, const Scene& sc, int x, int y, float out[12]);
 void pt_pixels(const Uniforms& u, const Scene& sc, const int* pix, long n, float* out, int threads);
+void extinction_probe(const Uniforms& u, const Scene& sc, const float* idx, long n, const float dir[3], int smooth,
+                      float* out, int threads);
 void pt_rows(const Uniforms& u, const Scene& sc, float* accum, float* albedo, float* normal, uint16_t* hdr,
              const int* rows, int nrows, int threads);
 void bspline(const Uniforms& u, const Scene& sc, const float* idx, long n, float* out);
@@ -153,6 +155,10 @@ void vvo_pt_pixel(const void* u, const vvo_scene* s, int x, int y, float out[12]
 }
 void vvo_pt_pixels(const void* u, const vvo_scene* s, const int* pix, long n, float* out, int threads) {
     pt_pixels(U(u), to_scene(s), pix, n, out, threads);
+}
+void vvo_extinction(const void* u, const vvo_scene* s, const float* idx, long n, const float* dir, int smooth,
+                    float* out, int threads) {
+    extinction_probe(U(u), to_scene(s), idx, n, dir, smooth, out, threads);
 }
 void vvo_bspline(const void* u, const vvo_scene* s, const float* idx, long n, float* out) {
     bspline(U(u), to_scene(s), idx, n, out);

@@ -1160,6 +1160,26 @@ void bspline(const Uniforms& u, const Scene& sc, const float* idx, long n, float
     }
 }
 
+// The extinction a flight samples at continuous indices idx[3n] (pt.comp:277-292
+// with path_sigma, pt.comp:143-145) and the flight majorant of the brick there
+// (pt.comp:157-163): out[4n] = sigma (rgb), majorant. `smooth` selects the
+// first flight's B-spline density; dir is the flight's direction.
+void extinction_probe(const Uniforms& u, const Scene& sc, const float* idx, long n, const float dir[3], int smooth,
+                      float* out, int threads) {
+    Units t = bind_scene(sc);
+    parallel_rows(n, threads, [&](long i) {
+        Tracer tr{Shading{u, t}};
+        vec3 p(idx[3 * i], idx[3 * i + 1], idx[3 * i + 2]);
+        Sample s;
+        int cap = -1;
+        float cut = 0.0f;
+        float ext = tr.extinction_at(p, vec3(dir[0], dir[1], dir[2]), smooth != 0, s, cap, cut);
+        vec3 sigma = ext > 0.0f ? tr.path_sigma(s, ext) : vec3(0.0f);
+        float v[4] = {sigma.x, sigma.y, sigma.z, tr.flight_majorant(p)};
+        std::memcpy(out + 4 * i, v, sizeof(v));
+    });
+}
+
 // ================================================================ denoise.comp
 static float lum(vec3 c) { return dot(c, vec3(0.2126f, 0.7152f, 0.0722f)); }
 

@@ -169,3 +169,37 @@ def test_ray_marcher_and_light_map_on_each_format(small_cfg, gpu_ctx, fmt):
     assert ok.mean() >= 0.99
     assert abs(d1[..., :3].mean() - d0[..., :3].mean()) <= 0.02 * d0[..., :3].mean()
     assert abs(a1.mean() - a0.mean()) <= 0.02 * a0.mean()
+
+
+@pytest.mark.parametrize("fmt", [abi.DENSITY_UNORM16] + FORMATS, ids=["unorm16", "fp16", "bf16", "fp32"])
+def test_majorants_are_true_bounds(small_cfg, gpu_ctx, fmt):
+    """Every extinction a flight samples on the device is at or below its
+    brick's flight majorant with VV_MAJORANTS_BOUND, in every storage format,
+    for transfer functions whose FP16 LUT exceeds the reference's FP32 bucket
+    maxima; the bucket maxima (uniforms) and the majorant grid are the
+    oracle's, bit for bit, in both modes. The reference's majorants are
+    reported: samples above them by up to an FP16 half-ulp."""
+    cfg = small_cfg
+    idx = np.random.default_rng(1).uniform(-0.5, 47.5, size=(200000, 3)).astype(np.float32)
+    for seed in (0, 3, 5):
+        tf = scene.random_transfer_function(seed)
+        for mode in (abi.MAJORANTS_REFERENCE, abi.MAJORANTS_BOUND):
+            gpu = R.Renderer(gpu_ctx, cfg["volume"], tf, abi.precision(density_format=fmt, majorants=mode))
+            cpu = O.CpuRenderer(cfg["volume"], tf, cfg["hu"], density_format=fmt, majorants=mode)
+            p = scene.frame_params_for(cfg, list(gpu.center), gpu.diagonal)
+            p.labels.mode = abi.LABEL_OFF
+            gpu.resize(16, 16)
+            cpu.resize(16, 16)
+            assert np.array_equal(gpu.pack_uniforms(p, 1), cpu.uniforms(p, 1, 16, 16))
+            counts = []
+            for smooth in (True, False):
+                out = gpu.probe_extinction(p, idx, smooth=smooth)
+                counts.append(int((out[:, :3].max(1) > out[:, 3]).sum()))
+            cpu.prepare(p, 16, 16)
+            assert np.array_equal(gpu.read_volume(abi.VOLUME_MAJORANT), cpu.majorant)
+            gpu.destroy()
+            name = "bound" if mode == abi.MAJORANTS_BOUND else "reference"
+            print(f"format {fmt}, transfer function {seed}, {name} majorants: {counts} of {len(idx)} samples "
+                  f"(B-spline, trilinear) above the majorant")
+            if mode == abi.MAJORANTS_BOUND:
+                assert counts == [0, 0]

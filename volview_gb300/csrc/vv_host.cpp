@@ -217,9 +217,9 @@ struct vv_renderer {
     float diagonal;
     // transfer function
     float bucket[64];
+    uint32_t majorants = VV_MAJORANTS_REFERENCE;  // VV_MAJORANTS_*: which bucket maxima
     // device volumes
     DBuf density, normals, mask_a, mask_b, labels, majorant, lut, bucket_dev, tables, soft, work, exposure;
-    DBuf occupancy;  // empty-space cells of the majorant grid (launch_occupancy)
     int soft_dims[3] = {1, 1, 1};
     int soft_push[4] = {0, 0, 0, 0};
     bool has_labels = false;
@@ -299,10 +299,12 @@ struct FormatLaunchers {
     decltype(&fmt0::launch_bspline_probe) bspline_probe;
     decltype(&fmt0::launch_light_sample_probe) light_sample_probe;
     decltype(&fmt0::launch_pt_pixels) pt_pixels;
+    decltype(&fmt0::launch_extinction_probe) extinction_probe;
 };
 #define VV_FORMAT_TABLE(ns)                                                                                   \
     {ns::launch_pt, ns::launch_pt_wavefront, ns::launch_ao, ns::launch_shadow_sweep, ns::launch_pad_lighting, \
-     ns::launch_dvr, ns::launch_bspline_probe, ns::launch_light_sample_probe, ns::launch_pt_pixels}
+     ns::launch_dvr, ns::launch_bspline_probe, ns::launch_light_sample_probe, ns::launch_pt_pixels,          \
+     ns::launch_extinction_probe}
 static const FormatLaunchers FORMAT_LAUNCHERS[4] = {VV_FORMAT_TABLE(fmt0), VV_FORMAT_TABLE(fmt1),
                                                     VV_FORMAT_TABLE(fmt2), VV_FORMAT_TABLE(fmt3)};
 static const FormatLaunchers& kernels_of(const vv_renderer* r) { return FORMAT_LAUNCHERS[r->vol.dfmt & 3]; }
@@ -373,14 +375,19 @@ static vv_status upload_tf(vv_renderer* r, const vv_transfer_function* tf) {
         float t = (float)i / 4095.0f;
         tf_eval(tf, -1024.0f + t * (3071.0f - -1024.0f), &lut[4 * i]);
     }
+    std::vector<float> lut_half(4 * 4096);
+    for (int i = 0; i < 4 * 4096; i++) lut_half[i] = (float)(_Float16)lut[i];
+    // VV_MAJORANTS_BOUND: the maxima of the FP16 entries the tracer samples,
+    // rounded up past the interpolation's rounding; else the reference's.
+    const bool bound = r->majorants == VV_MAJORANTS_BOUND;
+    const std::vector<float>& from = bound ? lut_half : lut;
     for (int b = 0; b < 64; b++) {
         int end = std::min((b + 1) * 64 + 1, 4096);
         float m = 0.0f;
-        for (int i = b * 64; i < end; i++) m = std::fmax(m, lut[4 * i + 3]);
+        for (int i = b * 64; i < end; i++) m = std::fmax(m, from[4 * i + 3]);
+        if (bound && m > 0.0f) m = std::nextafter(m * (1.0f + 0x1p-20f), INFINITY);
         r->bucket[b] = m;
     }
-    std::vector<float> lut_half(4 * 4096);
-    for (int i = 0; i < 4 * 4096; i++) lut_half[i] = (float)(_Float16)lut[i];
     CK(r->lut.alloc(lut_half.size() * sizeof(float)));
     CK(cudaMemcpyAsync(r->lut.p, lut_half.data(), lut_half.size() * sizeof(float), cudaMemcpyHostToDevice,
                        r->ctx->stream));
@@ -646,7 +653,7 @@ static m3 w2i_m3(const vv_renderer* r) {
 
 extern "C" vv_status vv_renderer_create(vv_context* ctx, const vv_volume* volume, const vv_transfer_function* tf,
                                         vv_renderer** out) {
-    vv_precision p = {VV_DENSITY_UNORM16, VV_SUMS_FP32, 0};
+    vv_precision p = {VV_DENSITY_UNORM16, VV_SUMS_FP32, 0, VV_MAJORANTS_REFERENCE};
     return vv_renderer_create_ex(ctx, volume, tf, &p, out);
 }
 
@@ -655,6 +662,7 @@ extern "C" vv_status vv_renderer_create_ex(vv_context* ctx, const vv_volume* vol
     if (!ctx || !volume || !tf || !out || !precision) return fail(VV_ERR_ARG, "null argument");
     if (precision->density_format > VV_DENSITY_FP32) return fail(VV_ERR_ARG, "unknown density format");
     if (precision->sums > VV_SUMS_KAHAN) return fail(VV_ERR_ARG, "unknown running-sum mode");
+    if (precision->majorants > VV_MAJORANTS_BOUND) return fail(VV_ERR_ARG, "unknown majorant mode");
     if (!volume->hu) return fail(VV_ERR_ARG, "volume has no voxels");
     for (int i = 0; i < 3; i++)
         if (volume->dims[i] == 0) return fail(VV_ERR_ARG, "volume has a zero dimension");
@@ -669,6 +677,7 @@ extern "C" vv_status vv_renderer_create_ex(vv_context* ctx, const vv_volume* vol
     r->vol = v;
     r->sums = precision->sums;
     r->fp64_after = precision->fp64_after;
+    r->majorants = precision->majorants;
     set_geometry(r, volume);
     r->tables_host = nullptr;
     cudaError_t e = cudaMallocHost((void**)&r->tables_host, sizeof(LabelTables));
@@ -689,7 +698,6 @@ extern "C" vv_status vv_renderer_create_ex(vv_context* ctx, const vv_volume* vol
     if ((e = r->density.alloc(elems * density_bytes(v.dfmt))) != cudaSuccess ||
         (e = r->normals.alloc(elems * sizeof(uint32_t))) != cudaSuccess ||
         (e = r->majorant.alloc((size_t)v.bx * v.by * v.bz * sizeof(float))) != cudaSuccess ||
-        (e = r->occupancy.alloc((size_t)occ_cells(v.bx) * occ_cells(v.by) * occ_cells(v.bz))) != cudaSuccess ||
         (e = r->tables.alloc(sizeof(LabelTables))) != cudaSuccess ||
         (e = r->work.alloc(256)) != cudaSuccess || (e = r->exposure.alloc(sizeof(float))) != cudaSuccess) {
         hu.release();
@@ -721,7 +729,7 @@ extern "C" vv_status vv_renderer_destroy(vv_renderer* r) {
         if (P.stream) cudaStreamDestroy(P.stream);
     }
     if (r->prep_done) cudaEventDestroy(r->prep_done);
-    DBuf* all[] = {&r->density, &r->normals, &r->mask_a, &r->mask_b, &r->labels, &r->majorant, &r->occupancy, &r->env_rad,
+    DBuf* all[] = {&r->density, &r->normals, &r->mask_a, &r->mask_b, &r->labels, &r->majorant, &r->env_rad,
                    &r->env_table, &r->env_diffuse, &r->env_guide, &r->preint, &r->shadow_vol, &r->ao_vol, &r->lut,
                    &r->bucket_dev, &r->tables, &r->soft, &r->work, &r->exposure, &r->accum, &r->albedo,
                    &r->normal, &r->ping, &r->pong, &r->guide_nd, &r->guide_alb, &r->hdr, &r->out, &r->bloom[0], &r->bloom[1], &r->bloom[2],
@@ -1107,7 +1115,7 @@ extern "C" vv_status vv_query(vv_renderer* r, int* idle) {
 
 extern "C" vv_status vv_renderer_memory(const vv_renderer* r, uint64_t* bytes) {
     if (!r || !bytes) return fail(VV_ERR_ARG, "null argument");
-    const DBuf* all[] = {&r->density, &r->normals, &r->mask_a, &r->mask_b, &r->labels, &r->majorant, &r->occupancy, &r->lut,
+    const DBuf* all[] = {&r->density, &r->normals, &r->mask_a, &r->mask_b, &r->labels, &r->majorant, &r->lut,
                          &r->bucket_dev, &r->tables, &r->soft, &r->work, &r->exposure, &r->accum, &r->albedo,
                          &r->normal, &r->ping, &r->pong, &r->guide_nd, &r->guide_alb, &r->hdr, &r->out,
                          &r->bloom[0], &r->bloom[1], &r->bloom[2], &r->bloom[3], &r->preint, &r->shadow_vol,
@@ -1162,11 +1170,6 @@ static PtArgs pt_args(vv_renderer* r, const UHead& u) {
     a.normals = r->normals.as<uint32_t>();
     a.labels = r->labels.as<uint8_t>();
     a.majorant = r->majorant.as<float>();
-    // Empty-space cells only where empty-space skipping is on (else no brick
-    // is skipped: every majorant is the cap).
-    a.occupancy = u.path[3] != 0u ? r->occupancy.as<uint8_t>() : nullptr;
-    a.occ_x = occ_cells(r->vol.bx);
-    a.occ_y = occ_cells(r->vol.by);
     a.env_rad = r->env_rad.as<ushort4>();
     a.env_diffuse = r->env_diffuse.as<ushort4>();
     a.preint = r->preint.as<float4>();
@@ -1324,8 +1327,7 @@ static vv_status prepare_frame(vv_renderer* r, const vv_frame_params& p, uint64_
         r->prep_work = true;
         CK(launch_majorant(r->density.p, r->mask_a.as<uint32_t>(), r->vol, key.mode, p.labels.extinction,
                            r->bucket_dev.as<float>(), r->majorant.as<float>(), st));
-        CK(launch_occupancy(r->majorant.as<float>(), r->vol, r->occupancy.as<uint8_t>(), st));
-        r->launches += 2;
+        r->launches += 1;
         r->majorant_key = key;
         r->have_majorant_key = true;
     }
@@ -1856,6 +1858,30 @@ extern "C" vv_status vv_probe_bspline(vv_renderer* r, const vv_frame_params* par
     di.release();
     dout.release();
     if (e != cudaSuccess) return cuda_fail(e, "bspline probe");
+    return VV_OK;
+}
+
+extern "C" vv_status vv_probe_extinction(vv_renderer* r, const vv_frame_params* params, const float* idx, size_t n,
+                                         const float dir[3], int smooth, float* out) {
+    if (!r || !params || !idx || !dir || !out) return fail(VV_ERR_ARG, "null argument");
+    if (n == 0) return VV_OK;
+    if (n > (size_t)INT32_MAX / 4) return fail(VV_ERR_LIMIT, "too many points for one probe");
+    UHead u;
+    vv_status s = prepare_frame(r, *params, 1, u);
+    if (s != VV_OK) return s;
+    DBuf di, dout;
+    CK(di.alloc(n * 12));
+    CK(dout.alloc(n * 16));
+    cudaStream_t st = r->ctx->stream;
+    PtArgs a = pt_args(r, u);
+    cudaError_t e = cudaMemcpyAsync(di.p, idx, n * 12, cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess)
+        e = kernels_of(r).extinction_probe(a, di.as<float>(), dout.as<float>(), (int)n, dir, smooth, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(out, dout.p, n * 16, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    di.release();
+    dout.release();
+    if (e != cudaSuccess) return cuda_fail(e, "extinction probe");
     return VV_OK;
 }
 

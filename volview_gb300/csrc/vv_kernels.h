@@ -30,11 +30,6 @@ struct PtArgs {
     const uint32_t* normals;
     const uint8_t* labels;
     const float* majorant;
-    // Empty-space cells of OCC_CELL^3 bricks: 1 where any brick's majorant is
-    // above 0 (launch_occupancy), or null. A flight or shadow ray crossing an
-    // empty cell steps through its bricks without loading their majorants.
-    const uint8_t* occupancy;
-    int occ_x, occ_y;           // cells along x and y
     const float4* preint;       // cumulative transfer-function integrals, 4096 (ray marcher)
     const ushort4* env_diffuse; // light map's diffuse convolution, 32 x 16 RGBA16F (ray marcher)
     const ushort4* env_rad;     // light map radiance, RGBA16F, env_w x env_h (lighting.w == 2)
@@ -74,8 +69,7 @@ enum {
     COUNT_PIXEL = 7,      // pixel accumulations, 3 x (16 B read + 16 B write) + 8 B
     COUNT_PATH = 8,       // paths started
     COUNT_VERTEX = 9,     // path vertices (bounce-loop iterations)
-    COUNT_OCCUPANCY = 10, // empty-space cell lookups, 1 B
-    COUNT_N = 11
+    COUNT_N = 10
 };
 
 cudaError_t launch_density(const int16_t* hu, void* out, const Vol& v, cudaStream_t s);
@@ -83,14 +77,6 @@ cudaError_t launch_normals(const void* d, uint32_t* out, const Vol& v, const m3&
 cudaError_t launch_masks(const MaskLaunch& L, cudaStream_t s);
 cudaError_t launch_majorant(const void* d, const uint32_t* mask, const Vol& v, int mode, float label_ext,
                             const float* bucket, float* out, cudaStream_t s);
-// Bricks per empty-space cell along each axis (2^OCC_SHIFT).
-#ifndef VV_OCC_SHIFT
-#define VV_OCC_SHIFT 2
-#endif
-constexpr int OCC_SHIFT = VV_OCC_SHIFT;
-inline int occ_cells(int bricks) { return (bricks + (1 << OCC_SHIFT) - 1) >> OCC_SHIFT; }
-// out[cell] = 1 if any brick of the cell has a majorant above 0, else 0.
-cudaError_t launch_occupancy(const float* majorant, const Vol& v, uint8_t* out, cudaStream_t s);
 cudaError_t launch_unbrick(const void* src, void* dst, const Vol& v, int elem, cudaStream_t s);
 cudaError_t launch_brick_u8(const uint8_t* src, uint8_t* dst, const Vol& v, cudaStream_t s);
 
@@ -154,7 +140,10 @@ struct LightTex {
     cudaError_t launch_bspline_probe(const PtArgs& a, const float* idx, float* out, int n, cudaStream_t s);     \
     cudaError_t launch_light_sample_probe(const PtArgs& a, const uint32_t* seeds, float* out, int n,            \
                                           cudaStream_t s);                                                      \
-    cudaError_t launch_pt_pixels(const PtArgs& a, const int* px, float* out, int n, cudaStream_t s);
+    cudaError_t launch_pt_pixels(const PtArgs& a, const int* px, float* out, int n, cudaStream_t s);            \
+    /* The sampled extinction and the brick's flight majorant at n indices. */                                  \
+    cudaError_t launch_extinction_probe(const PtArgs& a, const float* idx, float* out, int n, const float dir[3], \
+                                        int smooth, cudaStream_t s);
 namespace fmt0 { VV_FORMAT_LAUNCHERS }
 namespace fmt1 { VV_FORMAT_LAUNCHERS }
 namespace fmt2 { VV_FORMAT_LAUNCHERS }

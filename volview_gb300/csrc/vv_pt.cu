@@ -156,6 +156,26 @@ cudaError_t launch_bspline_probe(const PtArgs& a, const float* idx, float* out, 
     return cudaGetLastError();
 }
 
+// The extinction a flight samples at idx (extinction_at, pt.comp:277-292, with
+// path_sigma) and the flight majorant of the brick there: out[4n] = sigma.xyz, majorant.
+__global__ void k_extinction_probe(const __grid_constant__ PtArgs A, const float* idx, float* out, int n, f3 dir,
+                                   int smooth) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    f3 p = mk(idx[3 * i], idx[3 * i + 1], idx[3 * i + 2]);
+    int cap = -1;
+    float cut = clip_depth(A, p, cap);
+    Sample s;
+    float ext = cut > 0.0f ? 0.0f : extinction_unclipped(A, p, dir, smooth != 0, s, cap, cut);
+    f3 sigma = ext > 0.0f ? path_sigma(A, s, ext) : mk(0.0f);
+    out[4 * i] = sigma.x; out[4 * i + 1] = sigma.y; out[4 * i + 2] = sigma.z;
+    out[4 * i + 3] = flight_majorant_of(A, brick_index(A, p));
+}
+cudaError_t launch_extinction_probe(const PtArgs& a, const float* idx, float* out, int n, const float dir[3],
+                                    int smooth, cudaStream_t s) {
+    k_extinction_probe<<<(n + 127) / 128, 128, 0, s>>>(a, idx, out, n, mk(dir[0], dir[1], dir[2]), smooth);
+    return cudaGetLastError();
+}
 __global__ void k_light_sample_probe(const __grid_constant__ PtArgs A, const uint32_t* seeds, float* out, int n) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;

@@ -1077,38 +1077,7 @@ struct Flight {
     int iter;
     int brick;    // brick whose flight majorant `maj` holds (-1: none yet)
     float maj;
-    int cell;     // empty-space cell of `brick` (-1: none yet); `occupied`: it has a brick with a majorant
-    bool occupied;
 };
-
-// The flight majorant (pt.comp:157-163) of the brick at continuous index p,
-// through a ray's cache of its last brick and of that brick's empty-space
-// cell: entering a cell loads its occupancy beside the brick's majorant; the
-// other bricks of an empty cell have majorant 0 and are not loaded. The value
-// is flight_majorant_of's for the same brick in every case.
-__device__ __forceinline__ float majorant_at(const PtArgs& A, f3 p, int& brick, float& maj, int& cell,
-                                             bool& occupied) {
-    int bx = clampi((int)floorf((p.x + 0.5f) * 0.125f), 0, A.vol.bx - 1);
-    int by = clampi((int)floorf((p.y + 0.5f) * 0.125f), 0, A.vol.by - 1);
-    int bz = clampi((int)floorf((p.z + 0.5f) * 0.125f), 0, A.vol.bz - 1);
-    int b = (bz * A.vol.by + by) * A.vol.bx + bx;
-    if (b == brick) return maj;
-    brick = b;
-    if (!A.occupancy) {
-        maj = flight_majorant_of(A, b);
-        return maj;
-    }
-    int c = ((bz >> OCC_SHIFT) * A.occ_y + (by >> OCC_SHIFT)) * A.occ_x + (bx >> OCC_SHIFT);
-    if (c != cell) {
-        cell = c;
-        count(A, COUNT_OCCUPANCY);
-        occupied = __ldg(A.occupancy + c) != 0;
-        maj = flight_majorant_of(A, b);
-    } else {
-        maj = occupied ? flight_majorant_of(A, b) : 0.0f;
-    }
-    return maj;
-}
 enum { FF_CONTINUE = 0, FF_HIT = 1, FF_ESCAPE = 2 };
 
 __device__ __forceinline__ void ff_begin(const PtArgs& A, f3 origin, f3 dir, Flight& F) {
@@ -1119,8 +1088,6 @@ __device__ __forceinline__ void ff_begin(const PtArgs& A, f3 origin, f3 dir, Fli
     F.t_end = tr.y;
     F.iter = 0;
     F.brick = -1;
-    F.cell = -1;
-    F.occupied = true;
 }
 
 __device__ __forceinline__ int ff_step(const PtArgs& A, f3 origin, f3 dir, bool smooth, int hero, f3& spectral,
@@ -1134,8 +1101,13 @@ __device__ __forceinline__ int ff_step(const PtArgs& A, f3 origin, f3 dir, bool 
     for (;;) {
         if (!(F.iter < 4096 && F.tt < F.t_end)) return FF_ESCAPE;
         f3 p = origin + F.d_idx * F.tt;
-        majorant = majorant_at(A, p, F.brick, F.maj, F.cell, F.occupied);
+        int b = brick_index(A, p);
+        if (b != F.brick) {
+            F.brick = b;
+            F.maj = flight_majorant_of(A, b);
+        }
         F.iter++;
+        majorant = F.maj;
         float exit = F.tt + brick_exit(p, F.inv_d) + 1e-3f;
         if (majorant <= 0.0f) {
             F.tt = exit;
@@ -1180,9 +1152,6 @@ struct Shadow {
     f3 d_idx, inv_d, result;
     float tt, t_end;
     int iter;
-    int brick, cell;  // the ray's last brick and empty-space cell (majorant_at)
-    float maj;
-    bool occupied;
 };
 __device__ __forceinline__ void tr_begin(const PtArgs& A, f3 origin, f3 dir, Shadow& T) {
     T.d_idx = mul(w2i3(A), dir);
@@ -1192,9 +1161,6 @@ __device__ __forceinline__ void tr_begin(const PtArgs& A, f3 origin, f3 dir, Sha
     T.t_end = tr.y;
     T.iter = 0;
     T.result = mk(1.0f);
-    T.brick = -1;
-    T.cell = -1;
-    T.occupied = true;
 }
 // Returns false when the estimate is final.
 __device__ __forceinline__ bool tr_step(const PtArgs& A, f3 origin, Shadow& T, Rng& rng) {
@@ -1212,7 +1178,7 @@ __device__ __forceinline__ bool tr_step(const PtArgs& A, f3 origin, Shadow& T, R
         T.result *= 0.1f / peak;
     }
     f3 p = origin + T.d_idx * T.tt;
-    float majorant = majorant_at(A, p, T.brick, T.maj, T.cell, T.occupied);
+    float majorant = flight_majorant_of(A, brick_index(A, p));
     float exit = T.tt + brick_exit(p, T.inv_d) + 1e-3f;
     if (majorant <= 0.0f) {
         T.tt = exit;

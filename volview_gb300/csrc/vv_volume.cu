@@ -300,19 +300,6 @@ __global__ void k_majorant(const void* __restrict__ d, const uint32_t* __restric
     out[b] = bound;
 }
 
-// Empty-space cells: one thread per cell of OCC_CELL^3 bricks.
-__global__ void k_occupancy(const float* __restrict__ maj, Vol v, int cx, int cy, int cz, uint8_t* __restrict__ out) {
-    int c = blockIdx.x * blockDim.x + threadIdx.x;
-    if (c >= cx * cy * cz) return;
-    int x0 = (c % cx) << OCC_SHIFT, y0 = ((c / cx) % cy) << OCC_SHIFT, z0 = (c / (cx * cy)) << OCC_SHIFT;
-    int x1 = min(x0 + (1 << OCC_SHIFT), v.bx), y1 = min(y0 + (1 << OCC_SHIFT), v.by), z1 = min(z0 + (1 << OCC_SHIFT), v.bz);
-    uint8_t any = 0;
-    for (int z = z0; z < z1; z++)
-        for (int y = y0; y < y1; y++)
-            for (int x = x0; x < x1; x++) any |= __ldg(maj + (z * v.by + y) * v.bx + x) > 0.0f ? 1 : 0;
-    out[c] = any;
-}
-
 // Bricked -> x-fastest copy of `elem`-byte elements.
 __global__ void k_unbrick(const uint8_t* __restrict__ src, uint8_t* __restrict__ dst, Vol v, int elem) {
     long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -367,11 +354,6 @@ cudaError_t launch_majorant(const void* d, const uint32_t* mask, const Vol& v, i
                             const float* bucket, float* out, cudaStream_t s) {
     int nb = v.bx * v.by * v.bz;
     k_majorant<<<blocks_for(nb, 128), 128, 0, s>>>(d, mask, v, mode, label_ext, bucket, out);
-    return cudaGetLastError();
-}
-cudaError_t launch_occupancy(const float* majorant, const Vol& v, uint8_t* out, cudaStream_t s) {
-    int cx = occ_cells(v.bx), cy = occ_cells(v.by), cz = occ_cells(v.bz);
-    k_occupancy<<<blocks_for((long)cx * cy * cz, 128), 128, 0, s>>>(majorant, v, cx, cy, cz, out);
     return cudaGetLastError();
 }
 cudaError_t launch_unbrick(const void* src, void* dst, const Vol& v, int elem, cudaStream_t s) {

@@ -64,6 +64,7 @@ PROBES = [
     ("vv_probe_paths", C.c_int, [P, P, C.c_uint32, P, C.c_size_t, P]),
     ("vv_probe_paths_exact", C.c_int, [P, P, C.c_uint32, P, C.c_size_t, P]),
     ("vv_probe_light_samples", C.c_int, [P, P, P, C.c_size_t, P]),
+    ("vv_probe_extinction", C.c_int, [P, P, P, C.c_size_t, P, C.c_int, P]),
     ("vv_count_events", C.c_int, [P, C.c_int, P, C.c_size_t]),
     ("vv_time_pt", C.c_int, [P, C.c_int, P, P]),
 ]
@@ -89,10 +90,9 @@ NN = [
     ("vv_nn_prediction_to_hdr", I, [P, I, I, I, I, P, F, P, P]),
 ]
 
-COUNT_NAMES = ["majorant", "cubic", "trilinear", "mask", "label", "normal", "gradient", "pixel", "path", "vertex",
-               "occupancy"]
+COUNT_NAMES = ["majorant", "cubic", "trilinear", "mask", "label", "normal", "gradient", "pixel", "path", "vertex"]
 # Unique element bytes each event must read (and write, for pixels).
-COUNT_BYTES = [4, 128, 16, 32, 1, 32, 128, 104, 0, 0, 1]
+COUNT_BYTES = [4, 128, 16, 32, 1, 32, 128, 104, 0, 0]
 
 _lib = None
 
@@ -279,6 +279,16 @@ class Renderer:
         seeds = np.ascontiguousarray(seeds, np.uint32).ravel()
         out = np.zeros((seeds.size, 6), np.float32)
         check(load().vv_probe_light_samples(self.handle, C.byref(params), _ptr(seeds), seeds.size, _ptr(out)))
+        return out
+
+    def probe_extinction(self, params, idx, direction=(0.0, 0.0, 1.0), smooth=True):
+        """(n, 4): sampled extinction (rgb) at continuous indices idx and the
+        flight majorant of the brick there (vv_probe_extinction)."""
+        idx = np.ascontiguousarray(idx, np.float32).reshape(-1, 3)
+        d = np.ascontiguousarray(direction, np.float32)
+        out = np.zeros((idx.shape[0], 4), np.float32)
+        check(load().vv_probe_extinction(self.handle, C.byref(params), _ptr(idx), idx.shape[0], _ptr(d), int(smooth),
+                                         _ptr(out)))
         return out
 
     def probe_paths(self, params, accumulated, pixels, exact=False):

@@ -440,6 +440,16 @@ def mode_case(name, params, center):
     return True
 
 
+def random_transfer_function(seed):
+    """A seeded transfer function of six control points (HU, albedo, extinction
+    0..3 per mm) spread over the density range: a test input whose LUT entries
+    round up and down in FP16."""
+    rng = np.random.default_rng(seed)
+    hu = sorted(rng.uniform(HU_MIN, HU_MAX, 6))
+    return abi.tf_struct([(float(h), tuple(float(c) for c in rng.uniform(0.0, 1.0, 3)), float(rng.uniform(0.0, 3.0)))
+                          for h in hu])
+
+
 def synthetic_light_map(width=64, height=32, seed=3):
     """A seeded equirectangular studio-like HDR light map, (height, width, 3) linear RGB,
     rows from the zenith down: a graded sky, a small bright sun and two soft boxes,

@@ -1210,6 +1210,12 @@ static cudaError_t run_pt(vv_renderer* r, vv_renderer::Pass& P, PtArgs& a, cudaS
         a.persistent = std::strcmp(k, "persistent") == 0 || a.frames > 1;
         return kernels_of(r).pt(a, r->ctx->sms, s, launches);
     }
+    // A wavefront slot counts its pixel's samples in 20 bits; 2^20 or more
+    // samples per frame run on the persistent single-kernel tracer.
+    if (a.u.path[2] >= WF_MAX_SAMPLES) {
+        a.persistent = 1;
+        return kernels_of(r).pt(a, r->ctx->sms, s, launches);
+    }
     // Paths in flight: with several frames per pass, up to 16 frames' worth
     // (VV_WF_SLOTS overrides), at most 2^24 slots (4.6 GB of path state) unless
     // one frame needs more. Every frame of a 16-frame pass then runs in the
@@ -1229,8 +1235,14 @@ static cudaError_t run_pt(vv_renderer* r, vv_renderer::Pass& P, PtArgs& a, cudaS
     cap = P.slots.n / WF_SLOT_BYTES;
     WfArgs w;
     w.capacity = (uint32_t)cap;
-    w.slots = P.slots.as<float4>();
-    w.map = P.map.as<float4>();
+    // The records of vv_wavefront.cu, each an array over the slots.
+    float4* rec = P.slots.as<float4>();
+    w.path = rec;
+    w.acc = rec + 4 * cap;
+    w.vtx = rec + 8 * cap;
+    w.shd = rec + 12 * cap;
+    w.sh = rec + 16 * cap;
+    w.mapdir = P.map.as<float4>();
     uint32_t* q = P.queues.as<uint32_t>();
     w.ext[0] = q;
     w.ext[1] = q + cap;

@@ -80,10 +80,14 @@ cudaError_t launch_majorant(const void* d, const uint32_t* mask, const Vol& v, i
 cudaError_t launch_unbrick(const void* src, void* dst, const Vol& v, int elem, cudaStream_t s);
 cudaError_t launch_brick_u8(const uint8_t* src, uint8_t* dst, const Vol& v, cudaStream_t s);
 
-// Wavefront tracer state: one slot of WF_SLOT_BYTES per pixel, the stage
-// queues (slot indices) and their counters.
-constexpr int WF_SLOT_BYTES = 256;
-constexpr int WF_MAP_BYTES = 32;  // per slot: the light map's next-event sample
+// Wavefront tracer state: per slot (path in flight) WF_SLOT_BYTES of records
+// (path, accumulation, vertex, shaded vertex, shadow result; vv_wavefront.cu),
+// WF_MAP_BYTES more with a light map, the stage queues (slot indices) and
+// their counters. A slot's sample count has 20 bits: the wavefront takes
+// fewer than WF_MAX_SAMPLES samples per frame.
+constexpr int WF_SLOT_BYTES = 288;
+constexpr int WF_MAP_BYTES = 16;  // per slot: the light map sample's direction
+constexpr uint32_t WF_MAX_SAMPLES = 1u << 20;
 enum {
     WF_EXT0 = 0, WF_EXT1 = 1, WF_SHADE = 2, WF_SHADOW = 3, WF_SCATTER = 4,
     WF_ITEMS = 5,     // next (frame, pixel) work item
@@ -97,8 +101,12 @@ enum {
 };
 struct WfArgs {
     uint32_t capacity;     // slots (and queue entries) allocated
-    float4* slots;
-    float4* map;           // WF_MAP_BYTES per slot
+    float4* path;          // 4 x float4 per slot
+    float4* acc;           // 4 x float4 per slot
+    float4* vtx;           // 4 x float4 per slot
+    float4* shd;           // 4 x float4 per slot
+    float4* sh;            // 2 x float4 per slot
+    float4* mapdir;        // 1 x float4 per slot (light map)
     uint32_t* ext[2];      // later flights
     uint32_t* first[2];    // first flights
     uint32_t* esc[2];

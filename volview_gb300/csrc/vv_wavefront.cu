@@ -32,82 +32,111 @@
 namespace vv {
 namespace VV_FMT_NS {  // this density format's kernels and launchers
 
-// Slot layout: 16 x float4 = 256 bytes per pixel (WF_SLOT_BYTES); the light
-// map's sample, when there is a light map, in a parallel array of 2 x float4.
-enum {
-    Q_ORIGIN = 0,   // origin.xyz, last_pdf
-    Q_DIR = 1,      // dir.xyz, rng
-    Q_THRU = 2,     // throughput.xyz, pixel
-    Q_SPEC = 3,     // spectral.xyz, bounce | surfaces << 16
-    Q_RAD = 4,      // radiance.xyz, volumes
-    Q_SUM = 5,      // sum.xyz, background
-    Q_ALB = 6,      // albedo sum
-    Q_NOR = 7,      // normal sum
-    Q_IDX = 8,      // vertex idx.xyz, cut
-    Q_SA = 9,       // sample albedo.xyz, extinction
-    Q_SB = 10,      // roughness, metalness, density, subsurface
-    Q_SC = 11,      // coat, label, ghost | surface_event << 1, cap_plane
-    Q_N = 12,       // shading normal
-    Q_LD = 13,      // light direction
-    Q_LT = 14,      // light transmittance
-    Q_CTL = 15,     // frame, sample, hero, escape flag (extend -> scatter)
-    Q_COUNT = 16
-};
-// W.map entries per slot: light map sample direction.xyz and pdf (0: none);
-// its radiance / pdf x transmittance.
-enum { M_DIR = 0, M_LIGHT = 1, M_COUNT = 2 };
-static_assert(Q_COUNT * 16 == WF_SLOT_BYTES, "slot layout");
+// Path state, one record array per producer, indexed by slot. Each record is
+// a whole number of 32-byte DRAM sectors and every stage writes whole sectors,
+// so a stage reads only what it uses and no sector is left half-written:
+//
+//   record  bytes  written by            read by
+//   PATH    64     scatter, init         extend (all), shade (sector 0)
+//   ACC     64     scatter, init; shade  scatter (sector 0 each vertex, all at
+//                  (sector 1, bounce 0)  the path's end), shade (bounce 0)
+//   VTX     64     extend                shade; scatter (escapes: sector 1)
+//   SHD     64     shade                 shadow (sector 0), scatter
+//   SH      32     shadow                scatter
+//   MAPDIR  16     shadow (light map)    scatter (light map)
+//
+// PATH: P0 origin.xyz, rng | P1 dir.xyz, bounce | surfaces << 16
+//       P2 spectral.xyz, volumes | sample << 10 | hero << 30 | P3 throughput.xyz, last_pdf
+// ACC:  A0 radiance.xyz, item | A1 sum.xyz, background | A2 albedo sums | A3 normal sums
+// VTX:  V0 idx.xyz, cut | V1 sample albedo.xyz, extinction
+//       V2 roughness, metalness, density, subsurface | V3 coat, label word, rng, escape flag
+// SHD:  S0 idx.xyz, rng | S1 light direction.xyz, event word
+//       S2 albedo.xyz, roughness | S3 shading normal.xyz, metalness
+// SH:   H0 light transmittance.xyz, rng | H1 light map radiance / pdf x transmittance.xyz, pdf
+// MAPDIR: the light map sample's direction.xyz
+//
+// The SHD event word is the coat (a float in [0, 1]) for a surface event; for
+// a volume event, which needs no coat, roughness, metalness or normal, it is
+// EV_VOLUME | label | ghost << 16 (a NaN pattern no coat takes).
+enum { PATH_N = 4, ACC_N = 4, VTX_N = 4, SHD_N = 4, SH_N = 2 };
+static_assert((PATH_N + ACC_N + VTX_N + SHD_N + SH_N) * 16 == WF_SLOT_BYTES, "slot layout");
+static_assert(16 == WF_MAP_BYTES, "light map record");
+constexpr uint32_t EV_VOLUME = 0xFFC00000u;
+constexpr uint32_t SAMPLE_BITS = 20u;  // samples per frame below 2^20 (WF_MAX_SAMPLES)
+static_assert((1u << SAMPLE_BITS) == WF_MAX_SAMPLES, "sample field");
 
-__device__ __forceinline__ float4* slot_of(const WfArgs& W, uint32_t s) { return W.slots + (size_t)s * Q_COUNT; }
-__device__ __forceinline__ float4* map_of(const WfArgs& W, uint32_t s) { return W.map + (size_t)s * M_COUNT; }
+__device__ __forceinline__ float4* rec(float4* base, uint32_t s, int n) { return base + (size_t)s * n; }
 __device__ __forceinline__ float4 f4(f3 v, float w) { return make_float4(v.x, v.y, v.z, w); }
 __device__ __forceinline__ f3 xyz(float4 q) { return mk(q.x, q.y, q.z); }
 __device__ __forceinline__ uint32_t ubits(float f) { return __float_as_uint(f); }
 __device__ __forceinline__ float fbits(uint32_t u) { return __uint_as_float(u); }
 
-struct Ctl {
-    uint32_t pixel, frame, sample;
-};
-
-__device__ void load_path(const float4* q, Path& P, Ctl& c) {
-    float4 a = q[Q_ORIGIN], b = q[Q_DIR], t = q[Q_THRU], s = q[Q_SPEC], r = q[Q_RAD], k = q[Q_CTL];
+__device__ __forceinline__ uint32_t path_word(const Path& P, uint32_t sample) {
+    return P.volumes | (sample << 10) | ((uint32_t)P.hero << 30);
+}
+__device__ __forceinline__ void unpack_path_word(uint32_t w, Path& P, uint32_t& sample) {
+    P.volumes = w & 1023u;
+    sample = (w >> 10) & ((1u << SAMPLE_BITS) - 1u);
+    P.hero = (int)(w >> 30);
+}
+__device__ void load_path(const WfArgs& W, uint32_t s, Path& P, uint32_t& sample) {
+    const float4* q = rec(W.path, s, PATH_N);
+    float4 a = q[0], b = q[1], c = q[2], d = q[3];
     P.origin = xyz(a);
-    P.last_pdf = a.w;
+    P.rng.s = ubits(a.w);
     P.dir = xyz(b);
-    P.rng.s = ubits(b.w);
-    P.throughput = xyz(t);
-    c.pixel = ubits(t.w);
-    P.spectral = xyz(s);
-    P.bounce = ubits(s.w) & 0xffffu;
-    P.surfaces = ubits(s.w) >> 16;
-    P.radiance = xyz(r);
-    P.volumes = ubits(r.w);
-    c.frame = ubits(k.x);
-    c.sample = ubits(k.y);
-    P.hero = (int)ubits(k.z);
+    P.bounce = ubits(b.w) & 0xffffu;
+    P.surfaces = ubits(b.w) >> 16;
+    P.spectral = xyz(c);
+    unpack_path_word(ubits(c.w), P, sample);
+    P.throughput = xyz(d);
+    P.last_pdf = d.w;
 }
-__device__ void store_path(float4* q, const Path& P, const Ctl& c) {
-    q[Q_ORIGIN] = f4(P.origin, P.last_pdf);
-    q[Q_DIR] = f4(P.dir, fbits(P.rng.s));
-    q[Q_THRU] = f4(P.throughput, fbits(c.pixel));
-    q[Q_SPEC] = f4(P.spectral, fbits(P.bounce | (P.surfaces << 16)));
-    q[Q_RAD] = f4(P.radiance, fbits(P.volumes));
-    q[Q_CTL] = make_float4(fbits(c.frame), fbits(c.sample), fbits((uint32_t)P.hero), 0.0f);
+__device__ void store_path(const WfArgs& W, uint32_t s, const Path& P, uint32_t sample) {
+    float4* q = rec(W.path, s, PATH_N);
+    q[0] = f4(P.origin, fbits(P.rng.s));
+    q[1] = f4(P.dir, fbits(P.bounce | (P.surfaces << 16)));
+    q[2] = f4(P.spectral, fbits(path_word(P, sample)));
+    q[3] = f4(P.throughput, P.last_pdf);
 }
-__device__ void load_sums(const float4* q, PixelSums& S) {
-    float4 a = q[Q_SUM];
-    S.sum = xyz(a);
-    S.background = a.w;
-    S.albedo = q[Q_ALB];
-    S.normal = q[Q_NOR];
+// ACC sector 0: the path's radiance, its work item, the pixel's sum and background.
+__device__ void load_acc_head(const WfArgs& W, uint32_t s, Path& P, uint32_t& item, PixelSums& S) {
+    const float4* q = rec(W.acc, s, ACC_N);
+    float4 a = q[0], b = q[1];
+    P.radiance = xyz(a);
+    item = ubits(a.w);
+    S.sum = xyz(b);
+    S.background = b.w;
 }
-__device__ void store_sums(float4* q, const PixelSums& S) {
-    q[Q_SUM] = f4(S.sum, S.background);
-    q[Q_ALB] = S.albedo;
-    q[Q_NOR] = S.normal;
+__device__ void store_acc_head(const WfArgs& W, uint32_t s, const Path& P, uint32_t item, const PixelSums& S) {
+    float4* q = rec(W.acc, s, ACC_N);
+    q[0] = f4(P.radiance, fbits(item));
+    q[1] = f4(S.sum, S.background);
 }
-__device__ void load_vertex(const float4* q, Vertex& V) {
-    float4 a = q[Q_IDX], b = q[Q_SA], c = q[Q_SB], d = q[Q_SC];
+// ACC sector 1: the guides' sums (written at the first bounce and the path's end).
+__device__ void load_acc_guides(const WfArgs& W, uint32_t s, PixelSums& S) {
+    const float4* q = rec(W.acc, s, ACC_N);
+    S.albedo = q[2];
+    S.normal = q[3];
+}
+__device__ void store_acc_guides(const WfArgs& W, uint32_t s, const PixelSums& S) {
+    float4* q = rec(W.acc, s, ACC_N);
+    q[2] = S.albedo;
+    q[3] = S.normal;
+}
+__device__ __forceinline__ uint32_t label_word(const Sample& s, int cap_plane) {
+    return (s.label & 0xffffu) | (s.ghost ? 1u << 16 : 0u) | ((uint32_t)(cap_plane + 1) << 17);
+}
+__device__ void store_vertex(const WfArgs& W, uint32_t s, const Vertex& V, uint32_t rng) {
+    float4* q = rec(W.vtx, s, VTX_N);
+    q[0] = f4(V.idx, V.cut);
+    q[1] = f4(V.s.albedo, V.s.extinction);
+    q[2] = make_float4(V.s.roughness, V.s.metalness, V.s.density, V.s.subsurface);
+    q[3] = make_float4(V.s.coat, fbits(label_word(V.s, V.cap_plane)), fbits(rng), 0.0f);
+}
+__device__ void load_vertex(const WfArgs& W, uint32_t s, Vertex& V, uint32_t& rng) {
+    const float4* q = rec(W.vtx, s, VTX_N);
+    float4 a = q[0], b = q[1], c = q[2], d = q[3];
     V.idx = xyz(a);
     V.cut = a.w;
     V.s.albedo = xyz(b);
@@ -117,18 +146,47 @@ __device__ void load_vertex(const float4* q, Vertex& V) {
     V.s.density = c.z;
     V.s.subsurface = c.w;
     V.s.coat = d.x;
-    V.s.label = ubits(d.y);
-    uint32_t fl = ubits(d.z);
-    V.s.ghost = (fl & 1u) != 0u;
-    V.surface_event = (fl & 2u) != 0u;
-    V.cap_plane = (int)ubits(d.w);
+    uint32_t w = ubits(d.y);
+    V.s.label = w & 0xffffu;
+    V.s.ghost = (w >> 16) & 1u;
+    V.cap_plane = (int)(w >> 17) - 1;
+    rng = ubits(d.z);
 }
-__device__ void store_vertex(float4* q, const Vertex& V) {
-    q[Q_IDX] = f4(V.idx, V.cut);
-    q[Q_SA] = f4(V.s.albedo, V.s.extinction);
-    q[Q_SB] = make_float4(V.s.roughness, V.s.metalness, V.s.density, V.s.subsurface);
-    q[Q_SC] = make_float4(V.s.coat, fbits(V.s.label), fbits((V.s.ghost ? 1u : 0u) | (V.surface_event ? 2u : 0u)),
-                          fbits((uint32_t)V.cap_plane));
+// What scatter needs of the vertex after shade, and shadow of it (sector 0).
+__device__ void store_shaded(const WfArgs& W, uint32_t s, const Vertex& V, uint32_t rng) {
+    float4* q = rec(W.shd, s, SHD_N);
+    uint32_t ev = V.surface_event ? ubits(V.s.coat)
+                                  : EV_VOLUME | (V.s.label & 0xffffu) | (V.s.ghost ? 1u << 16 : 0u);
+    q[0] = f4(V.idx, fbits(rng));
+    q[1] = f4(V.light_dir, fbits(ev));
+    q[2] = f4(V.s.albedo, V.s.roughness);
+    q[3] = f4(V.n, V.s.metalness);
+}
+__device__ void load_shaded(const WfArgs& W, uint32_t s, Vertex& V) {
+    const float4* q = rec(W.shd, s, SHD_N);
+    float4 a = q[0], b = q[1], c = q[2], d = q[3];
+    V.idx = xyz(a);
+    V.light_dir = xyz(b);
+    uint32_t ev = ubits(b.w);
+    V.surface_event = (ev & EV_VOLUME) != EV_VOLUME;
+    V.s.albedo = xyz(c);
+    V.s.roughness = c.w;
+    V.n = xyz(d);
+    V.s.metalness = d.w;
+    if (V.surface_event) {
+        V.s.coat = b.w;
+        V.s.label = 0u;
+        V.s.ghost = false;
+    } else {
+        V.s.coat = 0.0f;
+        V.s.label = ev & 0xffffu;
+        V.s.ghost = (ev >> 16) & 1u;
+    }
+    V.s.extinction = 0.0f;  // not read after shade
+    V.s.density = 0.0f;
+    V.s.subsurface = 0.0f;
+    V.cut = 0.0f;
+    V.cap_plane = -1;
 }
 
 // Appends `slot` to queue `q` where `pred`; called by all 32 lanes together.
@@ -143,37 +201,37 @@ __device__ __forceinline__ void push(uint32_t* q, uint32_t* count, uint32_t slot
     if (pred) q[base + __popc(m & ((1u << lane) - 1u))] = slot;
 }
 
-// Ends a sample path: firefly clamp and sums, then the pixel's next sample
-// (pt.comp:403, 546-560). Returns true when the slot has a new path; false when
-// the work item (one pixel of one frame) is done and accumulated.
-__device__ bool end_path(const PtArgs& A, const Consts& C, Path& P, PixelSums& S, Ctl& c) {
+// The end of a sample path: firefly clamp and sums (pt.comp:546-551), then
+// the pixel's next sample in the same slot (pt.comp:403). Returns true when
+// the slot has a new path; false when the work item (one pixel of one frame)
+// is done and its sums are ready to accumulate.
+__device__ bool end_sample(const PtArgs& A, const Consts& C, Path& P, PixelSums& S, uint32_t item, uint32_t& sample) {
     finish_path(P, S);
-    uint32_t spf = A.u.path[2];
-    uint32_t px = c.pixel % A.width, py = c.pixel / A.width;
-    if (++c.sample < spf) {
-        start_path(A, C, P, px, py);
+    if (++sample < A.u.path[2]) {
+        uint32_t pixel = item / A.frames;
+        start_path(A, C, P, pixel % A.width, pixel / A.width);
         return true;
     }
-    // One frame per launch: this slot owns the pixel; several: frames of one
-    // pixel may finish concurrently in different slots.
-    bool multi = A.frames > 1;
-    accumulate(A, px, py, S, multi, !multi && A.write_hdr != 0, (float)(A.u.path[0] + spf));
     return false;
 }
 
-// Starts work item `item` (frame item % frames, pixel item / frames) in a slot.
-__device__ void start_item(const PtArgs& A, const Consts& C, uint32_t item, Path& P, PixelSums& S, Ctl& c) {
+// Starts work item `item` (frame item % frames, pixel item / frames).
+__device__ void start_item(const PtArgs& A, const Consts& C, uint32_t item, Path& P, PixelSums& S) {
     // Frames vary fastest: the frames of one pixel are neighbouring items, so a
     // warp traces two pixels' nearly identical primary rays (measured at 16
     // frames per pass: 239 -> 267 M path samples/s against pixels fastest).
-    c.frame = item % A.frames;
-    c.pixel = item / A.frames;
-    c.sample = 0u;
-    uint32_t px = c.pixel % A.width, py = c.pixel / A.width;
-    P.rng.s = seed_of(px, py, A.u.path[0] + c.frame * A.u.path[2]);
+    uint32_t frame = item % A.frames, pixel = item / A.frames;
+    uint32_t px = pixel % A.width, py = pixel / A.width;
+    P.rng.s = seed_of(px, py, A.u.path[0] + frame * A.u.path[2]);
     P.rng.pcg();
     S = {mk(0.0f), 0.0f, make_float4(0, 0, 0, 0), make_float4(0, 0, 0, 0)};
     start_path(A, C, P, px, py);
+}
+__device__ __forceinline__ void store_new_item(const WfArgs& W, uint32_t slot, const Path& P, uint32_t item,
+                                               const PixelSums& S) {
+    store_path(W, slot, P, 0u);
+    store_acc_head(W, slot, P, item, S);
+    store_acc_guides(W, slot, S);
 }
 
 // Hands the next work items to the lanes with `need` set (all 32 lanes call
@@ -196,12 +254,54 @@ __device__ __forceinline__ bool refill(const PtArgs& A, const WfArgs& W, const C
     if (item == ~0u) return false;
     Path P;
     PixelSums S;
-    Ctl c;
-    start_item(A, C, item, P, S, c);
-    float4* q = slot_of(W, slot);
-    store_path(q, P, c);
-    store_sums(q, S);
+    start_item(A, C, item, P, S);
+    store_new_item(W, slot, P, item, S);
     return true;
+}
+
+// pt.comp:554-560 for the items that ended in this warp (all 32 lanes call
+// it). With several frames in flight the adds are atomic, and the lanes that
+// finished frames of the same pixel first add their sums together, so each
+// pixel takes one set of atomics per warp: the frames of a pixel are
+// neighbouring items and tend to end in the same warp (background pixels all
+// in the first wave). With one frame per pass each pixel has one slot, which
+// adds to the sums directly.
+__device__ void accumulate_items(const PtArgs& A, bool done, uint32_t item, const PixelSums& S) {
+    uint32_t pixel = item / A.frames;
+    if (A.frames == 1u) {
+        if (done) accumulate(A, pixel % A.width, pixel / A.width, S, false, A.write_hdr != 0, (float)(A.u.path[0] + A.u.path[2]));
+        return;
+    }
+    if (!__any_sync(0xffffffffu, done)) return;
+    int lane = (int)(threadIdx.x & 31u);
+    unsigned grp = __match_any_sync(0xffffffffu, done ? pixel : 0x80000000u | (uint32_t)lane);
+    unsigned biggest = __reduce_max_sync(0xffffffffu, (unsigned)__popc(grp));
+    float v[12] = {S.sum.x, S.sum.y, S.sum.z, S.background, S.albedo.x, S.albedo.y,
+                   S.albedo.z, S.albedo.w, S.normal.x, S.normal.y, S.normal.z, S.normal.w};
+    if (biggest > 1u) {
+        // Suffix sums along each group's lanes by pointer jumping: after
+        // ceil(log2(size)) rounds the group's lowest lane holds its total.
+        unsigned higher = grp & ~((2u << lane) - 1u);
+        int next = higher ? __ffs(higher) - 1 : -1;
+        int rounds = 32 - __clz((int)biggest - 1);
+        for (int r = 0; r < rounds; r++) {
+            int src = next >= 0 ? next : lane;
+#pragma unroll
+            for (int k = 0; k < 12; k++) {
+                float o = __shfl_sync(0xffffffffu, v[k], src);
+                if (next >= 0) v[k] += o;
+            }
+            int nn = __shfl_sync(0xffffffffu, next, src);
+            next = next >= 0 ? nn : -1;
+        }
+    }
+    if (!done) return;
+    count(A, COUNT_PIXEL);
+    if (lane != __ffs(grp) - 1) return;
+    long i = (long)pixel;
+    atomicAdd(&A.accum[i], make_float4(v[0], v[1], v[2], v[3]));
+    atomicAdd(&A.albedo[i], make_float4(v[4], v[5], v[6], v[7]));
+    atomicAdd(&A.normal[i], make_float4(v[8], v[9], v[10], v[11]));
 }
 
 // Grid-stride loop over a queue with a warp-uniform bound, so that `push` sees
@@ -215,11 +315,8 @@ __global__ void __launch_bounds__(256) k_wf_init(const __grid_constant__ PtArgs 
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < slots; i += gridDim.x * blockDim.x) {
         Path P;
         PixelSums S;
-        Ctl c;
-        start_item(A, C, i, P, S, c);
-        float4* q = slot_of(W, i);
-        store_path(q, P, c);
-        store_sums(q, S);
+        start_item(A, C, i, P, S);
+        store_new_item(W, i, P, i, S);
         W.first[0][i] = i;
     }
     if (blockIdx.x == 0 && threadIdx.x == 0) {
@@ -268,7 +365,7 @@ __global__ void __launch_bounds__(128, VV_EXTEND_MIN_BLOCKS)
     uint32_t slot = 0;
     f3 origin, dir, spectral;
     Rng rng;
-    uint32_t hero = 0, bounce = 0;
+    uint32_t word = 0;  // P2.w: volumes, sample, hero
     Flight F;
     Vertex V;
     bool active = false, drained = false;
@@ -279,15 +376,14 @@ __global__ void __launch_bounds__(128, VV_EXTEND_MIN_BLOCKS)
             uint32_t k = take_item(taken, n, need);
             if (need && k != ~0u) {
                 slot = queue[k];
-                const float4* q = slot_of(W, slot);
-                float4 a = q[Q_ORIGIN], b = q[Q_DIR], s = q[Q_SPEC];
+                const float4* q = rec(W.path, slot, PATH_N);
+                float4 a = q[0], b = q[1], c = q[2];
                 origin = xyz(a);
+                rng.s = ubits(a.w);
                 dir = xyz(b);
-                rng.s = ubits(b.w);
-                spectral = xyz(s);
-                bounce = ubits(s.w) & 0xffffu;
-                uint32_t surfaces = ubits(s.w) >> 16, volumes = ubits(q[Q_RAD].w);
-                hero = ubits(q[Q_CTL].z);
+                spectral = xyz(c);
+                word = ubits(c.w);
+                uint32_t surfaces = ubits(b.w) >> 16, volumes = word & 1023u;
                 if (!(surfaces <= C.max_bounces && volumes <= C.volume_limit)) {
                     done = EXT_END;
                 } else {
@@ -299,7 +395,8 @@ __global__ void __launch_bounds__(128, VV_EXTEND_MIN_BLOCKS)
             drained = __any_sync(0xffffffffu, need && k == ~0u);
         }
         if (active) {
-            int r = ff_step(A, origin, dir, FIRST, (int)hero, spectral, F, V.idx, V.s, V.cap_plane, V.cut, rng);
+            int r = ff_step(A, origin, dir, FIRST, (int)(word >> 30), spectral, F, V.idx, V.s, V.cap_plane, V.cut,
+                            rng);
             if (r != FF_CONTINUE) {
                 active = false;
                 done = r;
@@ -307,13 +404,21 @@ __global__ void __launch_bounds__(128, VV_EXTEND_MIN_BLOCKS)
         }
         if (__any_sync(0xffffffffu, done != 0)) {
             if (done != 0) {
-                float4* q = slot_of(W, slot);
-                if (done == FF_HIT) store_vertex(q, V);
-                q[Q_DIR] = f4(dir, fbits(rng.s));
-                float4 s = q[Q_SPEC];
-                q[Q_SPEC] = f4(spectral, s.w);
-                // Q_CTL.w: whether the scatter kernel runs the escape (pt.comp:431-447).
-                if (done != FF_HIT) ((float*)(q + Q_CTL))[3] = fbits(done == FF_ESCAPE ? 1u : 0u);
+                if (done != EXT_END) {  // free flight changed the spectral ratios
+                    float4* q = rec(W.path, slot, PATH_N);
+                    float4 d = q[3];
+                    q[2] = f4(spectral, fbits(word));
+                    q[3] = d;
+                }
+                float4* v = rec(W.vtx, slot, VTX_N);
+                if (done == FF_HIT) {
+                    store_vertex(W, slot, V, rng.s);
+                } else {
+                    // Escapes and paths at the bounce limits: the random state
+                    // and whether the scatter kernel runs the escape (pt.comp:431-447).
+                    v[2] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+                    v[3] = make_float4(0.0f, 0.0f, fbits(rng.s), fbits(done == FF_ESCAPE ? 1u : 0u));
+                }
             }
             push(W.shade, &W.counts[WF_SHADE], slot, done == FF_HIT);
             push(W.esc[cur], &W.counts[WF_ESC0 + cur], slot, done != 0 && done != FF_HIT);
@@ -332,22 +437,17 @@ __global__ void __launch_bounds__(128, 4) k_wf_shade(const __grid_constant__ PtA
         bool valid = i < n;
         uint32_t slot = valid ? W.shade[i] : 0u;
         if (valid) {
-            float4* q = slot_of(W, slot);
             Path P;
-            float4 d = q[Q_DIR];
-            P.dir = xyz(d);
-            P.rng.s = ubits(d.w);
-            P.bounce = ubits(q[Q_SPEC].w) & 0xffffu;
-            PixelSums S;
-            if (P.bounce == 0u) load_sums(q, S);
+            float4 b = rec(W.path, slot, PATH_N)[1];
+            P.dir = xyz(b);
+            P.bounce = ubits(b.w) & 0xffffu;
             Vertex V;
-            load_vertex(q, V);
+            load_vertex(W, slot, V, P.rng.s);
+            PixelSums S;
+            if (P.bounce == 0u) load_acc_guides(W, slot, S);
             stage_shade(A, C, P, S, V);
-            q[Q_DIR] = f4(P.dir, fbits(P.rng.s));
-            store_vertex(q, V);
-            q[Q_N] = f4(V.n, 0.0f);
-            q[Q_LD] = f4(V.light_dir, 0.0f);
-            if (P.bounce == 0u) store_sums(q, S);
+            store_shaded(W, slot, V, P.rng.s);
+            if (P.bounce == 0u) store_acc_guides(W, slot, S);
         }
         push(W.shadow, &W.counts[WF_SHADOW], slot, valid);
     }
@@ -385,10 +485,11 @@ __global__ void __launch_bounds__(128, VV_SHADOW_MIN_BLOCKS) k_wf_shadow(const _
             uint32_t k = take_item(&W.counts[WF_TAKE_SHADOW], n, need);
             if (need && k != ~0u) {
                 slot = W.shadow[k];
-                const float4* q = slot_of(W, slot);
-                rng.s = ubits(q[Q_DIR].w);
-                origin = xyz(q[Q_IDX]);
-                tr_begin(A, origin, xyz(q[Q_LD]), T);
+                const float4* q = rec(W.shd, slot, SHD_N);
+                float4 a = q[0], b = q[1];
+                origin = xyz(a);
+                rng.s = ubits(a.w);
+                tr_begin(A, origin, xyz(b), T);
                 active = true;
                 map_ray = false;
             }
@@ -396,40 +497,32 @@ __global__ void __launch_bounds__(128, VV_SHADOW_MIN_BLOCKS) k_wf_shadow(const _
         }
         bool done = false;
         if (active && !tr_step(A, origin, T, rng)) {
+            float4* h = rec(W.sh, slot, SH_N);
             if (!MAP) {
+                h[0] = f4(T.result, fbits(rng.s));
+                h[1] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+                done = true;
+            } else if (map_ray) {
+                float4 h0 = h[0], h1 = h[1];
+                h[0] = make_float4(h0.x, h0.y, h0.z, fbits(rng.s));
+                h[1] = f4(xyz(h1) * T.result, h1.w);
                 done = true;
             } else {
-                float4* q = slot_of(W, slot);
-                float4* m = map_of(W, slot);
-                if (map_ray) {
-                    float4 ml = m[M_LIGHT];
-                    m[M_LIGHT] = f4(xyz(ml) * T.result, 0.0f);
-                    done = true;
+                Vertex V;
+                sample_map_light(A, rng, V);
+                h[0] = f4(T.result, fbits(rng.s));
+                h[1] = f4(V.map_light, V.map_pdf);
+                W.mapdir[slot] = f4(V.map_dir, 0.0f);
+                if (V.map_pdf > 0.0f) {
+                    tr_begin(A, origin, V.map_dir, T);
+                    map_ray = true;
                 } else {
-                    q[Q_LT] = f4(T.result, 0.0f);
-                    Vertex V;
-                    sample_map_light(A, rng, V);
-                    m[M_DIR] = f4(V.map_dir, V.map_pdf);
-                    m[M_LIGHT] = f4(V.map_light, 0.0f);
-                    if (V.map_pdf > 0.0f) {
-                        tr_begin(A, origin, V.map_dir, T);
-                        map_ray = true;
-                    } else {
-                        done = true;
-                    }
+                    done = true;
                 }
             }
             if (done) active = false;
         }
-        if (__any_sync(0xffffffffu, done)) {
-            if (done) {
-                float4* q = slot_of(W, slot);
-                float4 d = q[Q_DIR];
-                q[Q_DIR] = make_float4(d.x, d.y, d.z, fbits(rng.s));
-                if (!MAP) q[Q_LT] = f4(T.result, 0.0f);
-            }
-            push(W.scatter, &W.counts[WF_SCATTER], slot, done);
-        }
+        if (__any_sync(0xffffffffu, done)) push(W.scatter, &W.counts[WF_SCATTER], slot, done);
         if (drained && !__any_sync(0xffffffffu, active)) break;
     }
     if (blockIdx.x == 0 && threadIdx.x == 0) W.counts[WF_SHADE] = 0;
@@ -447,40 +540,45 @@ __global__ void __launch_bounds__(128, 6) k_wf_scatter(const __grid_constant__ P
         bool valid = i < n;
         bool ended = i >= n_scatter;
         uint32_t slot = valid ? (ended ? W.esc[cur][i - n_scatter] : W.scatter[i]) : 0u;
-        bool to_ext = false, to_first = false, need = false;
+        bool to_ext = false, to_first = false, done = false;
+        uint32_t item = 0;
+        PixelSums S;
         if (valid) {
-            float4* q = slot_of(W, slot);
             Path P;
-            Ctl c;
-            load_path(q, P, c);
-            bool escaped = ended && ubits(q[Q_CTL].w) != 0u;
+            uint32_t sample;
+            load_path(W, slot, P, sample);
+            load_acc_head(W, slot, P, item, S);
+            bool escaped = false;
             if (!ended) {
                 Vertex V;
-                load_vertex(q, V);
-                V.n = xyz(q[Q_N]);
-                V.light_dir = xyz(q[Q_LD]);
-                V.light_t = xyz(q[Q_LT]);
-                V.map_pdf = 0.0f;
-                if (A.u.lighting[3] == 2u) {
-                    const float4* m = map_of(W, slot);
-                    float4 md = m[M_DIR];
-                    V.map_dir = xyz(md);
-                    V.map_pdf = md.w;
-                    V.map_light = xyz(m[M_LIGHT]);
-                }
+                load_shaded(W, slot, V);
+                const float4* h = rec(W.sh, slot, SH_N);
+                float4 h0 = h[0], h1 = h[1];
+                V.light_t = xyz(h0);
+                P.rng.s = ubits(h0.w);
+                V.map_light = xyz(h1);
+                V.map_pdf = h1.w;
+                V.map_dir = A.u.lighting[3] == 2u ? xyz(W.mapdir[slot]) : mk(0.0f);
                 to_ext = stage_scatter(A, C, P, V);
+            } else {
+                float4 v3 = rec(W.vtx, slot, VTX_N)[3];
+                P.rng.s = ubits(v3.z);
+                escaped = ubits(v3.w) != 0u;
             }
             if (!to_ext) {
-                PixelSums S;
-                load_sums(q, S);
+                load_acc_guides(W, slot, S);
                 if (escaped) stage_escape(A, C, P, S);
-                to_first = end_path(A, C, P, S, c);
-                need = !to_first;
-                store_sums(q, S);
+                to_first = end_sample(A, C, P, S, item, sample);
+                done = !to_first;
+                if (to_first) store_acc_guides(W, slot, S);
             }
-            store_path(q, P, c);
+            if (!done) {
+                store_path(W, slot, P, sample);
+                store_acc_head(W, slot, P, item, S);
+            }
         }
-        if (refill(A, W, C, slot, need)) to_first = true;
+        accumulate_items(A, done, item, S);
+        if (refill(A, W, C, slot, done)) to_first = true;
         push(W.ext[nxt], &W.counts[nxt], slot, to_ext);
         push(W.first[nxt], &W.counts[WF_FIRST0 + nxt], slot, to_first);
     }
@@ -497,23 +595,28 @@ __global__ void __launch_bounds__(128, 4) k_wf_finish(const __grid_constant__ Pt
     if (stop != 0u) cur = (int)stop - 1;  // else the waves ran out first: `cur` is the next wave's queue
     uint32_t n_first = W.counts[WF_FIRST0 + cur], n = n_first + W.counts[cur];
     Consts C = make_consts(A);
+    bool multi = A.frames > 1u;
+    float n_total = (float)(A.u.path[0] + A.u.path[2]);
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         uint32_t slot = i < n_first ? W.first[cur][i] : W.ext[cur][i - n_first];
-        float4* q = slot_of(W, slot);
         Path P;
-        Ctl c;
         PixelSums S;
-        load_path(q, P, c);
-        load_sums(q, S);
+        uint32_t sample, item;
+        load_path(W, slot, P, sample);
+        load_acc_head(W, slot, P, item, S);
+        load_acc_guides(W, slot, S);
         uint32_t total = A.frames * A.width * A.height;
         for (;;) {
             do {
                 while (bounce_step(A, C, P, S)) {
                 }
-            } while (end_path(A, C, P, S, c));
-            uint32_t item = atomicAdd(&W.counts[WF_ITEMS], 1u);
+            } while (end_sample(A, C, P, S, item, sample));
+            uint32_t pixel = item / A.frames;
+            accumulate(A, pixel % A.width, pixel / A.width, S, multi, !multi && A.write_hdr != 0, n_total);
+            item = atomicAdd(&W.counts[WF_ITEMS], 1u);
             if (item >= total) break;
-            start_item(A, C, item, P, S, c);
+            sample = 0u;
+            start_item(A, C, item, P, S);
         }
     }
 }
@@ -535,6 +638,7 @@ cudaError_t launch_pt_wavefront(const PtArgs& a, const WfArgs& w, int sms, cudaS
         g_scatter = sms * blocks_per_sm(k_wf_scatter, 128);
         g_finish = sms * blocks_per_sm(k_wf_finish, 128);
     }
+    if (a.u.path[2] >= (uint32_t)WF_MAX_SAMPLES) return cudaErrorInvalidValue;  // the host routes these elsewhere
     const char* env = std::getenv("VV_WF_TAIL");
     uint32_t tail = env ? (uint32_t)std::atoi(env) : 1024u;
     uint32_t pixels = a.width * a.height;

@@ -49,8 +49,8 @@ def test_serving_request_stream():
 
 
 def test_ncu_traffic_only_on_the_captured_workload():
-    """The committed ncu traffic per frame was captured on the default workload:
-    the bench reports it there and nowhere else."""
+    """The DRAM traffic per frame, estimated from ncu captures for the default
+    workload: the bench reports it there and nowhere else."""
     b = _bench()
 
     class A:

@@ -315,10 +315,13 @@ __device__ __noinline__ float density_cubic(const PtArgs& A, f3 p) {
     bspline_w(c.fy, wy);
     bspline_w(c.fz, wz);
     float acc = 0.0f;
-#pragma unroll
+    // Loops, not 64 unrolled taps: the flight kernels wait on instruction
+    // fetch, and the smaller code runs faster (349.7 -> 377.4 M path samples/s
+    // with both loops rolled and extinction_unclipped out of line).
+#pragma unroll 1
     for (int z = 0; z < 4; z++) {
         float az = 0.0f;
-#pragma unroll
+#pragma unroll 1
         for (int y = 0; y < 4; y++) {
             const E* row = (const E*)A.density + c.oz[z] + c.oy[y];
             float r = wx[0] * density_decode<VV_DFMT>(__ldg(row + c.ox[0])) +
@@ -342,7 +345,10 @@ template <bool VALUE> __device__ __forceinline__ f3 density_gradient_cubic_impl(
     bspline_w(c.fx, wx); bspline_w(c.fy, wy); bspline_w(c.fz, wz);
     bspline_d(c.fx, dx); bspline_d(c.fy, dy); bspline_d(c.fz, dz);
     float acc = 0.0f, gx = 0.0f, gy = 0.0f, gz = 0.0f;
-#pragma unroll
+    // The ray marcher's value-and-gradient fetch runs its z slices as a loop
+    // (measured 32.7 -> 30.9 ms per 1024^2 frame); the path tracer's gradient
+    // stays unrolled (rolled: 370 -> 368 M path samples/s).
+#pragma unroll(VALUE ? 1 : 4)
     for (int z = 0; z < 4; z++) {
         float vz = 0.0f, gxz = 0.0f, gyz = 0.0f;
 #pragma unroll
@@ -1056,7 +1062,7 @@ __device__ __noinline__ float bsdf_pdf(f3 n, f3 v, f3 l, const Sample& s) {
 // pt.comp:277-292
 // extinction_at (pt.comp:277-292) after its clip test: the caller has found
 // `idx` inside the kept part (cut = clip_depth(idx) <= 0).
-__device__ float extinction_unclipped(const PtArgs& A, f3 idx, f3 dir, bool smooth, Sample& s, int& cap_plane,
+__device__ __noinline__ float extinction_unclipped(const PtArgs& A, f3 idx, f3 dir, bool smooth, Sample& s, int& cap_plane,
                                       float& cut) {
     float d = (smooth && A.u.env[1] > 0.5f) ? density_cubic(A, idx) : density_tri(A, idx);
     s = apply_labels(A, tf_point(A, d), idx);

@@ -16,12 +16,39 @@ FLAGS = ["-std=c++20", "-O2", "-fPIC", "-fsingle-precision-constant", "-ffp-cont
          "-fno-strict-aliasing", "-pthread", "-Wall", "-Wno-unused-variable", "-Wno-pedantic"]
 
 
+# The FP64 instance: the same restatement with `float` defined as `double`
+# (prelude.hpp), one translation unit, literals left at their single-precision
+# values (no -fsingle-precision-constant: the shaders' constants are float
+# literals with an f suffix).
+SOURCES64 = ["oracle_api64.cpp"]
+LIB64 = os.path.join(OUT_DIR, "liboracle64.so")
+FLAGS64 = ["-std=c++20", "-O2", "-fPIC", "-ffp-contract=off", "-fno-strict-aliasing", "-pthread", "-Wall",
+           "-Wno-unused-variable", "-Wno-pedantic"]
+
+
+def build64(verbose=False):
+    os.makedirs(OUT_DIR, exist_ok=True)
+    deps = [os.path.join(HERE, s) for s in SOURCES64 + SOURCES] + \
+        [os.path.join(HERE, f) for f in ("glsl.hpp", "oracle.hpp", "prelude.hpp")] + \
+        [os.path.join(HERE, "..", "include", "volpt.h")]
+    if os.path.exists(LIB64) and all(os.path.getmtime(LIB64) >= os.path.getmtime(d) for d in deps):
+        return LIB64
+    r = subprocess.run(["g++", *FLAGS64, "-shared", *[os.path.join(HERE, s) for s in SOURCES64], "-o", LIB64],
+                       capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"FP64 oracle build failed:\n{r.stderr[-6000:]}")
+    if verbose and r.stderr:
+        print(r.stderr, file=sys.stderr)
+    return LIB64
+
+
 def build(verbose=False):
     os.makedirs(OUT_DIR, exist_ok=True)
     srcs = [os.path.join(HERE, s) for s in SOURCES]
-    deps = srcs + [os.path.join(HERE, "glsl.hpp"), os.path.join(HERE, "oracle.hpp"),
+    deps = srcs + [os.path.join(HERE, "glsl.hpp"), os.path.join(HERE, "oracle.hpp"), os.path.join(HERE, "prelude.hpp"),
                    os.path.join(HERE, "..", "include", "volpt.h")]
     if os.path.exists(LIB) and all(os.path.getmtime(LIB) >= os.path.getmtime(d) for d in deps):
+        build64(verbose)
         return LIB
     objs = []
     procs = []
@@ -37,6 +64,7 @@ def build(verbose=False):
         if verbose and err:
             print(err, file=sys.stderr)
     subprocess.run(["g++", "-shared", "-pthread", *objs, "-o", LIB], check=True)
+    build64(verbose)
     return LIB
 
 

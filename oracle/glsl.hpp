@@ -20,24 +20,23 @@
 // member calls returning a proxy; single-letter components are data members.
 // Nothing here is used by the product library.
 #pragma once
-#include <cstdint>
-#include <cstring>
+#include "prelude.hpp"
 
 namespace glsl {
 
 typedef unsigned int uint;
 
 // ---------------------------------------------------------------- scalar math
-inline float abs(float x) { return __builtin_fabsf(x); }
+inline float abs(float x) { return gl_fabs(x); }
 inline int abs(int x) { return x < 0 ? -x : x; }
 inline float sign(float x) { return x > 0.0f ? 1.0f : (x < 0.0f ? -1.0f : 0.0f); }
-inline float floor(float x) { return __builtin_floorf(x); }
-inline float ceil(float x) { return __builtin_ceilf(x); }
-inline float trunc(float x) { return __builtin_truncf(x); }
-inline float fract(float x) { return x - __builtin_floorf(x); }
-inline float round(float x) { return __builtin_roundf(x); }
-inline float roundEven(float x) { return __builtin_rintf(x); }
-inline float mod(float x, float y) { return x - y * __builtin_floorf(x / y); }
+inline float floor(float x) { return gl_floor(x); }
+inline float ceil(float x) { return gl_ceil(x); }
+inline float trunc(float x) { return gl_trunc(x); }
+inline float fract(float x) { return x - gl_floor(x); }
+inline float round(float x) { return gl_round(x); }
+inline float roundEven(float x) { return gl_rint(x); }
+inline float mod(float x, float y) { return x - y * gl_floor(x / y); }
 // GLSL: min returns y if y < x, else x; max returns y if x < y, else x.
 inline float min(float x, float y) { return y < x ? y : x; }
 inline float max(float x, float y) { return x < y ? y : x; }
@@ -55,20 +54,20 @@ inline float smoothstep(float e0, float e1, float x) {
     float t = clamp((x - e0) / (e1 - e0), 0.0f, 1.0f);
     return t * t * (3.0f - 2.0f * t);
 }
-inline float sqrt(float x) { return __builtin_sqrtf(x); }
-inline float inversesqrt(float x) { return 1.0f / __builtin_sqrtf(x); }
-inline float pow(float x, float y) { return __builtin_powf(x, y); }
-inline float exp(float x) { return __builtin_expf(x); }
-inline float exp2(float x) { return __builtin_exp2f(x); }
-inline float log(float x) { return __builtin_logf(x); }
-inline float log2(float x) { return __builtin_log2f(x); }
-inline float sin(float x) { return __builtin_sinf(x); }
-inline float cos(float x) { return __builtin_cosf(x); }
-inline float tan(float x) { return __builtin_tanf(x); }
-inline float asin(float x) { return __builtin_asinf(x); }
-inline float acos(float x) { return __builtin_acosf(x); }
-inline float atan(float y, float x) { return __builtin_atan2f(y, x); }
-inline float atan(float x) { return __builtin_atanf(x); }
+inline float sqrt(float x) { return gl_sqrt(x); }
+inline float inversesqrt(float x) { return 1.0f / gl_sqrt(x); }
+inline float pow(float x, float y) { return gl_pow(x, y); }
+inline float exp(float x) { return gl_exp(x); }
+inline float exp2(float x) { return gl_exp2(x); }
+inline float log(float x) { return gl_log(x); }
+inline float log2(float x) { return gl_log2(x); }
+inline float sin(float x) { return gl_sin(x); }
+inline float cos(float x) { return gl_cos(x); }
+inline float tan(float x) { return gl_tan(x); }
+inline float asin(float x) { return gl_asin(x); }
+inline float acos(float x) { return gl_acos(x); }
+inline float atan(float y, float x) { return gl_atan2(y, x); }
+inline float atan(float x) { return gl_atan(x); }
 inline float radians(float d) { return d * (3.14159265358979f / 180.0f); }
 
 template <class T> struct tvec2;
@@ -356,14 +355,14 @@ inline vec4 decode(const void* data, Format f, long i) {
         case RG16_UNORM: { uint16_t v[2]; std::memcpy(v, b, 4); return vec4(float(v[0]) / 65535.0f, float(v[1]) / 65535.0f, 0, 1); }
         case RGBA8_SNORM: { int8_t v[4]; std::memcpy(v, b, 4); vec4 r; for (int k = 0; k < 4; k++) r[k] = max(float(v[k]) / 127.0f, -1.0f); return r; }
         case RGBA8_UNORM: { vec4 r; for (int k = 0; k < 4; k++) r[k] = float(b[k]) / 255.0f; return r; }
-        case R32F: { float v; std::memcpy(&v, b, 4); return vec4(v, 0, 0, 1); }
-        case RG32F: { float v[2]; std::memcpy(v, b, 8); return vec4(v[0], v[1], 0, 1); }
-        case RGBA32F: { float v[4]; std::memcpy(v, b, 16); return vec4(v[0], v[1], v[2], v[3]); }
+        case R32F: { f32 v; std::memcpy(&v, b, 4); return vec4(v, 0, 0, 1); }
+        case RG32F: { f32 v[2]; std::memcpy(v, b, 8); return vec4(v[0], v[1], 0, 1); }
+        case RGBA32F: { f32 v[4]; std::memcpy(v, b, 16); return vec4(v[0], v[1], v[2], v[3]); }
         case RGBA16F: { uint16_t v[4]; std::memcpy(v, b, 8); return vec4(half_to_float(v[0]), half_to_float(v[1]), half_to_float(v[2]), half_to_float(v[3])); }
         case R16F: { uint16_t v; std::memcpy(&v, b, 2); return vec4(half_to_float(v), 0, 0, 1); }
         case R16_BF16: {  // the upper half of a binary32 (not a Vulkan format: the precision variant's density)
             uint16_t v; std::memcpy(&v, b, 2);
-            uint32_t w = (uint32_t)v << 16; float x; std::memcpy(&x, &w, 4);
+            uint32_t w = (uint32_t)v << 16; f32 x; std::memcpy(&x, &w, 4);
             return vec4(x, 0, 0, 1);
         }
         case R8_UINT: return vec4(float(b[0]), 0, 0, 1);
@@ -371,9 +370,9 @@ inline vec4 decode(const void* data, Format f, long i) {
     }
     return vec4(0.0f);
 }
-inline uint16_t to_unorm16(float f) { return (uint16_t)__builtin_rintf(clamp(f, 0.0f, 1.0f) * 65535.0f); }
-inline uint8_t to_unorm8(float f) { return (uint8_t)__builtin_rintf(clamp(f, 0.0f, 1.0f) * 255.0f); }
-inline int8_t to_snorm8(float f) { return (int8_t)__builtin_rintf(clamp(f, -1.0f, 1.0f) * 127.0f); }
+inline uint16_t to_unorm16(float f) { return (uint16_t)gl_rint(clamp(f, 0.0f, 1.0f) * 65535.0f); }
+inline uint8_t to_unorm8(float f) { return (uint8_t)gl_rint(clamp(f, 0.0f, 1.0f) * 255.0f); }
+inline int8_t to_snorm8(float f) { return (int8_t)gl_rint(clamp(f, -1.0f, 1.0f) * 127.0f); }
 
 // Encodes `v` into texel `i` of `data` (the conversions of imageStore).
 inline void encode(void* data, Format f, long i, const vec4& v) {
@@ -383,13 +382,13 @@ inline void encode(void* data, Format f, long i, const vec4& v) {
         case RG16_UNORM: { uint16_t q[2] = {to_unorm16(v.x), to_unorm16(v.y)}; std::memcpy(b, q, 4); break; }
         case RGBA8_SNORM: { int8_t q[4]; for (int k = 0; k < 4; k++) q[k] = to_snorm8(v[k]); std::memcpy(b, q, 4); break; }
         case RGBA8_UNORM: { for (int k = 0; k < 4; k++) b[k] = to_unorm8(v[k]); break; }
-        case R32F: std::memcpy(b, &v.x, 4); break;
-        case RG32F: std::memcpy(b, &v.x, 8); break;
-        case RGBA32F: std::memcpy(b, &v.x, 16); break;
+        case R32F: { f32 q = (f32)v.x; std::memcpy(b, &q, 4); break; }
+        case RG32F: { f32 q[2] = {(f32)v.x, (f32)v.y}; std::memcpy(b, q, 8); break; }
+        case RGBA32F: { f32 q[4] = {(f32)v.x, (f32)v.y, (f32)v.z, (f32)v.w}; std::memcpy(b, q, 16); break; }
         case RGBA16F: { uint16_t q[4]; for (int k = 0; k < 4; k++) q[k] = float_to_half(v[k]); std::memcpy(b, q, 8); break; }
         case R16F: { uint16_t q = float_to_half(v.x); std::memcpy(b, &q, 2); break; }
         case R16_BF16: {  // round to nearest even (finite values)
-            uint32_t w; std::memcpy(&w, &v.x, 4);
+            f32 x = (f32)v.x; uint32_t w; std::memcpy(&w, &x, 4);
             uint16_t q = (uint16_t)((w + 0x7fffu + ((w >> 16) & 1u)) >> 16); std::memcpy(b, &q, 2); break;
         }
         case R8_UINT: b[0] = (uint8_t)v.x; break;

@@ -37,7 +37,9 @@ struct Uniforms {
     vec4 label_surface[256];
     vec4 label_optics[256];
 };
+#ifndef VVO_FP64
 static_assert(sizeof(Uniforms) == VV_UNIFORMS_BYTES, "std140 layout");
+#endif
 
 // Geometry derived from a volume (volio Volume + renderer.rs:819-834).
 struct Geometry {

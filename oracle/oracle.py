@@ -47,6 +47,22 @@ def lib():
     return _lib
 
 
+_lib64 = None
+
+
+def lib64():
+    """The FP64 instance of the path tracer's restatement (oracle_api64.cpp)."""
+    global _lib64
+    if _lib64 is None:
+        from . import build_oracle
+        build_oracle.build()
+        _lib64 = C.CDLL(build_oracle.LIB64)
+        _lib64.vvo64_real_bytes.restype = C.c_long
+        _lib64.vvo64_pt_pixel_sums.argtypes = [P, P, P, C.c_long, C.c_uint32, C.c_uint32, P, C.c_int]
+        assert _lib64.vvo64_real_bytes() == 8
+    return _lib64
+
+
 def ptr(a):
     return None if a is None else C.c_void_p(a.ctypes.data)
 
@@ -343,6 +359,25 @@ class CpuRenderer:
         out = np.zeros((pix.shape[0], 12), np.float32)
         lib().vvo_pt_pixels(ptr(u), C.byref(self.scene()), ptr(pix), C.c_long(pix.shape[0]), ptr(out),
                             threads or globals()["threads"]())
+        return out
+
+    def pixel_sums_fp64(self, params, pixels, first, count, threads=None):
+        """The FP64 oracle: for each (x, y) row of `pixels`, the double-precision
+        sums of `count` paths at accumulation indices first .. first + count - 1
+        (one path per frame, the per-pixel streams of pt.comp), traced by the
+        restatement compiled in double precision over this renderer's inputs:
+        (n, 12) float64 (radiance sum, background, albedo sums and
+        luminance^2, normal sums and depth)."""
+        self.prepare(params, self.width, self.height)
+        saved = self.accumulated
+        self.accumulated = 0
+        u = self.uniforms(params, 1, self.width, self.height)
+        self.accumulated = saved
+        pix = np.ascontiguousarray(pixels, np.int32).reshape(-1, 2)
+        out = np.zeros((pix.shape[0], 12), np.float64)
+        lib64().vvo64_pt_pixel_sums(ptr(u), C.byref(self.scene()), ptr(pix), C.c_long(pix.shape[0]),
+                                    C.c_uint32(first), C.c_uint32(count), ptr(out),
+                                    threads or globals()["threads"]())
         return out
 
     def denoise(self, params):

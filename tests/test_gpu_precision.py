@@ -203,3 +203,21 @@ def test_majorants_are_true_bounds(small_cfg, gpu_ctx, fmt):
                   f"(B-spline, trilinear) above the majorant")
             if mode == abi.MAJORANTS_BOUND:
                 assert counts == [0, 0]
+
+
+def test_formats_against_the_fp64_oracle(gpu_ctx):
+    """Every storage format and the compensated sums, judged by the FP64 oracle
+    (tests/precision_fp64_study.py) on the small scene at 256 paths per pixel,
+    the same random streams: each render's luminance RMSE against the oracle's
+    image is at most twice the oracle image's own Monte Carlo RMSE (what the
+    paths that a rounding difference diverts contribute), and every render's
+    error is nonzero only through such paths (the FP32 storage's at most the
+    coarser formats' plus that noise)."""
+    import precision_fp64_study as S
+    cfg = scene.small_config(n=48, size=48)
+    res = S.run(gpu_ctx, cfg, 256, crops=1, size=48, zoom=0.45)
+    mc = res["fp64_oracle"]["mc_rmse_per_crop"][0]
+    print({k: v["rmse_vs_fp64_oracle"] for k, v in res.items() if isinstance(v, dict) and "rmse_vs_fp64_oracle" in v},
+          "oracle MC RMSE", mc)
+    for key in ("fp32", "unorm16", "fp16", "bf16", "fp32+kahan+fp64_after_65536"):
+        assert 0.0 < res[key]["rmse_vs_fp64_oracle"] <= 2.0 * mc, (key, res[key], mc)

@@ -25,7 +25,9 @@ extern "C" {
 #endif
 
 /* y = act(conv3x3(x, weights) + bias), act = ReLU if relu else identity; bias
- * may be NULL. cout is one of 8, 16, 32, 48, 64, 80, 96, 112, 144, 176. */
+ * may be NULL. cout is one of 8, 16, 32, 48, 64, 80, 96, 112, 144, 176.
+ * Widths that are multiples of 128 with cout <= 96 and small enough weights
+ * and inputs run on tcgen05 (vv_nn_conv3x3_tc), the rest on mma.sync. */
 vv_status vv_nn_conv3x3(const void* x, int n, int h, int w, int cin, const void* weights, const float* bias,
                         int cout, int relu, void* y, void* stream);
 /* wt[ci][8 - tap][co] = weights[co][tap][ci]: with them vv_nn_conv3x3 of dy
@@ -77,6 +79,15 @@ vv_status vv_nn_prediction_to_hdr(const void* pred, int c, int wp, int w, int h,
                                   void* hdr, void* stream);
 /* rgb = exp(max(pred, 0)) - 1 of the first 3 of c channels (3 floats per pixel). */
 vv_status vv_nn_radiance(const void* pred, int c, long pixels, float* rgb, void* stream);
+/* vv_nn_conv3x3 on tcgen05.mma with TMEM accumulators and TMA-fed inputs:
+ * widths that are multiples of 128, cout a multiple of 8 up to 96, all nine
+ * taps' weights plus two 128-pixel segments' input rows within 220 KB of
+ * shared memory, 16-byte aligned pointers; VV_ERR_ARG for other shapes. */
+vv_status vv_nn_conv3x3_tc(const void* x, int n, int h, int w, int cin, const void* weights, const float* bias,
+                           int cout, int relu, void* y, void* stream);
+/* Whether a tensor-core convolution gave up a bounded wait (1) since the last
+ * clear; clear resets the flag. */
+vv_status vv_nn_tc_status(int* failed, int clear);
 
 #ifdef __cplusplus
 }

@@ -217,3 +217,37 @@ def test_renderer_runs_the_network_as_its_denoiser(gpu_ctx, small_cfg):
     assert np.allclose(hdr[..., 3], np.float16(acc[..., 3] / 4.0).astype(np.float32), atol=1e-3)
     r.set_denoiser_weights(None)
     r.destroy()
+
+
+@pytest.mark.parametrize("cin,cout,w", [(16, 32, 256), (32, 32, 128), (32, 48, 256), (48, 64, 128), (64, 64, 256),
+                                        (80, 32, 128), (64, 80, 128), (32, 16, 384), (16, 8, 128)])
+def test_tensor_core_convolution(lib, cin, cout, w):
+    """Widths that are multiples of 128 take the tcgen05 convolution (TMA-fed
+    rows, TMEM accumulators): its output against the reference at the
+    convolution tolerance, the product entry point the same to the bit, and no
+    bounded wait given up."""
+    import ctypes as C
+    rng = np.random.default_rng(cin * 1000 + cout + w)
+    n, h = 2, 12
+    x = rand_half(rng, (n, h, w, cin))
+    wt = rand_half(rng, (cout, 3, 3, cin), 0.1)
+    b = rng.standard_normal(cout).astype(np.float32)
+    X, W, B = dev(x, "half"), dev(wt, "half"), dev(b)
+    Y = torch.empty((n, h, w, cout), dtype=torch.float16, device="cuda")
+    Y2 = torch.empty_like(Y)
+    for relu in (0, 1):
+        assert lib.vv_nn_conv3x3_tc(X.data_ptr(), n, h, w, cin, W.data_ptr(), B.data_ptr(), cout, relu, Y.data_ptr(),
+                                    S) == 0
+        close(host(Y), N.conv3x3(x, wt, b, bool(relu)), 2e-3, 2e-3)
+        assert lib.vv_nn_conv3x3(X.data_ptr(), n, h, w, cin, W.data_ptr(), B.data_ptr(), cout, relu, Y2.data_ptr(),
+                                 S) == 0
+        assert torch.equal(Y, Y2)
+    failed = C.c_int(1)
+    assert lib.vv_nn_tc_status(C.byref(failed), 1) == 0 and failed.value == 0
+
+
+def test_tensor_core_convolution_refuses_other_shapes(lib):
+    X = torch.zeros((1, 16, 128, 176), dtype=torch.float16, device="cuda")
+    assert lib.vv_nn_conv3x3_tc(X.data_ptr(), 1, 16, 96, 16, X.data_ptr(), None, 16, 0, X.data_ptr(), S) != 0  # w
+    assert lib.vv_nn_conv3x3_tc(X.data_ptr(), 1, 16, 128, 176, X.data_ptr(), None, 80, 0, X.data_ptr(), S) != 0  # smem
+    assert lib.vv_nn_conv3x3_tc(X.data_ptr(), 1, 16, 128, 16, X.data_ptr(), None, 112, 0, X.data_ptr(), S) != 0  # cout

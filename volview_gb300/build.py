@@ -14,7 +14,7 @@ BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libvolpt.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 SOURCES = ["vv_volume.cu", "vv_pt.cu", "vv_pt_exact.cu", "vv_wavefront.cu", "vv_raymarch.cu", "vv_post.cu",
-           "vv_noalloc.cu", "vv_nn.cu", "vv_host.cpp"]
+           "vv_noalloc.cu", "vv_nn.cu", "vv_nn_tc.cu", "vv_host.cpp"]
 # Compiled once per density storage format (VV_DFMT = 0..3: R16_UNORM, FP16,
 # BF16, FP32), each into its own namespace, so each format's samplers are
 # specialised for it.

@@ -1,5 +1,6 @@
 // vv_nn.cu — the learned denoiser's operators: 3x3 convolutions as implicit
-// GEMMs on the FP16 tensor cores (mma.sync m16n8k16, FP32 accumulation), their
+// GEMMs on the FP16 tensor cores (tcgen05 for the shapes vv_nn_tc.cu takes,
+// mma.sync m16n8k16 for the rest, FP32 accumulation), their
 // weight and bias gradients, and the element-wise parts of a U-Net (ReLU, 2x2
 // average pooling, nearest upsampling, channel concatenation), its input
 // features from the path tracer's accumulation, an L1 loss in log radiance and
@@ -18,6 +19,10 @@
 
 namespace vv {
 namespace nn {
+
+// vv_nn_tc.cu: the tcgen05 convolution; false when the shape is not one it takes.
+bool conv3x3_tc(const __half* x, int n, int h, int w, int cin, const __half* wt, const float* bias, int cout,
+                int relu, __half* y, cudaStream_t s, cudaError_t* err);
 
 __device__ __forceinline__ void mma16816(float c[4], const uint32_t a[4], const uint32_t b[2]) {
     asm volatile(
@@ -390,6 +395,15 @@ extern "C" vv_status vv_nn_conv3x3(const void* x, int n, int h, int w, int cin, 
                                    const float* bias, int cout, int relu, void* y, void* stream) {
     if (!x || !weights || !y || n <= 0 || h <= 0 || w <= 0 || w % 16 || cin <= 0 || cin % 16) return VV_ERR_ARG;
     cudaStream_t s = (cudaStream_t)stream;
+    switch (cout) {
+        case 8: case 16: case 32: case 48: case 64: case 80: case 96: case 112: case 144: case 176: break;
+        default: return VV_ERR_ARG;
+    }
+    // Widths that are multiples of 128 with the weights and two segments'
+    // input rows in shared memory run on tcgen05 (vv_nn_tc.cu); the rest here.
+    cudaError_t te = cudaSuccess;
+    if (conv3x3_tc((const __half*)x, n, h, w, cin, (const __half*)weights, bias, cout, relu, (__half*)y, s, &te))
+        return te == cudaSuccess ? VV_OK : VV_ERR_CUDA;
     unsigned g = blocks((long)n * h * w / 16, CONV_WARPS);
     const __half* X = (const __half*)x;
     const __half* W = (const __half*)weights;

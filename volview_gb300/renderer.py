@@ -88,6 +88,8 @@ NN = [
     ("vv_nn_radiance", I, [P, I, L, P, P]),
     ("vv_nn_features_image", I, [P, P, P, F, I, I, I, I, P, P]),
     ("vv_nn_prediction_to_hdr", I, [P, I, I, I, I, P, F, P, P]),
+    ("vv_nn_conv3x3_tc", I, [P, I, I, I, I, P, P, I, I, P, P]),
+    ("vv_nn_tc_status", I, [P, I]),
 ]
 
 COUNT_NAMES = ["majorant", "cubic", "trilinear", "mask", "label", "normal", "gradient", "pixel", "path", "vertex"]

@@ -65,6 +65,9 @@ def parse():
     ap.add_argument("--denoised-rmse", type=int, default=0,
                     help="instead of the path-tracing bench, train the learned denoiser for this many steps on "
                          "the head/neck workload at 1024^2 and time the fixed RMSE with it on held-out views")
+    ap.add_argument("--bench-denoiser", type=int, default=1000,
+                    help="Adam steps of the reduced time-to-RMSE run with the learned denoiser in the default line "
+                         "(4 training views, 1 held out, the plain tracer's 256-path error; 0: skip)")
     ap.add_argument("--denoiser-study", type=int, default=0,
                     help="instead of the path-tracing bench, train the learned denoiser for this many Adam steps "
                          "on pairs the tracer renders (4 vs 256 paths/pixel) and compare it with a-trous")
@@ -518,6 +521,11 @@ def run_ours(args, rank, world, local):
     to_rmse = time_to_rmse(r, params, args, frame, stream) if args.rmse_requests > 0 else None
     if args.rmse_reference_spp > 0 and to_rmse is not None:
         to_rmse["check"] = rmse_against_reference(r, params, args, frame)
+    # The same fixed error with the learned denoiser, at a reduced scale
+    # (untimed by the step; its own wall times).
+    denoised = None
+    if args.bench_denoiser > 0 and rank == 0 and args.workload == "head_neck" and (W, H) == (1024, 1024):
+        denoised = denoised_time_to_rmse(r, params, 4, 1, args.bench_denoiser, plain_spp=256)
     # Roofline of the path-tracing pass (the wavefront stage kernels of a frame).
     # Consecutive passes overlap (one pass's last waves beside the next one's
     # first), so the time per frame is the timed region's, display included.
@@ -536,6 +544,7 @@ def run_ours(args, rank, world, local):
         "path_vertices_per_s": counts["vertex"] / max(counts["pixel"], 1) * value,
         "per_frame_record": per_frame,
         "time_to_rmse": to_rmse,
+        "denoised_time_to_rmse": denoised,
         "ray_march": ray_march,
         "e2e": e2e,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
@@ -752,27 +761,20 @@ def run_denoiser_study(args):
                       "study": res}))
 
 
-def run_denoised_rmse(args):
-    """Time to the plain tracer's error with the learned denoiser, head/neck
-    workload at 1024^2. The U-Net is trained on 256^2 crops of 12 full-size
-    views (4, 16, 64 and 256 paths/pixel in, 1024 as target). On 4 held-out
-    views the plain tracer's image at 1024 paths/pixel (the fixed RMSE's
-    sample count) and the network's output, blended per pixel with the raw
-    mean by inverse variance, at 4 to 512 paths/pixel, are compared with a
-    reference of 4096 further, independent paths; the fewest paths/pixel at
+def denoised_time_to_rmse(r, base, train_n, test_n, steps, plain_spp=1024):
+    """Time to the plain tracer's error at plain_spp paths/pixel with the
+    learned denoiser on renderer r (head/neck): the U-Net trained on 256^2
+    crops of `train_n` full-size views (4, 16, 64 and 256 paths/pixel in, 1024
+    as target); on `test_n` held-out views the plain image at plain_spp
+    paths/pixel and the network's output blended per pixel with the raw mean
+    by inverse variance, at 4 paths/pixel up to half of plain_spp, against a
+    reference of 4096 further, independent paths: the fewest paths/pixel at
     which the blend is as close as the plain image, and the wall times of
-    both (render, readback, network)."""
+    both (render, readback, network). A view the blend does not bring to the
+    plain error falls back to plain rendering (1x)."""
     import copy
     from volview_gb300 import abi
     from volview_gb300 import learned_denoiser as LD
-    from volview_gb300 import renderer as R
-    cfg = workload(args)
-    W, H = image_size(args)
-    ctx = R.Context(0)
-    r = R.Renderer(ctx, cfg["volume"], cfg["tf"])
-    r.set_labels(cfg["labels_vol"], abi.soft_struct(cfg["soft"]))
-    r.resize(W, H)
-    base = frame_params(cfg, list(r.center), r.diagonal, args.light_map)
 
     def views(n, seed):
         out = []
@@ -785,23 +787,39 @@ def run_denoised_rmse(args):
             out.append(p)
         return out
 
-    res = LD.time_to_rmse_study(r, views(12, 31), views(4, 32), steps=args.denoised_rmse)
+    t0 = time.perf_counter()
+    levels = tuple(k for k in (4, 8, 16, 32, 64, 128, 256, 512) if k <= plain_spp // 2)
+    res = LD.time_to_rmse_study(r, views(train_n, 31), views(test_n, 32), levels=levels, plain_spp=plain_spp,
+                                steps=steps)
     res.pop("net")
     losses = res.pop("losses")
     res["loss_first"], res["loss_last"] = losses[0], float(np.mean(losses[-20:]))
     spp = [v["spp_to_target"] for v in res["views"]]
-    # A view the blend does not bring to the plain error within 512 paths/pixel
-    # falls back to plain rendering (1x).
     speedup = [v["plain_ms"] / v["denoised_ms"] if v["denoised_ms"] else 1.0 for v in res["views"]]
+    return {"metric": "time to the plain tracer's %d-path error with the learned denoiser" % plain_spp,
+            "unit": "x faster (wall)", "higher_is_better": True, "value": float(np.median(speedup)),
+            "speedup_per_view": speedup, "paths_per_pixel_to_target": spp, "training_views": train_n,
+            "held_out_views": test_n, "adam_steps": steps, "seconds": time.perf_counter() - t0,
+            "views": "yaw +-0.6, pitch +-0.3 around the default view (training and held-out from different seeds)",
+            "study": res}
+
+
+def run_denoised_rmse(args):
+    """denoised_time_to_rmse at full scale: 12 training views, 4 held out."""
+    from volview_gb300 import abi
+    from volview_gb300 import renderer as R
+    cfg = workload(args)
+    W, H = image_size(args)
+    ctx = R.Context(0)
+    r = R.Renderer(ctx, cfg["volume"], cfg["tf"])
+    r.set_labels(cfg["labels_vol"], abi.soft_struct(cfg["soft"]))
+    r.resize(W, H)
+    base = frame_params(cfg, list(r.center), r.diagonal, args.light_map)
+    res = denoised_time_to_rmse(r, base, 12, 4, args.denoised_rmse)
     r.destroy()
     ctx.destroy()
-    print(json.dumps({"metric": "time to the plain tracer's 1024-path error with the learned denoiser",
-                      "unit": "x faster (wall)", "higher_is_better": True,
-                      "value": float(np.median(speedup)), "speedup_per_view": speedup,
-                      "config": {"workload": bench_config(args, 1)["workload"],
-                                 "views": "yaw +-0.6, pitch +-0.3 around the default view (training and held-out "
-                                          "from different seeds)"},
-                      "paths_per_pixel_to_target": spp, "study": res}))
+    res["config"] = {"workload": bench_config(args, 1)["workload"]}
+    print(json.dumps(res))
 
 
 def cpu_renderer_from_device(cfg, r, params):

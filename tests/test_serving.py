@@ -182,8 +182,9 @@ def test_request_bytes_model():
 
 def test_request_bytes_model_follows_the_library_sources():
     """The model's constants are the ones the library allocates with: slot,
-    light-map sample and stage-queue bytes per path slot, passes in flight,
-    frames per pass, frames' worth of slots and the slot cap."""
+    light-map sample, stage-queue and later-flight bin bytes per path slot,
+    passes in flight, frames per pass, frames' worth of slots and the slot
+    cap."""
     import os
     import re
     csrc = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "volview_gb300", "csrc")
@@ -198,7 +199,8 @@ def test_request_bytes_model_follows_the_library_sources():
     slot = num(r"constexpr int WF_SLOT_BYTES = (\d+);", kernels)
     light = num(r"constexpr int WF_MAP_BYTES = (\d+);", kernels)
     queues = num(r"P\.queues\.alloc\(cap \* (\d+) \* sizeof\(uint32_t\)\)", host)
-    assert S.SLOT_BYTES == slot + light + queues * 4
+    binned = num(r"P\.binq\.alloc\(cap \* (\d+) \* sizeof\(uint32_t\)\)", host)
+    assert S.SLOT_BYTES == slot + light + (queues + binned) * 4
     assert S.PASSES == num(r"#define VV_PASSES (\d+)", host)
     assert S.PASS_FRAMES == num(r"#define VV_SUBPASS_FRAMES (\d+)", host)
     assert S.SLOT_FRAMES == num(r"std::atoi\(e\)\) : (\d+);", host)

@@ -253,7 +253,7 @@ struct vv_renderer {
     // accumulation (and displayed) after the previous call's display, so a
     // call's pass overlaps the tail of the previous one.
     struct Pass {
-        DBuf slots, map, queues, counts, accum, albedo, normal;
+        DBuf slots, map, queues, counts, accum, albedo, normal, binq, bins;
         cudaStream_t stream = nullptr;
         cudaEvent_t shown = nullptr;  // after the pass's merge and display
     } pass[VV_PASSES];
@@ -723,7 +723,7 @@ extern "C" vv_status vv_renderer_destroy(vv_renderer* r) {
     cudaStreamSynchronize(r->ctx->stream);
     for (auto& P : r->pass) {
         if (P.stream) cudaStreamSynchronize(P.stream);
-        DBuf* pb[] = {&P.slots, &P.map, &P.queues, &P.counts, &P.accum, &P.albedo, &P.normal};
+        DBuf* pb[] = {&P.slots, &P.map, &P.queues, &P.counts, &P.accum, &P.albedo, &P.normal, &P.binq, &P.bins};
         for (DBuf* b : pb) b->release();
         if (P.shown) cudaEventDestroy(P.shown);
         if (P.stream) cudaStreamDestroy(P.stream);
@@ -1124,7 +1124,7 @@ extern "C" vv_status vv_renderer_memory(const vv_renderer* r, uint64_t* bytes) {
     uint64_t n = 0;
     for (const DBuf* b : all) n += b->n;
     for (const auto& P : r->pass) {
-        const DBuf* pb[] = {&P.slots, &P.map, &P.queues, &P.counts, &P.accum, &P.albedo, &P.normal};
+        const DBuf* pb[] = {&P.slots, &P.map, &P.queues, &P.counts, &P.accum, &P.albedo, &P.normal, &P.binq, &P.bins};
         for (const DBuf* b : pb) n += b->n;
     }
     if (r->shadow_tex.arr) n += (uint64_t)(r->shadow_dims[0] + 2) * (r->shadow_dims[1] + 2) * (r->shadow_dims[2] + 2) * 8;
@@ -1254,6 +1254,43 @@ static cudaError_t run_pt(vv_renderer* r, vv_renderer::Pass& P, PtArgs& a, cudaS
     w.first[0] = q + 7 * cap;
     w.first[1] = q + 8 * cap;
     w.counts = P.counts.as<uint32_t>();
+    // Later flights binned by the 32-voxel cell of their origin (coarser cells
+    // while there would be more than 2^16 bins) and the octant of their
+    // direction, so that a warp's lanes fly through the same region in the
+    // same direction (measured on the head/neck workload: 379.4 -> 392.4 M path
+    // samples/s; 16- and 64-voxel cells 386.0 and 390.3, no octant 388.0).
+    {
+        int shift = 5, cx, cy, cz;
+        for (;; shift++) {
+            cx = (r->vol.nx + (1 << shift) - 1) >> shift;
+            cy = (r->vol.ny + (1 << shift) - 1) >> shift;
+            cz = (r->vol.nz + (1 << shift) - 1) >> shift;
+            if ((size_t)cx * cy * cz * 8 <= 65536) break;
+        }
+        const uint32_t nbins = (uint32_t)(cx * cy * cz * 8);
+        cudaError_t ce = cudaSuccess;
+        if (P.binq.n < cap * 3 * sizeof(uint32_t)) {
+            ce = cudaStreamSynchronize(s);  // the pass's previous use of its state has ended
+            if (ce == cudaSuccess) ce = P.binq.alloc(cap * 3 * sizeof(uint32_t));
+        }
+        if (ce == cudaSuccess && P.bins.n < (size_t)nbins * 2 * sizeof(uint32_t)) {
+            ce = cudaStreamSynchronize(s);
+            if (ce == cudaSuccess) ce = P.bins.alloc((size_t)nbins * 2 * sizeof(uint32_t));
+            if (ce == cudaSuccess) ce = cudaMemsetAsync(P.bins.p, 0, P.bins.n, s);  // the counts start at zero
+        }
+        if (ce != cudaSuccess) return ce;
+        uint32_t* bq = P.binq.as<uint32_t>();
+        w.ext_key[0] = bq;
+        w.ext_key[1] = bq + cap;
+        w.sorted = bq + 2 * cap;
+        w.bin_count = P.bins.as<uint32_t>();
+        w.bin_next = w.bin_count + nbins;
+        w.nbins = nbins;
+        w.cell_shift = shift;
+        w.cells_x = cx;
+        w.cells_y = cy;
+        w.cells_z = cz;
+    }
     return kernels_of(r).pt_wavefront(a, w, r->ctx->sms, s, launches);
 }
 

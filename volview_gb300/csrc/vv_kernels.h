@@ -114,6 +114,17 @@ struct WfArgs {
     uint32_t* shadow;
     uint32_t* scatter;
     uint32_t* counts;      // WF_COUNTERS words
+    // Later flights binned by the coarse cell of their origin and the octant
+    // of their direction: the scatter kernel writes each queued slot's bin
+    // beside it, a counting sort orders the queue into `sorted`, which the
+    // next wave's later-flight extend reads.
+    uint32_t* ext_key[2];
+    uint32_t* sorted;
+    uint32_t* bin_count;   // nbins counters (zero between waves)
+    uint32_t* bin_next;    // nbins insertion points
+    uint32_t nbins;
+    int cell_shift;        // log2 of a cell's edge in voxels
+    int cells_x, cells_y, cells_z;
 };
 // A lighting volume as the image loop reads it: a 3D texture of its texels
 // inside a one-texel white border, filtered by the texture units (clamped

@@ -201,6 +201,33 @@ __device__ __forceinline__ void push(uint32_t* q, uint32_t* count, uint32_t slot
     if (pred) q[base + __popc(m & ((1u << lane) - 1u))] = slot;
 }
 
+// push, also writing `key` beside the slot in `keys`.
+__device__ __forceinline__ void push_key(uint32_t* q, uint32_t* keys, uint32_t* count, uint32_t slot, uint32_t key,
+                                         bool pred) {
+    unsigned m = __ballot_sync(0xffffffffu, pred);
+    if (!m) return;
+    int lane = (int)(threadIdx.x & 31u);
+    int leader = __ffs(m) - 1;
+    uint32_t base = 0;
+    if (lane == leader) base = atomicAdd(count, (uint32_t)__popc(m));
+    base = __shfl_sync(0xffffffffu, base, leader);
+    if (pred) {
+        uint32_t at = base + __popc(m & ((1u << lane) - 1u));
+        q[at] = slot;
+        keys[at] = key;
+    }
+}
+
+// The bin of a later flight: the coarse cell of its origin (x fastest), then
+// the octant of its direction.
+__device__ __forceinline__ uint32_t flight_bin(const WfArgs& W, f3 origin, f3 dir) {
+    int cx = min(max((int)floorf(origin.x) >> W.cell_shift, 0), W.cells_x - 1);
+    int cy = min(max((int)floorf(origin.y) >> W.cell_shift, 0), W.cells_y - 1);
+    int cz = min(max((int)floorf(origin.z) >> W.cell_shift, 0), W.cells_z - 1);
+    uint32_t oct = (dir.x < 0.0f ? 1u : 0u) | (dir.y < 0.0f ? 2u : 0u) | (dir.z < 0.0f ? 4u : 0u);
+    return ((uint32_t)((cz * W.cells_y + cy) * W.cells_x + cx) << 3) | oct;
+}
+
 // The end of a sample path: firefly clamp and sums (pt.comp:546-551), then
 // the pixel's next sample in the same slot (pt.comp:403). Returns true when
 // the slot has a new path; false when the work item (one pixel of one frame)
@@ -359,7 +386,7 @@ __global__ void __launch_bounds__(128, VV_EXTEND_MIN_BLOCKS)
         }
     }
     const uint32_t n = W.counts[FIRST ? WF_FIRST0 + cur : cur];
-    const uint32_t* queue = FIRST ? W.first[cur] : W.ext[cur];
+    const uint32_t* queue = FIRST ? W.first[cur] : W.sorted;
     uint32_t* taken = &W.counts[FIRST ? WF_TAKE_FIRST : WF_TAKE_EXT];
     const Consts C = make_consts(A);
     uint32_t slot = 0;
@@ -541,7 +568,7 @@ __global__ void __launch_bounds__(128, 6) k_wf_scatter(const __grid_constant__ P
         bool ended = i >= n_scatter;
         uint32_t slot = valid ? (ended ? W.esc[cur][i - n_scatter] : W.scatter[i]) : 0u;
         bool to_ext = false, to_first = false, done = false;
-        uint32_t item = 0;
+        uint32_t item = 0, key = 0;
         PixelSums S;
         if (valid) {
             Path P;
@@ -560,6 +587,7 @@ __global__ void __launch_bounds__(128, 6) k_wf_scatter(const __grid_constant__ P
                 V.map_pdf = h1.w;
                 V.map_dir = A.u.lighting[3] == 2u ? xyz(W.mapdir[slot]) : mk(0.0f);
                 to_ext = stage_scatter(A, C, P, V);
+                if (to_ext) key = flight_bin(W, P.origin, P.dir);
             } else {
                 float4 v3 = rec(W.vtx, slot, VTX_N)[3];
                 P.rng.s = ubits(v3.z);
@@ -579,13 +607,51 @@ __global__ void __launch_bounds__(128, 6) k_wf_scatter(const __grid_constant__ P
         }
         accumulate_items(A, done, item, S);
         if (refill(A, W, C, slot, done)) to_first = true;
-        push(W.ext[nxt], &W.counts[nxt], slot, to_ext);
+        push_key(W.ext[nxt], W.ext_key[nxt], &W.counts[nxt], slot, key, to_ext);
         push(W.first[nxt], &W.counts[WF_FIRST0 + nxt], slot, to_first);
     }
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         W.counts[WF_SHADOW] = 0;
         W.counts[WF_TAKE_SHADOW] = 0;
     }
+}
+
+// Counting sort of the next wave's later-flight queue by bin: counts, an
+// exclusive scan (one block), then placement. Order within a bin is free.
+__global__ void __launch_bounds__(256) k_wf_bin_count(const WfArgs W, int nxt) {
+    if (W.counts[WF_STOP] != 0u) return;
+    const uint32_t n = W.counts[nxt];
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        atomicAdd(&W.bin_count[W.ext_key[nxt][i]], 1u);
+}
+__global__ void __launch_bounds__(1024) k_wf_bin_scan(const WfArgs W) {
+    if (W.counts[WF_STOP] != 0u) return;
+    __shared__ uint32_t part[1024];
+    const uint32_t per = (W.nbins + 1023u) / 1024u, lo = threadIdx.x * per;
+    const uint32_t hi = min(lo + per, W.nbins);
+    uint32_t sum = 0;
+    for (uint32_t b = lo; b < hi; b++) sum += W.bin_count[b];
+    part[threadIdx.x] = sum;
+    __syncthreads();
+    for (int off = 1; off < 1024; off <<= 1) {  // inclusive scan of the 1024 partial sums
+        uint32_t v = threadIdx.x >= (unsigned)off ? part[threadIdx.x - off] : 0u;
+        __syncthreads();
+        part[threadIdx.x] += v;
+        __syncthreads();
+    }
+    uint32_t run = part[threadIdx.x] - sum;
+    for (uint32_t b = lo; b < hi; b++) {
+        uint32_t c = W.bin_count[b];
+        W.bin_next[b] = run;
+        run += c;
+        W.bin_count[b] = 0u;
+    }
+}
+__global__ void __launch_bounds__(256) k_wf_bin_place(const WfArgs W, int nxt) {
+    if (W.counts[WF_STOP] != 0u) return;
+    const uint32_t n = W.counts[nxt];
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        W.sorted[atomicAdd(&W.bin_next[W.ext_key[nxt][i]], 1u)] = W.ext[nxt][i];
 }
 
 // The paths still alive, run to completion one thread each (the reference's
@@ -665,6 +731,11 @@ cudaError_t launch_pt_wavefront(const PtArgs& a, const WfArgs& w, int sms, cudaS
         else k_wf_shadow<false><<<g_shadow, 128, 0, s>>>(a, w);
         k_wf_scatter<<<g_scatter, 128, 0, s>>>(a, w, cur);
         *launches += 5;
+        // The next wave's later flights, ordered by bin.
+        k_wf_bin_count<<<sms * 4, 256, 0, s>>>(w, cur ^ 1);
+        k_wf_bin_scan<<<1, 1024, 0, s>>>(w);
+        k_wf_bin_place<<<sms * 4, 256, 0, s>>>(w, cur ^ 1);
+        *launches += 3;
         cur ^= 1;
         cudaError_t e = cudaGetLastError();
         if (e != cudaSuccess) return e;

@@ -62,12 +62,15 @@ def parse():
                     help="instead of the path-tracing bench, run this many render requests (Poisson arrivals "
                          "at --serve-rate per second) over 8 resident phantoms through the request loop")
     ap.add_argument("--serve-rate", type=float, default=40.0)
+    ap.add_argument("--serve-modes", default="", help="comma-separated subset of the serving modes")
     ap.add_argument("--denoised-rmse", type=int, default=0,
                     help="instead of the path-tracing bench, train the learned denoiser for this many steps on "
                          "the head/neck workload at 1024^2 and time the fixed RMSE with it on held-out views")
     ap.add_argument("--bench-denoiser", type=int, default=1000,
                     help="Adam steps of the reduced time-to-RMSE run with the learned denoiser in the default line "
                          "(4 training views, 1 held out, the plain tracer's 256-path error; 0: skip)")
+    ap.add_argument("--nn-timing", action="store_true",
+                    help="time the learned denoiser's convolution shapes and U-Net forward pass at 1024^2")
     ap.add_argument("--denoiser-study", type=int, default=0,
                     help="instead of the path-tracing bench, train the learned denoiser for this many Adam steps "
                          "on pairs the tracer renders (4 vs 256 paths/pixel) and compare it with a-trous")
@@ -272,7 +275,7 @@ def peaks():
 # 512x512 case, times that kernel's time per frame in the full-size launch
 # list (gpu__time_duration.sum only). The small case's volumes nearly fit in
 # L2, so the volume traffic of the flight and shadow kernels is under-counted.
-PASS_TRAFFIC_BYTES_PER_FRAME = 1.137e9
+PASS_TRAFFIC_BYTES_PER_FRAME = 1.148e9
 
 
 def ncu_traffic(args):
@@ -683,8 +686,12 @@ def run_serve(args):
                                      "at %.0f/s" % (SERVE_DIMS, SERVE_SIZES, SERVE_SPP, args.serve_rate),
                          "requests": args.serve, "budget_bytes": budget, "phantom_generation_s": gen_s}}
     modes = (("continuous_shortest_first", dict(order="shortest", aging_s=2.0, max_per_volume=1)),
+             ("continuous_shortest_first_lean", dict(order="shortest", aging_s=2.0, max_per_volume=1, passes=2,
+                                                     slot_frames=8)),
              ("continuous_fifo", dict(order="fifo", max_per_volume=1)),
              ("one_at_a_time", dict(order="fifo", max_active=1)))
+    if args.serve_modes:
+        modes = tuple(m for m in modes if m[0] in args.serve_modes.split(","))
     for mode, kw in modes:
         make, base = S.renderer_factory(volumes)
         srv = S.Server(make, base, budget, **kw)
@@ -702,8 +709,58 @@ def run_serve(args):
                       "clocks": clocks.summary()})
         result[mode] = stats
         srv.close()
-    result["value"] = result["continuous_shortest_first"]["requests_per_s"]
+    first = "continuous_shortest_first" if "continuous_shortest_first" in result else modes[0][0]
+    result["value"] = result[first]["requests_per_s"]
     print(json.dumps(result))
+
+
+NN_SHAPES = [(16, 32), (32, 32), (32, 16), (48, 48), (64, 64), (80, 32), (64, 80)]
+
+
+def run_nn_timing(args):
+    """The learned denoiser's 3x3 convolution at 1024^2 for the shapes the
+    U-Net's full-resolution and deeper levels use (vv_nn_conv3x3: tcgen05
+    where it takes the shape, mma.sync otherwise), each timed over 20 launches
+    after 3 warm-up ones with CUDA events, and the whole U-Net forward pass at
+    1024^2 (random weights; the time does not depend on them)."""
+    import torch
+    from volview_gb300 import learned_denoiser as LD
+    from volview_gb300 import renderer as R
+    lib = R.load()
+    n, h, w = 1, 1024, 1024
+    out = {}
+
+    def timed(fn, reps=20):
+        for _ in range(3):
+            fn()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(reps):
+            fn()
+        e1.record()
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / reps
+
+    for cin, cout in NN_SHAPES:
+        X = torch.randn((n, h, w, cin), device="cuda").half()
+        W = (torch.randn((cout, 3, 3, cin), device="cuda") * 0.1).half()
+        B = torch.zeros(cout, device="cuda")
+        Y = torch.empty((n, h, w, cout), device="cuda", dtype=torch.float16)
+        ms = timed(lambda: lib.vv_nn_conv3x3(X.data_ptr(), n, h, w, cin, W.data_ptr(), B.data_ptr(), cout, 1,
+                                             Y.data_ptr(), None))
+        tc = lib.vv_nn_conv3x3_tc(X.data_ptr(), n, h, w, cin, W.data_ptr(), B.data_ptr(), cout, 1, Y.data_ptr(),
+                                  None) == 0
+        flops = 2.0 * n * h * w * cout * 9 * cin
+        out[f"{cin}->{cout}"] = {"us": ms * 1e3, "tflops": flops / ms / 1e9, "path": "tcgen05" if tc else "mma.sync"}
+    net = LD.UNet()
+    x = torch.zeros((1, 1024, 1024, LD.IN_CHANNELS), dtype=torch.float16, device="cuda")
+    unet_ms = timed(lambda: net.forward(x), reps=10)
+    flops = sum(2 * 9 * net.shapes[op[1]][0] * net.shapes[op[1]][1] *
+                (1024 >> (0 if op[1] == "head" else int(op[1][1]))) ** 2 for op in net.plan if op[0] == "conv")
+    print(json.dumps({"metric": "learned denoiser: 3x3 convolution and U-Net forward at 1024^2", "unit": "ms",
+                      "higher_is_better": False, "value": unet_ms, "unet_gflop": flops / 1e9,
+                      "unet_tflops": flops / (unet_ms / 1e3) / 1e12, "convolutions": out}))
 
 
 def run_denoiser_study(args):
@@ -928,6 +985,9 @@ def main():
     elif args.serve > 0:
         if rank == 0:
             run_serve(args)
+    elif args.nn_timing:
+        if rank == 0:
+            run_nn_timing(args)
     elif args.denoiser_study > 0:
         if rank == 0:
             run_denoiser_study(args)

@@ -375,6 +375,14 @@ vv_status vv_renderer_memory(const vv_renderer* r, uint64_t* bytes);
  * afresh, as in a renderer just created, so a reused renderer's next image
  * does not depend on the ones before it. */
 vv_status vv_reset_view(vv_renderer* r);
+/* The renderer's path-tracing pass state: `passes` passes in flight (1 to 6;
+ * 6 by default), each holding up to `slot_frames` frames' worth of path slots
+ * (1 to 16; 16 by default). Fewer passes and frames take less device memory
+ * (a pass at 1024^2 and 16 frames holds 5.7 GB) at some throughput when the
+ * renderer runs alone; several renderers serving at once keep the device busy
+ * between them. Waits for the renderer's work and frees the state of the
+ * passes it drops. VV_ERR_ARG outside the ranges. */
+vv_status vv_set_pass_budget(vv_renderer* r, uint32_t passes, uint32_t slot_frames);
 
 /* --------------------------------------------------- allocation-free denoise */
 

@@ -203,5 +203,27 @@ def test_request_bytes_model_follows_the_library_sources():
     assert S.SLOT_BYTES == slot + light + (queues + binned) * 4
     assert S.PASSES == num(r"#define VV_PASSES (\d+)", host)
     assert S.PASS_FRAMES == num(r"#define VV_SUBPASS_FRAMES (\d+)", host)
-    assert S.SLOT_FRAMES == num(r"std::atoi\(e\)\) : (\d+);", host)
+    assert S.SLOT_FRAMES == num(r"int slot_frames = (\d+);", host)
     assert S.SLOT_CAP == 1 << num(r"std::max\(px, \(size_t\)1 << (\d+)\)", host)
+
+
+def test_a_pass_budget_lowers_the_model_and_reaches_the_renderers():
+    """With fewer passes and frames in flight per renderer, the model asks for
+    less (the dropped passes' sums and slots), and every renderer the loop
+    makes gets the budget."""
+    full = S.request_bytes(1024, 1024, 1024)
+    lean = S.request_bytes(1024, 1024, 1024, passes=2, slot_frames=8)
+    assert lean == 1024 * 1024 * (S.IMAGE_BYTES_PER_PIXEL - 48 * 4) + 2 * 8 * 1024 * 1024 * S.SLOT_BYTES
+    assert lean < full / 5
+    budgets = []
+
+    class Budgeted(FakeRenderer):
+        def set_pass_budget(self, passes, frames):
+            budgets.append((passes, frames))
+
+    log = []
+    srv = S.Server(lambda v: Budgeted(v, 10 ** 9, log), lambda v: 10 ** 9, 10 ** 12, passes=2, slot_frames=8,
+                   clock=iter(range(10 ** 6)).__next__)
+    srv.preload("b")
+    run(srv, [S.Request("a", 256, 256, 16, params=0), S.Request("b", 256, 256, 16, params=1)])
+    assert budgets == [(2, 8), (2, 8)]

@@ -258,6 +258,8 @@ struct vv_renderer {
         cudaEvent_t shown = nullptr;  // after the pass's merge and display
     } pass[VV_PASSES];
     int next_pass = 0;
+    int passes = VV_PASSES;  // passes in use (vv_set_pass_budget)
+    int slot_frames = 16;    // frames' worth of path slots per pass (vv_set_pass_budget)
     bool prep_work = false;  // device work queued on the context stream by this call's set-up
     cudaEvent_t prep_done = nullptr;
     // accumulation
@@ -1056,15 +1058,22 @@ extern "C" vv_status vv_resize(vv_renderer* r, uint32_t width, uint32_t height) 
     if (s != VV_OK) return s;
     CK(cudaStreamSynchronize(r->ctx->stream));  // the context stream follows every pass's display
     size_t px = (size_t)width * height;
-    for (auto& P : r->pass) {
+    for (int k = 0; k < VV_PASSES; k++) {
+        vv_renderer::Pass& P = r->pass[k];
         if (!P.stream) {
             CK(cudaStreamCreateWithFlags(&P.stream, cudaStreamNonBlocking));
             CK(cudaEventCreateWithFlags(&P.shown, cudaEventDisableTiming));
         }
+        CK(P.counts.alloc(WF_COUNTERS * sizeof(uint32_t)));
+        if (k >= r->passes) {  // passes beyond the budget hold no sums
+            P.accum.release();
+            P.albedo.release();
+            P.normal.release();
+            continue;
+        }
         CK(P.accum.alloc(px * 16));
         CK(P.albedo.alloc(px * 16));
         CK(P.normal.alloc(px * 16));
-        CK(P.counts.alloc(WF_COUNTERS * sizeof(uint32_t)));
     }
     if (!r->prep_done) CK(cudaEventCreateWithFlags(&r->prep_done, cudaEventDisableTiming));
     CK(r->accum.alloc(px * 16));
@@ -1141,6 +1150,40 @@ extern "C" vv_status vv_reset_view(vv_renderer* r) {
     CK(cudaMemsetAsync(r->exposure.p, 0, sizeof(float), r->ctx->stream));
     r->prep_work = true;     // the next pass starts after it
     r->have_params = false;  // the next record restarts the accumulation
+    return VV_OK;
+}
+
+extern "C" vv_status vv_set_pass_budget(vv_renderer* r, uint32_t passes, uint32_t slot_frames) {
+    if (!r) return fail(VV_ERR_ARG, "null renderer");
+    if (passes < 1 || passes > VV_PASSES || slot_frames < 1 || slot_frames > 16)
+        return fail(VV_ERR_ARG, "passes must be 1..6 and slot_frames 1..16");
+    vv_status s = use_device(r);
+    if (s != VV_OK) return s;
+    CK(cudaStreamSynchronize(r->ctx->stream));
+    for (auto& P : r->pass)
+        if (P.stream) CK(cudaStreamSynchronize(P.stream));
+    for (int k = (int)passes; k < VV_PASSES; k++) {
+        vv_renderer::Pass& P = r->pass[k];
+        DBuf* pb[] = {&P.slots, &P.map, &P.queues, &P.accum, &P.albedo, &P.normal, &P.binq, &P.bins};
+        for (DBuf* b : pb) b->release();
+    }
+    if ((int)slot_frames < r->slot_frames)  // smaller slots: the next pass allocates anew
+        for (auto& P : r->pass) {
+            P.slots.release();
+            P.map.release();
+            P.queues.release();
+            P.binq.release();
+        }
+    r->passes = (int)passes;
+    r->slot_frames = (int)slot_frames;
+    r->next_pass = 0;
+    const size_t px = (size_t)r->width * r->height;
+    for (int k = 0; k < r->passes && px > 0; k++) {  // sums of passes now in use, at the image's size
+        vv_renderer::Pass& P = r->pass[k];
+        CK(P.accum.alloc(px * 16));
+        CK(P.albedo.alloc(px * 16));
+        CK(P.normal.alloc(px * 16));
+    }
     return VV_OK;
 }
 
@@ -1223,7 +1266,7 @@ static cudaError_t run_pt(vv_renderer* r, vv_renderer::Pass& P, PtArgs& a, cudaS
     // 171 M path samples/s with one frame's worth, 217 with 4, 238 with 16).
     size_t px = (size_t)r->width * r->height;
     const char* e = std::getenv("VV_WF_SLOTS");
-    size_t per_pixel = e ? (size_t)std::max(1, std::atoi(e)) : 16;
+    size_t per_pixel = e ? (size_t)std::max(1, std::atoi(e)) : (size_t)r->slot_frames;
     size_t cap = std::min(px * std::min<size_t>(per_pixel, a.frames), std::max(px, (size_t)1 << 24));
     if (P.slots.n < cap * WF_SLOT_BYTES) {
         cudaError_t ce = cudaStreamSynchronize(s);  // the pass's previous use of its state has ended
@@ -1290,6 +1333,8 @@ static cudaError_t run_pt(vv_renderer* r, vv_renderer::Pass& P, PtArgs& a, cudaS
         w.cells_x = cx;
         w.cells_y = cy;
         w.cells_z = cz;
+        const char* sh = std::getenv("VV_WF_SORT_SHADOW");
+        w.sort_shadows = sh ? std::atoi(sh) : 0;
     }
     return kernels_of(r).pt_wavefront(a, w, r->ctx->sms, s, launches);
 }
@@ -1627,9 +1672,9 @@ static vv_status run_unet(vv_renderer* r, float n, cudaStream_t s, int* launches
 // run beside the next pass's first ones.
 static vv_status record_pass(vv_renderer* r, const vv_frame_params& p, UHead& u, uint32_t frames,
                              bool display = true) {
-    vv_renderer::Pass& P = r->pass[r->next_pass];
-    vv_renderer::Pass& prev = r->pass[(r->next_pass + VV_PASSES - 1) % VV_PASSES];
-    r->next_pass = (r->next_pass + 1) % VV_PASSES;
+    vv_renderer::Pass& P = r->pass[r->next_pass % r->passes];
+    vv_renderer::Pass& prev = r->pass[(r->next_pass + r->passes - 1) % r->passes];
+    r->next_pass = (r->next_pass + 1) % r->passes;
     cudaStream_t s = P.stream;
     if (r->prep_work) {
         CK(cudaEventRecord(r->prep_done, r->ctx->stream));

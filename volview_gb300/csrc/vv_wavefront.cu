@@ -462,7 +462,7 @@ __global__ void __launch_bounds__(128, 4) k_wf_shade(const __grid_constant__ PtA
     WF_FOR_EACH(n) {
         uint32_t i = base_ + (threadIdx.x & 31u);
         bool valid = i < n;
-        uint32_t slot = valid ? W.shade[i] : 0u;
+        uint32_t slot = valid ? W.shade[i] : 0u, skey = 0;
         if (valid) {
             Path P;
             float4 b = rec(W.path, slot, PATH_N)[1];
@@ -474,9 +474,11 @@ __global__ void __launch_bounds__(128, 4) k_wf_shade(const __grid_constant__ PtA
             if (P.bounce == 0u) load_acc_guides(W, slot, S);
             stage_shade(A, C, P, S, V);
             store_shaded(W, slot, V, P.rng.s);
+            if (W.sort_shadows) skey = flight_bin(W, V.idx, V.light_dir);
             if (P.bounce == 0u) store_acc_guides(W, slot, S);
         }
-        push(W.shadow, &W.counts[WF_SHADOW], slot, valid);
+        if (W.sort_shadows) push_key(W.shadow, W.ext_key[cur], &W.counts[WF_SHADOW], slot, skey, valid);
+        else push(W.shadow, &W.counts[WF_SHADOW], slot, valid);
     }
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         W.counts[cur] = 0;
@@ -511,7 +513,7 @@ __global__ void __launch_bounds__(128, VV_SHADOW_MIN_BLOCKS) k_wf_shadow(const _
         if (__any_sync(0xffffffffu, need)) {
             uint32_t k = take_item(&W.counts[WF_TAKE_SHADOW], n, need);
             if (need && k != ~0u) {
-                slot = W.shadow[k];
+                slot = W.sort_shadows ? W.sorted[k] : W.shadow[k];
                 const float4* q = rec(W.shd, slot, SHD_N);
                 float4 a = q[0], b = q[1];
                 origin = xyz(a);
@@ -618,11 +620,11 @@ __global__ void __launch_bounds__(128, 6) k_wf_scatter(const __grid_constant__ P
 
 // Counting sort of the next wave's later-flight queue by bin: counts, an
 // exclusive scan (one block), then placement. Order within a bin is free.
-__global__ void __launch_bounds__(256) k_wf_bin_count(const WfArgs W, int nxt) {
+__global__ void __launch_bounds__(256) k_wf_bin_count(const WfArgs W, const uint32_t* keys, int count) {
     if (W.counts[WF_STOP] != 0u) return;
-    const uint32_t n = W.counts[nxt];
+    const uint32_t n = W.counts[count];
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
-        atomicAdd(&W.bin_count[W.ext_key[nxt][i]], 1u);
+        atomicAdd(&W.bin_count[keys[i]], 1u);
 }
 __global__ void __launch_bounds__(1024) k_wf_bin_scan(const WfArgs W) {
     if (W.counts[WF_STOP] != 0u) return;
@@ -647,11 +649,12 @@ __global__ void __launch_bounds__(1024) k_wf_bin_scan(const WfArgs W) {
         W.bin_count[b] = 0u;
     }
 }
-__global__ void __launch_bounds__(256) k_wf_bin_place(const WfArgs W, int nxt) {
+__global__ void __launch_bounds__(256) k_wf_bin_place(const WfArgs W, const uint32_t* queue, const uint32_t* keys,
+                                                      int count) {
     if (W.counts[WF_STOP] != 0u) return;
-    const uint32_t n = W.counts[nxt];
+    const uint32_t n = W.counts[count];
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
-        W.sorted[atomicAdd(&W.bin_next[W.ext_key[nxt][i]], 1u)] = W.ext[nxt][i];
+        W.sorted[atomicAdd(&W.bin_next[keys[i]], 1u)] = queue[i];
 }
 
 // The paths still alive, run to completion one thread each (the reference's
@@ -727,14 +730,22 @@ cudaError_t launch_pt_wavefront(const PtArgs& a, const WfArgs& w, int sms, cudaS
         k_wf_extend<true><<<g_ext, 128, 0, s>>>(a, w, cur, tail);
         k_wf_extend<false><<<g_ext, 128, 0, s>>>(a, w, cur, tail);
         k_wf_shade<<<g_shade, 128, 0, s>>>(a, w, cur);
+        if (w.sort_shadows) {
+            // The shadow rays ordered by the cell of their vertex and the octant
+            // of the light direction (keys in the current wave's spent key array).
+            k_wf_bin_count<<<sms * 4, 256, 0, s>>>(w, w.ext_key[cur], WF_SHADOW);
+            k_wf_bin_scan<<<1, 1024, 0, s>>>(w);
+            k_wf_bin_place<<<sms * 4, 256, 0, s>>>(w, w.shadow, w.ext_key[cur], WF_SHADOW);
+            *launches += 3;
+        }
         if (map) k_wf_shadow<true><<<g_shadow, 128, 0, s>>>(a, w);
         else k_wf_shadow<false><<<g_shadow, 128, 0, s>>>(a, w);
         k_wf_scatter<<<g_scatter, 128, 0, s>>>(a, w, cur);
         *launches += 5;
         // The next wave's later flights, ordered by bin.
-        k_wf_bin_count<<<sms * 4, 256, 0, s>>>(w, cur ^ 1);
+        k_wf_bin_count<<<sms * 4, 256, 0, s>>>(w, w.ext_key[cur ^ 1], cur ^ 1);
         k_wf_bin_scan<<<1, 1024, 0, s>>>(w);
-        k_wf_bin_place<<<sms * 4, 256, 0, s>>>(w, cur ^ 1);
+        k_wf_bin_place<<<sms * 4, 256, 0, s>>>(w, w.ext[cur ^ 1], w.ext_key[cur ^ 1], cur ^ 1);
         *launches += 3;
         cur ^= 1;
         cudaError_t e = cudaGetLastError();

@@ -55,6 +55,7 @@ EXPORTS = [
     ("vv_query", C.c_int, [P, P]),
     ("vv_renderer_memory", C.c_int, [P, P]),
     ("vv_reset_view", C.c_int, [P]),
+    ("vv_set_pass_budget", C.c_int, [P, C.c_uint32, C.c_uint32]),
     ("vv_set_denoiser_weights", C.c_int, [P, P, C.c_size_t]),
     ("vv_denoise_atrous_noalloc", C.c_int, [P, P, P, P, C.c_uint32, C.c_uint32, C.c_uint32, P]),
 ]
@@ -221,6 +222,11 @@ class Renderer:
             return
         blob = np.ascontiguousarray(params, np.float32).ravel()
         check(load().vv_set_denoiser_weights(self.handle, _ptr(blob), blob.size))
+
+    def set_pass_budget(self, passes, slot_frames):
+        """vv_set_pass_budget: passes in flight (1..6) and frames' worth of path
+        slots per pass (1..16)."""
+        check(load().vv_set_pass_budget(self.handle, passes, slot_frames))
 
     def reset_view(self):
         """A new view: the accumulation restarts and auto exposure meters afresh."""

@@ -37,13 +37,16 @@ SLOT_FRAMES = 16    # frames' worth of slots a pass holds at most ...
 SLOT_CAP = 1 << 24  # ... and at most this many slots, unless one frame needs more
 
 
-def request_bytes(width, height, spp):
-    """Device bytes a renderer's image and path state take for one request."""
+def request_bytes(width, height, spp, passes=PASSES, slot_frames=SLOT_FRAMES):
+    """Device bytes a renderer's image and path state take for one request,
+    with `passes` passes in flight of up to `slot_frames` frames' worth of
+    slots each (vv_set_pass_budget)."""
     px = width * height
     frames = min(spp, PASS_FRAMES)
-    slots = min(min(frames, SLOT_FRAMES) * px, max(SLOT_CAP, px))
-    passes = min(PASSES, -(-spp // PASS_FRAMES))
-    return px * IMAGE_BYTES_PER_PIXEL + passes * slots * SLOT_BYTES
+    slots = min(min(frames, slot_frames) * px, max(SLOT_CAP, px))
+    used = min(passes, -(-spp // PASS_FRAMES))
+    sums = 48 * px * (PASSES - passes)  # IMAGE_BYTES_PER_PIXEL counts every pass's sums
+    return px * IMAGE_BYTES_PER_PIXEL - sums + used * slots * SLOT_BYTES
 
 
 class Request:
@@ -85,12 +88,16 @@ class Server:
     of all younger ones, in arrival order, so long ones are not starved)."""
 
     def __init__(self, make_renderer, base_bytes, budget_bytes, max_active=None, keep_accumulation=False,
-                 clock=time.perf_counter, order="fifo", aging_s=2.0, max_per_volume=None):
+                 clock=time.perf_counter, order="fifo", aging_s=2.0, max_per_volume=None, passes=PASSES,
+                 slot_frames=SLOT_FRAMES):
         if order not in ("fifo", "shortest"):
             raise ValueError(f"unknown admission order {order!r}")
         self.make_renderer, self.base_bytes = make_renderer, base_bytes
         self.budget, self.max_active, self.keep_accumulation = int(budget_bytes), max_active, keep_accumulation
         self.clock, self.order, self.aging_s, self.max_per_volume = clock, order, aging_s, max_per_volume
+        # Each renderer's pass state (vv_set_pass_budget): fewer passes and
+        # frames in flight per renderer, when several renderers serve at once.
+        self.passes, self.slot_frames = passes, slot_frames
         self.queue = collections.deque()
         self.active = []
         self.idle = collections.OrderedDict()  # renderer -> volume, least recently used first
@@ -108,7 +115,7 @@ class Server:
     def _need(self, req, renderer):
         """Bytes admitting `req` adds: a new renderer's volumes and image, or
         the growth of a reused one."""
-        want = request_bytes(req.width, req.height, req.spp)
+        want = request_bytes(req.width, req.height, req.spp, self.passes, self.slot_frames)
         if renderer is None:
             return self.base_bytes(req.volume) + want
         return max(0, self.base_bytes(req.volume) + want - renderer.device_bytes())
@@ -174,6 +181,8 @@ class Server:
             self.queue.remove(req)
             if r is None:
                 r = self.make_renderer(req.volume)
+                if (self.passes, self.slot_frames) != (PASSES, SLOT_FRAMES):
+                    r.set_pass_budget(self.passes, self.slot_frames)
                 self.owned[r] = req.volume
                 self.created += 1
             else:
@@ -229,6 +238,8 @@ class Server:
     def preload(self, volume):
         """Makes a renderer of `volume` resident (idle) before requests come."""
         r = self.make_renderer(volume)
+        if (self.passes, self.slot_frames) != (PASSES, SLOT_FRAMES):
+            r.set_pass_budget(self.passes, self.slot_frames)
         self.owned[r] = volume
         self.idle[r] = volume
         self.created += 1

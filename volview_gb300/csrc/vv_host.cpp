@@ -1333,8 +1333,6 @@ static cudaError_t run_pt(vv_renderer* r, vv_renderer::Pass& P, PtArgs& a, cudaS
         w.cells_x = cx;
         w.cells_y = cy;
         w.cells_z = cz;
-        const char* sh = std::getenv("VV_WF_SORT_SHADOW");
-        w.sort_shadows = sh ? std::atoi(sh) : 0;
     }
     return kernels_of(r).pt_wavefront(a, w, r->ctx->sms, s, launches);
 }

@@ -125,7 +125,6 @@ struct WfArgs {
     uint32_t nbins;
     int cell_shift;        // log2 of a cell's edge in voxels
     int cells_x, cells_y, cells_z;
-    int sort_shadows;      // 1: the shadow queue is ordered the same way before the shadow kernel
 };
 // A lighting volume as the image loop reads it: a 3D texture of its texels
 // inside a one-texel white border, filtered by the texture units (clamped

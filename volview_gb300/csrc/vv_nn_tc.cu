@@ -9,16 +9,20 @@
 // core matrices, the 8-row groups of one 16-byte K slice 128 bytes apart (the
 // stride byte offset), consecutive K slices LBO bytes apart.
 //
-// A persistent CTA keeps all nine taps' weights in shared memory and takes
-// segments in turn. Per segment, TMA copies the three input rows with their
-// one-pixel halo (3 x 130 pixels), one box of 8 channels x 130 pixels per row
-// and 16-byte channel slice, zero-filled outside the image (same padding);
-// such a box is one K slice of the layout above. Tap (dy, dx)'s A operand is
-// row dy's slices starting dx pixels in: the descriptor's start address moves
-// by 16 bytes per pixel. Roles:
-//   warp 4 (one lane): waits for a segment's rows, issues its 9 x cin / 16
-//     MMAs into one of two TMEM accumulators, commits them to an mbarrier,
-//     and issues the TMA copies two segments ahead into the freed buffer;
+// A CTA keeps all nine taps' weights in shared memory and walks down a run
+// of rows of one column of segments (the same 128 pixels of consecutive
+// rows). Its input rows, each with its one-pixel halo (130 pixels), sit in a
+// ring of four row slots: a segment uses three (rows y-1, y, y+1) and the
+// fourth takes the next row, so every input row is copied once per run. TMA
+// copies a row as boxes of 8 channels x 130 pixels, one per 16-byte channel
+// slice, zero-filled outside the image (same padding); such a box is one K
+// slice of the layout above. Tap (dy, dx)'s A operand is row y+dy-1's slices
+// starting dx pixels in: the descriptor's start address moves by 16 bytes per
+// pixel. Roles:
+//   warp 4 (one lane): waits for a segment's three rows, issues its
+//     9 x cin / 16 MMAs into one of two TMEM accumulators, commits them to an
+//     mbarrier, and copies the next row into the slot the previous segment
+//     has finished with;
 //   warps 0-3: read the finished accumulator (warp w owns TMEM lanes
 //     32w..32w+31, one output pixel per lane), release it, add the bias,
 //     apply the ReLU and store FP16.
@@ -31,6 +35,8 @@
 #include <cuda_runtime.h>
 #include <cudaTypedefs.h>
 #include <stdint.h>
+
+#include <algorithm>
 
 #include "../../include/volpt_nn.h"
 
@@ -86,30 +92,37 @@ constexpr int TC_THREADS = EPI_THREADS + 32;  // + warp 4, the issuing warp
 __host__ __device__ constexpr uint32_t tmem_cols(int np) {
     return 2 * np <= 32 ? 32 : 2 * np <= 64 ? 64 : 2 * np <= 128 ? 128 : 2 * np <= 256 ? 256 : 512;
 }
-// Weights, two buffers of three row slices, and slack to align the buffers to 1024 bytes.
+constexpr int RING = 4;  // row slots
+// Weights, the ring of row slots, and slack to align the ring to 1024 bytes.
 static size_t tc_smem(int np, int cin) {
-    return 9 * (size_t)np * 2 * cin + 2 * 3 * (size_t)(cin / 8) * SLICE_STRIDE + 1024;
+    return 9 * (size_t)np * 2 * cin + RING * (size_t)(cin / 8) * SLICE_STRIDE + 1024;
 }
 
 template <int NP>
 __global__ void __launch_bounds__(TC_THREADS) k_conv3x3_tc(const __grid_constant__ CUtensorMap rows, int n, int h,
                                                            int w, int cin, const __half* __restrict__ wt,
                                                            const float* __restrict__ bias, int cout, int relu,
-                                                           __half* __restrict__ y) {
+                                                           __half* __restrict__ y, int run_rows) {
     constexpr uint32_t COLS = tmem_cols(NP);
     constexpr uint32_t IDESC = instr_desc(TC_M, NP);
     extern __shared__ __align__(1024) unsigned char smem[];
-    __shared__ __align__(8) uint64_t bars[6];  // full[2] (TMA), mma[2] (tcgen05.commit), free[2] (epilogue)
+    __shared__ __align__(8) uint64_t bars[RING + 4];  // full[RING] (TMA), mma[2] (tcgen05.commit), free[2]
     __shared__ uint32_t tmem_slot;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int chunks = cin >> 3;
     const int per_row = w / TC_M;
-    const long tiles = (long)n * h * per_row;
+    // This CTA's run: column (image, segment) blockIdx.x % columns, rows
+    // [y0, y1) of it.
+    const int columns = n * per_row;
+    const int column = (int)(blockIdx.x % columns), run = (int)(blockIdx.x / columns);
+    const int img = column / per_row, x0 = (column - img * per_row) * TC_M;
+    const int y0 = run * run_rows, y1 = min(h, y0 + run_rows);
+    const int ntiles = y1 > y0 ? y1 - y0 : 0;
     const uint32_t wbase = smem_u32(smem);
     const uint32_t w_tap = NP * 2 * cin;                        // one tap's weights
-    const uint32_t hbase = (wbase + 9 * w_tap + 1023u) & ~1023u;  // two buffers of three row slices
-    const uint32_t seg = chunks * SLICE_STRIDE, hbuf = 3 * seg;
-    const uint32_t full0 = smem_u32(&bars[0]), mma0 = smem_u32(&bars[2]), free0 = smem_u32(&bars[4]);
+    const uint32_t hbase = (wbase + 9 * w_tap + 1023u) & ~1023u;  // the ring of row slots
+    const uint32_t seg = chunks * SLICE_STRIDE;                 // one row slot
+    const uint32_t full0 = smem_u32(&bars[0]), mma0 = smem_u32(&bars[RING]), free0 = smem_u32(&bars[RING + 2]);
 
     if (warp == 0) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_slot)),
@@ -117,8 +130,8 @@ __global__ void __launch_bounds__(TC_THREADS) k_conv3x3_tc(const __grid_constant
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
     }
     if (tid == 0) {
+        for (int k = 0; k < RING; k++) asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(full0 + 8 * k));
         for (int k = 0; k < 2; k++) {
-            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(full0 + 8 * k));
             asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(mma0 + 8 * k));
             asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(free0 + 8 * k), "r"(EPI_THREADS));
         }
@@ -144,36 +157,33 @@ __global__ void __launch_bounds__(TC_THREADS) k_conv3x3_tc(const __grid_constant
     const uint32_t tmem = tmem_slot;
 
     if (warp == 4) {
-        if (lane == 0) {
-            const uint32_t bytes = 3u * chunks * SLICE;
-            auto load = [&](long tile, int b) {
-                const long img_row = tile / per_row;
-                const int x0 = (int)(tile - img_row * per_row) * TC_M;
-                const int img = (int)(img_row / h), yy = (int)(img_row - (long)img * h);
-                const uint32_t bar = full0 + 8 * b;
+        if (lane == 0 && ntiles > 0) {
+            const uint32_t bytes = chunks * SLICE;
+            // Relative row q of the run is image row y0 - 1 + q, in slot q % RING;
+            // its copy is that slot's (q / RING)-th.
+            auto load_row = [&](int q) {
+                const uint32_t bar = full0 + 8 * (q % RING);
                 asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
-                for (int dy = 0; dy < 3; dy++)
-                    for (int c = 0; c < chunks; c++) {
-                        const uint32_t dst = hbase + b * hbuf + dy * seg + c * SLICE_STRIDE;
-                        asm volatile(
-                            "cp.async.bulk.tensor.4d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
-                            " [%0], [%1, {%2, %3, %4, %5}], [%6];" ::"r"(dst),
-                            "l"((uint64_t)&rows), "r"(c * 8), "r"(x0 - 1), "r"(yy + dy - 1), "r"(img), "r"(bar)
-                            : "memory");
-                    }
+                for (int c = 0; c < chunks; c++) {
+                    const uint32_t dst = hbase + (q % RING) * seg + c * SLICE_STRIDE;
+                    asm volatile(
+                        "cp.async.bulk.tensor.4d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
+                        " [%0], [%1, {%2, %3, %4, %5}], [%6];" ::"r"(dst),
+                        "l"((uint64_t)&rows), "r"(c * 8), "r"(x0 - 1), "r"(y0 - 1 + q), "r"(img), "r"(bar)
+                        : "memory");
+                }
             };
-            int i = 0;
-            for (long tile = blockIdx.x; tile < tiles && i < 2; tile += gridDim.x, i++) load(tile, i);
-            i = 0;
-            for (long tile = blockIdx.x; tile < tiles; tile += gridDim.x, i++) {
+            load_row(0);
+            load_row(1);
+            load_row(2);
+            for (int i = 0; i < ntiles; i++) {
                 const int b = i & 1;
-                bar_wait(full0 + 8 * b, (i >> 1) & 1);  // this segment's rows have landed
+                for (int q = i; q < i + 3; q++) bar_wait(full0 + 8 * (q % RING), (q / RING) & 1);  // rows y-1, y, y+1
                 if (i >= 2) bar_wait(free0 + 8 * b, ((i >> 1) - 1) & 1);  // accumulator b read out
                 asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
                 const uint32_t acc = tmem + b * NP;
-                const uint32_t hb = hbase + b * hbuf;
                 for (int tap = 0; tap < 9; tap++) {
-                    const uint32_t a0 = hb + (tap / 3) * seg + (tap % 3) * 16;
+                    const uint32_t a0 = hbase + ((i + tap / 3) % RING) * seg + (tap % 3) * 16;
                     const uint32_t b0 = wbase + tap * w_tap;
                     for (int k = 0; k < cin / 16; k++) {
                         const uint64_t da = smem_desc(a0 + k * 2 * SLICE_STRIDE, SLICE_STRIDE, 128);
@@ -188,18 +198,18 @@ __global__ void __launch_bounds__(TC_THREADS) k_conv3x3_tc(const __grid_constant
                 asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
                                  mma0 + 8 * b)
                              : "memory");
-                const long ahead = tile + 2L * gridDim.x;
-                if (ahead < tiles) {
-                    bar_wait(mma0 + 8 * b, (i >> 1) & 1);  // buffer b read by this segment's MMAs
-                    load(ahead, b);
+                if (i + 1 < ntiles) {
+                    // The next segment's new row goes into the slot of row i - 1,
+                    // which the previous segment's MMAs were the last to read.
+                    if (i >= 1) bar_wait(mma0 + 8 * ((i - 1) & 1), ((i - 1) >> 1) & 1);
+                    load_row(i + 3);
                 }
             }
         }
         __syncwarp();
     } else {
         // Epilogue: warps 0-3, one output pixel per thread.
-        int i = 0;
-        for (long tile = blockIdx.x; tile < tiles; tile += gridDim.x, i++) {
+        for (int i = 0; i < ntiles; i++) {
             const int b = i & 1;
             const bool ok = bar_wait(mma0 + 8 * b, (i >> 1) & 1);
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
@@ -233,8 +243,7 @@ __global__ void __launch_bounds__(TC_THREADS) k_conv3x3_tc(const __grid_constant
             asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
             asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(free0 + 8 * b) : "memory");
             if (ok) {
-                const long img_row = tile / per_row;
-                const long p = img_row * w + (long)(tile - img_row * per_row) * TC_M + tid;
+                const long p = ((long)img * h + y0 + i) * w + x0 + tid;
                 __half* dst = y + p * cout;
 #pragma unroll
                 for (int c0 = 0; c0 < NP; c0 += 8)
@@ -293,9 +302,14 @@ static cudaError_t launch_tc(const CUtensorMap& map, int n, int h, int w, int ci
     per_sm = per_sm < 2048 / TC_THREADS ? per_sm : 2048 / TC_THREADS;
     per_sm = per_sm < (int)(512 / tmem_cols(NP)) ? per_sm : (int)(512 / tmem_cols(NP));
     per_sm = per_sm < 1 ? 1 : per_sm;
-    const long tiles = (long)n * h * (w / TC_M);
-    const long grid = tiles < (long)sms * per_sm ? tiles : (long)sms * per_sm;
-    k_conv3x3_tc<NP><<<(unsigned)grid, TC_THREADS, smem, s>>>(map, n, h, w, cin, wt, bias, cout, relu, y);
+    // Runs of rows: every resident CTA takes one, the runs of a column of
+    // segments as long as the CTAs per column allow.
+    const long columns = (long)n * (w / TC_M);
+    const long slots = (long)sms * per_sm;
+    const long per_column = std::max(1L, slots / columns);
+    const int run_rows = (int)((h + per_column - 1) / per_column);
+    const long grid = columns * ((h + run_rows - 1) / run_rows);
+    k_conv3x3_tc<NP><<<(unsigned)grid, TC_THREADS, smem, s>>>(map, n, h, w, cin, wt, bias, cout, relu, y, run_rows);
     return cudaGetLastError();
 }
 

@@ -462,7 +462,7 @@ __global__ void __launch_bounds__(128, 4) k_wf_shade(const __grid_constant__ PtA
     WF_FOR_EACH(n) {
         uint32_t i = base_ + (threadIdx.x & 31u);
         bool valid = i < n;
-        uint32_t slot = valid ? W.shade[i] : 0u, skey = 0;
+        uint32_t slot = valid ? W.shade[i] : 0u;
         if (valid) {
             Path P;
             float4 b = rec(W.path, slot, PATH_N)[1];
@@ -474,11 +474,9 @@ __global__ void __launch_bounds__(128, 4) k_wf_shade(const __grid_constant__ PtA
             if (P.bounce == 0u) load_acc_guides(W, slot, S);
             stage_shade(A, C, P, S, V);
             store_shaded(W, slot, V, P.rng.s);
-            if (W.sort_shadows) skey = flight_bin(W, V.idx, V.light_dir);
             if (P.bounce == 0u) store_acc_guides(W, slot, S);
         }
-        if (W.sort_shadows) push_key(W.shadow, W.ext_key[cur], &W.counts[WF_SHADOW], slot, skey, valid);
-        else push(W.shadow, &W.counts[WF_SHADOW], slot, valid);
+        push(W.shadow, &W.counts[WF_SHADOW], slot, valid);
     }
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         W.counts[cur] = 0;
@@ -513,7 +511,7 @@ __global__ void __launch_bounds__(128, VV_SHADOW_MIN_BLOCKS) k_wf_shadow(const _
         if (__any_sync(0xffffffffu, need)) {
             uint32_t k = take_item(&W.counts[WF_TAKE_SHADOW], n, need);
             if (need && k != ~0u) {
-                slot = W.sort_shadows ? W.sorted[k] : W.shadow[k];
+                slot = W.shadow[k];
                 const float4* q = rec(W.shd, slot, SHD_N);
                 float4 a = q[0], b = q[1];
                 origin = xyz(a);
@@ -730,14 +728,6 @@ cudaError_t launch_pt_wavefront(const PtArgs& a, const WfArgs& w, int sms, cudaS
         k_wf_extend<true><<<g_ext, 128, 0, s>>>(a, w, cur, tail);
         k_wf_extend<false><<<g_ext, 128, 0, s>>>(a, w, cur, tail);
         k_wf_shade<<<g_shade, 128, 0, s>>>(a, w, cur);
-        if (w.sort_shadows) {
-            // The shadow rays ordered by the cell of their vertex and the octant
-            // of the light direction (keys in the current wave's spent key array).
-            k_wf_bin_count<<<sms * 4, 256, 0, s>>>(w, w.ext_key[cur], WF_SHADOW);
-            k_wf_bin_scan<<<1, 1024, 0, s>>>(w);
-            k_wf_bin_place<<<sms * 4, 256, 0, s>>>(w, w.shadow, w.ext_key[cur], WF_SHADOW);
-            *launches += 3;
-        }
         if (map) k_wf_shadow<true><<<g_shadow, 128, 0, s>>>(a, w);
         else k_wf_shadow<false><<<g_shadow, 128, 0, s>>>(a, w);
         k_wf_scatter<<<g_scatter, 128, 0, s>>>(a, w, cur);

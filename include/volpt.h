@@ -239,7 +239,7 @@ vv_status vv_renderer_create(vv_context* ctx, const vv_volume* volume,
 /* Storage and running-sum precision: an extension beyond the reference
  * (whose density is R16_UNORM and whose sums are FP32), for the precision
  * variant of the workload. vv_renderer_create uses the reference's
- * {VV_DENSITY_UNORM16, VV_SUMS_FP32, 0, VV_MAJORANTS_REFERENCE}. */
+ * {VV_DENSITY_UNORM16, VV_SUMS_FP32, 0, VV_MAJORANTS_REFERENCE, VV_MASK_UNORM16}. */
 enum {
     VV_DENSITY_UNORM16 = 0, /* round(t * 65535), t = normalised density (the reference) */
     VV_DENSITY_FP16 = 1,    /* t as binary16, rounded to nearest even */
@@ -263,12 +263,22 @@ enum {
     VV_MAJORANTS_REFERENCE = 0, /* bucket maxima of the FP32 LUT (the reference) */
     VV_MAJORANTS_BOUND = 1      /* of the FP16 LUT, rounded up: true bounds */
 };
+/* The two label-mask volumes (the binary and the blurred mask; RG16_UNORM in
+ * the reference, renderer.rs:1455-1470). VV_MASK_FP16 / VV_MASK_BF16 store
+ * the mask values as binary16 / bfloat16 (rounded to nearest even) and need
+ * the density in the same format. */
+enum {
+    VV_MASK_UNORM16 = 0,    /* round(m * 65535) (the reference) */
+    VV_MASK_FP16 = 1,       /* m as binary16; density_format VV_DENSITY_FP16 */
+    VV_MASK_BF16 = 2        /* m as bfloat16; density_format VV_DENSITY_BF16 */
+};
 typedef struct vv_precision {
     uint32_t density_format; /* VV_DENSITY_* */
     uint32_t sums;           /* VV_SUMS_* */
     uint32_t fp64_after;     /* 0: never; else the running sums continue in FP64
                                 once they hold this many samples per pixel */
     uint32_t majorants;      /* VV_MAJORANTS_* */
+    uint32_t mask_format;    /* VV_MASK_* */
 } vv_precision;
 /* vv_renderer_create with a storage and running-sum precision. Frames
  * accumulated by the wavefront passes are summed per pass (FP32, atomically
@@ -341,7 +351,8 @@ vv_status vv_pack_uniforms(vv_renderer* r, const vv_frame_params* params, uint64
 enum {
     VV_VOLUME_DENSITY = 0,  /* uint16 per voxel (R16_UNORM; FP16 / BF16 bits, or float, per vv_precision) */
     VV_VOLUME_NORMALS = 1,  /* 4 x int8 per voxel (RGBA8_SNORM) */
-    VV_VOLUME_MASK = 2,     /* 2 x uint16 per voxel (RG16_UNORM) */
+    VV_VOLUME_MASK = 2,     /* 2 x 16-bit codes per voxel: RG16_UNORM, or binary16 /
+                               bfloat16 under VV_MASK_FP16 / VV_MASK_BF16 */
     VV_VOLUME_LABELS = 3,   /* uint8 per voxel */
     VV_VOLUME_MAJORANT = 4, /* float per brick, brick grid x-fastest */
     VV_VOLUME_SHADOW = 5,   /* ray marcher's shadow volume: RGBA16F, ceil(dims / 2), x-fastest */

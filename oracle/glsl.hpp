@@ -332,12 +332,14 @@ inline mat3 inverse(const mat3& m) {
 enum Format : int {
     R16_UNORM, RG16_UNORM, RGBA8_SNORM, RGBA8_UNORM, R32F, RG32F, RGBA32F, RGBA16F, R16F,
     R8_UINT, RGBA8_UINT,
-    R16_BF16  // appended: the values above are part of the reference harness's interface (oracle/ref.py)
+    R16_BF16,  // appended: the values above are part of the reference harness's interface (oracle/ref.py)
+    RG16F, RG16_BF16  // the precision variant's label mask (two binary16 / bfloat16 channels)
 };
 inline int format_bytes(Format f) {
     switch (f) {
         case R16_UNORM: case R16F: case R16_BF16: return 2;
-        case RG16_UNORM: case RGBA8_SNORM: case RGBA8_UNORM: case R32F: case RGBA8_UINT: return 4;
+        case RG16_UNORM: case RGBA8_SNORM: case RGBA8_UNORM: case R32F: case RGBA8_UINT: case RG16F:
+        case RG16_BF16: return 4;
         case RG32F: case RGBA16F: return 8;
         case RGBA32F: return 16;
         case R8_UINT: return 1;
@@ -346,6 +348,12 @@ inline int format_bytes(Format f) {
 }
 inline float half_to_float(uint16_t h) { _Float16 v; std::memcpy(&v, &h, 2); return (float)v; }
 inline uint16_t float_to_half(float f) { _Float16 v = (_Float16)f; uint16_t h; std::memcpy(&h, &v, 2); return h; }
+// bfloat16: the upper half of a binary32; rounding to nearest even (finite values).
+inline float bf16_to_float(uint16_t v) { uint32_t w = (uint32_t)v << 16; f32 x; std::memcpy(&x, &w, 4); return x; }
+inline uint16_t float_to_bf16(float f) {
+    f32 x = (f32)f; uint32_t w; std::memcpy(&w, &x, 4);
+    return (uint16_t)((w + 0x7fffu + ((w >> 16) & 1u)) >> 16);
+}
 
 // Decodes texel `i` (linear index) of `data` in format `f` to floats.
 inline vec4 decode(const void* data, Format f, long i) {
@@ -367,6 +375,8 @@ inline vec4 decode(const void* data, Format f, long i) {
         }
         case R8_UINT: return vec4(float(b[0]), 0, 0, 1);
         case RGBA8_UINT: return vec4(float(b[0]), float(b[1]), float(b[2]), float(b[3]));
+        case RG16F: { uint16_t v[2]; std::memcpy(v, b, 4); return vec4(half_to_float(v[0]), half_to_float(v[1]), 0, 1); }
+        case RG16_BF16: { uint16_t v[2]; std::memcpy(v, b, 4); return vec4(bf16_to_float(v[0]), bf16_to_float(v[1]), 0, 1); }
     }
     return vec4(0.0f);
 }
@@ -393,6 +403,8 @@ inline void encode(void* data, Format f, long i, const vec4& v) {
         }
         case R8_UINT: b[0] = (uint8_t)v.x; break;
         case RGBA8_UINT: for (int k = 0; k < 4; k++) b[k] = (uint8_t)v[k]; break;
+        case RG16F: { uint16_t q[2] = {float_to_half(v.x), float_to_half(v.y)}; std::memcpy(b, q, 4); break; }
+        case RG16_BF16: { uint16_t q[2] = {float_to_bf16(v.x), float_to_bf16(v.y)}; std::memcpy(b, q, 4); break; }
     }
 }
 

@@ -58,7 +58,8 @@ struct Scene {
     const void* density = nullptr;       // R16_UNORM, or the precision variant's format
     int density_format = 0;              // VV_DENSITY_*
     const int8_t* normals = nullptr;     // RGBA8_SNORM
-    const uint16_t* mask = nullptr;      // RG16_UNORM (final, blurred)
+    const uint16_t* mask = nullptr;      // RG16_UNORM (final, blurred), or the precision variant's format
+    int mask_format = 0;                 // VV_MASK_*
     const uint8_t* labels = nullptr;     // R8_UINT; 1 voxel placeholder if absent
     ivec3 label_dims = ivec3(1, 1, 1);
     const float* majorant = nullptr;     // R32F over the brick grid

@@ -19,7 +19,7 @@ class Scene(C.Structure):
     _fields_ = [("dims", C.c_int * 3), ("density", P), ("normals", P), ("mask", P), ("labels", P),
                 ("label_dims", C.c_int * 3), ("majorant", P), ("brick_dims", C.c_int * 3), ("tf_lut", P),
                 ("preint", P), ("env_rad", P), ("env_table", P), ("env_dims", C.c_int * 2),
-                ("density_format", C.c_int)]
+                ("density_format", C.c_int), ("mask_format", C.c_int)]
 
 
 class Geometry(C.Structure):
@@ -124,6 +124,9 @@ def hu_to_unorm16(hu):
 
 # Density storage formats of the precision variant (vv_precision.density_format).
 DENSITY_UNORM16, DENSITY_FP16, DENSITY_BF16, DENSITY_FP32 = 0, 1, 2, 3
+# Label-mask storage formats (vv_precision.mask_format): RG16_UNORM, or two
+# binary16 / bfloat16 channels.
+MASK_UNORM16, MASK_FP16, MASK_BF16 = 0, 1, 2
 
 
 def normalised_density(hu):
@@ -192,12 +195,14 @@ class CpuRenderer:
     every pass run by the oracle. Arrays are x-fastest, shaped (z, y, x, ...).
     """
 
-    def __init__(self, volume, tf, hu, density_format=DENSITY_UNORM16, majorants=MAJORANTS_REFERENCE):
+    def __init__(self, volume, tf, hu, density_format=DENSITY_UNORM16, majorants=MAJORANTS_REFERENCE,
+                 mask_format=MASK_UNORM16):
         self.volume = volume
         self.hu = np.ascontiguousarray(hu, np.int16)
         self.dims = tuple(volume.dims)
         self.geo = geometry(volume)
         self.density_format = density_format
+        self.mask_format = mask_format
         self.majorants = majorants
         self.density = density_encode(self.hu, density_format)
         self.set_transfer_function(tf)
@@ -260,6 +265,7 @@ class CpuRenderer:
         s.dims[:] = self.dims
         s.density = ptr(self.density)
         s.density_format = self.density_format
+        s.mask_format = self.mask_format
         s.normals = ptr(getattr(self, "normals", None))
         s.mask = ptr(self.mask)
         s.labels = ptr(self.labels)

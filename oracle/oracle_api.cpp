@@ -55,6 +55,7 @@ typedef struct vvo_scene {
     const float* env_table;
     int env_dims[2];
     int density_format;
+    int mask_format;
 } vvo_scene;
 
 typedef struct vvo_geometry {
@@ -83,6 +84,7 @@ static Scene to_scene(const vvo_scene* s) {
     sc.env_table = s->env_table;
     sc.env_dims = ivec2(s->env_dims[0], s->env_dims[1]);
     sc.density_format = s->density_format;
+    sc.mask_format = s->mask_format;
     return sc;
 }
 static const Uniforms& U(const void* p) { return *(const Uniforms*)p; }

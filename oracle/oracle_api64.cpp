@@ -74,6 +74,7 @@ typedef struct vvo64_scene {
     const f32* env_table;
     int env_dims[2];
     int density_format;
+    int mask_format;
 } vvo64_scene;
 
 static Scene scene64(const vvo64_scene* s) {
@@ -92,6 +93,7 @@ static Scene scene64(const vvo64_scene* s) {
     sc.env_table = (const double*)(const void*)s->env_table;
     sc.env_dims = ivec2(s->env_dims[0], s->env_dims[1]);
     sc.density_format = s->density_format;
+    sc.mask_format = s->mask_format;
     return sc;
 }
 

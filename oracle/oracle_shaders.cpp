@@ -32,12 +32,17 @@ static void bind3(glsl::Texture& t, const void* data, glsl::Format f, ivec3 d, g
     t.address = glsl::CLAMP_TO_EDGE;
 }
 
+static glsl::Format mask_format_of(const Scene& s) {
+    static const glsl::Format formats[3] = {glsl::RG16_UNORM, glsl::RG16F, glsl::RG16_BF16};
+    return formats[s.mask_format >= 0 && s.mask_format < 3 ? s.mask_format : 0];
+}
+
 Units bind_scene(const Scene& s) {
     Units t;
     static const glsl::Format density_formats[4] = {glsl::R16_UNORM, glsl::R16F, glsl::R16_BF16, glsl::R32F};
     bind3(t.density, s.density, density_formats[s.density_format & 3], s.dims, glsl::LINEAR);
     if (s.normals) bind3(t.normals, s.normals, glsl::RGBA8_SNORM, s.dims, glsl::LINEAR);
-    if (s.mask) bind3(t.mask, s.mask, glsl::RG16_UNORM, s.dims, glsl::LINEAR);
+    if (s.mask) bind3(t.mask, s.mask, mask_format_of(s), s.dims, glsl::LINEAR);
     if (s.majorant) bind3(t.majorant, s.majorant, glsl::R32F, s.brick_dims, glsl::NEAREST);
     if (s.labels) bind3(t.labels, s.labels, glsl::R8_UINT, s.label_dims, glsl::NEAREST);
     if (s.tf_lut) bind3(t.tf, s.tf_lut, glsl::RGBA16F, ivec3(4096, 1, 1), glsl::LINEAR);
@@ -989,10 +994,11 @@ void mask_passes(const Uniforms& u, const Scene& sc, const uint8_t* soft_data, i
     ivec3 D = sc.dims;
     long rows = (long)D.y * D.z;
     auto lin = [&](ivec3 p) { return ((long)p.z * D.y + p.y) * D.x + p.x; };
+    const glsl::Format mf = mask_format_of(sc);  // the stored mask's format, in every pass
     parallel_rows(rows, threads, [&](long row) {
         int y = int(row % D.y), z = int(row / D.y);
         for (int x = 0; x < D.x; x++)
-            glsl::encode(scratch_b, glsl::RG16_UNORM, lin(ivec3(x, y, z)), vec4(mp.binary_masks(ivec3(x, y, z)), 0.0f, 0.0f));
+            glsl::encode(scratch_b, mf, lin(ivec3(x, y, z)), vec4(mp.binary_masks(ivec3(x, y, z)), 0.0f, 0.0f));
     });
     // Passes 1-3: blur along x (B -> A), y (A -> B), z (B -> A) (mask.comp:260-278).
     for (int pass = 1; pass <= 3; pass++) {
@@ -1008,12 +1014,12 @@ void mask_passes(const Uniforms& u, const Scene& sc, const uint8_t* soft_data, i
                 float c = 1.0f;
                 for (int j = 0; j <= 2 * radius; j++) {
                     ivec3 q = clamp(p + axis * (j - radius), ivec3(0), D - 1);
-                    vec4 v = glsl::decode(src, glsl::RG16_UNORM, lin(q));
+                    vec4 v = glsl::decode(src, mf, lin(q));
                     sum += c * vec2(v.x, v.y);
                     c = c * float(2 * radius - j) / float(j + 1);
                 }
                 sum /= exp2(float(2 * radius));
-                glsl::encode(dst, glsl::RG16_UNORM, lin(p), vec4(sum, 0.0f, 0.0f));
+                glsl::encode(dst, mf, lin(p), vec4(sum, 0.0f, 0.0f));
             }
         });
     }

@@ -72,6 +72,7 @@ def oracle_from_device(cfg, r):
     cpu.geo = O.geometry(cfg["volume"])
     cpu.density = r.read_volume(abi.VOLUME_DENSITY)
     cpu.density_format = r.precision.density_format
+    cpu.mask_format = r.precision.mask_format
     cpu.majorants = r.precision.majorants
     cpu.set_transfer_function(cfg["tf"])
     cpu.normals = r.read_volume(abi.VOLUME_NORMALS)

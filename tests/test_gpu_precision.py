@@ -1,11 +1,14 @@
 """The precision variant (GPU): density stored as FP16, BF16 or FP32 instead of
-R16_UNORM, and running sums with Kahan compensation or in FP64 past a sample
-count (vv_renderer_create_ex / vv_precision).
+R16_UNORM, the label mask as FP16 or BF16 beside density of the same format,
+and running sums with Kahan compensation or in FP64 past a sample count
+(vv_renderer_create_ex / vv_precision).
 
 Tolerances (written here, checked below):
 * stored density, normals and majorant: bit-exact against the oracle run on
   the same format (round-to-nearest-even encodings of the same normalised
   density t = clamp((hu + 1024) / 4095, 0, 1));
+* stored mask: every code within one step of the oracle's in the same format
+  (the bar of the RG16_UNORM mask), 99.9 % of them equal;
 * single-path replays: the bars of tests/parity_util.py, for the parity build
   of the probe and the product build, on each format;
 * running sums over 300 single-frame passes: with Kahan compensation, and with
@@ -25,6 +28,11 @@ from volview_gb300 import renderer as R
 pytestmark = pytest.mark.gpu
 
 FORMATS = [abi.DENSITY_FP16, abi.DENSITY_BF16, abi.DENSITY_FP32]
+# (density format, mask format): the density formats with the RG16_UNORM mask,
+# then FP16 / BF16 density with the mask in the same format.
+STORAGE = [(f, abi.MASK_UNORM16) for f in FORMATS] + [(abi.DENSITY_FP16, abi.MASK_FP16),
+                                                      (abi.DENSITY_BF16, abi.MASK_BF16)]
+STORAGE_IDS = ["fp16", "bf16", "fp32", "fp16-mask", "bf16-mask"]
 
 
 def _params(cfg, gpu):
@@ -33,12 +41,12 @@ def _params(cfg, gpu):
     return p
 
 
-@pytest.fixture(scope="module", params=FORMATS, ids=["fp16", "bf16", "fp32"])
+@pytest.fixture(scope="module", params=STORAGE, ids=STORAGE_IDS)
 def fmt_pair(request, small_cfg, gpu_ctx):
-    cfg, fmt = small_cfg, request.param
-    gpu = R.Renderer(gpu_ctx, cfg["volume"], cfg["tf"], abi.precision(density_format=fmt))
+    cfg, (fmt, mfmt) = small_cfg, request.param
+    gpu = R.Renderer(gpu_ctx, cfg["volume"], cfg["tf"], abi.precision(density_format=fmt, mask_format=mfmt))
     gpu.set_labels(cfg["labels_vol"], abi.soft_struct(cfg["soft"]))
-    cpu = O.CpuRenderer(cfg["volume"], cfg["tf"], cfg["hu"], density_format=fmt)
+    cpu = O.CpuRenderer(cfg["volume"], cfg["tf"], cfg["hu"], density_format=fmt, mask_format=mfmt)
     cpu.set_labels(cfg["labels_vol"], cfg["soft"])
     params = _params(cfg, gpu)
     gpu.resize(48, 48)
@@ -64,6 +72,23 @@ def test_normals_bit_exact(fmt_pair):
     assert np.array_equal(gpu.read_volume(abi.VOLUME_NORMALS), cpu.normals)
 
 
+def test_mask_in_storage_format(fmt_pair):
+    """The binary and blur passes (mask.comp) store the mask in the renderer's
+    mask format: codes within one step of the oracle's in that format (codes of
+    non-negative FP16 / BF16 values are monotone, like UNORM16 codes)."""
+    cfg, gpu, cpu, params = fmt_pair
+    gpu.probe_bspline(params, np.zeros((1, 3), np.float32))  # runs record's mask and majorant passes
+    ref = O.CpuRenderer(cfg["volume"], cfg["tf"], cfg["hu"], density_format=gpu.precision.density_format,
+                        mask_format=gpu.precision.mask_format)
+    ref.set_labels(cfg["labels_vol"], cfg["soft"])
+    ref.prepare(params, 48, 48)
+    got = gpu.read_volume(abi.VOLUME_MASK)
+    d = np.abs(got.astype(np.int32) - ref.mask.astype(np.int32))
+    assert d.max() <= 1
+    assert (d == 0).mean() >= 0.999
+    assert ((ref.mask != 0) & (ref.mask != ref.mask.max())).any()  # a blurred edge was compared
+
+
 def test_majorant_bit_exact(fmt_pair):
     """The majorant from the stored values (majorant.comp:26-71): min/max of the
     decoded densities, so it bounds every interpolated sample of the format."""
@@ -81,7 +106,8 @@ def test_majorant_bit_exact(fmt_pair):
 def test_single_path_replays(fmt_pair):
     cfg, gpu, cpu, params = fmt_pair
     adopt_device_inputs(gpu, cpu, params)
-    check_replays(gpu, cpu, params, all_pixels(48, 48), label=f"density format {gpu.precision.density_format}")
+    check_replays(gpu, cpu, params, all_pixels(48, 48),
+                  label=f"density format {gpu.precision.density_format}, mask {gpu.precision.mask_format}")
 
 
 def test_bspline_matches_oracle(fmt_pair):
@@ -132,21 +158,24 @@ def test_running_sums(small_cfg, gpu_ctx):
 
 def test_create_rejects_unknown_precision(small_cfg, gpu_ctx):
     cfg = small_cfg
-    for bad in (abi.precision(density_format=7), abi.precision(sums=5)):
+    for bad in (abi.precision(density_format=7), abi.precision(sums=5), abi.precision(mask_format=3),
+                abi.precision(mask_format=abi.MASK_FP16),
+                abi.precision(density_format=abi.DENSITY_FP16, mask_format=abi.MASK_BF16),
+                abi.precision(density_format=abi.DENSITY_FP32, mask_format=abi.MASK_BF16)):
         with pytest.raises(R.VolptError) as e:
             R.Renderer(gpu_ctx, cfg["volume"], cfg["tf"], bad)
         assert e.value.status == abi.VV_ERR_ARG
 
 
-@pytest.mark.parametrize("fmt", FORMATS, ids=["fp16", "bf16", "fp32"])
-def test_ray_marcher_and_light_map_on_each_format(small_cfg, gpu_ctx, fmt):
+@pytest.mark.parametrize("fmt,mfmt", STORAGE, ids=STORAGE_IDS)
+def test_ray_marcher_and_light_map_on_each_format(small_cfg, gpu_ctx, fmt, mfmt):
     """The ray marcher (path tracing off) and light-map path tracing read the
     stored density through their format's samplers: images close to the
     R16_UNORM renderer's (mean radiance within 2 %, 99 % of the ray marcher's
     pixels within 2e-2 + 5 % of its values)."""
     cfg = small_cfg
     out = {}
-    for key, precision in (("unorm", None), ("fmt", abi.precision(density_format=fmt))):
+    for key, precision in (("unorm", None), ("fmt", abi.precision(density_format=fmt, mask_format=mfmt))):
         r = R.Renderer(gpu_ctx, cfg["volume"], cfg["tf"], precision)
         r.set_labels(cfg["labels_vol"], abi.soft_struct(cfg["soft"]))
         r.set_environment_map(abi.env_struct(scene.synthetic_light_map()))

@@ -179,6 +179,31 @@ def test_density_formats():
     assert np.array_equal(O.density_encode(hu), O.hu_to_unorm16(hu))
 
 
+def test_mask_formats(small_cfg):
+    """The label mask stored as two binary16 / bfloat16 channels: each stored
+    value is the format's round-to-nearest-even encoding (monotone codes), and
+    the decoded mask stays within the format's rounding, compounded over the
+    binary pass and three blur passes, of the RG16_UNORM mask."""
+    from volview_gb300 import scene
+    cfg = small_cfg
+    masks = {}
+    for dfmt, mfmt in ((O.DENSITY_UNORM16, O.MASK_UNORM16), (O.DENSITY_FP16, O.MASK_FP16),
+                       (O.DENSITY_BF16, O.MASK_BF16)):
+        cpu = O.CpuRenderer(cfg["volume"], cfg["tf"], cfg["hu"], density_format=dfmt, mask_format=mfmt)
+        cpu.set_labels(cfg["labels_vol"], cfg["soft"])
+        p = scene.frame_params_for(cfg, [0.0, 0.0, 0.0], 100.0)
+        cpu.prepare(p, 16, 16)
+        masks[mfmt] = cpu.mask
+    ref = masks[O.MASK_UNORM16].astype(np.float64) / 65535.0
+    half = masks[O.MASK_FP16].view(np.float16).astype(np.float64)
+    bf = (masks[O.MASK_BF16].astype(np.uint32) << 16).view(np.float32).astype(np.float64)
+    for got, bits in ((half, 11), (bf, 8)):
+        assert got.min() >= 0.0 and got.max() <= 1.0
+        assert np.all(np.abs(got - ref) <= 4 * 2.0 ** -bits * ref + 2.0 / 65535)
+    assert np.array_equal(half.astype(np.float16).view(np.uint16), masks[O.MASK_FP16])
+    assert (ref > 0).sum() > 0 and ((ref > 0) & (ref < 1)).sum() > 0  # a blurred edge to compare on
+
+
 def test_light_map_samples_follow_luminance(small_cfg):
     """The oracle's light map samples (pt.comp:204-233) land on texels in
     proportion to luminance x sin(theta), with the pdf of the texel they land on."""

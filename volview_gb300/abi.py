@@ -22,17 +22,19 @@ VOLUME_DENSITY, VOLUME_NORMALS, VOLUME_MASK, VOLUME_LABELS, VOLUME_MAJORANT, VOL
 DENSITY_UNORM16, DENSITY_FP16, DENSITY_BF16, DENSITY_FP32 = range(4)
 SUMS_FP32, SUMS_KAHAN = range(2)
 MAJORANTS_REFERENCE, MAJORANTS_BOUND = range(2)
+MASK_UNORM16, MASK_FP16, MASK_BF16 = range(3)
 
 
 class Precision(C.Structure):
     """vv_precision: density storage format, running-sum mode, FP64 threshold,
-    bucket maxima of the majorants."""
+    bucket maxima of the majorants, label-mask storage format."""
     _fields_ = [("density_format", C.c_uint32), ("sums", C.c_uint32), ("fp64_after", C.c_uint32),
-                ("majorants", C.c_uint32)]
+                ("majorants", C.c_uint32), ("mask_format", C.c_uint32)]
 
 
-def precision(density_format=DENSITY_UNORM16, sums=SUMS_FP32, fp64_after=0, majorants=MAJORANTS_REFERENCE):
-    return Precision(density_format, sums, fp64_after, majorants)
+def precision(density_format=DENSITY_UNORM16, sums=SUMS_FP32, fp64_after=0, majorants=MAJORANTS_REFERENCE,
+              mask_format=MASK_UNORM16):
+    return Precision(density_format, sums, fp64_after, majorants, mask_format)
 
 F4x256 = (C.c_float * 4) * VV_LABEL_COUNT
 

@@ -15,11 +15,11 @@ LIB = os.path.join(HERE, "libvolpt.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 SOURCES = ["vv_volume.cu", "vv_pt.cu", "vv_pt_exact.cu", "vv_wavefront.cu", "vv_raymarch.cu", "vv_post.cu",
            "vv_noalloc.cu", "vv_nn.cu", "vv_nn_tc.cu", "vv_host.cpp"]
-# Compiled once per density storage format (VV_DFMT = 0..3: R16_UNORM, FP16,
-# BF16, FP32), each into its own namespace, so each format's samplers are
-# specialised for it.
+# Compiled once per storage format (VV_DFMT = 0..3: R16_UNORM, FP16, BF16,
+# FP32 density with the RG16_UNORM mask; 4, 5: FP16 / BF16 density and mask),
+# each into its own namespace, so each format's samplers are specialised for it.
 PER_FORMAT = {"vv_pt.cu", "vv_pt_exact.cu", "vv_wavefront.cu", "vv_raymarch.cu"}
-FORMATS = 4
+FORMATS = 6
 # The parity build of the path probe: the oracle's texture-unit arithmetic and
 # no multiply-add contraction (every product and sum rounded on its own).
 UNIT_FLAGS = {"vv_pt_exact.cu": ["-DVV_EXACT=1", "--fmad=false"]}

@@ -101,12 +101,16 @@ struct Vol {
     int bx, by, bz;     // bricks per axis
     int sy, sz;         // element strides of a brick row / brick slab
     int dfmt;           // storage format of the density volume (DF_*)
+    int mfmt;           // storage format of the label mask volume's two channels (MF_*)
 };
 
 // Density storage formats (vv_precision::density_format): the reference's
 // R16_UNORM, or the density itself as FP16, BF16 or FP32.
 enum { DF_UNORM16 = 0, DF_FP16 = 1, DF_BF16 = 2, DF_FP32 = 3 };
 __host__ __device__ __forceinline__ int density_bytes(int dfmt) { return dfmt == DF_FP32 ? 4 : 2; }
+// Label mask storage formats (vv_precision::mask_format): two 16-bit channels
+// per voxel as the reference's RG16_UNORM, or as FP16 or BF16 values.
+enum { MF_UNORM16 = 0, MF_FP16 = 1, MF_BF16 = 2 };
 
 __host__ __device__ __forceinline__ Vol make_vol(int nx, int ny, int nz) {
     Vol v;
@@ -115,6 +119,7 @@ __host__ __device__ __forceinline__ Vol make_vol(int nx, int ny, int nz) {
     v.sy = v.bx * 512;
     v.sz = v.bx * v.by * 512;
     v.dfmt = DF_UNORM16;
+    v.mfmt = MF_UNORM16;
     return v;
 }
 __host__ __device__ __forceinline__ long vol_elems(const Vol& v) { return (long)v.bx * v.by * v.bz * 512; }
@@ -135,6 +140,25 @@ __host__ __device__ __forceinline__ void vcoord(const Vol& v, long e, int& x, in
 __device__ __forceinline__ int clampi(int v, int lo, int hi) { return v < lo ? lo : (v > hi ? hi : v); }
 
 __device__ __forceinline__ float unorm16(uint32_t u) { return (float)u / 65535.0f; }
+
+#ifdef __CUDACC__
+// One 16-bit mask channel: decode to a float, and the store's conversion
+// (UNORM16: clamp, scale, round to nearest even; FP16 and BF16: round to
+// nearest even).
+__device__ __forceinline__ float mask_decode(uint32_t code, int mfmt) {
+    if (mfmt == MF_FP16) return __half2float(__ushort_as_half((unsigned short)code));
+    if (mfmt == MF_BF16) return __uint_as_float(code << 16);
+    return unorm16(code);
+}
+__device__ __forceinline__ uint32_t mask_encode(float f, int mfmt) {
+    if (mfmt == MF_FP16) return __half_as_ushort(__float2half_rn(f));
+    if (mfmt == MF_BF16) {
+        uint32_t w = __float_as_uint(f);
+        return (w + 0x7fffu + ((w >> 16) & 1u)) >> 16;
+    }
+    return (uint32_t)rintf(__fmul_rn(fminf(fmaxf(f, 0.0f), 1.0f), 65535.0f));
+}
+#endif
 
 #ifdef __CUDACC__
 // A density element stored as F (its C type: 16 bits, or a float for FP32),

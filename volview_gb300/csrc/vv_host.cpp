@@ -307,9 +307,17 @@ struct FormatLaunchers {
     {ns::launch_pt, ns::launch_pt_wavefront, ns::launch_ao, ns::launch_shadow_sweep, ns::launch_pad_lighting, \
      ns::launch_dvr, ns::launch_bspline_probe, ns::launch_light_sample_probe, ns::launch_pt_pixels,          \
      ns::launch_extinction_probe}
-static const FormatLaunchers FORMAT_LAUNCHERS[4] = {VV_FORMAT_TABLE(fmt0), VV_FORMAT_TABLE(fmt1),
-                                                    VV_FORMAT_TABLE(fmt2), VV_FORMAT_TABLE(fmt3)};
-static const FormatLaunchers& kernels_of(const vv_renderer* r) { return FORMAT_LAUNCHERS[r->vol.dfmt & 3]; }
+static const FormatLaunchers FORMAT_LAUNCHERS[6] = {VV_FORMAT_TABLE(fmt0), VV_FORMAT_TABLE(fmt1),
+                                                    VV_FORMAT_TABLE(fmt2), VV_FORMAT_TABLE(fmt3),
+                                                    VV_FORMAT_TABLE(fmt4), VV_FORMAT_TABLE(fmt5)};
+// The build of the renderer's storage: the density format's, or 4 / 5 for
+// FP16 / BF16 density with the mask in the same format.
+static int build_of(const Vol& v) {
+    if (v.mfmt == MF_FP16) return 4;
+    if (v.mfmt == MF_BF16) return 5;
+    return v.dfmt & 3;
+}
+static const FormatLaunchers& kernels_of(const vv_renderer* r) { return FORMAT_LAUNCHERS[build_of(r->vol)]; }
 
 static void free_tex_vol(vv_renderer::TexVol& t) {
     if (t.tex) cudaDestroyTextureObject(t.tex);
@@ -655,7 +663,7 @@ static m3 w2i_m3(const vv_renderer* r) {
 
 extern "C" vv_status vv_renderer_create(vv_context* ctx, const vv_volume* volume, const vv_transfer_function* tf,
                                         vv_renderer** out) {
-    vv_precision p = {VV_DENSITY_UNORM16, VV_SUMS_FP32, 0, VV_MAJORANTS_REFERENCE};
+    vv_precision p = {VV_DENSITY_UNORM16, VV_SUMS_FP32, 0, VV_MAJORANTS_REFERENCE, VV_MASK_UNORM16};
     return vv_renderer_create_ex(ctx, volume, tf, &p, out);
 }
 
@@ -665,6 +673,10 @@ extern "C" vv_status vv_renderer_create_ex(vv_context* ctx, const vv_volume* vol
     if (precision->density_format > VV_DENSITY_FP32) return fail(VV_ERR_ARG, "unknown density format");
     if (precision->sums > VV_SUMS_KAHAN) return fail(VV_ERR_ARG, "unknown running-sum mode");
     if (precision->majorants > VV_MAJORANTS_BOUND) return fail(VV_ERR_ARG, "unknown majorant mode");
+    if (precision->mask_format > VV_MASK_BF16) return fail(VV_ERR_ARG, "unknown mask format");
+    if ((precision->mask_format == VV_MASK_FP16 && precision->density_format != VV_DENSITY_FP16) ||
+        (precision->mask_format == VV_MASK_BF16 && precision->density_format != VV_DENSITY_BF16))
+        return fail(VV_ERR_ARG, "an FP16 / BF16 mask needs the density in the same format");
     if (!volume->hu) return fail(VV_ERR_ARG, "volume has no voxels");
     for (int i = 0; i < 3; i++)
         if (volume->dims[i] == 0) return fail(VV_ERR_ARG, "volume has a zero dimension");
@@ -674,6 +686,8 @@ extern "C" vv_status vv_renderer_create_ex(vv_context* ctx, const vv_volume* vol
         return fail(VV_ERR_LIMIT, "volume exceeds 2^31 bricked voxels or 16384 per axis");
     CK(cudaSetDevice(ctx->device));
     v.dfmt = (int)precision->density_format;
+    v.mfmt = precision->mask_format == VV_MASK_FP16 ? MF_FP16 : precision->mask_format == VV_MASK_BF16 ? MF_BF16
+                                                                                                      : MF_UNORM16;
     vv_renderer* r = new vv_renderer();
     r->ctx = ctx;
     r->vol = v;
@@ -1999,8 +2013,9 @@ extern "C" vv_status vv_probe_light_samples(vv_renderer* r, const vv_frame_param
     return VV_OK;
 }
 
-static decltype(&exact0::launch_pt_pixels) const EXACT_PT_PIXELS[4] = {
-    exact0::launch_pt_pixels, exact1::launch_pt_pixels, exact2::launch_pt_pixels, exact3::launch_pt_pixels};
+static decltype(&exact0::launch_pt_pixels) const EXACT_PT_PIXELS[6] = {
+    exact0::launch_pt_pixels, exact1::launch_pt_pixels, exact2::launch_pt_pixels, exact3::launch_pt_pixels,
+    exact4::launch_pt_pixels, exact5::launch_pt_pixels};
 
 static vv_status probe_paths(vv_renderer* r, const vv_frame_params* params, uint32_t accumulated, const int* pixels,
                              size_t n, float* out, bool exact) {
@@ -2018,7 +2033,7 @@ static vv_status probe_paths(vv_renderer* r, const vv_frame_params* params, uint
     PtArgs a = pt_args(r, u);
     cudaError_t e = cudaMemcpyAsync(dp.p, pixels, n * 8, cudaMemcpyHostToDevice, st);
     if (e == cudaSuccess)
-        e = (exact ? EXACT_PT_PIXELS[r->vol.dfmt & 3] : kernels_of(r).pt_pixels)(a, dp.as<int>(), dout.as<float>(),
+        e = (exact ? EXACT_PT_PIXELS[build_of(r->vol)] : kernels_of(r).pt_pixels)(a, dp.as<int>(), dout.as<float>(),
                                                                                (int)n, st);
     if (e == cudaSuccess) e = cudaMemcpyAsync(out, dout.p, n * 48, cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);

@@ -136,9 +136,10 @@ struct LightTex {
 };
 
 // The launchers of the path tracer and the ray marcher (vv_pt.cu,
-// vv_wavefront.cu, vv_raymarch.cu), compiled once per density storage format:
-// namespace vv::fmtN holds those of format N (DF_*), whose samplers read that
-// format with no branch on it.
+// vv_wavefront.cu, vv_raymarch.cu), compiled once per storage format:
+// namespace vv::fmtN holds those of density format N (DF_*, N < 4) with the
+// RG16_UNORM mask, fmt4 and fmt5 those of FP16 and BF16 density with the mask
+// in the same format; each build's samplers read its formats with no branch.
 #define VV_FORMAT_LAUNCHERS                                                                                      \
     /* One or more accumulate-frames (pt.comp) with the single-kernel tracers. */                                \
     cudaError_t launch_pt(const PtArgs& a, int sms, cudaStream_t s, int* launches);                             \
@@ -167,6 +168,8 @@ namespace fmt0 { VV_FORMAT_LAUNCHERS }
 namespace fmt1 { VV_FORMAT_LAUNCHERS }
 namespace fmt2 { VV_FORMAT_LAUNCHERS }
 namespace fmt3 { VV_FORMAT_LAUNCHERS }
+namespace fmt4 { VV_FORMAT_LAUNCHERS }  // FP16 density and FP16 mask
+namespace fmt5 { VV_FORMAT_LAUNCHERS }  // BF16 density and BF16 mask
 // The parity build of the single-path probe (vv_pt_exact.cu), per format: the
 // oracle's texture-unit arithmetic, no fused multiply-adds.
 #define VV_EXACT_LAUNCHERS \
@@ -175,6 +178,8 @@ namespace exact0 { VV_EXACT_LAUNCHERS }
 namespace exact1 { VV_EXACT_LAUNCHERS }
 namespace exact2 { VV_EXACT_LAUNCHERS }
 namespace exact3 { VV_EXACT_LAUNCHERS }
+namespace exact4 { VV_EXACT_LAUNCHERS }
+namespace exact5 { VV_EXACT_LAUNCHERS }
 
 struct PostArgs {
     UHead u;

@@ -9,10 +9,24 @@
 
 // The density storage format this translation unit's samplers read (DF_*):
 // the path tracer's and ray marcher's sources are compiled once per format,
-// each into its own namespace (vv::fmt0 .. vv::fmt3), so every format runs
+// each into its own namespace (vv::fmt0 .. vv::fmt5), so every format runs
 // code specialised for it and the reference's format has no format branch.
 #ifndef VV_DFMT
 #define VV_DFMT 0
+#endif
+// Builds 4 and 5 store the label mask in the density's format too: FP16
+// density and mask, BF16 density and mask (vv_precision::mask_format). The
+// others keep the reference's RG16_UNORM mask. VV_DENS is the density format
+// the samplers read, VV_MASKF the mask format (MF_*).
+#if VV_DFMT == 4
+#define VV_DENS 1
+#define VV_MASKF 1
+#elif VV_DFMT == 5
+#define VV_DENS 2
+#define VV_MASKF 2
+#else
+#define VV_DENS VV_DFMT
+#define VV_MASKF 0
 #endif
 // VV_EXACT = 1: the parity build of the path probe (namespace vv::exactN,
 // compiled with --fmad=false). Its samplers take the texture-unit model of the
@@ -132,9 +146,9 @@ __device__ __forceinline__ float tri_sum_exact(const float c[8], const TriX& t) 
 // A density texel as the sampler decodes it: R16_UNORM code / 65535, the
 // other formats their value.
 __device__ __forceinline__ float density_texel_exact(const void* d, int o) {
-    typedef DensityStore<VV_DFMT>::type E;
-    float x = density_decode<VV_DFMT>(__ldg((const E*)d + o));
-    return VV_DFMT == DF_UNORM16 ? x / 65535.0f : x;
+    typedef DensityStore<VV_DENS>::type E;
+    float x = density_decode<VV_DENS>(__ldg((const E*)d + o));
+    return VV_DENS == DF_UNORM16 ? x / 65535.0f : x;
 }
 __device__ __forceinline__ float density_at_index_exact(const PtArgs& A, f3 p) {
     TriX t = tri_taps_exact(A, p);
@@ -179,18 +193,18 @@ __device__ __forceinline__ float cubic_fetch_exact(const PtArgs& A, f3 h0, f3 h1
 #endif
 
 // textureLod(density_tex, index_to_tex(idx)) (common.glsl:76-78), the density
-// stored as this translation unit's format (VV_DFMT).
+// stored as this translation unit's format (VV_DENS).
 __device__ float density_tri(const PtArgs& A, f3 p) {
     count(A, COUNT_TRILINEAR);
 #if VV_EXACT
     return density_at_index_exact(A, p);
 #else
-    typedef DensityStore<VV_DFMT>::type E;
+    typedef DensityStore<VV_DENS>::type E;
     Tri t = tri_taps(A.vol, p);
     float c[8];
 #pragma unroll
-    for (int k = 0; k < 8; k++) c[k] = density_decode<VV_DFMT>(__ldg((const E*)A.density + t.o[k]));
-    return tri_mix(c, t) * density_unit<VV_DFMT>();
+    for (int k = 0; k < 8; k++) c[k] = density_decode<VV_DENS>(__ldg((const E*)A.density + t.o[k]));
+    return tri_mix(c, t) * density_unit<VV_DENS>();
 #endif
 }
 
@@ -203,8 +217,8 @@ __device__ float2 mask_tri(const PtArgs& A, f3 p) {
 #pragma unroll
     for (int k = 0; k < 8; k++) {
         uint32_t m = __ldg(A.mask + x.o[k]);
-        er[k] = (float)(m & 0xffffu) / 65535.0f;
-        eg[k] = (float)(m >> 16) / 65535.0f;
+        er[k] = VV_MASKF == MF_UNORM16 ? (float)(m & 0xffffu) / 65535.0f : mask_decode(m & 0xffffu, VV_MASKF);
+        eg[k] = VV_MASKF == MF_UNORM16 ? (float)(m >> 16) / 65535.0f : mask_decode(m >> 16, VV_MASKF);
     }
     return make_float2(tri_sum_exact(er, x), tri_sum_exact(eg, x));
 #endif
@@ -213,10 +227,12 @@ __device__ float2 mask_tri(const PtArgs& A, f3 p) {
 #pragma unroll
     for (int k = 0; k < 8; k++) {
         uint32_t m = __ldg(A.mask + t.o[k]);
-        r[k] = (float)(m & 0xffffu);
-        g[k] = (float)(m >> 16);
+        // UNORM16 codes are filtered as integers, then scaled; FP16/BF16 as values.
+        r[k] = VV_MASKF == MF_UNORM16 ? (float)(m & 0xffffu) : mask_decode(m & 0xffffu, VV_MASKF);
+        g[k] = VV_MASKF == MF_UNORM16 ? (float)(m >> 16) : mask_decode(m >> 16, VV_MASKF);
     }
-    return make_float2(tri_mix(r, t) * INV65535, tri_mix(g, t) * INV65535);
+    const float unit = VV_MASKF == MF_UNORM16 ? INV65535 : 1.0f;
+    return make_float2(tri_mix(r, t) * unit, tri_mix(g, t) * unit);
 }
 __device__ float mask_tri_ch(const PtArgs& A, f3 p, int ch) {
     count(A, COUNT_MASK);
@@ -226,7 +242,8 @@ __device__ float mask_tri_ch(const PtArgs& A, f3 p, int ch) {
 #pragma unroll
     for (int k = 0; k < 8; k++) {
         uint32_t m = __ldg(A.mask + x.o[k]);
-        c[k] = (float)(ch == 0 ? (m & 0xffffu) : (m >> 16)) / 65535.0f;
+        uint32_t code = ch == 0 ? (m & 0xffffu) : (m >> 16);
+        c[k] = VV_MASKF == MF_UNORM16 ? (float)code / 65535.0f : mask_decode(code, VV_MASKF);
     }
     return tri_sum_exact(c, x);
 #endif
@@ -235,9 +252,10 @@ __device__ float mask_tri_ch(const PtArgs& A, f3 p, int ch) {
 #pragma unroll
     for (int k = 0; k < 8; k++) {
         uint32_t m = __ldg(A.mask + t.o[k]);
-        r[k] = (float)(ch == 0 ? (m & 0xffffu) : (m >> 16));
+        uint32_t code = ch == 0 ? (m & 0xffffu) : (m >> 16);
+        r[k] = VV_MASKF == MF_UNORM16 ? (float)code : mask_decode(code, VV_MASKF);
     }
-    return tri_mix(r, t) * INV65535;
+    return tri_mix(r, t) * (VV_MASKF == MF_UNORM16 ? INV65535 : 1.0f);
 }
 
 // textureLod(normal_tex, ...): RGBA8_SNORM. The volume holds no -128, so the
@@ -308,7 +326,7 @@ __device__ __noinline__ float density_cubic(const PtArgs& A, f3 p) {
     AxisTaps x = cubic_axis_exact(p.x), y = cubic_axis_exact(p.y), z = cubic_axis_exact(p.z);
     return cubic_fetch_exact(A, mk(x.h0, y.h0, z.h0), mk(x.h1, y.h1, z.h1), mk(x.g0, y.g0, z.g0), mk(x.g1, y.g1, z.g1));
 #endif
-    typedef DensityStore<VV_DFMT>::type E;
+    typedef DensityStore<VV_DENS>::type E;
     Cubic c = cubic_taps(A.vol, p);
     float wx[4], wy[4], wz[4];
     bspline_w(c.fx, wx);
@@ -324,22 +342,22 @@ __device__ __noinline__ float density_cubic(const PtArgs& A, f3 p) {
 #pragma unroll 1
         for (int y = 0; y < 4; y++) {
             const E* row = (const E*)A.density + c.oz[z] + c.oy[y];
-            float r = wx[0] * density_decode<VV_DFMT>(__ldg(row + c.ox[0])) +
-                      wx[1] * density_decode<VV_DFMT>(__ldg(row + c.ox[1])) +
-                      wx[2] * density_decode<VV_DFMT>(__ldg(row + c.ox[2])) +
-                      wx[3] * density_decode<VV_DFMT>(__ldg(row + c.ox[3]));
+            float r = wx[0] * density_decode<VV_DENS>(__ldg(row + c.ox[0])) +
+                      wx[1] * density_decode<VV_DENS>(__ldg(row + c.ox[1])) +
+                      wx[2] * density_decode<VV_DENS>(__ldg(row + c.ox[2])) +
+                      wx[3] * density_decode<VV_DENS>(__ldg(row + c.ox[3]));
             az = fmaf(wy[y], r, az);
         }
         acc = fmaf(wz[z], az, acc);
     }
-    return acc * density_unit<VV_DFMT>();
+    return acc * density_unit<VV_DENS>();
 }
 
 // density_gradient_cubic (common.glsl:130-136) from the same 64 voxels; with
 // VALUE, also density_cubic's value, with its arithmetic (the value's z-slices
 // are the gradient's vz sums), from the same read.
 template <bool VALUE> __device__ __forceinline__ f3 density_gradient_cubic_impl(const PtArgs& A, f3 p, float& value) {
-    typedef DensityStore<VV_DFMT>::type E;
+    typedef DensityStore<VV_DENS>::type E;
     Cubic c = cubic_taps(A.vol, p);
     float wx[4], wy[4], wz[4], dx[4], dy[4], dz[4];
     bspline_w(c.fx, wx); bspline_w(c.fy, wy); bspline_w(c.fz, wz);
@@ -354,8 +372,8 @@ template <bool VALUE> __device__ __forceinline__ f3 density_gradient_cubic_impl(
 #pragma unroll
         for (int y = 0; y < 4; y++) {
             const E* row = (const E*)A.density + c.oz[z] + c.oy[y];
-            float v0 = density_decode<VV_DFMT>(__ldg(row + c.ox[0])), v1 = density_decode<VV_DFMT>(__ldg(row + c.ox[1]));
-            float v2 = density_decode<VV_DFMT>(__ldg(row + c.ox[2])), v3 = density_decode<VV_DFMT>(__ldg(row + c.ox[3]));
+            float v0 = density_decode<VV_DENS>(__ldg(row + c.ox[0])), v1 = density_decode<VV_DENS>(__ldg(row + c.ox[1]));
+            float v2 = density_decode<VV_DENS>(__ldg(row + c.ox[2])), v3 = density_decode<VV_DENS>(__ldg(row + c.ox[3]));
             float rw = wx[0] * v0 + wx[1] * v1 + wx[2] * v2 + wx[3] * v3;
             float rd = dx[0] * v0 + dx[1] * v1 + dx[2] * v2 + dx[3] * v3;
             vz = fmaf(wy[y], rw, vz);
@@ -367,8 +385,8 @@ template <bool VALUE> __device__ __forceinline__ f3 density_gradient_cubic_impl(
         gy = fmaf(wz[z], gyz, gy);
         gz = fmaf(dz[z], vz, gz);
     }
-    if (VALUE) value = acc * density_unit<VV_DFMT>();
-    return mk(gx, gy, gz) * density_unit<VV_DFMT>();
+    if (VALUE) value = acc * density_unit<VV_DENS>();
+    return mk(gx, gy, gz) * density_unit<VV_DENS>();
 }
 __device__ __noinline__ f3 density_gradient_cubic(const PtArgs& A, f3 p) {
     count(A, COUNT_GRADIENT);

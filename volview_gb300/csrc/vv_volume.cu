@@ -186,10 +186,6 @@ __device__ void soft_masks(const MaskArgs& A, int px, int py, int pz, const floa
     mg = fminf(fmaxf(__fadd_rn(0.5f, __fdiv_rn(b, 2.0f * CERTAIN)), 0.0f), 1.0f);
 }
 
-__device__ __forceinline__ uint16_t to_unorm16(float f) {
-    return (uint16_t)rintf(__fmul_rn(fminf(fmaxf(f, 0.0f), 1.0f), 65535.0f));
-}
-
 // mask.comp:107-138 (pass 0): binary or soft masks, and the tint-mode cut margin.
 __global__ void k_mask_binary(MaskArgs A, uint32_t* __restrict__ out) {
     long e = (long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -232,7 +228,7 @@ __global__ void k_mask_binary(MaskArgs A, uint32_t* __restrict__ out) {
                     }
                 }
     }
-    out[e] = (uint32_t)to_unorm16(mr) | ((uint32_t)to_unorm16(mg) << 16);
+    out[e] = mask_encode(mr, A.v.mfmt) | (mask_encode(mg, A.v.mfmt) << 16);
 }
 
 // mask.comp:260-278 (passes 1-3): binomial blur of radius r along one axis.
@@ -250,14 +246,14 @@ __global__ void k_mask_blur(const uint32_t* __restrict__ src, uint32_t* __restri
         q[1] = clampi(q[1], 0, v.ny - 1);
         q[2] = clampi(q[2], 0, v.nz - 1);
         uint32_t m = __ldg(src + voff(v, q[0], q[1], q[2]));
-        sx = __fadd_rn(sx, __fmul_rn(c, unorm16(m & 0xffffu)));
-        sy = __fadd_rn(sy, __fmul_rn(c, unorm16(m >> 16)));
+        sx = __fadd_rn(sx, __fmul_rn(c, mask_decode(m & 0xffffu, v.mfmt)));
+        sy = __fadd_rn(sy, __fmul_rn(c, mask_decode(m >> 16, v.mfmt)));
         c = __fdiv_rn(__fmul_rn(c, (float)(2 * r - j)), (float)(j + 1));
     }
     float n = exp2f((float)(2 * r));
     sx = __fdiv_rn(sx, n);
     sy = __fdiv_rn(sy, n);
-    dst[e] = (uint32_t)to_unorm16(sx) | ((uint32_t)to_unorm16(sy) << 16);
+    dst[e] = mask_encode(sx, v.mfmt) | (mask_encode(sy, v.mfmt) << 16);
 }
 
 // majorant.comp:26-71: one thread per brick over the brick and two voxels of border.
@@ -281,7 +277,7 @@ __global__ void k_majorant(const void* __restrict__ d, const uint32_t* __restric
                 dmax = gmax(dmax, dv);
                 if (mode != 0) {
                     uint32_t m = __ldg(mask + o);
-                    mmax = gmax(mmax, gmax(unorm16(m & 0xffffu), unorm16(m >> 16)));
+                    mmax = gmax(mmax, gmax(mask_decode(m & 0xffffu, v.mfmt), mask_decode(m >> 16, v.mfmt)));
                 }
             }
         }

@@ -686,6 +686,7 @@ def run_serve(args):
                                      "at %.0f/s" % (SERVE_DIMS, SERVE_SIZES, SERVE_SPP, args.serve_rate),
                          "requests": args.serve, "budget_bytes": budget, "phantom_generation_s": gen_s}}
     modes = (("continuous_shortest_first", dict(order="shortest", aging_s=2.0, max_per_volume=1)),
+             ("batched_shortest_first", dict(batched=True, order="shortest", aging_s=2.0, frames_per_pass=16)),
              ("continuous_shortest_first_lean", dict(order="shortest", aging_s=2.0, max_per_volume=1, passes=2,
                                                      slot_frames=8)),
              ("continuous_fifo", dict(order="fifo", max_per_volume=1)),
@@ -693,12 +694,21 @@ def run_serve(args):
     if args.serve_modes:
         modes = tuple(m for m in modes if m[0] in args.serve_modes.split(","))
     for mode, kw in modes:
-        make, base = S.renderer_factory(volumes)
-        srv = S.Server(make, base, budget, **kw)
-        for name in volumes:
-            srv.preload(name)  # resident before the requests come
-        for r in list(srv.owned):
-            r.synchronize()
+        kw = dict(kw)
+        if kw.pop("batched", False):
+            # One resident copy of each volume, a view per concurrent request,
+            # batched passes of up to 8 requests of a volume (vv_batch_record).
+            make_base, make_view, engine, base, view, reserve = S.batched_factory(volumes, passes=2)
+            srv = S.BatchedServer(make_base, make_view, engine, budget, base, view, reserve, **kw)
+            for name in volumes:
+                srv.preload(name).synchronize()
+        else:
+            make, base = S.renderer_factory(volumes)
+            srv = S.Server(make, base, budget, **kw)
+            for name in volumes:
+                srv.preload(name)  # resident before the requests come
+            for r in list(srv.owned):
+                r.synchronize()
         reqs = [copy.copy(q) for q in serve_requests(volumes, args.serve, args.serve_rate)]
         with Clocks(0) as clocks:
             t0 = time.perf_counter()
@@ -707,6 +717,10 @@ def run_serve(args):
         stats = S.summary(done, wall)
         stats.update({"renderers_created": srv.created, "peak_device_bytes": srv.peak_bytes,
                       "clocks": clocks.summary()})
+        if isinstance(srv, S.BatchedServer):
+            stats.update({"batched_passes": srv.passes,
+                          "mean_requests_per_pass": float(np.mean(srv.batch_sizes)) if srv.batch_sizes else 0.0,
+                          "engine_device_bytes": srv.engine.device_bytes()})
         result[mode] = stats
         srv.close()
     first = "continuous_shortest_first" if "continuous_shortest_first" in result else modes[0][0]

@@ -43,6 +43,7 @@ typedef enum vv_status {
 
 typedef struct vv_context vv_context;
 typedef struct vv_renderer vv_renderer;
+typedef struct vv_batch vv_batch;
 
 /* ------------------------------------------------------------------ inputs */
 
@@ -285,8 +286,18 @@ typedef struct vv_precision {
  * for several frames per pass), then merged into the running sums. */
 vv_status vv_renderer_create_ex(vv_context* ctx, const vv_volume* volume, const vv_transfer_function* tf,
                                 const vv_precision* precision, vv_renderer** out);
-/* Renderer::destroy (renderer.rs:2072). */
+/* Renderer::destroy (renderer.rs:2072). VV_ERR_STATE (nothing freed) while
+ * views of the renderer's volume exist. */
 vv_status vv_renderer_destroy(vv_renderer* r);
+/* A view of `base`'s volume: a renderer on context `ctx` (same device) that
+ * reads base's device volumes (density, normals, labels, soft label grid),
+ * transfer function and light map instead of holding copies, with label
+ * masks, majorants, images and path-tracing passes of its own. An extension
+ * beyond the reference, for serving several views of one resident volume at
+ * once. A view of a view is a view of its base. While views exist the base's
+ * vv_set_transfer_function, vv_set_labels, vv_set_environment_map and
+ * vv_renderer_destroy return VV_ERR_STATE, as do those calls on a view. */
+vv_status vv_renderer_create_view(vv_context* ctx, vv_renderer* base, vv_renderer** out);
 /* The renderer's public fields bounds, min_spacing, center and diagonal
  * (renderer.rs:545-551), and the volume's dimensions. */
 vv_status vv_renderer_get_info(const vv_renderer* r, vv_renderer_info* out);
@@ -394,6 +405,46 @@ vv_status vv_reset_view(vv_renderer* r);
  * between them. Waits for the renderer's work and frees the state of the
  * passes it drops. VV_ERR_ARG outside the ranges. */
 vv_status vv_set_pass_budget(vv_renderer* r, uint32_t passes, uint32_t slot_frames);
+
+/* ------------------------------------------------------------ batched passes */
+
+/* A batch engine on context `ctx`: `passes` batched passes in flight (1 to 6)
+ * on streams of its own, each holding the path state that its requests share,
+ * up to `slot_frames` frames' worth of slots per request (1 to 16) and 2^24
+ * slots in all unless one frame of each request needs more. An extension
+ * beyond the reference (whose Renderer::record serves one view per call,
+ * renderer.rs:1499): the serving loop's one wavefront over several requests. */
+vv_status vv_batch_create(vv_context* ctx, uint32_t passes, uint32_t slot_frames, vv_batch** out);
+vv_status vv_batch_destroy(vv_batch* b);
+/* One request of a batched pass: `frames` accumulate-frames (1 to 64) of
+ * `params` from frame index `first_frame`, as vv_record_frames(r,
+ * first_frame, frames, params) adds them; display != 0 runs the denoiser and
+ * the display after them (a request's last pass). */
+typedef struct vv_batch_request {
+    const vv_frame_params* params;
+    uint64_t first_frame;
+    uint32_t frames;
+    uint32_t display;
+} vv_batch_request;
+/* Queues one pass whose waves trace the frames of every request at once:
+ * request i accumulates into renderers[i] with the same paths, random streams
+ * and sums as vv_record_frames (summed in a different order: equal to within
+ * FP32 rounding). 1 to 8 distinct renderers of one volume (a base and its
+ * views), created with the reference's storage formats, resized, path
+ * tracing enabled. Each renderer's context stream waits for its share, so
+ * vv_query and vv_synchronize on it see the pass. VV_ERR_ARG / VV_ERR_LIMIT
+ * for a batch outside these bounds (below 2^28 pixels and 2^20 samples per
+ * frame per request). */
+vv_status vv_batch_record(vv_batch* b, uint32_t n, vv_renderer* const* renderers,
+                          const vv_batch_request* requests);
+/* Device bytes of the engine's shared path state, and a wait for its passes. */
+vv_status vv_batch_memory(const vv_batch* b, uint64_t* bytes);
+vv_status vv_batch_synchronize(vv_batch* b);
+/* Kernel launches of the engine's path tracing so far. */
+uint64_t vv_batch_launches(const vv_batch* b);
+/* Batched passes queued and not yet finished, without blocking (at most the
+ * engine's passes in flight: each pass stream's latest pass). */
+vv_status vv_batch_in_flight(vv_batch* b, uint32_t* passes);
 
 /* --------------------------------------------------- allocation-free denoise */
 

@@ -20,6 +20,7 @@ STRUCTS = {
     "vv_orbit_camera": abi.OrbitCamera, "vv_label_params": abi.LabelParams, "vv_lighting": abi.Lighting,
     "vv_clip_plane": abi.ClipPlane, "vv_clipping": abi.Clipping, "vv_path_tracing": abi.PathTracing,
     "vv_frame_params": abi.FrameParams, "vv_renderer_info": abi.RendererInfo, "vv_precision": abi.Precision,
+    "vv_batch_request": abi.BatchRequest,
 }
 
 

@@ -115,3 +115,135 @@ def test_same_under_a_pass_budget(volumes):
     finally:
         a.destroy()
         b.destroy()
+
+
+# ------------------------------------------------------------ batched passes
+def _alone(cfg, params, w, h, spp, env=None):
+    """A request rendered by a renderer of its own with vv_record_frames."""
+    from volview_gb300 import renderer as R
+    ctx = R.Context(0)
+    r = R.Renderer(ctx, cfg["volume"], cfg["tf"])
+    try:
+        r.set_labels(cfg["labels_vol"], abi.soft_struct(cfg["soft"]) if cfg.get("soft") is not None else None)
+        if env is not None:
+            r.set_environment_map(abi.env_struct(env))
+        r.resize(w, h)
+        r.record_frames(1, spp, params)
+        r.synchronize()
+        return r.read_accumulation()[0], r.read_output()
+    finally:
+        r.destroy()
+        ctx.destroy()
+
+
+class _Result:
+    def __init__(self, acc, image):
+        self.accumulation, self.image = (acc,), image
+
+
+def test_batched_pass_matches_record_frames(volumes):
+    """Two views of one volume in the same batched passes (different image
+    sizes, paths per pixel, cameras, hidden labels, and one with the light map
+    while the other has the studio light) give each request the result of a
+    renderer of its own: the same paths, summed in another order."""
+    from volview_gb300 import renderer as R
+    cfg = volumes["small"]
+    env = scene.synthetic_light_map()
+    p1 = _params(cfg, yaw=0.3, hidden=(2,))
+    p2 = _params(cfg, yaw=-0.4, clip=False)
+    p2.lighting.environment = abi.ENV_MAP
+    ref1 = _alone(cfg, p1, 64, 48, 40)
+    ref2 = _alone(cfg, p2, 40, 40, 24, env=env)
+    ctx = R.Context(0)
+    base = R.Renderer(ctx, cfg["volume"], cfg["tf"])
+    base.set_labels(cfg["labels_vol"], abi.soft_struct(cfg["soft"]))
+    base.set_environment_map(abi.env_struct(env))
+    ctxs = [R.Context(0), R.Context(0)]
+    views = [R.Renderer.view(c, base) for c in ctxs]
+    engine = R.BatchEngine(ctx, passes=2, slot_frames=16)
+    try:
+        views[0].resize(64, 48)
+        views[1].resize(40, 40)
+        # Passes of 16 frames: request 1 takes three, request 2 two (the
+        # second with 8 frames, then its display), request 1 alone last.
+        engine.record([(views[0], p1, 1, 16, False), (views[1], p2, 1, 16, False)])
+        engine.record([(views[0], p1, 17, 16, False), (views[1], p2, 17, 8, True)])
+        engine.record([(views[0], p1, 33, 8, True)])
+        for v in views:
+            v.synchronize()
+        assert views[0].accumulated_samples() == 40 and views[1].accumulated_samples() == 24
+        _same(_Result(*ref1), _Result(views[0].read_accumulation()[0], views[0].read_output()))
+        _same(_Result(*ref2), _Result(views[1].read_accumulation()[0], views[1].read_output()))
+        assert engine.kernel_launches() > 0 and engine.in_flight() == 0
+    finally:
+        engine.destroy()
+        for v in views:
+            v.destroy()
+        base.destroy()
+        for c in ctxs + [ctx]:
+            c.destroy()
+
+
+def test_views_share_the_volume_and_guard_it(volumes):
+    from volview_gb300 import renderer as R
+    cfg = volumes["torso"]
+    ctx = R.Context(0)
+    base = R.Renderer(ctx, cfg["volume"], cfg["tf"])
+    base.set_labels(cfg["labels_vol"], None)
+    view = R.Renderer.view(ctx, base)
+    fp16 = R.Renderer(ctx, cfg["volume"], cfg["tf"], abi.precision(density_format=abi.DENSITY_FP16))
+    engine = R.BatchEngine(ctx)
+    try:
+        assert np.array_equal(view.read_volume(abi.VOLUME_DENSITY), base.read_volume(abi.VOLUME_DENSITY))
+        assert np.array_equal(view.read_volume(abi.VOLUME_LABELS), base.read_volume(abi.VOLUME_LABELS))
+        shared = S.volume_bytes(cfg["volume"].dims) - S.view_volume_bytes(cfg["volume"].dims)
+        assert base.device_bytes() - view.device_bytes() >= 0.9 * shared
+        for call in (lambda: view.set_transfer_function(cfg["tf"]), lambda: base.set_labels(cfg["labels_vol"]),
+                     lambda: view.set_environment_map(None), lambda: base.destroy()):
+            with pytest.raises(R.VolptError) as e:
+                call()
+            assert e.value.status == abi.VV_ERR_STATE
+        p = _params(cfg)
+        view.resize(32, 32)
+        fp16.resize(32, 32)
+        for items in ([(view, p, 1, 0, True)], [(view, p, 1, 65, True)], [(view, p, 1, 4, True)] * 2,
+                      [(view, p, 1, 4, True), (fp16, p, 1, 4, True)], [(fp16, p, 1, 4, True)]):
+            with pytest.raises(R.VolptError) as e:
+                engine.record(items)
+            assert e.value.status == abi.VV_ERR_ARG
+    finally:
+        engine.destroy()
+        fp16.destroy()
+        view.destroy()
+        base.destroy()
+        ctx.destroy()
+
+
+def test_batched_server_same_alone_and_in_a_mix(volumes):
+    """The batched serving loop: a request's result equals its lone render
+    through vv_record_frames, with requests of two volumes, several sizes and
+    paths per pixel in flight, one view per concurrent request and one base
+    per volume."""
+    def target():
+        return S.Request("small", 64, 48, 40, _params(volumes["small"], yaw=0.3, hidden=(2,)))
+
+    alone, _ = _serve(volumes, [target()])
+    mix = [S.Request("torso", 96, 64, 64, _params(volumes["torso"], yaw=-0.5)),
+           S.Request("small", 40, 40, 16, _params(volumes["small"], clip=False)),
+           target(),
+           S.Request("small", 32, 32, 100, _params(volumes["small"], yaw=1.0)),
+           S.Request("torso", 32, 32, 24, _params(volumes["torso"], hidden=(1, 4)))]
+    make_base, make_view, engine, base, view, reserve = S.batched_factory(volumes)
+    srv = S.BatchedServer(make_base, make_view, engine, 60 << 30, base, view, reserve, keep_accumulation=True,
+                          frames_per_pass=16)
+    try:
+        for q in mix:
+            srv.submit(q)
+        while srv.queue or srv.active:
+            srv.step()
+        assert all(q.image is not None and q.image.shape == (q.height, q.width, 4) for q in mix)
+        assert len(srv.bases) == 2 and srv.created == 5
+        assert max(srv.batch_sizes) >= 2  # requests shared passes
+        _same(alone[0], mix[2])
+    finally:
+        srv.close()

@@ -227,3 +227,141 @@ def test_a_pass_budget_lowers_the_model_and_reaches_the_renderers():
     srv.preload("b")
     run(srv, [S.Request("a", 256, 256, 16, params=0), S.Request("b", 256, 256, 16, params=1)])
     assert budgets == [(2, 8), (2, 8)]
+
+
+# ------------------------------------------------------------ batched passes
+class FakeEngine:
+    """The batch engine without a device: each queued pass takes `ticks`
+    in_flight polls to finish."""
+
+    def __init__(self, ticks=2):
+        self.ticks, self.pending, self.passes = ticks, [], []
+
+    def record(self, items):
+        self.passes.append([(r.name, params, first, n, display) for r, params, first, n, display in items])
+        self.pending.append([self.ticks, {id(r) for r, *_ in items}])
+        for r, params, first, n, display in items:
+            r.frames.append((first, n, display))
+            r.params = params
+
+    def in_flight(self):
+        for p in self.pending:
+            p[0] -= 1
+        self.pending = [p for p in self.pending if p[0] > 0]
+        return len(self.pending)
+
+    def busy(self, r):
+        return any(id(r) in p[1] for p in self.pending)
+
+    def destroy(self):
+        pass
+
+
+class FakeView:
+    def __init__(self, base, engine, n):
+        self.base, self.engine, self.name = base, engine, f"{base.volume}{n}"
+        self.w = self.h = 0
+        self.frames, self.params, self.destroyed = [], None, False
+
+    def device_bytes(self):
+        return 10 ** 6 + S.view_image_bytes(self.w, self.h, 2)
+
+    def set_pass_budget(self, passes, frames):
+        pass
+
+    def reset_view(self):
+        self.frames = []
+
+    def resize(self, w, h):
+        self.w, self.h = w, h
+
+    def idle(self):
+        return not self.engine.busy(self)
+
+    def read_output(self):
+        return ("image", self.base.volume, self.params)
+
+    def read_accumulation(self):
+        return ("accumulation", self.params)
+
+    def destroy(self):
+        self.destroyed = True
+
+
+class FakeBase:
+    def __init__(self, volume):
+        self.volume, self.destroyed = volume, False
+
+    def device_bytes(self):
+        return 10 ** 9
+
+    def destroy(self):
+        self.destroyed = True
+
+
+def make_batched(budget=10 ** 12, ticks=2, **kw):
+    engine = FakeEngine(ticks)
+    bases, views = [], []
+
+    def make_base(volume):
+        bases.append(FakeBase(volume))
+        return bases[-1]
+
+    def make_view(base):
+        views.append(FakeView(base, engine, len(views)))
+        return views[-1]
+
+    srv = S.BatchedServer(make_base, make_view, engine, budget, lambda v: 10 ** 9, lambda v: 10 ** 6, 10 ** 8,
+                          clock=iter(range(10 ** 6)).__next__, **kw)
+    return srv, engine, bases, views
+
+
+def test_batched_passes_cover_every_frame_once_and_display_last():
+    srv, engine, bases, views = make_batched(frames_per_pass=16, max_batch=3)
+    reqs = [S.Request("ab"[k % 2], 64 << (k % 3), 64, (16, 40, 100)[k % 3], params=k) for k in range(9)]
+    run(srv, reqs)
+    assert all(q.image == ("image", q.volume, q.params) for q in reqs)
+    assert len(bases) == 2 and srv.created <= len(reqs)
+    for p in engine.passes:
+        assert 1 <= len(p) <= 3
+        assert len({name[0] for name, *_ in p}) == 1  # one volume per batched pass
+    for q in reqs:  # the request's passes, in order, on its view
+        chunks = [(first, n, display) for p in engine.passes for name, params, first, n, display in p
+                  if params == q.params]
+        assert [c[0] for c in chunks] == [1 + sum(c[1] for c in chunks[:k]) for k in range(len(chunks))]
+        assert sum(c[1] for c in chunks) == q.spp and all(c[1] <= 16 for c in chunks)
+        assert [c[2] for c in chunks] == [False] * (len(chunks) - 1) + [True]
+
+
+def test_batched_requests_share_passes_and_late_ones_join():
+    srv, engine, bases, views = make_batched(frames_per_pass=8, in_flight=1, ticks=3)
+    first = S.Request("a", 256, 256, 64, params="first")
+    srv.submit(first)
+    srv.step()
+    second = S.Request("a", 64, 64, 16, params="second")
+    srv.submit(second)
+    for _ in range(4):
+        srv.step()
+    assert second.started is not None and first.finished is None
+    joined = [p for p in engine.passes if {"first", "second"} <= {params for _, params, *_ in p}]
+    assert joined  # a later pass carries both requests
+    run(srv, [])
+    assert second.finished < first.finished
+    assert srv.created == 2 and len(bases) == 1  # one resident volume, a view per concurrent request
+
+
+def test_batched_views_are_reused_and_memory_stays_in_budget():
+    one = 10 ** 8 + 10 ** 9 + 10 ** 6 + S.view_image_bytes(256, 256, 2)
+    srv, engine, bases, views = make_batched(budget=one + 10 ** 6 + S.view_image_bytes(256, 256, 2) + 10,
+                                             max_batch=8)
+    reqs = [S.Request("a", 256, 256, 16, params=k) for k in range(6)]
+    run(srv, reqs)
+    assert srv.peak_bytes <= srv.budget
+    assert srv.created <= 2 and all(q.image is not None for q in reqs)
+
+
+def test_batched_refuses_what_cannot_fit():
+    srv, engine, bases, views = make_batched(budget=10 ** 9)
+    srv.submit(S.Request("a", 64, 64, 16, params=0))
+    with pytest.raises(MemoryError):
+        srv.step()

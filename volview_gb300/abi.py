@@ -39,6 +39,12 @@ def precision(density_format=DENSITY_UNORM16, sums=SUMS_FP32, fp64_after=0, majo
 F4x256 = (C.c_float * 4) * VV_LABEL_COUNT
 
 
+class BatchRequest(C.Structure):
+    """vv_batch_request: one request's frames in a batched pass."""
+    _fields_ = [("params", C.c_void_p), ("first_frame", C.c_uint64), ("frames", C.c_uint32),
+                ("display", C.c_uint32)]
+
+
 class Volume(C.Structure):
     _fields_ = [("dims", C.c_uint32 * 3), ("spacing", C.c_double * 3), ("origin", C.c_double * 3),
                 ("direction", C.c_double * 9), ("hu", C.POINTER(C.c_int16))]

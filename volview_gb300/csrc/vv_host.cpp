@@ -163,8 +163,9 @@ extern "C" vv_status vv_context_destroy(vv_context* c) {
 struct DBuf {
     void* p = nullptr;
     size_t n = 0;
+    bool borrowed = false;  // another renderer's buffer (a view's shared volume): never freed or resized here
     cudaError_t alloc(size_t bytes) {
-        if (p && n == bytes) return cudaSuccess;
+        if (p && n == bytes && !borrowed) return cudaSuccess;
         release();
         cudaError_t e = cudaMalloc(&p, bytes);
         if (e == cudaSuccess) n = bytes;
@@ -172,10 +173,18 @@ struct DBuf {
         return e;
     }
     void release() {
-        if (p) cudaFree(p);
+        if (p && !borrowed) cudaFree(p);
         p = nullptr;
         n = 0;
+        borrowed = false;
     }
+    void borrow(const DBuf& owner) {
+        release();
+        p = owner.p;
+        n = owner.n;
+        borrowed = p != nullptr;
+    }
+    size_t owned_bytes() const { return borrowed ? 0 : n; }
     template <class T> T* as() const { return (T*)p; }
 };
 
@@ -206,6 +215,11 @@ struct OpacityKey {
 
 struct vv_renderer {
     vv_context* ctx;
+    // A view (vv_renderer_create_view) reads the volume, transfer function,
+    // labels and light map of `base` (never a view itself), which counts its
+    // live views and keeps those unchanged while any exist.
+    vv_renderer* base = nullptr;
+    int views = 0;
     Vol vol;
     double spacing[3];
     // geometry
@@ -651,6 +665,14 @@ static bool same_accumulation(const vv_frame_params& a, const vv_frame_params& b
 }
 
 // ---------------------------------------------------------------- renderer
+// The volume, transfer function, labels and light map of a renderer change
+// only while no view shares them (and never through a view).
+static vv_status check_unshared(const vv_renderer* r) {
+    if (r->base) return fail(VV_ERR_STATE, "a view shares its base's volume, transfer function, labels and light map");
+    if (r->views > 0) return fail(VV_ERR_STATE, "the renderer's volume has live views: destroy them first");
+    return VV_OK;
+}
+
 static vv_status use_device(const vv_renderer* r) {
     CK(cudaSetDevice(r->ctx->device));
     return VV_OK;
@@ -733,9 +755,83 @@ extern "C" vv_status vv_renderer_create_ex(vv_context* ctx, const vv_volume* vol
     return VV_OK;
 }
 
+// A renderer that reads `base`'s device volume (density, normals, labels,
+// soft label grid), transfer function and light map instead of holding its
+// own copies: the per-request state of several requests on one resident
+// volume. Its label masks, majorants, label tables, images and passes are its
+// own, so each view renders with its own frame parameters.
+extern "C" vv_status vv_renderer_create_view(vv_context* ctx, vv_renderer* base, vv_renderer** out) {
+    if (!ctx || !base || !out) return fail(VV_ERR_ARG, "null argument");
+    vv_renderer* root = base->base ? base->base : base;
+    if (ctx->device != root->ctx->device) return fail(VV_ERR_ARG, "a view must be on its volume's device");
+    CK(cudaSetDevice(ctx->device));
+    CK(cudaStreamSynchronize(root->ctx->stream));  // the volume's uploads have finished
+    vv_renderer* r = new vv_renderer();
+    r->ctx = ctx;
+    r->base = root;
+    r->vol = root->vol;
+    std::memcpy(r->spacing, root->spacing, sizeof(r->spacing));
+    std::memcpy(r->w2i, root->w2i, sizeof(r->w2i));
+    std::memcpy(r->i2w, root->i2w, sizeof(r->i2w));
+    std::memcpy(r->dims, root->dims, sizeof(r->dims));
+    std::memcpy(r->bounds_lo, root->bounds_lo, sizeof(r->bounds_lo));
+    std::memcpy(r->bounds_hi, root->bounds_hi, sizeof(r->bounds_hi));
+    std::memcpy(r->center, root->center, sizeof(r->center));
+    r->min_spacing = root->min_spacing;
+    r->max_spacing = root->max_spacing;
+    r->diagonal = root->diagonal;
+    std::memcpy(r->bucket, root->bucket, sizeof(r->bucket));
+    r->majorants = root->majorants;
+    std::memcpy(r->soft_dims, root->soft_dims, sizeof(r->soft_dims));
+    std::memcpy(r->soft_push, root->soft_push, sizeof(r->soft_push));
+    r->has_labels = root->has_labels;
+    r->generation = root->generation;
+    r->env_w = root->env_w;
+    r->env_h = root->env_h;
+    r->env_gm = root->env_gm;
+    r->env_gr = root->env_gr;
+    r->has_env = root->has_env;
+    r->env_peak_u = root->env_peak_u;
+    r->sums = root->sums;
+    r->fp64_after = root->fp64_after;
+    DBuf* shared[][2] = {{&r->density, &root->density}, {&r->normals, &root->normals}, {&r->labels, &root->labels},
+                         {&r->soft, &root->soft}, {&r->lut, &root->lut}, {&r->bucket_dev, &root->bucket_dev},
+                         {&r->preint, &root->preint}, {&r->env_rad, &root->env_rad},
+                         {&r->env_table, &root->env_table}, {&r->env_diffuse, &root->env_diffuse},
+                         {&r->env_guide, &root->env_guide}};
+    for (auto& b : shared) b[0]->borrow(*b[1]);
+    r->tables_host = nullptr;
+    cudaError_t e = cudaMallocHost((void**)&r->tables_host, sizeof(LabelTables));
+    if (e != cudaSuccess) {
+        delete r;
+        return cuda_fail(e, "cudaMallocHost");
+    }
+    root->views++;
+    const long elems = vol_elems(r->vol);
+    if ((e = r->majorant.alloc((size_t)r->vol.bx * r->vol.by * r->vol.bz * sizeof(float))) != cudaSuccess ||
+        (e = r->tables.alloc(sizeof(LabelTables))) != cudaSuccess || (e = r->work.alloc(256)) != cudaSuccess ||
+        (e = r->exposure.alloc(sizeof(float))) != cudaSuccess ||
+        (r->has_labels && ((e = r->mask_a.alloc(elems * sizeof(uint32_t))) != cudaSuccess ||
+                           (e = r->mask_b.alloc(elems * sizeof(uint32_t))) != cudaSuccess))) {
+        vv_renderer_destroy(r);
+        return cuda_fail(e, "cudaMalloc");
+    }
+    e = cudaMemsetAsync(r->exposure.p, 0, sizeof(float), ctx->stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(r->work.p, 0, 256, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    if (e != cudaSuccess) {
+        vv_renderer_destroy(r);
+        return cuda_fail(e, "view set-up");
+    }
+    *out = r;
+    return VV_OK;
+}
+
 extern "C" vv_status vv_renderer_destroy(vv_renderer* r) {
     if (!r) return VV_OK;
+    if (r->views > 0) return fail(VV_ERR_STATE, "the renderer's volume has live views: destroy them first");
     cudaSetDevice(r->ctx->device);
+    if (r->base) r->base->views--;
     cudaStreamSynchronize(r->ctx->stream);
     for (auto& P : r->pass) {
         if (P.stream) cudaStreamSynchronize(P.stream);
@@ -801,6 +897,7 @@ extern "C" vv_status vv_default_camera(const vv_renderer* r, vv_orbit_camera* ou
 
 extern "C" vv_status vv_set_transfer_function(vv_renderer* r, const vv_transfer_function* tf) {
     if (!r) return fail(VV_ERR_ARG, "null renderer");
+    if (check_unshared(r) != VV_OK) return VV_ERR_STATE;
     vv_status s = use_device(r);
     if (s != VV_OK) return s;
     CK(cudaStreamSynchronize(r->ctx->stream));
@@ -822,6 +919,7 @@ extern "C" vv_status vv_set_labels(vv_renderer* r, const uint8_t* labels, size_t
             if (soft->src_axis[a] > 2) return fail(VV_ERR_ARG, "soft label grid axis out of range");
         }
     }
+    if (check_unshared(r) != VV_OK) return VV_ERR_STATE;
     vv_status s = use_device(r);
     if (s != VV_OK) return s;
     cudaStream_t st = r->ctx->stream;
@@ -1022,6 +1120,7 @@ static void search_guides(int w, int h, const std::vector<float>& table, int& gm
 
 extern "C" vv_status vv_set_environment_map(vv_renderer* r, const vv_environment_map* map) {
     if (!r) return fail(VV_ERR_ARG, "null renderer");
+    if (check_unshared(r) != VV_OK) return VV_ERR_STATE;
     vv_status st = use_device(r);
     if (st != VV_OK) return st;
     CK(cudaStreamSynchronize(r->ctx->stream));  // the reference waits for the device to go idle
@@ -1145,7 +1244,7 @@ extern "C" vv_status vv_renderer_memory(const vv_renderer* r, uint64_t* bytes) {
                          &r->ao_vol, &r->env_rad, &r->env_table, &r->env_diffuse, &r->env_guide, &r->comp[0],
                          &r->comp[1], &r->comp[2], &r->wide[0], &r->wide[1], &r->wide[2]};
     uint64_t n = 0;
-    for (const DBuf* b : all) n += b->n;
+    for (const DBuf* b : all) n += b->owned_bytes();  // a view's shared volumes count for its base
     for (const auto& P : r->pass) {
         const DBuf* pb[] = {&P.slots, &P.map, &P.queues, &P.counts, &P.accum, &P.albedo, &P.normal, &P.binq, &P.bins};
         for (const DBuf* b : pb) n += b->n;
@@ -1257,31 +1356,10 @@ static PtArgs pt_args(vv_renderer* r, const UHead& u) {
     return a;
 }
 
-// The path-tracing launches of one pass on stream `s`: the wavefront tracer,
-// or with VV_PT_KERNEL=persistent / frame the single-kernel tracers
-// (persistent warps with path regeneration / one thread per pixel, the
-// reference's shape).
-static cudaError_t run_pt(vv_renderer* r, vv_renderer::Pass& P, PtArgs& a, cudaStream_t s, int* launches) {
-    const char* k = std::getenv("VV_PT_KERNEL");
-    if (k && (std::strcmp(k, "persistent") == 0 || std::strcmp(k, "frame") == 0)) {
-        a.persistent = std::strcmp(k, "persistent") == 0 || a.frames > 1;
-        return kernels_of(r).pt(a, r->ctx->sms, s, launches);
-    }
-    // A wavefront slot counts its pixel's samples in 20 bits; 2^20 or more
-    // samples per frame run on the persistent single-kernel tracer.
-    if (a.u.path[2] >= WF_MAX_SAMPLES) {
-        a.persistent = 1;
-        return kernels_of(r).pt(a, r->ctx->sms, s, launches);
-    }
-    // Paths in flight: with several frames per pass, up to 16 frames' worth
-    // (VV_WF_SLOTS overrides), at most 2^24 slots (4.6 GB of path state) unless
-    // one frame needs more. Every frame of a 16-frame pass then runs in the
-    // same waves: fewer, fuller waves and no refills (measured at 1024^2:
-    // 171 M path samples/s with one frame's worth, 217 with 4, 238 with 16).
-    size_t px = (size_t)r->width * r->height;
-    const char* e = std::getenv("VV_WF_SLOTS");
-    size_t per_pixel = e ? (size_t)std::max(1, std::atoi(e)) : (size_t)r->slot_frames;
-    size_t cap = std::min(px * std::min<size_t>(per_pixel, a.frames), std::max(px, (size_t)1 << 24));
+// The wavefront state of pass `P` for `cap` paths in flight on stream `s`:
+// its records, queues, counters and later-flight bins over volume `v`
+// (allocated when the pass needs more than it has).
+static cudaError_t wf_state(vv_renderer::Pass& P, size_t cap, const Vol& v, cudaStream_t s, WfArgs& w) {
     if (P.slots.n < cap * WF_SLOT_BYTES) {
         cudaError_t ce = cudaStreamSynchronize(s);  // the pass's previous use of its state has ended
         if (ce == cudaSuccess) ce = P.slots.alloc(cap * WF_SLOT_BYTES);
@@ -1290,7 +1368,7 @@ static cudaError_t run_pt(vv_renderer* r, vv_renderer::Pass& P, PtArgs& a, cudaS
         if (ce != cudaSuccess) return ce;
     }
     cap = P.slots.n / WF_SLOT_BYTES;
-    WfArgs w;
+    w = WfArgs();
     w.capacity = (uint32_t)cap;
     // The records of vv_wavefront.cu, each an array over the slots.
     float4* rec = P.slots.as<float4>();
@@ -1319,9 +1397,9 @@ static cudaError_t run_pt(vv_renderer* r, vv_renderer::Pass& P, PtArgs& a, cudaS
     {
         int shift = 5, cx, cy, cz;
         for (;; shift++) {
-            cx = (r->vol.nx + (1 << shift) - 1) >> shift;
-            cy = (r->vol.ny + (1 << shift) - 1) >> shift;
-            cz = (r->vol.nz + (1 << shift) - 1) >> shift;
+            cx = (v.nx + (1 << shift) - 1) >> shift;
+            cy = (v.ny + (1 << shift) - 1) >> shift;
+            cz = (v.nz + (1 << shift) - 1) >> shift;
             if ((size_t)cx * cy * cz * 8 <= 65536) break;
         }
         const uint32_t nbins = (uint32_t)(cx * cy * cz * 8);
@@ -1348,6 +1426,37 @@ static cudaError_t run_pt(vv_renderer* r, vv_renderer::Pass& P, PtArgs& a, cudaS
         w.cells_y = cy;
         w.cells_z = cz;
     }
+    return cudaSuccess;
+}
+
+// The path-tracing launches of one pass on stream `s`: the wavefront tracer,
+// or with VV_PT_KERNEL=persistent / frame the single-kernel tracers
+// (persistent warps with path regeneration / one thread per pixel, the
+// reference's shape).
+static cudaError_t run_pt(vv_renderer* r, vv_renderer::Pass& P, PtArgs& a, cudaStream_t s, int* launches) {
+    const char* k = std::getenv("VV_PT_KERNEL");
+    if (k && (std::strcmp(k, "persistent") == 0 || std::strcmp(k, "frame") == 0)) {
+        a.persistent = std::strcmp(k, "persistent") == 0 || a.frames > 1;
+        return kernels_of(r).pt(a, r->ctx->sms, s, launches);
+    }
+    // A wavefront slot counts its pixel's samples in 20 bits; 2^20 or more
+    // samples per frame run on the persistent single-kernel tracer.
+    if (a.u.path[2] >= WF_MAX_SAMPLES) {
+        a.persistent = 1;
+        return kernels_of(r).pt(a, r->ctx->sms, s, launches);
+    }
+    // Paths in flight: with several frames per pass, up to 16 frames' worth
+    // (VV_WF_SLOTS overrides), at most 2^24 slots (4.6 GB of path state) unless
+    // one frame needs more. Every frame of a 16-frame pass then runs in the
+    // same waves: fewer, fuller waves and no refills (measured at 1024^2:
+    // 171 M path samples/s with one frame's worth, 217 with 4, 238 with 16).
+    size_t px = (size_t)r->width * r->height;
+    const char* e = std::getenv("VV_WF_SLOTS");
+    size_t per_pixel = e ? (size_t)std::max(1, std::atoi(e)) : (size_t)r->slot_frames;
+    size_t cap = std::min(px * std::min<size_t>(per_pixel, a.frames), std::max(px, (size_t)1 << 24));
+    WfArgs w;
+    cudaError_t ce = wf_state(P, cap, r->vol, s, w);
+    if (ce != cudaSuccess) return ce;
     return kernels_of(r).pt_wavefront(a, w, r->ctx->sms, s, launches);
 }
 
@@ -1682,6 +1791,11 @@ static vv_status run_unet(vv_renderer* r, float n, cudaStream_t s, int* launches
 // displayed, and the context stream waits for that display. So a call returns
 // at once, and consecutive calls overlap: one pass's last, nearly empty waves
 // run beside the next pass's first ones.
+static cudaError_t pass_args(vv_renderer* r, vv_renderer::Pass& P, const UHead& u, uint32_t frames, cudaStream_t s,
+                             PtArgs& a);
+static vv_status end_pass(vv_renderer* r, vv_renderer::Pass& P, vv_renderer::Pass& prev, const vv_frame_params& p,
+                          UHead& u, uint32_t frames, bool display, cudaStream_t s, int launches);
+
 static vv_status record_pass(vv_renderer* r, const vv_frame_params& p, UHead& u, uint32_t frames,
                              bool display = true) {
     vv_renderer::Pass& P = r->pass[r->next_pass % r->passes];
@@ -1695,21 +1809,39 @@ static vv_status record_pass(vv_renderer* r, const vv_frame_params& p, UHead& u,
     }
     const char* single = std::getenv("VV_PT_KERNEL");
     if (single) CK(cudaStreamWaitEvent(s, prev.shown, 0));  // the single-kernel tracers share one work counter
-    uint32_t spf = std::max(p.path_tracing.samples_per_frame, 1u);
+    PtArgs a;
+    CK(pass_args(r, P, u, frames, s, a));
+    int launches = 0;
+    pt_timer_start(r, s);
+    CK(run_pt(r, P, a, s, &launches));
+    pt_timer_stop(r, s);
+    return end_pass(r, P, prev, p, u, frames, display, s, launches);
+}
+
+// A pass's arguments with its own sums (zeroed on stream `s` once their last
+// use, possibly a batched pass on another stream, has ended).
+static cudaError_t pass_args(vv_renderer* r, vv_renderer::Pass& P, const UHead& u, uint32_t frames, cudaStream_t s,
+                             PtArgs& a) {
+    cudaError_t e = cudaStreamWaitEvent(s, P.shown, 0);
     size_t bytes = (size_t)r->width * r->height * 16;
-    CK(cudaMemsetAsync(P.accum.p, 0, bytes, s));
-    CK(cudaMemsetAsync(P.albedo.p, 0, bytes, s));
-    CK(cudaMemsetAsync(P.normal.p, 0, bytes, s));
-    PtArgs a = pt_args(r, u);
+    if (e == cudaSuccess) e = cudaMemsetAsync(P.accum.p, 0, bytes, s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(P.albedo.p, 0, bytes, s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(P.normal.p, 0, bytes, s);
+    a = pt_args(r, u);
     a.frames = frames;
     a.accum = P.accum.as<float4>();
     a.albedo = P.albedo.as<float4>();
     a.normal = P.normal.as<float4>();
     a.write_hdr = 0;
-    int launches = 0;
-    pt_timer_start(r, s);
-    CK(run_pt(r, P, a, s, &launches));
-    pt_timer_stop(r, s);
+    return e;
+}
+
+// The end of a pass whose path tracing is queued on stream `s`: its sums (P)
+// merged into the running sums after the previous pass's display (prev), the
+// denoiser and the display, then P.shown, which the context stream waits for.
+static vv_status end_pass(vv_renderer* r, vv_renderer::Pass& P, vv_renderer::Pass& prev, const vv_frame_params& p,
+                          UHead& u, uint32_t frames, bool display, cudaStream_t s, int launches) {
+    uint32_t spf = std::max(p.path_tracing.samples_per_frame, 1u);
     // The last frame's view of the counts: accumulated before it, spf after.
     r->accumulated += (frames - 1) * spf;
     u.path[0] = r->accumulated;
@@ -1792,6 +1924,190 @@ extern "C" vv_status vv_record_frames(vv_renderer* r, uint64_t first_frame, uint
         if (s != VV_OK) return s;
         done += n;
     }
+    return VV_OK;
+}
+
+// ------------------------------------------------------------ batched passes
+// A batch engine: passes in flight on streams of its own, each with the
+// wavefront state (slots, queues, bins) that the requests of one batched
+// pass share, and each request's item counter and constants.
+struct vv_batch {
+    vv_context* ctx;
+    struct BatchPass {
+        vv_renderer::Pass p;  // its sums stay empty: each request's go to its renderer's pass sums
+        DBuf items, consts;
+    } pass[VV_PASSES];
+    int passes = 2;
+    int next = 0;
+    int slot_frames = 16;
+    uint64_t launches = 0;
+};
+
+extern "C" vv_status vv_batch_create(vv_context* ctx, uint32_t passes, uint32_t slot_frames, vv_batch** out) {
+    if (!ctx || !out) return fail(VV_ERR_ARG, "null argument");
+    if (passes < 1 || passes > VV_PASSES || slot_frames < 1 || slot_frames > 16)
+        return fail(VV_ERR_ARG, "passes must be 1..6 and slot_frames 1..16");
+    CK(cudaSetDevice(ctx->device));
+    vv_batch* b = new vv_batch();
+    b->ctx = ctx;
+    b->passes = (int)passes;
+    b->slot_frames = (int)slot_frames;
+    for (int k = 0; k < b->passes; k++) {
+        auto& B = b->pass[k];
+        cudaError_t e = cudaStreamCreateWithFlags(&B.p.stream, cudaStreamNonBlocking);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&B.p.shown, cudaEventDisableTiming);
+        if (e == cudaSuccess) e = B.p.counts.alloc(WF_COUNTERS * sizeof(uint32_t));
+        if (e == cudaSuccess) e = B.items.alloc(VV_BATCH_MAX * sizeof(uint32_t));
+        if (e == cudaSuccess) e = B.consts.alloc(VV_BATCH_MAX * WF_CONSTS_BYTES);
+        if (e != cudaSuccess) {
+            vv_batch_destroy(b);
+            return cuda_fail(e, "batch engine");
+        }
+    }
+    *out = b;
+    return VV_OK;
+}
+
+extern "C" vv_status vv_batch_destroy(vv_batch* b) {
+    if (!b) return VV_OK;
+    cudaSetDevice(b->ctx->device);
+    for (auto& B : b->pass) {
+        if (B.p.stream) cudaStreamSynchronize(B.p.stream);
+        DBuf* pb[] = {&B.p.slots, &B.p.map, &B.p.queues, &B.p.counts, &B.p.binq, &B.p.bins, &B.items, &B.consts};
+        for (DBuf* d : pb) d->release();
+        if (B.p.shown) cudaEventDestroy(B.p.shown);
+        if (B.p.stream) cudaStreamDestroy(B.p.stream);
+    }
+    delete b;
+    return VV_OK;
+}
+
+extern "C" vv_status vv_batch_memory(const vv_batch* b, uint64_t* bytes) {
+    if (!b || !bytes) return fail(VV_ERR_ARG, "null argument");
+    uint64_t n = 0;
+    for (const auto& B : b->pass) {
+        const DBuf* pb[] = {&B.p.slots, &B.p.map, &B.p.queues, &B.p.counts, &B.p.binq, &B.p.bins, &B.items,
+                            &B.consts};
+        for (const DBuf* d : pb) n += d->n;
+    }
+    *bytes = n;
+    return VV_OK;
+}
+
+extern "C" vv_status vv_batch_synchronize(vv_batch* b) {
+    if (!b) return fail(VV_ERR_ARG, "null batch engine");
+    CK(cudaSetDevice(b->ctx->device));
+    for (auto& B : b->pass)
+        if (B.p.stream) CK(cudaStreamSynchronize(B.p.stream));
+    return VV_OK;
+}
+
+extern "C" uint64_t vv_batch_launches(const vv_batch* b) { return b ? b->launches : 0; }
+
+extern "C" vv_status vv_batch_in_flight(vv_batch* b, uint32_t* passes) {
+    if (!b || !passes) return fail(VV_ERR_ARG, "null argument");
+    CK(cudaSetDevice(b->ctx->device));
+    uint32_t n = 0;
+    for (int k = 0; k < b->passes; k++) {
+        cudaError_t e = cudaEventQuery(b->pass[k].p.shown);
+        if (e == cudaErrorNotReady) n++;
+        else if (e != cudaSuccess) return cuda_fail(e, "cudaEventQuery");
+    }
+    *passes = n;
+    return VV_OK;
+}
+
+// One batched pass: request i adds requests[i].frames accumulate-frames to
+// renderer i, exactly as vv_record_frames would for a call of that many
+// frames (the same paths, random streams and sums), with the work items of
+// every request in the same waves. All renderers read one volume (a base and
+// its views) with the reference's storage formats. Each renderer's merge,
+// denoiser and display follow on the engine's stream, and its context stream
+// waits for them, so vv_query / vv_synchronize on the renderer see the pass.
+extern "C" vv_status vv_batch_record(vv_batch* b, uint32_t n, vv_renderer* const* renderers,
+                                     const vv_batch_request* requests) {
+    if (!b || !renderers || !requests) return fail(VV_ERR_ARG, "null argument");
+    if (n == 0) return VV_OK;
+    if (n > (uint32_t)VV_BATCH_MAX) return fail(VV_ERR_LIMIT, "at most 8 requests per batched pass");
+    const vv_renderer* root = nullptr;
+    for (uint32_t i = 0; i < n; i++) {
+        vv_renderer* r = renderers[i];
+        const vv_batch_request& q = requests[i];
+        if (!r || !q.params) return fail(VV_ERR_ARG, "null renderer or frame parameters");
+        for (uint32_t j = 0; j < i; j++)
+            if (renderers[j] == r) return fail(VV_ERR_ARG, "a renderer appears twice in one batched pass");
+        const vv_renderer* rr = r->base ? r->base : r;
+        if (root && rr != root) return fail(VV_ERR_ARG, "the renderers of a batched pass share one volume");
+        root = rr;
+        if (r->ctx->device != b->ctx->device) return fail(VV_ERR_ARG, "renderer and batch engine on different devices");
+        if (build_of(r->vol) != 0)
+            return fail(VV_ERR_ARG, "batched passes take the reference's storage (R16_UNORM density, RG16_UNORM mask)");
+        if (!q.params->path_tracing.enabled) return fail(VV_ERR_ARG, "a batched pass path-traces (path_tracing.enabled = 0)");
+        if (q.frames == 0 || q.frames > VV_SUBPASS_FRAMES) return fail(VV_ERR_ARG, "frames per request must be 1..64");
+        if (!r->accum.p) return fail(VV_ERR_STATE, "resize() must be called before record()");
+        if (check_denoiser(r, q.params) != VV_OK) return VV_ERR_STATE;
+        const uint64_t px = (uint64_t)r->width * r->height;
+        if (px >= (1ull << 28) || px * q.frames >= (1ull << 31))
+            return fail(VV_ERR_LIMIT, "a batched request has fewer than 2^28 pixels and 2^31 work items");
+        if (std::max(q.params->path_tracing.samples_per_frame, 1u) >= WF_MAX_SAMPLES)
+            return fail(VV_ERR_LIMIT, "a batched request takes fewer than 2^20 samples per frame");
+    }
+    CK(cudaSetDevice(b->ctx->device));
+    auto& E = b->pass[b->next % b->passes];
+    b->next = (b->next + 1) % b->passes;
+    cudaStream_t s = E.p.stream;
+    PtBatch B;
+    std::memset(&B, 0, sizeof(B));
+    B.n = n;
+    std::vector<UHead> heads(n);
+    std::vector<vv_renderer::Pass*> own(n), prev(n);
+    std::vector<size_t> cap(n);
+    size_t total = 0, budget = (size_t)1 << 24;
+    for (uint32_t i = 0; i < n; i++) {
+        vv_renderer* r = renderers[i];
+        const vv_batch_request& q = requests[i];
+        vv_status st = prepare_frame(r, *q.params, q.first_frame + q.frames - 1, heads[i]);
+        if (st != VV_OK) return st;
+        own[i] = &r->pass[r->next_pass % r->passes];
+        prev[i] = &r->pass[(r->next_pass + r->passes - 1) % r->passes];
+        r->next_pass = (r->next_pass + 1) % r->passes;
+        if (r->prep_work) {
+            CK(cudaEventRecord(r->prep_done, r->ctx->stream));
+            CK(cudaStreamWaitEvent(s, r->prep_done, 0));
+            r->prep_work = false;
+        }
+        CK(pass_args(r, *own[i], heads[i], q.frames, s, B.a[i]));
+        const size_t px = (size_t)r->width * r->height;
+        const size_t items = px * q.frames;
+        cap[i] = std::min(items, px * (size_t)std::min(b->slot_frames, r->slot_frames));
+        total += cap[i];
+        budget = std::max(budget, px);
+    }
+    // Paths in flight: each request's share of at most 2^24 slots (4.8 GB of
+    // path state), and at least one frame's worth (or all its items).
+    size_t end = 0;
+    for (uint32_t i = 0; i < n; i++) {
+        if (total > budget) {
+            const size_t px = (size_t)renderers[i]->width * renderers[i]->height;
+            const size_t floor_i = std::min(px * requests[i].frames, px);
+            cap[i] = std::max(floor_i, (size_t)((double)cap[i] * (double)budget / (double)total));
+        }
+        end += cap[i];
+        B.slot_end[i] = (uint32_t)end;
+    }
+    WfArgs w;
+    CK(wf_state(E.p, end, root->vol, s, w));
+    w.items = E.items.as<uint32_t>();
+    w.consts = E.consts.p;
+    int launches = 0;
+    CK(fmt0::launch_pt_wavefront_batch(B, w, b->ctx->sms, s, &launches));
+    b->launches += launches;
+    for (uint32_t i = 0; i < n; i++) {
+        vv_status st = end_pass(renderers[i], *own[i], *prev[i], *requests[i].params, heads[i], requests[i].frames,
+                                requests[i].display != 0, s, 0);
+        if (st != VV_OK) return st;
+    }
+    CK(cudaEventRecord(E.p.shown, s));
     return VV_OK;
 }
 

@@ -125,6 +125,23 @@ struct WfArgs {
     uint32_t nbins;
     int cell_shift;        // log2 of a cell's edge in voxels
     int cells_x, cells_y, cells_z;
+    // Batched passes only: each request's next work item (VV_BATCH_MAX words)
+    // and its constants derived from the uniforms (VV_BATCH_MAX records of
+    // WF_CONSTS_BYTES), written by the pass's first launch.
+    uint32_t* items;
+    void* consts;
+};
+// A batched pass (vv_batch_record): the work items of up to VV_BATCH_MAX
+// requests on one volume share the pass's slots, queues and waves. Each
+// request has its own uniforms, label tables, masks, majorants, image and
+// frame count (its PtArgs) and owns the slots [slot_end[r - 1], slot_end[r])
+// (slot_end[-1] = 0); a slot serves its request for the whole pass.
+constexpr int VV_BATCH_MAX = 8;
+constexpr int WF_CONSTS_BYTES = 256;
+struct PtBatch {
+    uint32_t n;
+    uint32_t slot_end[VV_BATCH_MAX];
+    PtArgs a[VV_BATCH_MAX];
 };
 // A lighting volume as the image loop reads it: a 3D texture of its texels
 // inside a one-texel white border, filtered by the texture units (clamped
@@ -170,6 +187,11 @@ namespace fmt2 { VV_FORMAT_LAUNCHERS }
 namespace fmt3 { VV_FORMAT_LAUNCHERS }
 namespace fmt4 { VV_FORMAT_LAUNCHERS }  // FP16 density and FP16 mask
 namespace fmt5 { VV_FORMAT_LAUNCHERS }  // BF16 density and BF16 mask
+// Batched passes run with the reference's storage (R16_UNORM density,
+// RG16_UNORM mask): the wavefront of every request of the batch at once.
+namespace fmt0 {
+cudaError_t launch_pt_wavefront_batch(const PtBatch& b, const WfArgs& w, int sms, cudaStream_t s, int* launches);
+}
 // The parity build of the single-path probe (vv_pt_exact.cu), per format: the
 // oracle's texture-unit arithmetic, no fused multiply-adds.
 #define VV_EXACT_LAUNCHERS \

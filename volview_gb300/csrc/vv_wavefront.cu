@@ -228,6 +228,37 @@ __device__ __forceinline__ uint32_t flight_bin(const WfArgs& W, f3 origin, f3 di
     return ((uint32_t)((cz * W.cells_y + cy) * W.cells_x + cx) << 3) | oct;
 }
 
+// A pass serves one request (PtArgs) or a batch of requests on one volume
+// (PtBatch). The stage kernels are templates over the two: a slot's request
+// (request_of), its arguments (args_of) and its constants (consts_of). For a
+// single request these fold to the kernel's own parameter and the constants
+// it derives once, so that pass compiles to the same code as without batches.
+template <class X> struct IsBatch { static constexpr bool value = false; };
+template <> struct IsBatch<PtBatch> { static constexpr bool value = true; };
+
+__device__ __forceinline__ uint32_t request_of(const PtArgs&, uint32_t) { return 0u; }
+__device__ __forceinline__ uint32_t request_of(const PtBatch& B, uint32_t slot) {
+    uint32_t r = 0;
+#pragma unroll 1
+    while (r + 1u < B.n && slot >= B.slot_end[r]) r++;
+    return r;
+}
+__device__ __forceinline__ const PtArgs& args_of(const PtArgs& A, uint32_t) { return A; }
+__device__ __forceinline__ const PtArgs& args_of(const PtBatch& B, uint32_t r) { return B.a[r]; }
+__device__ __forceinline__ uint32_t slot_begin(const PtArgs&, uint32_t) { return 0u; }
+__device__ __forceinline__ uint32_t slot_begin(const PtBatch& B, uint32_t r) { return r ? B.slot_end[r - 1] : 0u; }
+static_assert(sizeof(Consts) <= WF_CONSTS_BYTES, "batched constants record");
+__device__ __forceinline__ const Consts& consts_of(const PtArgs&, const WfArgs&, uint32_t, const Consts& C0) {
+    return C0;
+}
+__device__ __forceinline__ const Consts& consts_of(const PtBatch&, const WfArgs& W, uint32_t r, const Consts&) {
+    return *reinterpret_cast<const Consts*>(static_cast<const char*>(W.consts) + (size_t)r * WF_CONSTS_BYTES);
+}
+// The constants a single-request kernel derives once (a batch reads each
+// request's from the table its first launch wrote).
+__device__ __forceinline__ Consts kernel_consts(const PtArgs& A) { return make_consts(A); }
+__device__ __forceinline__ Consts kernel_consts(const PtBatch&) { return Consts(); }
+
 // The end of a sample path: firefly clamp and sums (pt.comp:546-551), then
 // the pixel's next sample in the same slot (pt.comp:403). Returns true when
 // the slot has a new path; false when the work item (one pixel of one frame)
@@ -274,10 +305,30 @@ __device__ __forceinline__ uint32_t take_item(uint32_t* counter, uint32_t total,
     uint32_t item = base + __popc(m & ((1u << lane) - 1u));
     return (need && item < total) ? item : ~0u;
 }
+// take_item in a batched pass: each lane draws from its request's counter,
+// one atomicAdd per request present among the warp's needing lanes.
+__device__ __forceinline__ uint32_t take_item_of(uint32_t* counters, uint32_t r, uint32_t total, bool need) {
+    unsigned m = __ballot_sync(0xffffffffu, need);
+    if (!m) return ~0u;
+    int lane = (int)(threadIdx.x & 31u);
+    unsigned grp = __match_any_sync(0xffffffffu, need ? r : 0x80000000u | (uint32_t)lane);
+    int leader = __ffs(grp) - 1;
+    uint32_t base = 0;
+    if (need && lane == leader) base = atomicAdd(&counters[r], (uint32_t)__popc(grp));
+    base = __shfl_sync(0xffffffffu, base, leader);
+    uint32_t item = base + __popc(grp & ((1u << lane) - 1u));
+    return (need && item < total) ? item : ~0u;
+}
 
-// A lane whose item ended takes the next one and starts it in its slot.
-__device__ __forceinline__ bool refill(const PtArgs& A, const WfArgs& W, const Consts& C, uint32_t slot, bool need) {
-    uint32_t item = take_item(&W.counts[WF_ITEMS], A.frames * A.width * A.height, need);
+// A lane whose item ended takes its request's next one and starts it in its slot.
+template <class X>
+__device__ __forceinline__ bool refill(const X& B, const WfArgs& W, uint32_t r, const Consts& C, uint32_t slot,
+                                       bool need) {
+    const PtArgs& A = args_of(B, r);
+    const uint32_t total = A.frames * A.width * A.height;
+    uint32_t item;
+    if constexpr (IsBatch<X>::value) item = take_item_of(W.items, r, total, need);
+    else item = take_item(&W.counts[WF_ITEMS], total, need);
     if (item == ~0u) return false;
     Path P;
     PixelSums S;
@@ -292,16 +343,21 @@ __device__ __forceinline__ bool refill(const PtArgs& A, const WfArgs& W, const C
 // pixel takes one set of atomics per warp: the frames of a pixel are
 // neighbouring items and tend to end in the same warp (background pixels all
 // in the first wave). With one frame per pass each pixel has one slot, which
-// adds to the sums directly.
-__device__ void accumulate_items(const PtArgs& A, bool done, uint32_t item, const PixelSums& S) {
+// adds to the sums directly. In a batched pass (BATCH) the lanes are grouped
+// by request and pixel, and every request's pass sums take atomic adds (into
+// sums that start at zero, so one add per pixel is the same as a store).
+template <bool BATCH>
+__device__ void accumulate_items(const PtArgs& A, bool done, uint32_t item, const PixelSums& S, uint32_t r) {
     uint32_t pixel = item / A.frames;
-    if (A.frames == 1u) {
+    if (!BATCH && A.frames == 1u) {
         if (done) accumulate(A, pixel % A.width, pixel / A.width, S, false, A.write_hdr != 0, (float)(A.u.path[0] + A.u.path[2]));
         return;
     }
     if (!__any_sync(0xffffffffu, done)) return;
     int lane = (int)(threadIdx.x & 31u);
-    unsigned grp = __match_any_sync(0xffffffffu, done ? pixel : 0x80000000u | (uint32_t)lane);
+    // A batched request's pixels are below 2^28 (checked by the host).
+    uint32_t key = BATCH ? (r << 28) | pixel : pixel;
+    unsigned grp = __match_any_sync(0xffffffffu, done ? key : 0x80000000u | (uint32_t)lane);
     unsigned biggest = __reduce_max_sync(0xffffffffu, (unsigned)__popc(grp));
     float v[12] = {S.sum.x, S.sum.y, S.sum.z, S.background, S.albedo.x, S.albedo.y,
                    S.albedo.z, S.albedo.w, S.normal.x, S.normal.y, S.normal.z, S.normal.w};
@@ -311,7 +367,7 @@ __device__ void accumulate_items(const PtArgs& A, bool done, uint32_t item, cons
         unsigned higher = grp & ~((2u << lane) - 1u);
         int next = higher ? __ffs(higher) - 1 : -1;
         int rounds = 32 - __clz((int)biggest - 1);
-        for (int r = 0; r < rounds; r++) {
+        for (int k2 = 0; k2 < rounds; k2++) {
             int src = next >= 0 ? next : lane;
 #pragma unroll
             for (int k = 0; k < 12; k++) {
@@ -337,19 +393,36 @@ __device__ void accumulate_items(const PtArgs& A, bool done, uint32_t item, cons
     for (uint32_t base_ = (blockIdx.x * blockDim.x + threadIdx.x) & ~31u; base_ < (n);          \
          base_ += gridDim.x * blockDim.x)
 
-__global__ void __launch_bounds__(256) k_wf_init(const __grid_constant__ PtArgs A, const WfArgs W, uint32_t slots) {
-    Consts C = make_consts(A);
+template <class X>
+__global__ void __launch_bounds__(256) k_wf_init(const __grid_constant__ X B, const WfArgs W, uint32_t slots) {
+    Consts C0 = kernel_consts(B);
+    uint32_t last = ~0u;
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < slots; i += gridDim.x * blockDim.x) {
+        const uint32_t r = request_of(B, i);
+        const PtArgs& A = args_of(B, r);
+        if (IsBatch<X>::value && r != last) {
+            C0 = make_consts(A);
+            last = r;
+        }
+        const uint32_t item = i - slot_begin(B, r);  // a request's slots start at its item 0
         Path P;
         PixelSums S;
-        start_item(A, C, i, P, S);
-        store_new_item(W, i, P, i, S);
+        start_item(A, C0, item, P, S);
+        store_new_item(W, i, P, item, S);
         W.first[0][i] = i;
     }
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         for (int k = 0; k < WF_COUNTERS; k++) W.counts[k] = 0;
         W.counts[WF_FIRST0] = slots;
         W.counts[WF_ITEMS] = slots;
+    }
+    if constexpr (IsBatch<X>::value) {
+        if (blockIdx.x == 0 && threadIdx.x < B.n) {
+            const uint32_t r = threadIdx.x;
+            W.items[r] = B.slot_end[r] - slot_begin(B, r);
+            *reinterpret_cast<Consts*>(static_cast<char*>(W.consts) + (size_t)r * WF_CONSTS_BYTES) =
+                make_consts(B.a[r]);
+        }
     }
 }
 
@@ -370,9 +443,9 @@ enum { EXT_END = 3 };
 // sampler. Every wave launches both; with all of a pass's frames in flight
 // first flights occur in the first wave only (and with several samples per
 // pixel), so the other launch finds its queue empty.
-template <bool FIRST>
+template <bool FIRST, class X>
 __global__ void __launch_bounds__(128, VV_EXTEND_MIN_BLOCKS)
-    k_wf_extend(const __grid_constant__ PtArgs A, const WfArgs W, int cur, uint32_t tail) {
+    k_wf_extend(const __grid_constant__ X B, const WfArgs W, int cur, uint32_t tail) {
     if (W.counts[WF_STOP] != 0u) return;
     if (FIRST) {
         // The wave's first launch decides whether the waves go on: with at most
@@ -388,8 +461,8 @@ __global__ void __launch_bounds__(128, VV_EXTEND_MIN_BLOCKS)
     const uint32_t n = W.counts[FIRST ? WF_FIRST0 + cur : cur];
     const uint32_t* queue = FIRST ? W.first[cur] : W.sorted;
     uint32_t* taken = &W.counts[FIRST ? WF_TAKE_FIRST : WF_TAKE_EXT];
-    const Consts C = make_consts(A);
-    uint32_t slot = 0;
+    const Consts C0 = kernel_consts(B);
+    uint32_t slot = 0, r = 0;
     f3 origin, dir, spectral;
     Rng rng;
     uint32_t word = 0;  // P2.w: volumes, sample, hero
@@ -403,6 +476,9 @@ __global__ void __launch_bounds__(128, VV_EXTEND_MIN_BLOCKS)
             uint32_t k = take_item(taken, n, need);
             if (need && k != ~0u) {
                 slot = queue[k];
+                r = request_of(B, slot);
+                const PtArgs& A = args_of(B, r);
+                const Consts& C = consts_of(B, W, r, C0);
                 const float4* q = rec(W.path, slot, PATH_N);
                 float4 a = q[0], b = q[1], c = q[2];
                 origin = xyz(a);
@@ -422,11 +498,11 @@ __global__ void __launch_bounds__(128, VV_EXTEND_MIN_BLOCKS)
             drained = __any_sync(0xffffffffu, need && k == ~0u);
         }
         if (active) {
-            int r = ff_step(A, origin, dir, FIRST, (int)(word >> 30), spectral, F, V.idx, V.s, V.cap_plane, V.cut,
-                            rng);
-            if (r != FF_CONTINUE) {
+            int res = ff_step(args_of(B, r), origin, dir, FIRST, (int)(word >> 30), spectral, F, V.idx, V.s,
+                              V.cap_plane, V.cut, rng);
+            if (res != FF_CONTINUE) {
                 active = false;
-                done = r;
+                done = res;
             }
         }
         if (__any_sync(0xffffffffu, done != 0)) {
@@ -455,15 +531,17 @@ __global__ void __launch_bounds__(128, VV_EXTEND_MIN_BLOCKS)
     if (blockIdx.x == 0 && threadIdx.x == 0) W.counts[WF_SCATTER] = 0;
 }
 
-__global__ void __launch_bounds__(128, 4) k_wf_shade(const __grid_constant__ PtArgs A, const WfArgs W, int cur) {
+template <class X>
+__global__ void __launch_bounds__(128, 4) k_wf_shade(const __grid_constant__ X B, const WfArgs W, int cur) {
     if (W.counts[WF_STOP] != 0u) return;
     uint32_t n = W.counts[WF_SHADE];
-    Consts C = make_consts(A);
+    const Consts C0 = kernel_consts(B);
     WF_FOR_EACH(n) {
         uint32_t i = base_ + (threadIdx.x & 31u);
         bool valid = i < n;
         uint32_t slot = valid ? W.shade[i] : 0u;
         if (valid) {
+            const uint32_t r = request_of(B, slot);
             Path P;
             float4 b = rec(W.path, slot, PATH_N)[1];
             P.dir = xyz(b);
@@ -472,7 +550,7 @@ __global__ void __launch_bounds__(128, 4) k_wf_shade(const __grid_constant__ PtA
             load_vertex(W, slot, V, P.rng.s);
             PixelSums S;
             if (P.bounce == 0u) load_acc_guides(W, slot, S);
-            stage_shade(A, C, P, S, V);
+            stage_shade(args_of(B, r), consts_of(B, W, r, C0), P, S, V);
             store_shaded(W, slot, V, P.rng.s);
             if (P.bounce == 0u) store_acc_guides(W, slot, S);
         }
@@ -496,12 +574,13 @@ __global__ void __launch_bounds__(128, 4) k_wf_shade(const __grid_constant__ PtA
 #define VV_SHADOW_MIN_BLOCKS 8
 #endif
 // MAP: the frame has a light map (lighting.w == 2); the kernel without it is
-// the key light's shadow rays alone.
-template <bool MAP>
-__global__ void __launch_bounds__(128, VV_SHADOW_MIN_BLOCKS) k_wf_shadow(const __grid_constant__ PtArgs A, const WfArgs W) {
+// the key light's shadow rays alone. In a batched pass MAP is set when any
+// request has a light map, and each lane follows its own request's lighting.
+template <bool MAP, class X>
+__global__ void __launch_bounds__(128, VV_SHADOW_MIN_BLOCKS) k_wf_shadow(const __grid_constant__ X B, const WfArgs W) {
     if (W.counts[WF_STOP] != 0u) return;
     const uint32_t n = W.counts[WF_SHADOW];
-    uint32_t slot = 0;
+    uint32_t slot = 0, r = 0;
     f3 origin;
     Rng rng;
     Shadow T;
@@ -512,20 +591,23 @@ __global__ void __launch_bounds__(128, VV_SHADOW_MIN_BLOCKS) k_wf_shadow(const _
             uint32_t k = take_item(&W.counts[WF_TAKE_SHADOW], n, need);
             if (need && k != ~0u) {
                 slot = W.shadow[k];
+                r = request_of(B, slot);
                 const float4* q = rec(W.shd, slot, SHD_N);
                 float4 a = q[0], b = q[1];
                 origin = xyz(a);
                 rng.s = ubits(a.w);
-                tr_begin(A, origin, xyz(b), T);
+                tr_begin(args_of(B, r), origin, xyz(b), T);
                 active = true;
                 map_ray = false;
             }
             drained = __any_sync(0xffffffffu, need && k == ~0u);
         }
         bool done = false;
-        if (active && !tr_step(A, origin, T, rng)) {
+        if (active && !tr_step(args_of(B, r), origin, T, rng)) {
+            const PtArgs& A = args_of(B, r);
+            const bool map = MAP && (!IsBatch<X>::value || A.u.lighting[3] == 2u);
             float4* h = rec(W.sh, slot, SH_N);
-            if (!MAP) {
+            if (!map) {
                 h[0] = f4(T.result, fbits(rng.s));
                 h[1] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
                 done = true;
@@ -557,16 +639,20 @@ __global__ void __launch_bounds__(128, VV_SHADOW_MIN_BLOCKS) k_wf_shadow(const _
 
 // Scatter, and the end of the flights that left the volume or hit the bounce
 // limits in this wave's extend (queued after the scatter entries).
-__global__ void __launch_bounds__(128, 6) k_wf_scatter(const __grid_constant__ PtArgs A, const WfArgs W, int cur) {
+template <class X>
+__global__ void __launch_bounds__(128, 6) k_wf_scatter(const __grid_constant__ X B, const WfArgs W, int cur) {
     if (W.counts[WF_STOP] != 0u) return;
     uint32_t n_scatter = W.counts[WF_SCATTER], n = n_scatter + W.counts[WF_ESC0 + cur];
     int nxt = cur ^ 1;
-    Consts C = make_consts(A);
+    const Consts C0 = kernel_consts(B);
     WF_FOR_EACH(n) {
         uint32_t i = base_ + (threadIdx.x & 31u);
         bool valid = i < n;
         bool ended = i >= n_scatter;
         uint32_t slot = valid ? (ended ? W.esc[cur][i - n_scatter] : W.scatter[i]) : 0u;
+        const uint32_t r = request_of(B, slot);
+        const PtArgs& A = args_of(B, r);
+        const Consts& C = consts_of(B, W, r, C0);
         bool to_ext = false, to_first = false, done = false;
         uint32_t item = 0, key = 0;
         PixelSums S;
@@ -605,8 +691,8 @@ __global__ void __launch_bounds__(128, 6) k_wf_scatter(const __grid_constant__ P
                 store_acc_head(W, slot, P, item, S);
             }
         }
-        accumulate_items(A, done, item, S);
-        if (refill(A, W, C, slot, done)) to_first = true;
+        accumulate_items<IsBatch<X>::value>(A, done, item, S, r);
+        if (refill(B, W, r, C, slot, done)) to_first = true;
         push_key(W.ext[nxt], W.ext_key[nxt], &W.counts[nxt], slot, key, to_ext);
         push(W.first[nxt], &W.counts[WF_FIRST0 + nxt], slot, to_first);
     }
@@ -656,16 +742,22 @@ __global__ void __launch_bounds__(256) k_wf_bin_place(const WfArgs W, const uint
 }
 
 // The paths still alive, run to completion one thread each (the reference's
-// loop), including their pixels' remaining samples and frames.
-__global__ void __launch_bounds__(128, 4) k_wf_finish(const __grid_constant__ PtArgs A, const WfArgs W, int cur) {
+// loop), including their pixels' remaining samples and frames (a batched
+// pass's from each path's own request).
+template <class X>
+__global__ void __launch_bounds__(128, 4) k_wf_finish(const __grid_constant__ X B, const WfArgs W, int cur) {
     uint32_t stop = W.counts[WF_STOP];
     if (stop != 0u) cur = (int)stop - 1;  // else the waves ran out first: `cur` is the next wave's queue
     uint32_t n_first = W.counts[WF_FIRST0 + cur], n = n_first + W.counts[cur];
-    Consts C = make_consts(A);
-    bool multi = A.frames > 1u;
-    float n_total = (float)(A.u.path[0] + A.u.path[2]);
+    const Consts C0 = kernel_consts(B);
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         uint32_t slot = i < n_first ? W.first[cur][i] : W.ext[cur][i - n_first];
+        const uint32_t r = request_of(B, slot);
+        const PtArgs& A = args_of(B, r);
+        const Consts& C = consts_of(B, W, r, C0);
+        const bool multi = IsBatch<X>::value || A.frames > 1u;
+        const float n_total = (float)(A.u.path[0] + A.u.path[2]);
+        uint32_t* counter = IsBatch<X>::value ? &W.items[r] : &W.counts[WF_ITEMS];
         Path P;
         PixelSums S;
         uint32_t sample, item;
@@ -680,7 +772,7 @@ __global__ void __launch_bounds__(128, 4) k_wf_finish(const __grid_constant__ Pt
             } while (end_sample(A, C, P, S, item, sample));
             uint32_t pixel = item / A.frames;
             accumulate(A, pixel % A.width, pixel / A.width, S, multi, !multi && A.write_hdr != 0, n_total);
-            item = atomicAdd(&W.counts[WF_ITEMS], 1u);
+            item = atomicAdd(counter, 1u);
             if (item >= total) break;
             sample = 0u;
             start_item(A, C, item, P, S);
@@ -694,25 +786,23 @@ template <class K> static int blocks_per_sm(K kernel, int threads) {
     return n;
 }
 
-// Host side: waves of the four stages until few paths are left, then one
-// finishing launch. Checks the live count every `check` waves (one 4-byte read).
-cudaError_t launch_pt_wavefront(const PtArgs& a, const WfArgs& w, int sms, cudaStream_t s, int* launches) {
+// The waves of a pass over `slots` paths in flight and `items` work items
+// (the largest count of one request's items per slot sets the rounds): waves
+// of the four stages until few paths are left, then one finishing launch.
+template <class X>
+static cudaError_t run_waves(const X& a, const WfArgs& w, int sms, cudaStream_t s, int* launches, uint32_t slots,
+                             uint32_t rounds, bool map) {
     static int g_ext = 0, g_shade = 0, g_shadow = 0, g_scatter = 0, g_finish = 0;
     if (!g_ext) {
-        g_ext = sms * blocks_per_sm(k_wf_extend<false>, 128);
-        g_shade = sms * blocks_per_sm(k_wf_shade, 128);
-        g_shadow = sms * blocks_per_sm(k_wf_shadow<false>, 128);
-        g_scatter = sms * blocks_per_sm(k_wf_scatter, 128);
-        g_finish = sms * blocks_per_sm(k_wf_finish, 128);
+        g_ext = sms * blocks_per_sm(k_wf_extend<false, X>, 128);
+        g_shade = sms * blocks_per_sm(k_wf_shade<X>, 128);
+        g_shadow = sms * blocks_per_sm(k_wf_shadow<false, X>, 128);
+        g_scatter = sms * blocks_per_sm(k_wf_scatter<X>, 128);
+        g_finish = sms * blocks_per_sm(k_wf_finish<X>, 128);
     }
-    if (a.u.path[2] >= (uint32_t)WF_MAX_SAMPLES) return cudaErrorInvalidValue;  // the host routes these elsewhere
     const char* env = std::getenv("VV_WF_TAIL");
     uint32_t tail = env ? (uint32_t)std::atoi(env) : 1024u;
-    uint32_t pixels = a.width * a.height;
-    uint32_t items = a.frames * pixels;
-    uint32_t slots = items < w.capacity ? items : w.capacity;  // paths in flight
-    const bool map = a.u.lighting[3] == 2u;
-    k_wf_init<<<(slots + 255) / 256 < (uint32_t)(sms * 8) ? (slots + 255) / 256 : sms * 8, 256, 0, s>>>(a, w, slots);
+    k_wf_init<X><<<(slots + 255) / 256 < (uint32_t)(sms * 8) ? (slots + 255) / 256 : sms * 8, 256, 0, s>>>(a, w, slots);
     *launches += 1;
     // All waves are queued at once, with no host round trip: the first launch
     // of each wave stops the waves on the device once at most `tail` paths
@@ -721,16 +811,15 @@ cudaError_t launch_pt_wavefront(const PtArgs& a, const WfArgs& w, int sms, cudaS
     // for the pass: about 10 per round of slots plus the tail of long random
     // walks (a path has at most 4 surface and 80 volume events at g = 0.6);
     // if they still run out, the finishing launch takes what is left.
-    uint32_t rounds = (items + slots - 1) / slots;
     int waves = (int)std::min<uint32_t>(24u + 10u * rounds, 4096u);
     int cur = 0;
     for (int wave = 0; wave < waves; wave++) {
-        k_wf_extend<true><<<g_ext, 128, 0, s>>>(a, w, cur, tail);
-        k_wf_extend<false><<<g_ext, 128, 0, s>>>(a, w, cur, tail);
-        k_wf_shade<<<g_shade, 128, 0, s>>>(a, w, cur);
-        if (map) k_wf_shadow<true><<<g_shadow, 128, 0, s>>>(a, w);
-        else k_wf_shadow<false><<<g_shadow, 128, 0, s>>>(a, w);
-        k_wf_scatter<<<g_scatter, 128, 0, s>>>(a, w, cur);
+        k_wf_extend<true, X><<<g_ext, 128, 0, s>>>(a, w, cur, tail);
+        k_wf_extend<false, X><<<g_ext, 128, 0, s>>>(a, w, cur, tail);
+        k_wf_shade<X><<<g_shade, 128, 0, s>>>(a, w, cur);
+        if (map) k_wf_shadow<true, X><<<g_shadow, 128, 0, s>>>(a, w);
+        else k_wf_shadow<false, X><<<g_shadow, 128, 0, s>>>(a, w);
+        k_wf_scatter<X><<<g_scatter, 128, 0, s>>>(a, w, cur);
         *launches += 5;
         // The next wave's later flights, ordered by bin.
         k_wf_bin_count<<<sms * 4, 256, 0, s>>>(w, w.ext_key[cur ^ 1], cur ^ 1);
@@ -741,10 +830,42 @@ cudaError_t launch_pt_wavefront(const PtArgs& a, const WfArgs& w, int sms, cudaS
         cudaError_t e = cudaGetLastError();
         if (e != cudaSuccess) return e;
     }
-    k_wf_finish<<<g_finish, 128, 0, s>>>(a, w, cur);
+    k_wf_finish<X><<<g_finish, 128, 0, s>>>(a, w, cur);
     *launches += 1;
     return cudaGetLastError();
 }
+
+// Host side: one request's pass.
+cudaError_t launch_pt_wavefront(const PtArgs& a, const WfArgs& w, int sms, cudaStream_t s, int* launches) {
+    if (a.u.path[2] >= (uint32_t)WF_MAX_SAMPLES) return cudaErrorInvalidValue;  // the host routes these elsewhere
+    uint32_t pixels = a.width * a.height;
+    uint32_t items = a.frames * pixels;
+    uint32_t slots = items < w.capacity ? items : w.capacity;  // paths in flight
+    uint32_t rounds = (items + slots - 1) / slots;
+    return run_waves(a, w, sms, s, launches, slots, rounds, a.u.lighting[3] == 2u);
+}
+
+#if VV_DFMT == 0
+// A batched pass: request r's items start in its own slots and refill them
+// from its own counter. The host has checked the batch (at most VV_BATCH_MAX
+// requests, each with at least one slot and fewer than 2^28 pixels).
+cudaError_t launch_pt_wavefront_batch(const PtBatch& b, const WfArgs& w, int sms, cudaStream_t s, int* launches) {
+    if (b.n == 0 || b.n > (uint32_t)VV_BATCH_MAX || !w.items || !w.consts) return cudaErrorInvalidValue;
+    uint32_t rounds = 1, begin = 0;
+    bool map = false;
+    for (uint32_t r = 0; r < b.n; r++) {
+        const PtArgs& a = b.a[r];
+        if (a.u.path[2] >= (uint32_t)WF_MAX_SAMPLES) return cudaErrorInvalidValue;
+        uint32_t slots = b.slot_end[r] - begin, items = a.frames * a.width * a.height;
+        if (b.slot_end[r] <= begin || slots > items) return cudaErrorInvalidValue;
+        rounds = std::max(rounds, (items + slots - 1) / slots);
+        map = map || a.u.lighting[3] == 2u;
+        begin = b.slot_end[r];
+    }
+    if (begin > w.capacity) return cudaErrorInvalidValue;
+    return run_waves(b, w, sms, s, launches, begin, rounds, map);
+}
+#endif
 
 }  // namespace VV_FMT_NS
 }  // namespace vv

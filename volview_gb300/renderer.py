@@ -35,6 +35,14 @@ EXPORTS = [
     ("vv_renderer_create", C.c_int, [P, P, P, P]),
     ("vv_renderer_create_ex", C.c_int, [P, P, P, P, P]),
     ("vv_renderer_destroy", C.c_int, [P]),
+    ("vv_renderer_create_view", C.c_int, [P, P, P]),
+    ("vv_batch_create", C.c_int, [P, C.c_uint32, C.c_uint32, P]),
+    ("vv_batch_destroy", C.c_int, [P]),
+    ("vv_batch_record", C.c_int, [P, C.c_uint32, P, P]),
+    ("vv_batch_memory", C.c_int, [P, P]),
+    ("vv_batch_synchronize", C.c_int, [P]),
+    ("vv_batch_launches", C.c_uint64, [P]),
+    ("vv_batch_in_flight", C.c_int, [P, P]),
     ("vv_renderer_get_info", C.c_int, [P, P]),
     ("vv_default_camera", C.c_int, [P, P]),
     ("vv_set_transfer_function", C.c_int, [P, P]),
@@ -152,14 +160,20 @@ class Context:
 
 
 class Renderer:
-    def __init__(self, ctx, volume, tf, precision=None):
+    def __init__(self, ctx, volume, tf, precision=None, view_of=None):
         """`precision` (abi.Precision) selects the density storage and running sums;
-        None is the reference's (R16_UNORM, FP32 sums)."""
+        None is the reference's (R16_UNORM, FP32 sums). With `view_of` (a
+        Renderer) the renderer is a view of that renderer's volume
+        (vv_renderer_create_view): `volume`, `tf` and `precision` are unused."""
         self.ctx = ctx
         self.handle = C.c_void_p()
-        self.precision = precision if precision is not None else abi.precision()
-        check(load().vv_renderer_create_ex(ctx.handle, C.byref(volume), C.byref(tf), C.byref(self.precision),
-                                           C.byref(self.handle)))
+        if view_of is not None:
+            self.precision = view_of.precision
+            check(load().vv_renderer_create_view(ctx.handle, view_of.handle, C.byref(self.handle)))
+        else:
+            self.precision = precision if precision is not None else abi.precision()
+            check(load().vv_renderer_create_ex(ctx.handle, C.byref(volume), C.byref(tf), C.byref(self.precision),
+                                               C.byref(self.handle)))
         info = abi.RendererInfo()
         check(load().vv_renderer_get_info(self.handle, C.byref(info)))
         self.info = info
@@ -319,9 +333,59 @@ class Renderer:
         check(load().vv_count_events(self.handle, int(enable), _ptr(out), out.size))
         return None if enable else dict(zip(COUNT_NAMES, (int(v) for v in out)))
 
+    @classmethod
+    def view(cls, ctx, base):
+        """A view of `base`'s resident volume on context `ctx`."""
+        return cls(ctx, None, None, view_of=base)
+
     def destroy(self):
         if self.handle:
-            load().vv_renderer_destroy(self.handle)
+            check(load().vv_renderer_destroy(self.handle))
+            self.handle = C.c_void_p()
+
+
+class BatchEngine:
+    """vv_batch: batched passes over several renderers of one volume."""
+
+    def __init__(self, ctx, passes=2, slot_frames=16):
+        self.ctx = ctx
+        self.handle = C.c_void_p()
+        check(load().vv_batch_create(ctx.handle, passes, slot_frames, C.byref(self.handle)))
+
+    def record(self, items):
+        """One batched pass over `items`: (renderer, params, first_frame,
+        frames, display) tuples."""
+        n = len(items)
+        handles = (C.c_void_p * max(n, 1))(*[r.handle for r, *_ in items])
+        reqs = (abi.BatchRequest * max(n, 1))()
+        keep = []
+        for k, (r, params, first, frames, display) in enumerate(items):
+            keep.append(params)
+            reqs[k].params = C.cast(C.pointer(params), C.c_void_p)
+            reqs[k].first_frame = first
+            reqs[k].frames = frames
+            reqs[k].display = 1 if display else 0
+        check(load().vv_batch_record(self.handle, n, handles, reqs))
+
+    def device_bytes(self):
+        n = C.c_uint64()
+        check(load().vv_batch_memory(self.handle, C.byref(n)))
+        return int(n.value)
+
+    def synchronize(self):
+        check(load().vv_batch_synchronize(self.handle))
+
+    def kernel_launches(self):
+        return int(load().vv_batch_launches(self.handle))
+
+    def in_flight(self):
+        n = C.c_uint32()
+        check(load().vv_batch_in_flight(self.handle, C.byref(n)))
+        return int(n.value)
+
+    def destroy(self):
+        if self.handle:
+            check(load().vv_batch_destroy(self.handle))
             self.handle = C.c_void_p()
 
 

@@ -19,6 +19,12 @@ The loop itself is host logic over the C ABI: `vv_query` polls for finished
 work without blocking, and `vv_renderer_memory` reports what each renderer
 holds. Renderers come from a factory, so the scheduling is tested on the CPU
 with stand-ins (tests/test_serving.py).
+
+`BatchedServer` serves the same requests from one resident copy of each
+volume: a request runs on a view of the volume's base renderer
+(`vv_renderer_create_view`), and batched passes (`vv_batch_record`) trace the
+frames of several requests of a volume in the same waves, a pass at a time,
+so requests that arrive while others run join the next pass.
 """
 import collections
 import time
@@ -250,6 +256,254 @@ class Server:
             r.destroy()
         self.owned.clear()
         self.idle.clear()
+
+
+def view_image_bytes(width, height, passes=PASSES):
+    """Device bytes of a view's image for one request in batched passes: its
+    images and `passes` passes' sums, no path slots (the batch engine holds
+    those)."""
+    return width * height * (IMAGE_BYTES_PER_PIXEL - 48 * (PASSES - passes))
+
+
+def view_volume_bytes(dims):
+    """Device bytes of a view before any image: its two label masks (8 bytes
+    per bricked voxel; the base's density, normals and labels are shared)."""
+    bricked = 1
+    for d in dims:
+        bricked *= -(-int(d) // 8) * 8
+    return 8 * bricked
+
+
+class BatchedServer:
+    """Requests served by batched passes (vv_batch_record) over shared volumes.
+
+    Each resident volume has one base renderer (its density, normals, labels
+    and transfer function on the device once); a request runs on a view of it
+    (vv_renderer_create_view: its own masks, images and sums, no copy of the
+    volume), reused by later requests of that volume. Requests advance in
+    passes of up to `frames_per_pass` frames: every step, while fewer than
+    `in_flight` batched passes are queued, one pass takes the next frames of
+    up to `max_batch` admitted requests of one volume, so requests of any
+    size and paths per pixel share waves and a request that arrives while
+    others run joins the next pass. A request's last pass displays it.
+
+    Factories: `make_base(volume)` a base renderer with its labels set,
+    `make_view(base)` a view of it, `engine` the batch engine (`record`,
+    `in_flight`, `device_bytes`). `base_bytes(volume)` and `view_bytes(volume)`
+    are the memory of a base and of a view before any image; the engine's
+    path state is reserved up front (`engine_bytes`)."""
+
+    def __init__(self, make_base, make_view, engine, budget_bytes, base_bytes, view_bytes, engine_bytes,
+                 max_active=None, keep_accumulation=False, clock=time.perf_counter, order="fifo", aging_s=2.0,
+                 frames_per_pass=16, max_batch=8, in_flight=2, view_passes=2):
+        if order not in ("fifo", "shortest"):
+            raise ValueError(f"unknown admission order {order!r}")
+        self.make_base, self.make_view, self.engine = make_base, make_view, engine
+        self.budget, self.base_bytes, self.view_bytes = int(budget_bytes), base_bytes, view_bytes
+        self.engine_bytes = int(engine_bytes)
+        self.max_active, self.keep_accumulation, self.clock = max_active, keep_accumulation, clock
+        self.order, self.aging_s = order, aging_s
+        self.frames_per_pass, self.max_batch, self.in_flight = frames_per_pass, max_batch, in_flight
+        self.view_passes = view_passes
+        self.bases = {}                        # volume -> base renderer
+        self.views = {}                        # view -> volume
+        self.idle = collections.OrderedDict()  # idle view -> volume, least recently used first
+        self.queue = collections.deque()
+        self.active = []
+        self.done, self.refused = [], []
+        self.next_id = 0
+        self.peak_bytes = 0
+        self.created = 0                       # views made
+        self.passes = 0                        # batched passes queued
+        self.batch_sizes = []
+
+    # ------------------------------------------------------------- accounting
+    def used_bytes(self):
+        return (self.engine_bytes + sum(b.device_bytes() for b in self.bases.values()) +
+                sum(v.device_bytes() for v in self.views))
+
+    def _need(self, req, view):
+        want = view_image_bytes(req.width, req.height, self.view_passes)
+        fresh = self.view_bytes(req.volume) + want
+        if view is not None:
+            return max(0, fresh - view.device_bytes())
+        return fresh + (0 if req.volume in self.bases else self.base_bytes(req.volume))
+
+    def _evict(self, need, keep):
+        """Destroys idle views (least recently used first, never `keep`), then
+        bases without views, until `need` more bytes fit."""
+        used = self.used_bytes()
+        for v in list(self.idle):
+            if used + need <= self.budget:
+                break
+            if v is keep:
+                continue
+            used -= v.device_bytes()
+            del self.idle[v]
+            del self.views[v]
+            v.destroy()
+        for name in list(self.bases):
+            if used + need <= self.budget:
+                break
+            if any(vol == name for vol in self.views.values()):
+                continue
+            if any(q.volume == name for q in self.queue):
+                continue
+            used -= self.bases[name].device_bytes()
+            self.bases.pop(name).destroy()
+        return used + need <= self.budget
+
+    # --------------------------------------------------------------- the loop
+    def submit(self, req):
+        req.id = self.next_id
+        self.next_id += 1
+        req.submitted = self.clock()
+        req.queued_frames = 0
+        self.queue.append(req)
+        return req.id
+
+    def preload(self, volume):
+        """Makes `volume` resident (its base renderer) before requests come."""
+        if volume not in self.bases:
+            self.bases[volume] = self.make_base(volume)
+        return self.bases[volume]
+
+    def _candidates(self):
+        if self.order == "fifo":
+            return list(self.queue)
+        now = self.clock()
+        aged = [q for q in self.queue if now - q.submitted > self.aging_s]
+        young = sorted((q for q in self.queue if now - q.submitted <= self.aging_s), key=lambda q: (q.paths, q.id))
+        return aged + young
+
+    def _idle_view(self, volume):
+        for v, name in self.idle.items():
+            if name == volume:
+                return v
+        return None
+
+    def _admit(self):
+        for req in self._candidates():
+            if self.max_active is not None and len(self.active) >= self.max_active:
+                return
+            view = self._idle_view(req.volume)
+            need = self._need(req, view)
+            if not self._evict(need, view):
+                if not self.active and all(v is view for v in self.idle):
+                    self.queue.remove(req)
+                    self.refused.append(req)
+                    raise MemoryError(f"request {req.id} needs {need} bytes, budget {self.budget}")
+                continue
+            self.queue.remove(req)
+            if view is None:
+                view = self.make_view(self.preload(req.volume))
+                if self.view_passes != PASSES:
+                    view.set_pass_budget(self.view_passes, SLOT_FRAMES)
+                self.views[view] = req.volume
+                self.created += 1
+            else:
+                del self.idle[view]
+            req.renderer = view
+            req.started = self.clock()
+            req.queued_frames = 0
+            view.reset_view()
+            view.resize(req.width, req.height)
+            self.active.append(req)
+            self.peak_bytes = max(self.peak_bytes, self.used_bytes())
+
+    def _dispatch(self):
+        """Queues batched passes while fewer than `in_flight` are running:
+        each takes the next frames of up to `max_batch` requests of the volume
+        whose waiting request is oldest."""
+        while self.engine.in_flight() < self.in_flight:
+            waiting = [q for q in self.active if q.queued_frames < q.spp]
+            if not waiting:
+                return
+            volume = min(waiting, key=lambda q: q.id).volume
+            batch = [q for q in waiting if q.volume == volume][:self.max_batch]
+            items = []
+            for q in batch:
+                n = min(self.frames_per_pass, q.spp - q.queued_frames)
+                items.append((q.renderer, q.params, 1 + q.queued_frames, n, q.queued_frames + n == q.spp))
+                q.queued_frames += n
+            self.engine.record(items)
+            self.passes += 1
+            self.batch_sizes.append(len(items))
+
+    def _collect(self):
+        finished = []
+        for req in list(self.active):
+            if req.queued_frames < req.spp or not req.renderer.idle():
+                continue
+            v = req.renderer
+            req.image = v.read_output()
+            if self.keep_accumulation:
+                req.accumulation = v.read_accumulation()
+            req.finished = self.clock()
+            self.active.remove(req)
+            self.idle[v] = req.volume
+            self.idle.move_to_end(v)
+            req.renderer = None
+            finished.append(req)
+        self.done += finished
+        return finished
+
+    def step(self):
+        """Collects finished requests, admits queued ones and queues passes."""
+        finished = self._collect()
+        self._admit()
+        self._dispatch()
+        return finished
+
+    run = Server.run
+
+    def close(self):
+        for v in list(self.views):
+            v.destroy()
+        self.views.clear()
+        self.idle.clear()
+        for b in list(self.bases.values()):
+            b.destroy()
+        self.bases.clear()
+        self.engine.destroy()
+
+
+def batched_factory(volumes, device=0, passes=2, slot_frames=16):
+    """(make_base, make_view, engine, base_bytes, view_bytes, engine_bytes) for
+    resident `volumes` ({name: scene config}) served by batched passes: bases
+    and views each on a context (CUDA stream) of its own, and one engine."""
+    from . import abi
+    from . import renderer as R
+
+    class Owned(R.Renderer):
+        def destroy(self):
+            super().destroy()
+            self.ctx.destroy()
+
+    def make_base(name):
+        cfg = volumes[name]
+        r = Owned(R.Context(device), cfg["volume"], cfg["tf"])
+        soft = cfg.get("soft")
+        r.set_labels(cfg["labels_vol"], abi.soft_struct(soft) if soft is not None else None)
+        return r
+
+    def make_view(base):
+        return Owned(R.Context(device), None, None, view_of=base)
+
+    class OwnedEngine(R.BatchEngine):
+        def destroy(self):
+            super().destroy()
+            self.ctx.destroy()
+
+    engine = OwnedEngine(R.Context(device), passes, slot_frames)
+
+    def base(name):
+        return volume_bytes(volumes[name]["volume"].dims)
+
+    def view(name):
+        return view_volume_bytes(volumes[name]["volume"].dims)
+
+    return make_base, make_view, engine, base, view, passes * SLOT_CAP * SLOT_BYTES
 
 
 def volume_bytes(dims):

@@ -686,7 +686,7 @@ def run_serve(args):
                                      "at %.0f/s" % (SERVE_DIMS, SERVE_SIZES, SERVE_SPP, args.serve_rate),
                          "requests": args.serve, "budget_bytes": budget, "phantom_generation_s": gen_s}}
     modes = (("continuous_shortest_first", dict(order="shortest", aging_s=2.0, max_per_volume=1)),
-             ("batched_shortest_first", dict(batched=True, order="shortest", aging_s=2.0, frames_per_pass=16)),
+             ("batched_shortest_first", dict(batched=True, order="shortest", aging_s=2.0)),
              ("continuous_shortest_first_lean", dict(order="shortest", aging_s=2.0, max_per_volume=1, passes=2,
                                                      slot_frames=8)),
              ("continuous_fifo", dict(order="fifo", max_per_volume=1)),
@@ -698,7 +698,7 @@ def run_serve(args):
         if kw.pop("batched", False):
             # One resident copy of each volume, a view per concurrent request,
             # batched passes of up to 8 requests of a volume (vv_batch_record).
-            make_base, make_view, engine, base, view, reserve = S.batched_factory(volumes, passes=2)
+            make_base, make_view, engine, base, view, reserve = S.batched_factory(volumes)
             srv = S.BatchedServer(make_base, make_view, engine, budget, base, view, reserve, **kw)
             for name in volumes:
                 srv.preload(name).synchronize()

@@ -429,7 +429,7 @@ typedef struct vv_batch_request {
 /* Queues one pass whose waves trace the frames of every request at once:
  * request i accumulates into renderers[i] with the same paths, random streams
  * and sums as vv_record_frames (summed in a different order: equal to within
- * FP32 rounding). 1 to 8 distinct renderers of one volume (a base and its
+ * FP32 rounding). 1 to 8 distinct renderers, of any volumes (bases and
  * views), created with the reference's storage formats, resized, path
  * tracing enabled. Each renderer's context stream waits for its share, so
  * vv_query and vv_synchronize on it see the pass. VV_ERR_ARG / VV_ERR_LIMIT

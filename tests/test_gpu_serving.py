@@ -247,3 +247,40 @@ def test_batched_server_same_alone_and_in_a_mix(volumes):
         _same(alone[0], mix[2])
     finally:
         srv.close()
+
+
+def test_one_engine_pass_alternates_and_mixes_volumes(volumes):
+    """One engine pass (its path state and later-flight bins) serving two
+    volumes of different sizes in turn, then both in the same passes: each
+    request still gets its lone render's result."""
+    from volview_gb300 import renderer as R
+    ctx = R.Context(0)
+    engine = R.BatchEngine(ctx, passes=1, slot_frames=16)
+    bases, views, refs, reqs = [], [], [], []
+    try:
+        for name, yaw in (("small", 0.2), ("torso", -0.3), ("small", 0.5), ("torso", 0.9)):
+            cfg = volumes[name]
+            p = _params(cfg, yaw=yaw)
+            refs.append(_alone(cfg, p, 48, 40, 32))
+            base = R.Renderer(ctx, cfg["volume"], cfg["tf"])
+            base.set_labels(cfg["labels_vol"], abi.soft_struct(cfg["soft"]) if cfg.get("soft") is not None else None)
+            view = R.Renderer.view(ctx, base)
+            view.resize(48, 40)
+            bases.append(base)
+            views.append(view)
+            reqs.append(p)
+        engine.record([(views[0], reqs[0], 1, 16, False)])  # small alone, then torso alone
+        engine.record([(views[1], reqs[1], 1, 16, False)])
+        engine.record([(views[2], reqs[2], 1, 16, False), (views[3], reqs[3], 1, 16, False)])  # mixed
+        engine.record([(v, p, 17, 16, True) for v, p in zip(views, reqs)])
+        engine.synchronize()
+        for v, ref in zip(views, refs):
+            v.synchronize()
+            _same(_Result(*ref), _Result(v.read_accumulation()[0], v.read_output()))
+    finally:
+        engine.destroy()
+        for v in views:
+            v.destroy()
+        for b in bases:
+            b.destroy()
+        ctx.destroy()

@@ -324,7 +324,7 @@ def test_batched_passes_cover_every_frame_once_and_display_last():
     assert len(bases) == 2 and srv.created <= len(reqs)
     for p in engine.passes:
         assert 1 <= len(p) <= 3
-        assert len({name[0] for name, *_ in p}) == 1  # one volume per batched pass
+    assert any(len({name[0] for name, *_ in p}) == 2 for p in engine.passes)  # volumes share passes
     for q in reqs:  # the request's passes, in order, on its view
         chunks = [(first, n, display) for p in engine.passes for name, params, first, n, display in p
                   if params == q.params]

@@ -268,14 +268,15 @@ struct vv_renderer {
     // call's pass overlaps the tail of the previous one.
     struct Pass {
         DBuf slots, map, queues, counts, accum, albedo, normal, binq, bins;
+        uint32_t nbins = 0;  // the bin count `bins` is laid out for (counts, then insertion points)
         cudaStream_t stream = nullptr;
         cudaEvent_t shown = nullptr;  // after the pass's merge and display
     } pass[VV_PASSES];
     int next_pass = 0;
     int passes = VV_PASSES;  // passes in use (vv_set_pass_budget)
     int slot_frames = 16;    // frames' worth of path slots per pass (vv_set_pass_budget)
-    bool prep_work = false;  // device work queued on the context stream by this call's set-up
-    cudaEvent_t prep_done = nullptr;
+    bool prep_work = false;  // set-up queued on the context stream since prep_done was last recorded
+    cudaEvent_t prep_done = nullptr;  // the latest set-up's end, which every pass waits for
     // accumulation
     uint32_t accumulated = 0;
     bool have_params = false;
@@ -1411,7 +1412,15 @@ static cudaError_t wf_state(vv_renderer::Pass& P, size_t cap, const Vol& v, cuda
         if (ce == cudaSuccess && P.bins.n < (size_t)nbins * 2 * sizeof(uint32_t)) {
             ce = cudaStreamSynchronize(s);
             if (ce == cudaSuccess) ce = P.bins.alloc((size_t)nbins * 2 * sizeof(uint32_t));
-            if (ce == cudaSuccess) ce = cudaMemsetAsync(P.bins.p, 0, P.bins.n, s);  // the counts start at zero
+            P.nbins = 0;
+        }
+        // The counts start at zero and every wave's scan leaves them at zero,
+        // but only for the layout of the volume they were last used with: the
+        // insertion points follow the counts, so a pass over another volume
+        // (a batch engine's passes change volumes) zeroes the buffer first.
+        if (ce == cudaSuccess && P.nbins != nbins) {
+            ce = cudaMemsetAsync(P.bins.p, 0, P.bins.n, s);
+            P.nbins = nbins;
         }
         if (ce != cudaSuccess) return ce;
         uint32_t* bq = P.binq.as<uint32_t>();
@@ -1796,17 +1805,26 @@ static cudaError_t pass_args(vv_renderer* r, vv_renderer::Pass& P, const UHead& 
 static vv_status end_pass(vv_renderer* r, vv_renderer::Pass& P, vv_renderer::Pass& prev, const vv_frame_params& p,
                           UHead& u, uint32_t frames, bool display, cudaStream_t s, int launches);
 
+// Every pass waits for the renderer's latest set-up on its context stream
+// (masks, majorants, label tables, zeroed running sums): passes run on
+// several streams, so the one right after the set-up is not the only one
+// that may read what it writes.
+static cudaError_t wait_for_set_up(vv_renderer* r, cudaStream_t s) {
+    if (r->prep_work) {
+        cudaError_t e = cudaEventRecord(r->prep_done, r->ctx->stream);
+        if (e != cudaSuccess) return e;
+        r->prep_work = false;
+    }
+    return cudaStreamWaitEvent(s, r->prep_done, 0);
+}
+
 static vv_status record_pass(vv_renderer* r, const vv_frame_params& p, UHead& u, uint32_t frames,
                              bool display = true) {
     vv_renderer::Pass& P = r->pass[r->next_pass % r->passes];
     vv_renderer::Pass& prev = r->pass[(r->next_pass + r->passes - 1) % r->passes];
     r->next_pass = (r->next_pass + 1) % r->passes;
     cudaStream_t s = P.stream;
-    if (r->prep_work) {
-        CK(cudaEventRecord(r->prep_done, r->ctx->stream));
-        CK(cudaStreamWaitEvent(s, r->prep_done, 0));
-        r->prep_work = false;
-    }
+    CK(wait_for_set_up(r, s));
     const char* single = std::getenv("VV_PT_KERNEL");
     if (single) CK(cudaStreamWaitEvent(s, prev.shown, 0));  // the single-kernel tracers share one work counter
     PtArgs a;
@@ -2020,8 +2038,8 @@ extern "C" vv_status vv_batch_in_flight(vv_batch* b, uint32_t* passes) {
 // One batched pass: request i adds requests[i].frames accumulate-frames to
 // renderer i, exactly as vv_record_frames would for a call of that many
 // frames (the same paths, random streams and sums), with the work items of
-// every request in the same waves. All renderers read one volume (a base and
-// its views) with the reference's storage formats. Each renderer's merge,
+// every request in the same waves. The renderers (of any resident volumes)
+// use the reference's storage formats. Each renderer's merge,
 // denoiser and display follow on the engine's stream, and its context stream
 // waits for them, so vv_query / vv_synchronize on the renderer see the pass.
 extern "C" vv_status vv_batch_record(vv_batch* b, uint32_t n, vv_renderer* const* renderers,
@@ -2029,16 +2047,19 @@ extern "C" vv_status vv_batch_record(vv_batch* b, uint32_t n, vv_renderer* const
     if (!b || !renderers || !requests) return fail(VV_ERR_ARG, "null argument");
     if (n == 0) return VV_OK;
     if (n > (uint32_t)VV_BATCH_MAX) return fail(VV_ERR_LIMIT, "at most 8 requests per batched pass");
-    const vv_renderer* root = nullptr;
+    // The bin grid of the later flights spans the largest volume of the batch
+    // (each request's own volume, geometry and transfer function are in its
+    // arguments; the grid only orders the flights).
+    Vol grid = make_vol(1, 1, 1);
     for (uint32_t i = 0; i < n; i++) {
         vv_renderer* r = renderers[i];
         const vv_batch_request& q = requests[i];
         if (!r || !q.params) return fail(VV_ERR_ARG, "null renderer or frame parameters");
         for (uint32_t j = 0; j < i; j++)
             if (renderers[j] == r) return fail(VV_ERR_ARG, "a renderer appears twice in one batched pass");
-        const vv_renderer* rr = r->base ? r->base : r;
-        if (root && rr != root) return fail(VV_ERR_ARG, "the renderers of a batched pass share one volume");
-        root = rr;
+        grid.nx = std::max(grid.nx, r->vol.nx);
+        grid.ny = std::max(grid.ny, r->vol.ny);
+        grid.nz = std::max(grid.nz, r->vol.nz);
         if (r->ctx->device != b->ctx->device) return fail(VV_ERR_ARG, "renderer and batch engine on different devices");
         if (build_of(r->vol) != 0)
             return fail(VV_ERR_ARG, "batched passes take the reference's storage (R16_UNORM density, RG16_UNORM mask)");
@@ -2071,11 +2092,7 @@ extern "C" vv_status vv_batch_record(vv_batch* b, uint32_t n, vv_renderer* const
         own[i] = &r->pass[r->next_pass % r->passes];
         prev[i] = &r->pass[(r->next_pass + r->passes - 1) % r->passes];
         r->next_pass = (r->next_pass + 1) % r->passes;
-        if (r->prep_work) {
-            CK(cudaEventRecord(r->prep_done, r->ctx->stream));
-            CK(cudaStreamWaitEvent(s, r->prep_done, 0));
-            r->prep_work = false;
-        }
+        CK(wait_for_set_up(r, s));
         CK(pass_args(r, *own[i], heads[i], q.frames, s, B.a[i]));
         const size_t px = (size_t)r->width * r->height;
         const size_t items = px * q.frames;
@@ -2096,7 +2113,7 @@ extern "C" vv_status vv_batch_record(vv_batch* b, uint32_t n, vv_renderer* const
         B.slot_end[i] = (uint32_t)end;
     }
     WfArgs w;
-    CK(wf_state(E.p, end, root->vol, s, w));
+    CK(wf_state(E.p, end, grid, s, w));
     w.items = E.items.as<uint32_t>();
     w.consts = E.consts.p;
     int launches = 0;

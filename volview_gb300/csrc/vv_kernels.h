@@ -132,10 +132,11 @@ struct WfArgs {
     void* consts;
 };
 // A batched pass (vv_batch_record): the work items of up to VV_BATCH_MAX
-// requests on one volume share the pass's slots, queues and waves. Each
-// request has its own uniforms, label tables, masks, majorants, image and
-// frame count (its PtArgs) and owns the slots [slot_end[r - 1], slot_end[r])
-// (slot_end[-1] = 0); a slot serves its request for the whole pass.
+// requests share the pass's slots, queues and waves. Each request has its own
+// volume, transfer function, uniforms, label tables, masks, majorants, image
+// and frame count (its PtArgs) and owns the slots [slot_end[r - 1],
+// slot_end[r]) (slot_end[-1] = 0); a slot serves its request for the whole
+// pass.
 constexpr int VV_BATCH_MAX = 8;
 constexpr int WF_CONSTS_BYTES = 256;
 struct PtBatch {

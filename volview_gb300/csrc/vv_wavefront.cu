@@ -737,8 +737,10 @@ __global__ void __launch_bounds__(256) k_wf_bin_place(const WfArgs W, const uint
                                                       int count) {
     if (W.counts[WF_STOP] != 0u) return;
     const uint32_t n = W.counts[count];
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
-        W.sorted[atomicAdd(&W.bin_next[keys[i]], 1u)] = queue[i];
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const uint32_t at = atomicAdd(&W.bin_next[keys[i]], 1u);
+        if (at < W.capacity) W.sorted[at] = queue[i];  // always below n when the counts started at zero
+    }
 }
 
 // The paths still alive, run to completion one thread each (the reference's

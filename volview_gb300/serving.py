@@ -23,8 +23,8 @@ with stand-ins (tests/test_serving.py).
 `BatchedServer` serves the same requests from one resident copy of each
 volume: a request runs on a view of the volume's base renderer
 (`vv_renderer_create_view`), and batched passes (`vv_batch_record`) trace the
-frames of several requests of a volume in the same waves, a pass at a time,
-so requests that arrive while others run join the next pass.
+frames of up to 8 requests, of any volumes, in the same waves, a pass at a
+time, so requests that arrive while others run join the next pass.
 """
 import collections
 import time
@@ -283,9 +283,9 @@ class BatchedServer:
     volume), reused by later requests of that volume. Requests advance in
     passes of up to `frames_per_pass` frames: every step, while fewer than
     `in_flight` batched passes are queued, one pass takes the next frames of
-    up to `max_batch` admitted requests of one volume, so requests of any
-    size and paths per pixel share waves and a request that arrives while
-    others run joins the next pass. A request's last pass displays it.
+    up to `max_batch` admitted requests, of any volumes, so requests of any
+    volume, size and paths per pixel share waves and a request that arrives
+    while others run joins the next pass. A request's last pass displays it.
 
     Factories: `make_base(volume)` a base renderer with its labels set,
     `make_view(base)` a view of it, `engine` the batch engine (`record`,
@@ -295,7 +295,7 @@ class BatchedServer:
 
     def __init__(self, make_base, make_view, engine, budget_bytes, base_bytes, view_bytes, engine_bytes,
                  max_active=None, keep_accumulation=False, clock=time.perf_counter, order="fifo", aging_s=2.0,
-                 frames_per_pass=16, max_batch=8, in_flight=2, view_passes=2):
+                 frames_per_pass=64, max_batch=8, in_flight=4, view_passes=None, pass_paths=1 << 25):
         if order not in ("fifo", "shortest"):
             raise ValueError(f"unknown admission order {order!r}")
         self.make_base, self.make_view, self.engine = make_base, make_view, engine
@@ -304,7 +304,10 @@ class BatchedServer:
         self.max_active, self.keep_accumulation, self.clock = max_active, keep_accumulation, clock
         self.order, self.aging_s = order, aging_s
         self.frames_per_pass, self.max_batch, self.in_flight = frames_per_pass, max_batch, in_flight
-        self.view_passes = view_passes
+        self.pass_paths = pass_paths
+        # A view's pass sums: one per batched pass it may be in at once, so
+        # that no pass waits for an earlier one to free its request's sums.
+        self.view_passes = view_passes if view_passes is not None else min(PASSES, max(1, in_flight))
         self.bases = {}                        # volume -> base renderer
         self.views = {}                        # view -> volume
         self.idle = collections.OrderedDict()  # idle view -> volume, least recently used first
@@ -411,21 +414,49 @@ class BatchedServer:
             self.active.append(req)
             self.peak_bytes = max(self.peak_bytes, self.used_bytes())
 
+    @staticmethod
+    def _remaining(q):
+        return (q.spp - q.queued_frames) * q.width * q.height
+
+    def _lead(self, waiting):
+        """The request the next pass is for: the oldest (fifo), or the one
+        with the fewest paths left, requests queued longer than `aging_s`
+        first in arrival order (shortest)."""
+        if self.order == "fifo":
+            return min(waiting, key=lambda q: q.id)
+        now = self.clock()
+        aged = [q for q in waiting if now - q.submitted > self.aging_s]
+        if aged:
+            return min(aged, key=lambda q: q.id)
+        return min(waiting, key=lambda q: (self._remaining(q), q.id))
+
     def _dispatch(self):
         """Queues batched passes while fewer than `in_flight` are running:
-        each takes the next frames of up to `max_batch` requests of the volume
-        whose waiting request is oldest."""
+        each takes the next frames of the lead request (`_lead`) and of up to
+        `max_batch` - 1 more requests, of any volume, those with the fewest
+        paths left first, up to about `pass_paths` paths in all (at least one
+        frame of the lead). A pass ends when its longest request's frames do,
+        so short passes let short requests finish in their first one while
+        long ones advance over many."""
         while self.engine.in_flight() < self.in_flight:
             waiting = [q for q in self.active if q.queued_frames < q.spp]
             if not waiting:
                 return
-            volume = min(waiting, key=lambda q: q.id).volume
-            batch = [q for q in waiting if q.volume == volume][:self.max_batch]
-            items = []
-            for q in batch:
-                n = min(self.frames_per_pass, q.spp - q.queued_frames)
+            lead = self._lead(waiting)
+            rest = sorted((q for q in waiting if q is not lead), key=lambda q: (self._remaining(q), q.id))
+            items, left = [], self.pass_paths
+            for q in [lead] + rest:
+                if len(items) == self.max_batch:
+                    break
+                px = q.width * q.height
+                n = min(self.frames_per_pass, q.spp - q.queued_frames, left // px)
+                if n < 1:
+                    if items:
+                        continue
+                    n = 1
                 items.append((q.renderer, q.params, 1 + q.queued_frames, n, q.queued_frames + n == q.spp))
                 q.queued_frames += n
+                left -= n * px
             self.engine.record(items)
             self.passes += 1
             self.batch_sizes.append(len(items))
@@ -468,7 +499,7 @@ class BatchedServer:
         self.engine.destroy()
 
 
-def batched_factory(volumes, device=0, passes=2, slot_frames=16):
+def batched_factory(volumes, device=0, passes=4, slot_frames=16):
     """(make_base, make_view, engine, base_bytes, view_bytes, engine_bytes) for
     resident `volumes` ({name: scene config}) served by batched passes: bases
     and views each on a context (CUDA stream) of its own, and one engine."""

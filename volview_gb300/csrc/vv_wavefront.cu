@@ -752,7 +752,15 @@ __global__ void __launch_bounds__(128, 4) k_wf_finish(const __grid_constant__ X 
     if (stop != 0u) cur = (int)stop - 1;  // else the waves ran out first: `cur` is the next wave's queue
     uint32_t n_first = W.counts[WF_FIRST0 + cur], n = n_first + W.counts[cur];
     const Consts C0 = kernel_consts(B);
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    // With no more paths than warps (the usual tail: at most 1024 paths), each
+    // path runs alone in its warp, on every SM, instead of 32 to a warp on a
+    // few SMs, where the lanes would take turns through each other's divergent
+    // random walks. More paths (the waves ran out first) take a lane each.
+    const uint32_t tid = blockIdx.x * blockDim.x + threadIdx.x, threads = gridDim.x * blockDim.x;
+    const bool alone = n <= (threads >> 5);
+    if (alone && (threadIdx.x & 31u) != 0u) return;
+    const uint32_t first = alone ? tid >> 5 : tid, stride = alone ? threads >> 5 : threads;
+    for (uint32_t i = first; i < n; i += stride) {
         uint32_t slot = i < n_first ? W.first[cur][i] : W.ext[cur][i - n_first];
         const uint32_t r = request_of(B, slot);
         const PtArgs& A = args_of(B, r);

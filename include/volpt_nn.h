@@ -50,6 +50,12 @@ vv_status vv_nn_avgpool2(const void* x, int n, int h, int w, int c, void* y, int
 vv_status vv_nn_upsample2(const void* x, int n, int h, int w, int c, void* y, int backward, void* stream);
 /* y[p] = a[p] (ca channels) followed by b[p] (cb channels). */
 vv_status vv_nn_concat(const void* a, int ca, const void* b, int cb, long pixels, void* y, void* stream);
+/* y (n, 2h, 2w, ca + cb) = vv_nn_upsample2 of a (n, h, w, ca) followed by b
+ * (n, 2h, 2w, cb), channel-wise, in one pass (the decoder's input): ca and cb
+ * multiples of 8, a, b and y 16-byte aligned; VV_ERR_ARG otherwise (then
+ * vv_nn_upsample2 and vv_nn_concat give the same tensor). */
+vv_status vv_nn_upsample_concat(const void* a, int n, int h, int w, int ca, const void* b, int cb, void* y,
+                                void* stream);
 /* The gradient of vv_nn_concat: da, db (either may be NULL) from dy. */
 vv_status vv_nn_split(const void* dy, int ca, int cb, long pixels, void* da, void* db, void* stream);
 /* The network's 16-channel input from an accumulation of n paths per pixel

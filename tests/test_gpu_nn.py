@@ -114,6 +114,17 @@ def test_pool_upsample_concat_relu(lib):
     CAT = torch.empty((n, h, w, c + 16), dtype=torch.float16, device="cuda")
     assert lib.vv_nn_concat(X.data_ptr(), c, Y.data_ptr(), 16, n * h * w, CAT.data_ptr(), S) == 0
     assert np.array_equal(host(CAT), np.concatenate([x, y], -1))
+    # Upsampling and concat in one pass: the same tensor as the two passes.
+    Z = dev(rand_half(rng, (n, 2 * h, 2 * w, 16)), "half")
+    UC = torch.empty((n, 2 * h, 2 * w, c + 16), dtype=torch.float16, device="cuda")
+    assert lib.vv_nn_upsample_concat(X.data_ptr(), n, h, w, c, Z.data_ptr(), 16, UC.data_ptr(), S) == 0
+    assert np.array_equal(host(UC), np.concatenate([N.upsample2(x), host(Z)], -1))
+    assert lib.vv_nn_upsample_concat(X.data_ptr(), n, h, w, 12, Z.data_ptr(), 16, UC.data_ptr(), S) != 0  # ca % 8
+    # Pooling with a channel count that is not a multiple of 8 (the per-element path).
+    x6 = rand_half(rng, (n, h, w, 6))
+    P6 = torch.empty((n, h // 2, w // 2, 6), dtype=torch.float16, device="cuda")
+    assert lib.vv_nn_avgpool2(dev(x6, "half").data_ptr(), n, h, w, 6, P6.data_ptr(), 0, S) == 0
+    assert np.array_equal(host(P6), N.half(N.avgpool2(x6)))
     DA, DB = torch.empty_like(X), torch.empty_like(Y)
     assert lib.vv_nn_split(CAT.data_ptr(), c, 16, n * h * w, DA.data_ptr(), DB.data_ptr(), S) == 0
     assert np.array_equal(host(DA), x) and np.array_equal(host(DB), y)
@@ -251,3 +262,27 @@ def test_tensor_core_convolution_refuses_other_shapes(lib):
     assert lib.vv_nn_conv3x3_tc(X.data_ptr(), 1, 16, 96, 16, X.data_ptr(), None, 16, 0, X.data_ptr(), S) != 0  # w
     assert lib.vv_nn_conv3x3_tc(X.data_ptr(), 1, 16, 128, 176, X.data_ptr(), None, 80, 0, X.data_ptr(), S) != 0  # smem
     assert lib.vv_nn_conv3x3_tc(X.data_ptr(), 1, 16, 128, 16, X.data_ptr(), None, 112, 0, X.data_ptr(), S) != 0  # cout
+
+
+@pytest.mark.parametrize("cin,cout", [(80, 32), (32, 32)])
+def test_tensor_core_convolution_long_runs(lib, cin, cout):
+    """Tall images give every CTA a run of several segments, so the ring of row
+    slots reloads slots as the run walks down its column: three slots for
+    80 -> 32 (two CTAs per SM), four for 32 -> 32. Checked against PyTorch's
+    FP32 convolution (same padding) at the convolution tolerance."""
+    import ctypes as C
+    torch.manual_seed(cin + cout)
+    n, h, w = 1, 1536, 128
+    x = (torch.randn((n, h, w, cin), device="cuda") * 0.5).half()
+    wt = (torch.randn((cout, 3, 3, cin), device="cuda") * 0.1).half()
+    b = torch.randn(cout, device="cuda", dtype=torch.float32)
+    y = torch.empty((n, h, w, cout), dtype=torch.float16, device="cuda")
+    assert lib.vv_nn_conv3x3_tc(x.data_ptr(), n, h, w, cin, wt.data_ptr(), b.data_ptr(), cout, 1, y.data_ptr(),
+                                S) == 0
+    ref = torch.nn.functional.conv2d(x.float().permute(0, 3, 1, 2), wt.float().permute(0, 3, 1, 2), b, padding=1)
+    ref = torch.relu(ref).permute(0, 2, 3, 1)
+    torch.cuda.synchronize()
+    got, want = y.float().cpu().numpy(), ref.cpu().numpy()
+    close(got.astype(np.float64), want.astype(np.float64), 2e-3, 2e-3)
+    failed = C.c_int(1)
+    assert lib.vv_nn_tc_status(C.byref(failed), 1) == 0 and failed.value == 0

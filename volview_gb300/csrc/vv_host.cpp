@@ -1740,7 +1740,6 @@ static vv_status run_unet(vv_renderer* r, float n, cudaStream_t s, int* launches
             CK(U.eb[l].alloc(px * UNET_LEVELS[l] * 2));
             if (l) CK(U.pool[l].alloc(px * UNET_LEVELS[l - 1] * 2));
             if (l < 4) {
-                CK(U.up[l].alloc(px * UNET_LEVELS[l + 1] * 2));
                 CK(U.cat[l].alloc(px * (UNET_LEVELS[l + 1] + UNET_LEVELS[l]) * 2));
                 CK(U.da[l].alloc(px * UNET_LEVELS[l] * 2));
                 CK(U.db[l].alloc(px * UNET_LEVELS[l] * 2));
@@ -1775,10 +1774,12 @@ static vv_status run_unet(vv_renderer* r, float n, cudaStream_t s, int* launches
     const DBuf* y = &U.eb[4];
     int cy = UNET_LEVELS[4];
     for (int l = 3; l >= 0 && v == VV_OK; l--) {
-        v = ok(vv_nn_upsample2(y->p, 1, hp >> (l + 1), wp >> (l + 1), cy, U.up[l].p, 0, st), "upsampling");
-        long px = (long)(wp >> l) * (hp >> l);
-        if (v == VV_OK) v = ok(vv_nn_concat(U.up[l].p, cy, U.eb[l].p, UNET_LEVELS[l], px, U.cat[l].p, st), "concat");
-        *launches += 2;
+        // The level's channel counts are multiples of 8 and the buffers are
+        // cudaMalloc'd: the upsampling and the concat in one pass.
+        v = ok(vv_nn_upsample_concat(y->p, 1, hp >> (l + 1), wp >> (l + 1), cy, U.eb[l].p, UNET_LEVELS[l],
+                                     U.cat[l].p, st),
+               "upsampling and concat");
+        *launches += 1;
         int k = 10 + 2 * (3 - l);
         if (v == VV_OK) v = conv(U.cat[l], l, k, U.da[l], 1);
         if (v == VV_OK) v = conv(U.da[l], l, k + 1, U.db[l], 1);

@@ -15,6 +15,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <algorithm>
+
 #include "../../include/volpt_nn.h"
 
 namespace vv {
@@ -38,25 +40,27 @@ __device__ __forceinline__ uint32_t pack(__half lo, __half hi) {
 }
 
 // y = act(conv3x3(x, w) + bias). A block of CONV_WARPS warps takes as many
-// 16-pixel row segments, one per warp, and all COUT channels. For each of the
-// 9 taps the block first copies that tap's weights (COUT x CIN) into shared
-// memory, rows padded to CIN + 8 halves so that the B fragment loads of a
-// warp fall in distinct banks; each warp then reduces over CIN in steps of 16
-// on the tensor cores, its A fragments (the input pixels at the tap's offset,
-// zeros outside the image: same padding) read as aligned 32-bit words.
+// 16-pixel row segments, one per warp, and NT x 8 of the cout output channels
+// (from blockIdx.y * NT * 8: small images split their channels over several
+// blocks so that the grid covers the GPU). For each of the 9 taps the block
+// first copies that tap's weights of its channels (NT x 8 x CIN) into shared
+// memory, rows padded to CIN + 8 halves so that the B fragment loads of a warp
+// fall in distinct banks; each warp then reduces over CIN in steps of 16 on the
+// tensor cores, its A fragments (the input pixels at the tap's offset, zeros
+// outside the image: same padding) read as aligned 32-bit words.
 // Fragment layouts of m16n8k16 (g = lane / 4, t = lane % 4): A row g / g + 8,
 // columns 2t, 2t + 1 / + 8; B column g, rows 2t, 2t + 1 / + 8; C row g / g + 8,
 // columns 2t, 2t + 1.
 constexpr int CONV_WARPS = 8;
-template <int COUT>
+template <int NT>
 __global__ void __launch_bounds__(CONV_WARPS * 32) k_conv3x3(const __half* __restrict__ x, int n, int h, int w, int cin,
                                                              const __half* __restrict__ wt,
                                                              const float* __restrict__ bias, int relu,
-                                                             __half* __restrict__ y) {
-    constexpr int NT = COUT / 8;
+                                                             __half* __restrict__ y, int cout) {
     extern __shared__ __align__(16) unsigned char smem[];
     __half* sw = (__half*)smem;
     const int stride = cin + 8;  // halves per staged weight row
+    const int co0 = blockIdx.y * NT * 8;
     const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
     const long tile = (long)blockIdx.x * CONV_WARPS + (threadIdx.x >> 5);  // 16-pixel tile
     const long pixels = (long)n * h * w;
@@ -68,12 +72,13 @@ __global__ void __launch_bounds__(CONV_WARPS * 32) k_conv3x3(const __half* __res
     float acc[NT][4];
 #pragma unroll
     for (int j = 0; j < NT; j++) acc[j][0] = acc[j][1] = acc[j][2] = acc[j][3] = 0.0f;
-    const int chunks = COUT * (cin / 8);  // 16-byte pieces of one tap's weights
+    const int chunks = NT * 8 * (cin / 8);  // 16-byte pieces of one tap's weights of the block's channels
     for (int tap = 0; tap < 9; tap++) {
         __syncthreads();  // the previous tap's weights are no longer read
         for (int i = threadIdx.x; i < chunks; i += CONV_WARPS * 32) {
             int co = i / (cin / 8), c8 = i % (cin / 8);
-            *(uint4*)(sw + co * stride + c8 * 8) = __ldg((const uint4*)(wt + ((long)co * 9 + tap) * cin + c8 * 8));
+            *(uint4*)(sw + co * stride + c8 * 8) =
+                __ldg((const uint4*)(wt + ((long)(co0 + co) * 9 + tap) * cin + c8 * 8));
         }
         __syncthreads();
         if (!active) continue;
@@ -98,12 +103,12 @@ __global__ void __launch_bounds__(CONV_WARPS * 32) k_conv3x3(const __half* __res
         }
     }
     if (!active) return;
-    __half* o0 = y + (p0 + g) * COUT;
-    __half* o1 = y + (p0 + g + 8) * COUT;
+    __half* o0 = y + (p0 + g) * cout + co0;
+    __half* o1 = y + (p0 + g + 8) * cout + co0;
 #pragma unroll
     for (int j = 0; j < NT; j++) {
         const int co = j * 8 + 2 * t;
-        float b0 = bias ? bias[co] : 0.0f, b1 = bias ? bias[co + 1] : 0.0f;
+        float b0 = bias ? bias[co0 + co] : 0.0f, b1 = bias ? bias[co0 + co + 1] : 0.0f;
         float v[4] = {acc[j][0] + b0, acc[j][1] + b1, acc[j][2] + b0, acc[j][3] + b1};
         if (relu)
             for (int k = 0; k < 4; k++) v[k] = fmaxf(v[k], 0.0f);
@@ -220,6 +225,35 @@ __global__ void k_avgpool2(const __half* __restrict__ x, int n, int h, int w, in
     float s = __half2float(b[0]) + __half2float(b[c]) + __half2float(b[(long)w * c]) + __half2float(b[(long)w * c + c]);
     y[i] = __float2half_rn(0.25f * s);
 }
+// k_avgpool2 for channel counts that are a multiple of 8: 8 channels (16
+// bytes) per thread from each of the 2x2 inputs, the same sums in the same
+// order.
+__global__ void k_avgpool2_q(const uint4* __restrict__ x, int n, int h, int w, int q, uint4* __restrict__ y) {
+    const int ho = h / 2, wo = w / 2;
+    const long total = (long)n * ho * wo * q;
+    for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (long)gridDim.x * blockDim.x) {
+        const long p = i / q;
+        const int k = (int)(i - p * q);
+        const long row = p / wo;  // img * ho + yo
+        const int xo = (int)(p - row * wo);
+        const long img = row / ho;
+        const int yo = (int)(row - img * ho);
+        const uint4* b = x + (((img * h + 2 * yo) * w + 2 * xo) * q + k);
+        const uint4 v00 = __ldg(b), v01 = __ldg(b + q), v10 = __ldg(b + (long)w * q), v11 = __ldg(b + (long)w * q + q);
+        const __half* h00 = (const __half*)&v00;
+        const __half* h01 = (const __half*)&v01;
+        const __half* h10 = (const __half*)&v10;
+        const __half* h11 = (const __half*)&v11;
+        uint4 out;
+        __half* o = (__half*)&out;
+#pragma unroll
+        for (int j = 0; j < 8; j++) {
+            float sum = __half2float(h00[j]) + __half2float(h01[j]) + __half2float(h10[j]) + __half2float(h11[j]);
+            o[j] = __float2half_rn(0.25f * sum);
+        }
+        y[i] = out;
+    }
+}
 __global__ void k_avgpool2_backward(const __half* __restrict__ dy, int n, int h, int w, int c, __half* __restrict__ dx) {
     long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= (long)n * h * w * c) return;
@@ -247,6 +281,30 @@ __global__ void k_upsample2_backward(const __half* __restrict__ dy, int n, int h
     const __half* b = dy + (((long)img * 2 * h + 2 * yy) * 2 * w + 2 * xx) * c + ch;
     float s = __half2float(b[0]) + __half2float(b[c]) + __half2float(b[2L * w * c]) + __half2float(b[2L * w * c + c]);
     dx[i] = __float2half_rn(s);
+}
+
+// The decoder's input in one pass: y (n, 2h, 2w, 8 qa + 8 qb) = the nearest 2x
+// upsampling of a (n, h, w, 8 qa) followed by b (n, 2h, 2w, 8 qb), channel-wise;
+// 8 channels (16 bytes) per thread, each source read once, y written once.
+__global__ void k_upsample_concat(const uint4* __restrict__ a, int h, int w, int qa, const uint4* __restrict__ b,
+                                  int qb, long pixels, uint4* __restrict__ y) {
+    const int q = qa + qb;
+    const long total = pixels * q, w2 = 2L * w, h2 = 2L * h;
+    for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (long)gridDim.x * blockDim.x) {
+        const long p = i / q;
+        const int k = (int)(i - p * q);
+        uint4 v;
+        if (k < qa) {
+            const long row = p / w2;  // img * 2h + yy
+            const long xx = p - row * w2;
+            const long img = row / h2;
+            const long yy = row - img * h2;
+            v = __ldg(a + ((img * h + (yy >> 1)) * w + (xx >> 1)) * qa + k);
+        } else {
+            v = __ldg(b + p * qb + (k - qa));
+        }
+        y[i] = v;
+    }
 }
 
 // y[p] = a[p] ++ b[p] (channels), and the split of its gradient.
@@ -380,6 +438,10 @@ __global__ void k_prediction_to_hdr(const __half* __restrict__ pred, int c, int 
 }
 
 static inline unsigned blocks(long n, int t) { return (unsigned)((n + t - 1) / t); }
+static inline bool aligned16(const void* p) { return ((uintptr_t)p & 15u) == 0; }
+// Blocks of 256 threads for a grid-stride loop over n items: enough to fill
+// the GPU many times over, capped so that each thread takes a few items.
+static inline unsigned grid_for(long n) { return (unsigned)std::min<long>(std::max<long>((n + 255) / 256, 1), 152L * 64); }
 
 }  // namespace nn
 }  // namespace vv
@@ -404,23 +466,43 @@ extern "C" vv_status vv_nn_conv3x3(const void* x, int n, int h, int w, int cin, 
     cudaError_t te = cudaSuccess;
     if (conv3x3_tc((const __half*)x, n, h, w, cin, (const __half*)weights, bias, cout, relu, (__half*)y, s, &te))
         return te == cudaSuccess ? VV_OK : VV_ERR_CUDA;
-    unsigned g = blocks((long)n * h * w / 16, CONV_WARPS);
+    const unsigned g = blocks((long)n * h * w / 16, CONV_WARPS);
     const __half* X = (const __half*)x;
     const __half* W = (const __half*)weights;
     __half* Y = (__half*)y;
-    const size_t smem = (size_t)cout * (cin + 8) * sizeof(__half);
+    // All of cout per block, unless the grid would not cover the SMs: then the
+    // channels split into groups of 6 to 2 tiles of 8 (the largest that
+    // divides cout / 8 and gives a block per SM, else the smallest).
+    int sms = 152, dev = 0;
+    if (cudaGetDevice(&dev) == cudaSuccess) cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const int tiles = cout / 8;
+    int nt = tiles;
+    if ((long)g < sms) {
+        const int groups[5] = {6, 5, 4, 3, 2};
+        int pick = 0;
+        for (int k = 0; k < 5; k++) {
+            if (groups[k] >= tiles || tiles % groups[k]) continue;
+            pick = groups[k];
+            if ((long)g * (tiles / pick) >= sms) break;
+        }
+        if (pick) nt = pick;
+    }
+    const size_t smem = (size_t)nt * 8 * (cin + 8) * sizeof(__half);
     if (smem > 48 * 1024) return VV_ERR_ARG;  // one tap's weights staged in shared memory
-    switch (cout) {
-        case 8: k_conv3x3<8><<<g, CONV_WARPS * 32, smem, s>>>(X, n, h, w, cin, W, bias, relu, Y); break;
-        case 16: k_conv3x3<16><<<g, CONV_WARPS * 32, smem, s>>>(X, n, h, w, cin, W, bias, relu, Y); break;
-        case 32: k_conv3x3<32><<<g, CONV_WARPS * 32, smem, s>>>(X, n, h, w, cin, W, bias, relu, Y); break;
-        case 48: k_conv3x3<48><<<g, CONV_WARPS * 32, smem, s>>>(X, n, h, w, cin, W, bias, relu, Y); break;
-        case 64: k_conv3x3<64><<<g, CONV_WARPS * 32, smem, s>>>(X, n, h, w, cin, W, bias, relu, Y); break;
-        case 80: k_conv3x3<80><<<g, CONV_WARPS * 32, smem, s>>>(X, n, h, w, cin, W, bias, relu, Y); break;
-        case 96: k_conv3x3<96><<<g, CONV_WARPS * 32, smem, s>>>(X, n, h, w, cin, W, bias, relu, Y); break;
-        case 112: k_conv3x3<112><<<g, CONV_WARPS * 32, smem, s>>>(X, n, h, w, cin, W, bias, relu, Y); break;
-        case 144: k_conv3x3<144><<<g, CONV_WARPS * 32, smem, s>>>(X, n, h, w, cin, W, bias, relu, Y); break;
-        case 176: k_conv3x3<176><<<g, CONV_WARPS * 32, smem, s>>>(X, n, h, w, cin, W, bias, relu, Y); break;
+    const dim3 grid(g, tiles / nt);
+    switch (nt) {
+        case 1: k_conv3x3<1><<<grid, CONV_WARPS * 32, smem, s>>>(X, n, h, w, cin, W, bias, relu, Y, cout); break;
+        case 2: k_conv3x3<2><<<grid, CONV_WARPS * 32, smem, s>>>(X, n, h, w, cin, W, bias, relu, Y, cout); break;
+        case 3: k_conv3x3<3><<<grid, CONV_WARPS * 32, smem, s>>>(X, n, h, w, cin, W, bias, relu, Y, cout); break;
+        case 4: k_conv3x3<4><<<grid, CONV_WARPS * 32, smem, s>>>(X, n, h, w, cin, W, bias, relu, Y, cout); break;
+        case 5: k_conv3x3<5><<<grid, CONV_WARPS * 32, smem, s>>>(X, n, h, w, cin, W, bias, relu, Y, cout); break;
+        case 6: k_conv3x3<6><<<grid, CONV_WARPS * 32, smem, s>>>(X, n, h, w, cin, W, bias, relu, Y, cout); break;
+        case 8: k_conv3x3<8><<<grid, CONV_WARPS * 32, smem, s>>>(X, n, h, w, cin, W, bias, relu, Y, cout); break;
+        case 10: k_conv3x3<10><<<grid, CONV_WARPS * 32, smem, s>>>(X, n, h, w, cin, W, bias, relu, Y, cout); break;
+        case 12: k_conv3x3<12><<<grid, CONV_WARPS * 32, smem, s>>>(X, n, h, w, cin, W, bias, relu, Y, cout); break;
+        case 14: k_conv3x3<14><<<grid, CONV_WARPS * 32, smem, s>>>(X, n, h, w, cin, W, bias, relu, Y, cout); break;
+        case 18: k_conv3x3<18><<<grid, CONV_WARPS * 32, smem, s>>>(X, n, h, w, cin, W, bias, relu, Y, cout); break;
+        case 22: k_conv3x3<22><<<grid, CONV_WARPS * 32, smem, s>>>(X, n, h, w, cin, W, bias, relu, Y, cout); break;
         default: return VV_ERR_ARG;
     }
     return launched();
@@ -465,8 +547,13 @@ extern "C" vv_status vv_nn_avgpool2(const void* x, int n, int h, int w, int c, v
     if (!x || !y || n <= 0 || h <= 0 || w <= 0 || h % 2 || w % 2 || c <= 0) return VV_ERR_ARG;
     cudaStream_t s = (cudaStream_t)stream;
     long out = backward ? (long)n * h * w * c : (long)n * (h / 2) * (w / 2) * c;
-    if (backward) k_avgpool2_backward<<<blocks(out, 256), 256, 0, s>>>((const __half*)x, n, h, w, c, (__half*)y);
-    else k_avgpool2<<<blocks(out, 256), 256, 0, s>>>((const __half*)x, n, h, w, c, (__half*)y);
+    if (backward) {
+        k_avgpool2_backward<<<blocks(out, 256), 256, 0, s>>>((const __half*)x, n, h, w, c, (__half*)y);
+    } else if (c % 8 == 0 && aligned16(x) && aligned16(y)) {
+        k_avgpool2_q<<<grid_for(out / 8), 256, 0, s>>>((const uint4*)x, n, h, w, c / 8, (uint4*)y);
+    } else {
+        k_avgpool2<<<blocks(out, 256), 256, 0, s>>>((const __half*)x, n, h, w, c, (__half*)y);
+    }
     return launched();
 }
 
@@ -487,6 +574,19 @@ extern "C" vv_status vv_nn_concat(const void* a, int ca, const void* b, int cb, 
     k_concat<<<blocks(total, 256), 256, 0, (cudaStream_t)stream>>>((const __half*)a, ca, (const __half*)b, cb,
                                                                    pixels, (__half*)y);
     return launched();
+}
+
+extern "C" vv_status vv_nn_upsample_concat(const void* a, int n, int h, int w, int ca, const void* b, int cb,
+                                           void* y, void* stream) {
+    if (!a || !b || !y || n <= 0 || h <= 0 || w <= 0 || ca <= 0 || cb <= 0) return VV_ERR_ARG;
+    cudaStream_t s = (cudaStream_t)stream;
+    const long pixels = 4L * n * h * w;
+    if (ca % 8 == 0 && cb % 8 == 0 && aligned16(a) && aligned16(b) && aligned16(y)) {
+        k_upsample_concat<<<grid_for(pixels * ((ca + cb) / 8)), 256, 0, s>>>(
+            (const uint4*)a, h, w, ca / 8, (const uint4*)b, cb / 8, pixels, (uint4*)y);
+        return launched();
+    }
+    return VV_ERR_ARG;  // other shapes: vv_nn_upsample2, then vv_nn_concat
 }
 
 extern "C" vv_status vv_nn_split(const void* dy, int ca, int cb, long pixels, void* da, void* db, void* stream) {

@@ -92,13 +92,16 @@ constexpr int TC_THREADS = EPI_THREADS + 32;  // + warp 4, the issuing warp
 __host__ __device__ constexpr uint32_t tmem_cols(int np) {
     return 2 * np <= 32 ? 32 : 2 * np <= 64 ? 64 : 2 * np <= 128 ? 128 : 2 * np <= 256 ? 256 : 512;
 }
-constexpr int RING = 4;  // row slots
+// Row slots of the ring: four (a segment reads three while the next row
+// loads), or three where that fits twice as many CTAs in an SM's shared memory
+// (the next row then loads once the segment's MMAs are done with its slot).
+constexpr int RING = 4;
 // Weights, the ring of row slots, and slack to align the ring to 1024 bytes.
-static size_t tc_smem(int np, int cin) {
-    return 9 * (size_t)np * 2 * cin + RING * (size_t)(cin / 8) * SLICE_STRIDE + 1024;
+static size_t tc_smem(int np, int cin, int ring = RING) {
+    return 9 * (size_t)np * 2 * cin + ring * (size_t)(cin / 8) * SLICE_STRIDE + 1024;
 }
 
-template <int NP>
+template <int NP, int RING>
 __global__ void __launch_bounds__(TC_THREADS) k_conv3x3_tc(const __grid_constant__ CUtensorMap rows, int n, int h,
                                                            int w, int cin, const __half* __restrict__ wt,
                                                            const float* __restrict__ bias, int cout, int relu,
@@ -199,9 +202,12 @@ __global__ void __launch_bounds__(TC_THREADS) k_conv3x3_tc(const __grid_constant
                                  mma0 + 8 * b)
                              : "memory");
                 if (i + 1 < ntiles) {
-                    // The next segment's new row goes into the slot of row i - 1,
-                    // which the previous segment's MMAs were the last to read.
-                    if (i >= 1) bar_wait(mma0 + 8 * ((i - 1) & 1), ((i - 1) >> 1) & 1);
+                    // The next segment's new row goes into the slot of row
+                    // i + 3 - RING, which segment i + 3 - RING's MMAs were the
+                    // last to read (the previous segment's with four slots, this
+                    // one's with three).
+                    const int last = i + 3 - RING;
+                    if (last >= 0) bar_wait(mma0 + 8 * (last & 1), (last >> 1) & 1);
                     load_row(i + 3);
                 }
             }
@@ -280,28 +286,28 @@ static bool encode_rows_map(CUtensorMap* map, const void* x, int n, int h, int w
                   CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
-template <int NP>
+// Resident CTAs per SM for `smem` bytes of dynamic shared memory: by shared
+// memory (with 1 KB per CTA the system reserves and the static barriers), by
+// threads, and by TMEM (at most 512 columns per SM between them, so that no
+// allocation waits).
+static int resident_ctas(size_t smem, int np, int sm_smem) {
+    int per_sm = sm_smem / (int)(smem + 2048);
+    per_sm = per_sm < 2048 / TC_THREADS ? per_sm : 2048 / TC_THREADS;
+    per_sm = per_sm < (int)(512 / tmem_cols(np)) ? per_sm : (int)(512 / tmem_cols(np));
+    return per_sm < 1 ? 1 : per_sm;
+}
+
+template <int NP, int RING>
 static cudaError_t launch_tc(const CUtensorMap& map, int n, int h, int w, int cin, const __half* wt, const float* bias,
-                             int cout, int relu, __half* y, cudaStream_t s) {
-    const size_t smem = tc_smem(NP, cin);
+                             int cout, int relu, __half* y, cudaStream_t s, int sms, int per_sm) {
+    const size_t smem = tc_smem(NP, cin, RING);
     static bool configured = false;
     if (!configured) {
-        cudaError_t e = cudaFuncSetAttribute(k_conv3x3_tc<NP>, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
+        cudaError_t e =
+            cudaFuncSetAttribute(k_conv3x3_tc<NP, RING>, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
         if (e != cudaSuccess) return e;
         configured = true;
     }
-    int dev = 0, sms = 0, sm_smem = 0;
-    cudaError_t e = cudaGetDevice(&dev);
-    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sm_smem, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
-    if (e != cudaSuccess) return e;
-    // Resident CTAs per SM: by shared memory (with 1 KB per CTA the system
-    // reserves and the static barriers), by threads, and by TMEM (at most 512
-    // columns per SM between them, so that no allocation waits).
-    int per_sm = sm_smem / (int)(smem + 2048);
-    per_sm = per_sm < 2048 / TC_THREADS ? per_sm : 2048 / TC_THREADS;
-    per_sm = per_sm < (int)(512 / tmem_cols(NP)) ? per_sm : (int)(512 / tmem_cols(NP));
-    per_sm = per_sm < 1 ? 1 : per_sm;
     // Runs of rows: every resident CTA takes one, the runs of a column of
     // segments as long as the CTAs per column allow.
     const long columns = (long)n * (w / TC_M);
@@ -309,8 +315,27 @@ static cudaError_t launch_tc(const CUtensorMap& map, int n, int h, int w, int ci
     const long per_column = std::max(1L, slots / columns);
     const int run_rows = (int)((h + per_column - 1) / per_column);
     const long grid = columns * ((h + run_rows - 1) / run_rows);
-    k_conv3x3_tc<NP><<<(unsigned)grid, TC_THREADS, smem, s>>>(map, n, h, w, cin, wt, bias, cout, relu, y, run_rows);
+    k_conv3x3_tc<NP, RING><<<(unsigned)grid, TC_THREADS, smem, s>>>(map, n, h, w, cin, wt, bias, cout, relu, y,
+                                                                    run_rows);
     return cudaGetLastError();
+}
+
+// Four row slots, or three where that fits more CTAs per SM (the U-Net's
+// full-resolution decoder, 80 -> 32 channels: one CTA per SM with four slots,
+// two with three).
+template <int NP>
+static cudaError_t launch_tc_ring(const CUtensorMap& map, int n, int h, int w, int cin, const __half* wt,
+                                  const float* bias, int cout, int relu, __half* y, cudaStream_t s) {
+    int dev = 0, sms = 0, sm_smem = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sm_smem, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
+    if (e != cudaSuccess) return e;
+    const int four = resident_ctas(tc_smem(NP, cin, 4), NP, sm_smem);
+    const int three = resident_ctas(tc_smem(NP, cin, 3), NP, sm_smem);
+    if (four == 1 && three > 1)
+        return launch_tc<NP, 3>(map, n, h, w, cin, wt, bias, cout, relu, y, s, sms, three);
+    return launch_tc<NP, 4>(map, n, h, w, cin, wt, bias, cout, relu, y, s, sms, four);
 }
 
 // The tensor-core convolution when the shape suits it (widths that are
@@ -325,12 +350,12 @@ bool conv3x3_tc(const __half* x, int n, int h, int w, int cin, const __half* wt,
     CUtensorMap map;
     if (!encode_rows_map(&map, x, n, h, w, cin)) return false;
     switch (np) {
-        case 16: *err = launch_tc<16>(map, n, h, w, cin, wt, bias, cout, relu, y, s); break;
-        case 32: *err = launch_tc<32>(map, n, h, w, cin, wt, bias, cout, relu, y, s); break;
-        case 48: *err = launch_tc<48>(map, n, h, w, cin, wt, bias, cout, relu, y, s); break;
-        case 64: *err = launch_tc<64>(map, n, h, w, cin, wt, bias, cout, relu, y, s); break;
-        case 80: *err = launch_tc<80>(map, n, h, w, cin, wt, bias, cout, relu, y, s); break;
-        case 96: *err = launch_tc<96>(map, n, h, w, cin, wt, bias, cout, relu, y, s); break;
+        case 16: *err = launch_tc_ring<16>(map, n, h, w, cin, wt, bias, cout, relu, y, s); break;
+        case 32: *err = launch_tc_ring<32>(map, n, h, w, cin, wt, bias, cout, relu, y, s); break;
+        case 48: *err = launch_tc_ring<48>(map, n, h, w, cin, wt, bias, cout, relu, y, s); break;
+        case 64: *err = launch_tc_ring<64>(map, n, h, w, cin, wt, bias, cout, relu, y, s); break;
+        case 80: *err = launch_tc_ring<80>(map, n, h, w, cin, wt, bias, cout, relu, y, s); break;
+        case 96: *err = launch_tc_ring<96>(map, n, h, w, cin, wt, bias, cout, relu, y, s); break;
         default: return false;
     }
     return true;

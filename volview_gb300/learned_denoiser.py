@@ -150,11 +150,15 @@ class UNet:
                 _check(self.lib.vv_nn_avgpool2(a.data_ptr(), n, h, w, c, y.data_ptr(), 0, s), name)
             else:
                 k = acts[op[3]]
-                u = t.empty((n, 2 * h, 2 * w, c), dtype=t.float16, device=self.device)
-                _check(self.lib.vv_nn_upsample2(a.data_ptr(), n, h, w, c, u.data_ptr(), 0, s), name)
                 y = t.empty((n, 2 * h, 2 * w, c + k.shape[3]), dtype=t.float16, device=self.device)
-                _check(self.lib.vv_nn_concat(u.data_ptr(), c, k.data_ptr(), k.shape[3], n * 4 * h * w, y.data_ptr(),
-                                             s), name)
+                if c % 8 == 0 and k.shape[3] % 8 == 0:  # upsampling and concat in one pass
+                    _check(self.lib.vv_nn_upsample_concat(a.data_ptr(), n, h, w, c, k.data_ptr(), k.shape[3],
+                                                          y.data_ptr(), s), name)
+                else:
+                    u = t.empty((n, 2 * h, 2 * w, c), dtype=t.float16, device=self.device)
+                    _check(self.lib.vv_nn_upsample2(a.data_ptr(), n, h, w, c, u.data_ptr(), 0, s), name)
+                    _check(self.lib.vv_nn_concat(u.data_ptr(), c, k.data_ptr(), k.shape[3], n * 4 * h * w,
+                                                 y.data_ptr(), s), name)
             acts[name] = y
         self.acts = acts
         return acts["head"]

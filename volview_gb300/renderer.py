@@ -89,6 +89,7 @@ NN = [
     ("vv_nn_avgpool2", I, [P, I, I, I, I, P, I, P]),
     ("vv_nn_upsample2", I, [P, I, I, I, I, P, I, P]),
     ("vv_nn_concat", I, [P, I, P, I, L, P, P]),
+    ("vv_nn_upsample_concat", I, [P, I, I, I, I, P, I, P, P]),
     ("vv_nn_split", I, [P, I, I, L, P, P, P]),
     ("vv_nn_features", I, [P, P, P, F, L, P, P]),
     ("vv_nn_l1_loss", I, [P, I, P, L, F, P, P, P]),

@@ -66,6 +66,8 @@ def parse():
     ap.add_argument("--denoised-rmse", type=int, default=0,
                     help="instead of the path-tracing bench, train the learned denoiser for this many steps on "
                          "the head/neck workload at 1024^2 and time the fixed RMSE with it on held-out views")
+    ap.add_argument("--denoised-train-views", type=int, default=12,
+                    help="training views of --denoised-rmse (4 held-out views)")
     ap.add_argument("--bench-denoiser", type=int, default=1000,
                     help="Adam steps of the reduced time-to-RMSE run with the learned denoiser in the default line "
                          "(4 training views, 1 held out, the plain tracer's 256-path error; 0: skip)")
@@ -876,7 +878,8 @@ def denoised_time_to_rmse(r, base, train_n, test_n, steps, plain_spp=1024):
 
 
 def run_denoised_rmse(args):
-    """denoised_time_to_rmse at full scale: 12 training views, 4 held out."""
+    """denoised_time_to_rmse at full scale: --denoised-train-views training
+    views (12 by default), 4 held out."""
     from volview_gb300 import abi
     from volview_gb300 import renderer as R
     cfg = workload(args)
@@ -886,7 +889,7 @@ def run_denoised_rmse(args):
     r.set_labels(cfg["labels_vol"], abi.soft_struct(cfg["soft"]))
     r.resize(W, H)
     base = frame_params(cfg, list(r.center), r.diagonal, args.light_map)
-    res = denoised_time_to_rmse(r, base, 12, 4, args.denoised_rmse)
+    res = denoised_time_to_rmse(r, base, args.denoised_train_views, 4, args.denoised_rmse)
     r.destroy()
     ctx.destroy()
     res["config"] = {"workload": bench_config(args, 1)["workload"]}

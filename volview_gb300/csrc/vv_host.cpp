@@ -1434,6 +1434,12 @@ static cudaError_t wf_state(vv_renderer::Pass& P, size_t cap, const Vol& v, cuda
         w.cells_x = cx;
         w.cells_y = cy;
         w.cells_z = cz;
+        // Queues of fewer than 16384 later flights go unordered (the late
+        // waves, whose chains of launches the ordering lengthened): 392.7 ->
+        // 394.2 M path samples/s, one vv_record per frame 7.08 -> 6.90 ms
+        // (65536: 393.0 and 7.07; 262144: 392.2 and 7.03).
+        const char* e = std::getenv("VV_WF_BIN_MIN");
+        w.bin_min = e ? (uint32_t)std::max(0, std::atoi(e)) : 16384u;
     }
     return cudaSuccess;
 }

@@ -125,6 +125,7 @@ struct WfArgs {
     uint32_t nbins;
     int cell_shift;        // log2 of a cell's edge in voxels
     int cells_x, cells_y, cells_z;
+    uint32_t bin_min;      // queues shorter than this are not ordered (the extend reads them as queued)
     // Batched passes only: each request's next work item (VV_BATCH_MAX words)
     // and its constants derived from the uniforms (VV_BATCH_MAX records of
     // WF_CONSTS_BYTES), written by the pass's first launch.

@@ -459,7 +459,7 @@ __global__ void __launch_bounds__(128, VV_EXTEND_MIN_BLOCKS)
         }
     }
     const uint32_t n = W.counts[FIRST ? WF_FIRST0 + cur : cur];
-    const uint32_t* queue = FIRST ? W.first[cur] : W.sorted;
+    const uint32_t* queue = FIRST ? W.first[cur] : n < W.bin_min ? W.ext[cur] : W.sorted;
     uint32_t* taken = &W.counts[FIRST ? WF_TAKE_FIRST : WF_TAKE_EXT];
     const Consts C0 = kernel_consts(B);
     uint32_t slot = 0, r = 0;
@@ -704,14 +704,18 @@ __global__ void __launch_bounds__(128, 6) k_wf_scatter(const __grid_constant__ X
 
 // Counting sort of the next wave's later-flight queue by bin: counts, an
 // exclusive scan (one block), then placement. Order within a bin is free.
+// Queues shorter than W.bin_min (the late waves' few long walks, where a
+// warp's lanes rarely share a region anyway) skip the three launches' work,
+// which would otherwise add to every wave's chain of dependent launches.
 __global__ void __launch_bounds__(256) k_wf_bin_count(const WfArgs W, const uint32_t* keys, int count) {
     if (W.counts[WF_STOP] != 0u) return;
     const uint32_t n = W.counts[count];
+    if (n < W.bin_min) return;
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
         atomicAdd(&W.bin_count[keys[i]], 1u);
 }
-__global__ void __launch_bounds__(1024) k_wf_bin_scan(const WfArgs W) {
-    if (W.counts[WF_STOP] != 0u) return;
+__global__ void __launch_bounds__(1024) k_wf_bin_scan(const WfArgs W, int count) {
+    if (W.counts[WF_STOP] != 0u || W.counts[count] < W.bin_min) return;
     __shared__ uint32_t part[1024];
     const uint32_t per = (W.nbins + 1023u) / 1024u, lo = threadIdx.x * per;
     const uint32_t hi = min(lo + per, W.nbins);
@@ -737,6 +741,7 @@ __global__ void __launch_bounds__(256) k_wf_bin_place(const WfArgs W, const uint
                                                       int count) {
     if (W.counts[WF_STOP] != 0u) return;
     const uint32_t n = W.counts[count];
+    if (n < W.bin_min) return;
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const uint32_t at = atomicAdd(&W.bin_next[keys[i]], 1u);
         if (at < W.capacity) W.sorted[at] = queue[i];  // always below n when the counts started at zero
@@ -839,7 +844,7 @@ static cudaError_t run_waves(const X& a, const WfArgs& w, int sms, cudaStream_t 
         *launches += 5;
         // The next wave's later flights, ordered by bin.
         k_wf_bin_count<<<sms * 4, 256, 0, s>>>(w, w.ext_key[cur ^ 1], cur ^ 1);
-        k_wf_bin_scan<<<1, 1024, 0, s>>>(w);
+        k_wf_bin_scan<<<1, 1024, 0, s>>>(w, cur ^ 1);
         k_wf_bin_place<<<sms * 4, 256, 0, s>>>(w, w.ext[cur ^ 1], w.ext_key[cur ^ 1], cur ^ 1);
         *launches += 3;
         cur ^= 1;

@@ -531,8 +531,12 @@ __global__ void __launch_bounds__(128, VV_EXTEND_MIN_BLOCKS)
     if (blockIdx.x == 0 && threadIdx.x == 0) W.counts[WF_SCATTER] = 0;
 }
 
+#ifndef VV_SHADE_MIN_BLOCKS
+#define VV_SHADE_MIN_BLOCKS 4
+#endif
 template <class X>
-__global__ void __launch_bounds__(128, 4) k_wf_shade(const __grid_constant__ X B, const WfArgs W, int cur) {
+__global__ void __launch_bounds__(128, VV_SHADE_MIN_BLOCKS) k_wf_shade(const __grid_constant__ X B, const WfArgs W,
+                                                                      int cur) {
     if (W.counts[WF_STOP] != 0u) return;
     uint32_t n = W.counts[WF_SHADE];
     const Consts C0 = kernel_consts(B);
@@ -639,8 +643,12 @@ __global__ void __launch_bounds__(128, VV_SHADOW_MIN_BLOCKS) k_wf_shadow(const _
 
 // Scatter, and the end of the flights that left the volume or hit the bounce
 // limits in this wave's extend (queued after the scatter entries).
+#ifndef VV_SCATTER_MIN_BLOCKS
+#define VV_SCATTER_MIN_BLOCKS 6
+#endif
 template <class X>
-__global__ void __launch_bounds__(128, 6) k_wf_scatter(const __grid_constant__ X B, const WfArgs W, int cur) {
+__global__ void __launch_bounds__(128, VV_SCATTER_MIN_BLOCKS) k_wf_scatter(const __grid_constant__ X B,
+                                                                          const WfArgs W, int cur) {
     if (W.counts[WF_STOP] != 0u) return;
     uint32_t n_scatter = W.counts[WF_SCATTER], n = n_scatter + W.counts[WF_ESC0 + cur];
     int nxt = cur ^ 1;

@@ -1,6 +1,6 @@
 // oracle_api64.cpp — the path tracer's restatement in double precision
-// (test infrastructure): the FP64 oracle that judges the precision variant's
-// storage formats.
+// (test infrastructure): the FP64 oracle, the reference that the precision
+// variant's storage formats are measured against.
 //
 // The same source as the FP32 oracle (oracle_shaders.cpp), compiled with
 // `float` defined as `double` (prelude.hpp): every product, sum, texture

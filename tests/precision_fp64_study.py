@@ -1,9 +1,9 @@
-"""The precision variant judged by the FP64 oracle (GPU + host cores).
+"""The precision variant measured against the FP64 oracle (GPU + host cores).
 
 Renders one view to `spp` paths per pixel with the density stored as FP32,
 R16_UNORM, FP16 and BF16 (and FP32 with Kahan running sums continuing in FP64),
 every render on the same per-pixel random streams (accumulation indices
-0 .. spp - 1). The judge is the FP64 oracle: the restatement of pt.comp
+0 .. spp - 1). The reference image comes from the FP64 oracle: the restatement of pt.comp
 compiled in double precision (arithmetic, texture filtering, sums), over the
 FP32-storage renderer's stored density, normals, masks and majorants, tracing
 the same paths on a few crops of the image. Each render's luminance RMSE
@@ -93,7 +93,7 @@ def run(ctx, cfg, spp, crops=3, size=32, zoom=None, log=None):
     from volview_gb300 import renderer as R
     W, H = cfg["width"], cfg["height"]
     out = {"paths_per_pixel": spp, "image": [W, H]}
-    judge, origins = None, None
+    oracle_lum, origins = None, None
     for density, sums, fp64_after in RUNS:
         fmt = {"unorm16": abi.DENSITY_UNORM16, "fp16": abi.DENSITY_FP16, "bf16": abi.DENSITY_BF16,
                "fp32": abi.DENSITY_FP32}[density]
@@ -115,18 +115,18 @@ def run(ctx, cfg, spp, crops=3, size=32, zoom=None, log=None):
         r.synchronize()
         gpu_s = time.perf_counter() - t0
         acc, _, _ = r.read_accumulation(normal=False)
-        if judge is None:
+        if oracle_lum is None:
             origins = crop_origins(acc[..., 3] / spp, size, crops)
             out["crops"] = [[x, y, size, size] for x, y in origins]
             t0 = time.perf_counter()
             cpu = oracle_from_device(cfg, r)
-            judge, mc = [], []
+            oracle_lum, mc = [], []
             for x0, y0 in origins:
                 ys, xs = np.mgrid[y0:y0 + size, x0:x0 + size]
                 pix = np.stack([xs.ravel(), ys.ravel()], 1).astype(np.int32)
                 s = cpu.pixel_sums_fp64(p, pix, 0, spp)
                 l1 = s[:, :3] @ LUMA
-                judge.append(l1 / spp)
+                oracle_lum.append(l1 / spp)
                 var = np.maximum(s[:, 7] - l1 * l1 / spp, 0.0) / max(spp - 1.0, 1.0) / spp
                 mc.append(float(np.sqrt(var.mean())))
             from oracle import oracle as O
@@ -135,7 +135,7 @@ def run(ctx, cfg, spp, crops=3, size=32, zoom=None, log=None):
         r.destroy()
         lum = np.asarray(acc[..., :3], np.float64) @ LUMA / spp
         errs = [float(np.sqrt(np.mean((lum[y0:y0 + size, x0:x0 + size].ravel() - jl) ** 2)))
-                for (x0, y0), jl in zip(origins, judge)]
+                for (x0, y0), jl in zip(origins, oracle_lum)]
         key = density if sums == "fp32" else f"{density}+{sums}+fp64_after_{fp64_after}"
         out[key] = {"rmse_vs_fp64_oracle_per_crop": errs, "rmse_vs_fp64_oracle": float(np.sqrt(np.mean(np.square(errs)))),
                     "gpu_seconds": gpu_s}

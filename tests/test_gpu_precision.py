@@ -235,7 +235,7 @@ def test_majorants_are_true_bounds(small_cfg, gpu_ctx, fmt):
 
 
 def test_formats_against_the_fp64_oracle(gpu_ctx):
-    """Every storage format and the compensated sums, judged by the FP64 oracle
+    """Every storage format and the compensated sums, measured against the FP64 oracle
     (tests/precision_fp64_study.py) on the small scene at 256 paths per pixel,
     the same random streams: each render's luminance RMSE against the oracle's
     image is at most twice the oracle image's own Monte Carlo RMSE (what the

@@ -1,5 +1,5 @@
 """The FP64 oracle (CPU): the path tracer's restatement compiled in double
-precision (oracle/oracle_api64.cpp), the judge of the precision variant.
+precision (oracle/oracle_api64.cpp), the reference of the precision variant's error figures.
 
 It is the FP32 oracle's source with `float` defined as `double`, over the same
 stored inputs, so on the same per-pixel random streams:

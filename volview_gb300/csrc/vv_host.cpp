@@ -1365,7 +1365,7 @@ static cudaError_t wf_state(vv_renderer::Pass& P, size_t cap, const Vol& v, cuda
         cudaError_t ce = cudaStreamSynchronize(s);  // the pass's previous use of its state has ended
         if (ce == cudaSuccess) ce = P.slots.alloc(cap * WF_SLOT_BYTES);
         if (ce == cudaSuccess) ce = P.map.alloc(cap * WF_MAP_BYTES);
-        if (ce == cudaSuccess) ce = P.queues.alloc(cap * 9 * sizeof(uint32_t));
+        if (ce == cudaSuccess) ce = P.queues.alloc(cap * 10 * sizeof(uint32_t));
         if (ce != cudaSuccess) return ce;
     }
     cap = P.slots.n / WF_SLOT_BYTES;
@@ -1389,6 +1389,7 @@ static cudaError_t wf_state(vv_renderer::Pass& P, size_t cap, const Vol& v, cuda
     w.esc[1] = q + 6 * cap;
     w.first[0] = q + 7 * cap;
     w.first[1] = q + 8 * cap;
+    w.map = q + 9 * cap;
     w.counts = P.counts.as<uint32_t>();
     // Later flights binned by the 32-voxel cell of their origin (coarser cells
     // while there would be more than 2^16 bins) and the octant of their

@@ -97,7 +97,9 @@ enum {
     WF_FIRST0 = 10, WF_FIRST1 = 11,  // first flights (bounce 0): a queue of their own
     WF_TAKE_FIRST = 12,  // entries of the first-flight queue taken so far
     WF_STOP = 13,     // 0 while waves run; 1 + the queue index the finishing launch takes over
-    WF_COUNTERS = 14
+    WF_MAP = 14,      // light map shadow rays queued by the key light's shadow rays
+    WF_TAKE_MAP = 15, // entries of the light map shadow queue taken so far
+    WF_COUNTERS = 16
 };
 struct WfArgs {
     uint32_t capacity;     // slots (and queue entries) allocated
@@ -113,6 +115,7 @@ struct WfArgs {
     uint32_t* shade;
     uint32_t* shadow;
     uint32_t* scatter;
+    uint32_t* map;         // slots whose light map shadow ray is next
     uint32_t* counts;      // WF_COUNTERS words
     // Later flights binned by the coarse cell of their origin and the octant
     // of their direction: the scatter kernel writes each queued slot's bin

@@ -572,8 +572,10 @@ __global__ void __launch_bounds__(128, VV_SHADE_MIN_BLOCKS) k_wf_shade(const __g
 // Shadow rays, persistent over their queue like extend: one ratio-tracking
 // step (tr_step, the loop body of transmittance, pt.comp:344-369) per
 // iteration, lanes refilled as their rays finish. With a light map, a lane
-// whose key-light ray finished draws the light map's sample and traces its
-// ray next (pt.comp:466-476, in the reference's order of random numbers).
+// whose key-light ray finished draws the light map's sample (pt.comp:466-476,
+// in the reference's order of random numbers) and queues the slot for
+// k_wf_shadow_map, which traces the sample's ray: a lane here traces one kind
+// of ray, and the random state travels in the shadow record between them.
 #ifndef VV_SHADOW_MIN_BLOCKS
 #define VV_SHADOW_MIN_BLOCKS 8
 #endif
@@ -588,7 +590,7 @@ __global__ void __launch_bounds__(128, VV_SHADOW_MIN_BLOCKS) k_wf_shadow(const _
     f3 origin;
     Rng rng;
     Shadow T;
-    bool active = false, drained = false, map_ray = false;
+    bool active = false, drained = false;
     for (;;) {
         bool need = !active && !drained;
         if (__any_sync(0xffffffffu, need)) {
@@ -602,11 +604,10 @@ __global__ void __launch_bounds__(128, VV_SHADOW_MIN_BLOCKS) k_wf_shadow(const _
                 rng.s = ubits(a.w);
                 tr_begin(args_of(B, r), origin, xyz(b), T);
                 active = true;
-                map_ray = false;
             }
             drained = __any_sync(0xffffffffu, need && k == ~0u);
         }
-        bool done = false;
+        bool done = false, to_map = false;
         if (active && !tr_step(args_of(B, r), origin, T, rng)) {
             const PtArgs& A = args_of(B, r);
             const bool map = MAP && (!IsBatch<X>::value || A.u.lighting[3] == 2u);
@@ -615,30 +616,64 @@ __global__ void __launch_bounds__(128, VV_SHADOW_MIN_BLOCKS) k_wf_shadow(const _
                 h[0] = f4(T.result, fbits(rng.s));
                 h[1] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
                 done = true;
-            } else if (map_ray) {
-                float4 h0 = h[0], h1 = h[1];
-                h[0] = make_float4(h0.x, h0.y, h0.z, fbits(rng.s));
-                h[1] = f4(xyz(h1) * T.result, h1.w);
-                done = true;
             } else {
                 Vertex V;
                 sample_map_light(A, rng, V);
                 h[0] = f4(T.result, fbits(rng.s));
                 h[1] = f4(V.map_light, V.map_pdf);
                 W.mapdir[slot] = f4(V.map_dir, 0.0f);
-                if (V.map_pdf > 0.0f) {
-                    tr_begin(A, origin, V.map_dir, T);
-                    map_ray = true;
-                } else {
-                    done = true;
-                }
+                to_map = V.map_pdf > 0.0f;
+                done = !to_map;
             }
-            if (done) active = false;
+            active = false;
         }
+        if (MAP) push(W.map, &W.counts[WF_MAP], slot, to_map);
         if (__any_sync(0xffffffffu, done)) push(W.scatter, &W.counts[WF_SCATTER], slot, done);
         if (drained && !__any_sync(0xffffffffu, active)) break;
     }
     if (blockIdx.x == 0 && threadIdx.x == 0) W.counts[WF_SHADE] = 0;
+}
+
+// The light map sample's shadow rays (after k_wf_shadow<true>): the ray from
+// the vertex along the sample's direction, continuing the slot's random
+// stream from the key light's ray and the sample; its transmittance scales
+// the sample's radiance for scatter.
+template <class X>
+__global__ void __launch_bounds__(128, VV_SHADOW_MIN_BLOCKS) k_wf_shadow_map(const __grid_constant__ X B,
+                                                                            const WfArgs W) {
+    if (W.counts[WF_STOP] != 0u) return;
+    const uint32_t n = W.counts[WF_MAP];
+    uint32_t slot = 0, r = 0;
+    f3 origin;
+    Rng rng;
+    Shadow T;
+    bool active = false, drained = false;
+    for (;;) {
+        bool need = !active && !drained;
+        if (__any_sync(0xffffffffu, need)) {
+            uint32_t k = take_item(&W.counts[WF_TAKE_MAP], n, need);
+            if (need && k != ~0u) {
+                slot = W.map[k];
+                r = request_of(B, slot);
+                origin = xyz(rec(W.shd, slot, SHD_N)[0]);
+                rng.s = ubits(rec(W.sh, slot, SH_N)[0].w);
+                tr_begin(args_of(B, r), origin, xyz(W.mapdir[slot]), T);
+                active = true;
+            }
+            drained = __any_sync(0xffffffffu, need && k == ~0u);
+        }
+        bool done = false;
+        if (active && !tr_step(args_of(B, r), origin, T, rng)) {
+            float4* h = rec(W.sh, slot, SH_N);
+            float4 h0 = h[0], h1 = h[1];
+            h[0] = make_float4(h0.x, h0.y, h0.z, fbits(rng.s));
+            h[1] = f4(xyz(h1) * T.result, h1.w);
+            done = true;
+            active = false;
+        }
+        if (__any_sync(0xffffffffu, done)) push(W.scatter, &W.counts[WF_SCATTER], slot, done);
+        if (drained && !__any_sync(0xffffffffu, active)) break;
+    }
 }
 
 // Scatter, and the end of the flights that left the volume or hit the bounce
@@ -707,6 +742,8 @@ __global__ void __launch_bounds__(128, VV_SCATTER_MIN_BLOCKS) k_wf_scatter(const
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         W.counts[WF_SHADOW] = 0;
         W.counts[WF_TAKE_SHADOW] = 0;
+        W.counts[WF_MAP] = 0;
+        W.counts[WF_TAKE_MAP] = 0;
     }
 }
 
@@ -846,8 +883,13 @@ static cudaError_t run_waves(const X& a, const WfArgs& w, int sms, cudaStream_t 
         k_wf_extend<true, X><<<g_ext, 128, 0, s>>>(a, w, cur, tail);
         k_wf_extend<false, X><<<g_ext, 128, 0, s>>>(a, w, cur, tail);
         k_wf_shade<X><<<g_shade, 128, 0, s>>>(a, w, cur);
-        if (map) k_wf_shadow<true, X><<<g_shadow, 128, 0, s>>>(a, w);
-        else k_wf_shadow<false, X><<<g_shadow, 128, 0, s>>>(a, w);
+        if (map) {
+            k_wf_shadow<true, X><<<g_shadow, 128, 0, s>>>(a, w);
+            k_wf_shadow_map<X><<<g_shadow, 128, 0, s>>>(a, w);
+            *launches += 1;
+        } else {
+            k_wf_shadow<false, X><<<g_shadow, 128, 0, s>>>(a, w);
+        }
         k_wf_scatter<X><<<g_scatter, 128, 0, s>>>(a, w, cur);
         *launches += 5;
         // The next wave's later flights, ordered by bin.

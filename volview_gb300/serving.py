@@ -34,9 +34,9 @@ import time
 # own sums (vv_resize).
 IMAGE_BYTES_PER_PIXEL = 48 + 32 + 32 + 8 + 4 + 2 + 6 * 48
 # Device bytes per path slot of a pass: the slot's records, the light map
-# sample's direction, the nine stage queues and the later-flight bins' keys
+# sample's direction, the ten stage queues and the later-flight bins' keys
 # and sorted queue (vv_wavefront.cu).
-SLOT_BYTES = 288 + 16 + 9 * 4 + 3 * 4
+SLOT_BYTES = 288 + 16 + 10 * 4 + 3 * 4
 PASSES = 6          # passes in flight per renderer
 PASS_FRAMES = 64    # frames per pass of a long vv_record_frames call
 SLOT_FRAMES = 16    # frames' worth of slots a pass holds at most ...

@@ -365,3 +365,34 @@ def test_batched_refuses_what_cannot_fit():
     srv.submit(S.Request("a", 64, 64, 16, params=0))
     with pytest.raises(MemoryError):
         srv.step()
+
+
+def test_batched_passes_stay_within_their_path_budget():
+    """A pass takes about pass_paths paths: the lead request at least one
+    frame, the others only frames that fit what is left."""
+    srv, engine, bases, views = make_batched(pass_paths=4 * 256 * 256, max_batch=8, frames_per_pass=64)
+    reqs = [S.Request("a", 256, 256, 16, params="small"), S.Request("a", 1024, 1024, 8, params="big"),
+            S.Request("b", 512, 512, 4, params="mid")]
+    run(srv, reqs)
+    sizes = {"small": 256 * 256, "big": 1024 * 1024, "mid": 512 * 512}
+    for p in engine.passes:
+        paths = [sizes[params] * n for _, params, _, n, _ in p]
+        # Over the budget only when the lead alone takes its one frame.
+        assert sum(paths) <= 4 * 256 * 256 or (len(p) == 1 and p[0][3] == 1)
+    assert all(q.image is not None for q in reqs)
+
+
+def test_view_memory_model_follows_the_library_sources():
+    """A view allocates the two label masks (4 bytes per bricked voxel each)
+    and no volume of its own; its image holds the passes' sums it keeps."""
+    import os
+    import re
+    csrc = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "volview_gb300", "csrc")
+    host = open(os.path.join(csrc, "vv_host.cpp")).read()
+    view = host[host.index("vv_renderer_create_view"):host.index("extern \"C\" vv_status vv_renderer_destroy")]
+    assert re.search(r"mask_a\.alloc\(elems \* sizeof\(uint32_t\)\)", view)
+    assert re.search(r"mask_b\.alloc\(elems \* sizeof\(uint32_t\)\)", view)
+    for shared in ("density", "normals", "labels"):
+        assert f"&r->{shared}, &root->{shared}" in view  # borrowed, not allocated
+    assert S.view_volume_bytes((8, 8, 8)) == 8 * 512
+    assert S.view_image_bytes(64, 32, passes=2) == 64 * 32 * (S.IMAGE_BYTES_PER_PIXEL - 48 * (S.PASSES - 2))
